@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 path tracer on the ReSTIR workload.
+
+Workload ("Plain method with ReSTIR"): 4x4 chunks (128x32x128 blocks) of the
+seeded value-noise heightfield, 0.5% emissive surface blocks, 1920x1080,
+64-frame orbit camera path, 3 bounces, light-BVH NEE, ReSTIR with 1 temporal
+neighbour (1-slot history), 3 spatial neighbours in a 30-px box, M-cap 20,
+FP32 reservoirs.  One step = one frame.
+
+Metric: Mrays/s (closest-hit queries + light any-hit queries issued, the
+reference's own ray count) with ms/frame.  `value` is device-timed (CUDA
+events on the library stream, scene and frame state resident in HBM);
+`e2e` is the same metric through the public C ABI with the frame copied back
+to host memory inside the timed region.
+
+--impl reference times the reference's CPU path (the oracle restatement,
+OpenMP over pixels on every host core) on a bounded pixel sample of the same
+workload.  With N > 1 ranks (torchrun) the frames are rendered by N
+independent replicas (the path has no exchange step) and rank 0 prints one
+line with the whole-job throughput.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "vulkan-voxel-restir-gi_gb300"))
+
+METRIC = "Mrays/s and ms/frame @1080p ReSTIR; relMSE vs FP64 GT, cache vs plain at equal time"
+SEED = 20240601
+NX = NZ = 4
+EMISSIVE = 0.005
+W, H, NB = 1920, 1080, 3
+ORBIT = 64
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.ws)
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
+    """The oracle on the same workload, only `rows` image rows traced per frame.
+    Returns (Mrays/s, seconds, rays)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import vrg
+    ow = oracle.build_world(mats, n, world)
+    orr = oracle.Renderer(W, H, NB)
+    rays = 0
+    t0 = time.perf_counter()
+    for f in range(frames):
+        cam = vrg.orbit_camera(NX, NZ, (start_frame + f) % ORBIT, ORBIT, W, H)
+        p = vrg.RenderParams(1, 1, 3, NB, vrg.MODE_CONFIG, f, 1000 + f, 2000 + f, 30.0, 20, 1, 0, 0)
+        y0 = (H // 2 - rows // 2)
+        orr.render(ow, cam, p, (y0 * W, (y0 + rows) * W))
+        a, b = orr.ray_counts()
+        rays += a + b
+    dt = time.perf_counter() - t0
+    orr.close()
+    ow.close()
+    return rays / dt / 1e6, dt, rays
+
+
+def run_reference(args, d):
+    import vrg
+    if d.rank != 0:
+        d.close()
+        return
+    mats, n = vrg.terrain_materials(SEED)
+    world = vrg.terrain_blocks(SEED, NX, NZ, EMISSIVE)
+    rows = args.ref_rows
+    threads = cpu_threads()
+    for w in range(args.warmup):
+        oracle_sample(world, mats, n, rows, 1, w)
+    times, rays_all = [], 0
+    for s in range(args.steps):
+        mr, dt, rays = oracle_sample(world, mats, n, rows, 1, args.warmup + s)
+        times.append(dt)
+        rays_all += rays
+    total = sum(times)
+    value = rays_all / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value-noise voxel terrain)",
+        "config": {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
+                   "bounces": NB, "spatial_neighbours": 3, "radius_px": 30, "m_cap": 20,
+                   "sample_rows_per_frame": rows},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} of {H} rows per frame, {args.steps} frames of the orbit"},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    d.close()
+
+
+def run_ours(args, d):
+    import vrg
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    ctx = vrg.Context(d.local if args.gpus > 1 else 0)
+    mats, n = vrg.terrain_materials(SEED)
+    ctx.set_materials(mats, n)
+    world = vrg.terrain_blocks(SEED, NX, NZ, EMISSIVE)
+    t0 = time.perf_counter()
+    scene, objs = vrg.build_world(ctx, world)
+    scene.commit()
+    build_s = time.perf_counter() - t0
+    r = vrg.Renderer(ctx, W, H, NB)
+    lib = ctx.lib
+    stats = vrg.FrameStats()
+    out_dev = vrg.FrameOutput(None, None, 0, 0)
+
+    def frame_params(f):
+        return vrg.RenderParams(1, 1, 3, NB, vrg.MODE_CONFIG, f, 1000 + f, 2000 + f, 30.0, 20, 1, 0, 0)
+
+    def render(f, out, st):
+        cam = vrg.orbit_camera(NX, NZ, f % ORBIT, ORBIT, W, H)
+        p = frame_params(f)
+        vrg.check(lib.vrg_render(r.h, scene.h, C.byref(cam), C.byref(p), C.byref(out),
+                                 C.byref(st) if st is not None else None), "vrg_render")
+
+    for f in range(args.warmup):
+        render(f, out_dev, stats)
+    # device-timed frames
+    d.barrier()
+    clk = ClockSampler(d.local)
+    clk.start()
+    ms, rays, ms_b, ms_res, ms_sp = [], 0, [0.0] * NB, 0.0, 0.0
+    for s in range(args.steps):
+        render(args.warmup + s, out_dev, stats)
+        if stats.error_flags:
+            raise RuntimeError(f"device error flags {stats.error_flags:#x}")
+        ms.append(stats.ms_total)
+        rays += stats.rays_closest + stats.rays_any
+        for b in range(NB):
+            ms_b[b] += stats.ms_bounce[b]
+        ms_res += stats.ms_resolve
+        ms_sp += stats.ms_spatial
+    clocks = clk.stop()
+    total_s = sum(ms) / 1000.0
+    d.barrier()
+    total_s_max = d.max(total_s)
+    rays_all = d.sum(rays)
+    value = rays_all / total_s_max / 1e6
+    # end to end through the public API with host buffers
+    img = np.empty(W * H * 4, np.uint8)
+    out_host = vrg.FrameOutput(img.ctypes.data, None, 1, 0)
+    # pin the host image buffer for the device->host copy
+    cudart_pinned = False
+    d.barrier()
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    for s in range(args.steps):
+        render(args.warmup + args.steps + s, out_host, stats)
+        e2e_rays += stats.rays_closest + stats.rays_any
+    e2e_s = d.max(time.perf_counter() - t0)
+    e2e_value = d.sum(e2e_rays) / e2e_s / 1e6
+    if d.rank != 0:
+        d.close()
+        return
+    # roofline of the dominant kernel (the bounce kernel): compulsory HBM bytes
+    # per ray-bounce (ray in/out, queue, per-bounce record, sample geometry)
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    bounce_ms = sum(ms_b)
+    bytes_per_ray = 36 + 32 + 36 + 16  # ray+queue in, record out, ray+queue out, sample geometry (avg)
+    achieved = (rays - 0) * bytes_per_ray / (bounce_ms / 1000.0) / 1e9 if bounce_ms > 0 else 0.0
+    stream_bytes = W * H * 252  # ReSTIR compulsory stream bytes per frame (reservoirs + radiance)
+    stream_gbs = stream_bytes * args.steps / ((ms_res + ms_sp) / 1000.0) / 1e9 if ms_res + ms_sp > 0 else 0.0
+    cpu_mr, cpu_dt, cpu_rays = oracle_sample(world, mats, n, args.ref_rows, 1, 0) if not args.no_cpu else (None, 0, 0)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total_s_max / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded value-noise voxel terrain, no dataset)",
+        "config": {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
+                   "bounces": NB, "temporal_history": 1, "spatial_neighbours": 3, "radius_px": 30,
+                   "m_cap": 20, "emissive_fraction": EMISSIVE, "orbit_frames": ORBIT,
+                   "l2": "per-frame state (~1.2 GB of rays, records, reservoirs) exceeds L2; BVH L2-resident",
+                   "parallelism": f"replicas{args.gpus}"},
+        "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b], "resolve_temporal": round(ms_res / args.steps, 4),
+                         "spatial_finalize_pack": round(ms_sp / args.steps, 4)},
+        "rays_per_frame": rays // max(args.steps, 1),
+        "scene_build_ms": round(build_s * 1000, 2),
+        "roofline": {"bound": "hbm", "kernel": "k_bounce", "achieved": round(achieved, 2), "peak": hbm_peak,
+                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                     "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
+                     "note": "traversal is L2-latency bound; stream kernels reported in stream_roofline"},
+        "stream_roofline": {"kernels": "k_resolve+k_spatial", "achieved": round(stream_gbs, 2), "peak": hbm_peak,
+                            "unit": "GB/s", "frac": round(stream_gbs / hbm_peak, 4), "bytes_per_px": 252},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),
+                "d2h_bytes_per_step": W * H * 4},
+        "gpu_launches": (NB + 2) * args.steps,
+        "clocks": clocks,
+        "cpu_baseline": None if cpu_mr is None else {
+            "value": round(cpu_mr, 4), "unit": "Mrays/s", "cores": cpu_threads(), "kind": "port",
+            "sample": f"{args.ref_rows} of {H} rows of frame 0 ({cpu_dt:.1f} s, {cpu_rays} rays)"},
+    }
+    print(json.dumps(line), flush=True)
+    d.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-rows", type=int, default=96, help="image rows the CPU baseline traces per frame")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    import vrg
+    if not os.path.exists(vrg.LIB_PATH):
+        sys.path.insert(0, ROOT)
+        import __graft_entry__
+        __graft_entry__.build()
+    d = Dist()
+    if args.impl == "reference":
+        run_reference(args, d)
+    else:
+        run_ours(args, d)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,283 @@
+/*
+ * vrg.h — C ABI of the GB300-native voxel path tracer (binned-SAH BVH build,
+ * wavefront trace/shade with light-BVH next-event estimation, ReSTIR temporal
+ * and spatial resampling, finalize and pack).
+ *
+ * Every entry point returns a vrg_status (0 == VRG_OK).  Handles are opaque.
+ * Host arrays passed in are copied; device memory is owned by the library.
+ * Upload entry points (vrg_upload_chunk) are thread-safe; scene and render
+ * calls on one scene/renderer must be externally synchronised, as the
+ * reference's Rc<RefCell<Scene>> / &mut Renderer are.
+ *
+ * Reference interfaces replaced (paths inside pimpale/vulkan-voxel-restir-gi):
+ *   SceneUploader::upload_object        src/render_system/scene.rs:547
+ *   Scene::new / add_object / update_object / remove_object /
+ *         dispose_old_objects / get_tlas src/render_system/scene.rs:112,150,205,218,227,234
+ *   Renderer::new / render / rebuild    src/render_system/interactive_rendering.rs:447,952,818
+ *   bvh::build::build_bl_bvh / build_tl_bvh  src/render_system/bvh/build.rs:249,374
+ *   BvhNode                             src/render_system/bvh/mod.rs:8-25
+ *   gen_mesh face order                 src/game_system/chunk.rs:158-292
+ */
+#ifndef VRG_H
+#define VRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VRG_API __declspec(dllexport)
+#else
+#define VRG_API __attribute__((visibility("default")))
+#endif
+
+typedef int32_t vrg_status;
+enum {
+    VRG_OK = 0,
+    VRG_ERR_INVALID_ARGUMENT = 1,
+    VRG_ERR_NOT_FOUND = 2,        /* reference panics instead (scene.rs:214) */
+    VRG_ERR_OUT_OF_MEMORY = 3,
+    VRG_ERR_CUDA = 4,
+    VRG_ERR_UNSUPPORTED = 5,
+    VRG_ERR_OVERFLOW = 6,         /* a bounded device structure overflowed */
+    VRG_ERR_STATE = 7,            /* call made in the wrong order */
+    VRG_ERR_NO_DEVICE = 8
+};
+
+/* Chunk geometry, as the reference's game_system/chunk.rs:14-20. */
+#define VRG_CHUNK_DIM 32
+#define VRG_CHUNK_BLOCKS (32 * 32 * 32) /* index = x*1024 + y*32 + z */
+
+/* Block faces in gen_mesh emission order (block.rs:9-17, chunk.rs:225-285). */
+enum { VRG_FACE_LEFT = 0, VRG_FACE_RIGHT, VRG_FACE_DOWN, VRG_FACE_UP, VRG_FACE_BACK, VRG_FACE_FRONT };
+
+/* 32-byte BVH node, the reference's wire format (bvh/mod.rs:8-25).
+ * left_node_idx == 0xFFFFFFFF marks a leaf; both indices 0xFFFFFFFF marks
+ * the dummy node of an empty light BVH. */
+typedef struct vrg_bvh_node {
+    uint32_t left_node_idx;
+    uint32_t right_node_idx_or_prim_idx;
+    float min[3];
+    float power;
+    float max[3];
+    uint32_t parent_idx;
+} vrg_bvh_node;
+
+/* One material per (block type, face): index t = 6*block + face, as the
+ * reference's texture index (block.rs:116-119).  The three texture maps of
+ * the reference become constants:
+ *   reflectivity/alpha = tex0.rgba, emission = 1000*tex1.rgb,
+ *   metallic = tex2.r (raytrace.rs:465-478);
+ *   luminance = the light power weight of the face, the reference's
+ *   get_texture_luminances value, mean(r8+g8+b8) of the emissivity texture
+ *   (utils.rs:223-235).  A face is a light iff luminance > 0 (scene.rs:560).
+ * flags bit 0 (VRG_MAT_TRANSLUCENT) on face 0 of a block type marks the block
+ * translucent for face culling (block.rs:125-127). */
+#define VRG_MAT_TRANSLUCENT 1u
+typedef struct vrg_material {
+    float reflectivity[3];
+    float alpha;
+    float emission[3];
+    float metallic;
+    float luminance;
+    uint32_t flags;
+    uint32_t reserved[2];
+} vrg_material;
+
+typedef struct vrg_context_desc {
+    int32_t device;          /* CUDA device ordinal */
+    uint32_t flags;          /* reserved, 0 */
+} vrg_context_desc;
+
+/* eye/front/right/up as Renderer::render takes them (interactive_rendering.rs:952). */
+typedef struct vrg_camera {
+    float eye[3];
+    float front[3];
+    float right[3];
+    float up[3];
+    uint32_t width;
+    uint32_t height;
+} vrg_camera;
+
+/* Render modes.  PARITY reproduces the reference's constants and quirks;
+ * CONFIG enables the extensions that have no reference counterpart
+ * (M-cap, 1-frame history ring, accumulation). */
+enum { VRG_MODE_PARITY = 0, VRG_MODE_CONFIG = 1 };
+
+/* Per-frame parameters: RenderingPreferences (camera.rs:38-56) plus the
+ * compile-time constants and the invocation seeds the reference draws from
+ * ThreadRng (interactive_rendering.rs:1044,1448,1491). */
+typedef struct vrg_render_params {
+    uint32_t nee_type;            /* 0 none, 1 light-BVH NEE, 2 NEE at bounce 1 only */
+    uint32_t debug_view;          /* 0 plain path, 1 ReSTIR, 2 debug (W/10) */
+    uint32_t spatial_iterations;  /* ReSTIR spatial neighbours, 0..20 */
+    uint32_t num_bounces;         /* >= 2 when ReSTIR is read (view 1) */
+    uint32_t mode;                /* VRG_MODE_* */
+    uint32_t raygen_seed;         /* unused by the math (jitter is x0.00), kept for the API */
+    uint32_t temporal_seed;
+    uint32_t spatial_seed;
+    float spatial_radius;         /* reference: 15 (restir_spatial_resampling.rs:314) */
+    uint32_t m_cap;               /* 0 = none (reference) */
+    uint32_t history_slots;       /* reservoir ring length; reference: 3 (frame % 3) */
+    uint32_t accumulate;          /* 1 = add this frame's radiance to the accumulator */
+    uint32_t flags;               /* VRG_RENDER_* */
+    uint32_t reserved[3];
+} vrg_render_params;
+
+#define VRG_RENDER_CAPTURE 1u      /* keep the full per-bounce SoA for vrg_debug_readback */
+#define VRG_RENDER_NO_PACK 2u      /* skip the u8 pack (radiance output only) */
+
+/* Where the frame goes.  Pointers may be NULL (not written).  host != 0 means
+ * the pointers are host memory and the library copies the frame back before
+ * vrg_render returns (the e2e path); host == 0 means device pointers written
+ * on the library's stream. */
+typedef struct vrg_frame_output {
+    uint8_t *bgra8;        /* W*H*4 bytes, B,G,R,255 (postprocess.rs:78) */
+    float *radiance;       /* W*H*3 floats: the view selected by debug_view */
+    uint32_t host;
+    uint32_t reserved;
+} vrg_frame_output;
+
+typedef struct vrg_frame_stats {
+    float ms_total;            /* device time of the whole frame (CUDA events) */
+    float ms_bounce[8];        /* per bounce kernel */
+    float ms_resolve;          /* outgoing radiance + temporal */
+    float ms_spatial;          /* spatial + finalize + pack */
+    uint64_t rays_closest;     /* closest-hit queries issued */
+    uint64_t rays_any;         /* light any-hit queries issued */
+    uint32_t error_flags;      /* device-side error word (stack overflow etc.) */
+    uint32_t reserved;
+} vrg_frame_stats;
+
+typedef struct vrg_context vrg_context;
+typedef struct vrg_object vrg_object;
+typedef struct vrg_scene vrg_scene;
+typedef struct vrg_renderer vrg_renderer;
+
+/* ---- context ---------------------------------------------------------- */
+VRG_API vrg_status vrg_context_create(const vrg_context_desc *desc, vrg_context **out);
+VRG_API vrg_status vrg_context_destroy(vrg_context *ctx);
+VRG_API const char *vrg_status_string(vrg_status s);
+VRG_API const char *vrg_last_error(void);
+
+/* Replaces the texture atlas + texture_luminances given to Renderer::new /
+ * Scene::new (interactive_rendering.rs:379-444, scene.rs:112).  n must be a
+ * multiple of 6; air is block id n/6 (block.rs:106-107,121-123). */
+VRG_API vrg_status vrg_material_table_set(vrg_context *ctx, const vrg_material *mats, uint32_t n);
+
+/* ---- objects (SceneUploader::upload_object, scene.rs:547) -------------- */
+/* One 32^3 chunk of u8 block ids plus its six neighbours (L,R,D,U,B,F as
+ * gen_mesh's NeighboringChunkData, chunk.rs:149-156); a NULL neighbour is air.
+ * Extraction of exposed faces, light triangles and both BVHs runs on the GPU,
+ * batched with the other pending uploads at the next vrg_scene_commit or
+ * vrg_flush_uploads.  An all-air chunk yields an empty object (the
+ * reference's SceneUploadedObjectHandle::Empty).  Thread-safe. */
+VRG_API vrg_status vrg_upload_chunk(vrg_context *ctx, const uint8_t *blocks,
+                                    const uint8_t *const neighbours[6], vrg_object **out);
+/* Runs every pending upload now (one batched launch sequence). */
+VRG_API vrg_status vrg_flush_uploads(vrg_context *ctx);
+VRG_API vrg_status vrg_object_release(vrg_object *obj);
+/* Counts of an uploaded object (after a flush): exposed faces, triangles,
+ * light triangles, geometry prims (surface blocks). */
+VRG_API vrg_status vrg_object_info(vrg_object *obj, uint32_t *n_faces, uint32_t *n_triangles,
+                                   uint32_t *n_light_triangles, uint32_t *n_surface_blocks);
+/* Copies the object's light BLAS (build_bl_bvh output, chunk-local) and its
+ * geometry BLAS (build_tl_bvh semantics over per-block AABBs) into host
+ * arrays of 2n-1 nodes; prim_order receives the final primitive permutation. */
+VRG_API vrg_status vrg_object_read_bvh(vrg_object *obj, uint32_t which /*0 light, 1 geometry*/,
+                                       vrg_bvh_node *nodes, uint32_t cap_nodes, uint32_t *n_nodes,
+                                       uint32_t *prim_order, uint32_t cap_prims, uint32_t *n_prims);
+
+/* ---- scene (Scene, scene.rs:86-497) ----------------------------------- */
+VRG_API vrg_status vrg_scene_create(vrg_context *ctx, vrg_scene **out);
+VRG_API vrg_status vrg_scene_destroy(vrg_scene *scene);
+/* xform3x4 is row-major [R|t]; only identity rotation is supported (chunks
+ * are translated, chunk_manager.rs:234-248). */
+VRG_API vrg_status vrg_scene_add(vrg_scene *scene, uint64_t key, vrg_object *obj, const float xform3x4[12]);
+VRG_API vrg_status vrg_scene_update(vrg_scene *scene, uint64_t key, const float xform3x4[12]);
+VRG_API vrg_status vrg_scene_remove(vrg_scene *scene, uint64_t key);
+/* = get_tlas: rebuilds the top levels (light TL BVH, geometry TL BVH) and
+ * the traversal layouts when something changed; frees retired objects. */
+VRG_API vrg_status vrg_scene_commit(vrg_scene *scene);
+/* Copies the top-level BVHs (which: 0 light TL, 1 geometry TL). */
+VRG_API vrg_status vrg_scene_read_tl(vrg_scene *scene, uint32_t which, vrg_bvh_node *nodes,
+                                     uint32_t cap, uint32_t *n_nodes);
+
+/* ---- renderer (Renderer, interactive_rendering.rs:328-1669) ----------- */
+VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_t height,
+                                       uint32_t max_bounces, vrg_renderer **out);
+VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r);
+/* Renderer::rebuild: new extent, all per-pixel state reset. */
+VRG_API vrg_status vrg_renderer_resize(vrg_renderer *r, uint32_t width, uint32_t height);
+/* Renderer::render.  frame_index = the renderer's frame counter, advanced by
+ * one per call (interactive_rendering.rs:1668); the raytrace invocation seed
+ * is frame_index*num_bounces + bounce (:1189). */
+VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
+                              const vrg_render_params *params, const vrg_frame_output *out,
+                              vrg_frame_stats *stats);
+VRG_API vrg_status vrg_renderer_frame_index(vrg_renderer *r, uint32_t *frame_index);
+VRG_API vrg_status vrg_renderer_reset_accumulation(vrg_renderer *r);
+/* Accumulated mean radiance (W*H*3 floats, host) after n frames with accumulate=1. */
+VRG_API vrg_status vrg_renderer_read_accumulation(vrg_renderer *r, float *rgb, uint32_t *n_frames);
+
+/* Debug / parity readback of the last frame rendered with VRG_RENDER_CAPTURE.
+ * what selects an array; the layout is W*H*comps floats per bounce slice:
+ *   VRG_DBG_ORIGIN (nb+1 slices, 3), VRG_DBG_DIRECTION (nb+1, 3),
+ *   VRG_DBG_NORMAL (nb, 3), VRG_DBG_EMISSIVITY (nb, 3), VRG_DBG_REFLECTIVITY (nb, 3),
+ *   VRG_DBG_MIS (nb, 1), VRG_DBG_BSDF_PDF (nb, 1), VRG_DBG_NEE_PDF (nb, 1),
+ *   VRG_DBG_RADIANCE (nb, 3), VRG_DBG_Q (nb, 1),
+ *   VRG_DBG_HIT (nb, 4 u32: instance, triangle, block index, face|half<<8),
+ *   VRG_DBG_TEMPORAL / VRG_DBG_SPATIAL (1, 20: x_v,n_v,x_s,n_s,l_o_hat,p_omega,
+ *       seed,ucw,m,w_sum as floats with seed/m bit-cast u32),
+ *   VRG_DBG_FINAL (1, 3). */
+enum {
+    VRG_DBG_ORIGIN = 0, VRG_DBG_DIRECTION, VRG_DBG_NORMAL, VRG_DBG_EMISSIVITY,
+    VRG_DBG_REFLECTIVITY, VRG_DBG_MIS, VRG_DBG_BSDF_PDF, VRG_DBG_NEE_PDF,
+    VRG_DBG_RADIANCE, VRG_DBG_Q, VRG_DBG_HIT, VRG_DBG_TEMPORAL, VRG_DBG_SPATIAL,
+    VRG_DBG_FINAL, VRG_DBG_COUNT
+};
+VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes);
+
+/* ---- standalone SAH builds (build.rs:249,374), batched, device-side --- */
+/* Builds `count` independent trees in one launch sequence.  Tree i owns
+ * prims [prim_offset[i], prim_offset[i]+n[i]) of the input arrays and writes
+ * 2n-1 nodes at node_offset[i].  All pointers are HOST arrays; the library
+ * stages them to the device, builds on the GPU and copies the nodes back.
+ *   tl variant: aabbs (6 floats: min, max) + translation (3 floats)
+ *   bl variant: triangles (9 floats) */
+VRG_API vrg_status vrg_build_tl_bvh_batched(vrg_context *ctx, uint32_t count, const uint32_t *n,
+                                            const uint32_t *prim_offset, const uint32_t *node_offset,
+                                            const float *translations, const float *aabbs,
+                                            const float *power, const uint32_t *ids,
+                                            vrg_bvh_node *nodes_out, uint32_t *prim_order_out);
+VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, const uint32_t *n,
+                                            const uint32_t *prim_offset, const uint32_t *node_offset,
+                                            const float *luminance, const float *triangles,
+                                            const uint32_t *ids, vrg_bvh_node *nodes_out,
+                                            uint32_t *prim_order_out);
+
+/* ---- synthetic scenes (no reference counterpart; the reference uses
+ *      OpenSimplex worldgen, chunk.rs:56-109) -------------------------- */
+/* Fills mats (capacity >= 6*(6+16)) with 6 opaque Lambertian block types
+ * (albedo U[0.2,0.8]^3) and 16 emissive types (radiance U[5,20]^3); returns
+ * the count in *n.  Air is block id (*n)/6. */
+VRG_API vrg_status vrg_terrain_materials(uint64_t seed, vrg_material *mats, uint32_t cap, uint32_t *n);
+/* World of nx*nz chunks (one chunk tall): 2-octave value-noise heightfield,
+ * heights 8..24, solid blocks uniform over the 6 Lambertian types, a fraction
+ * `emissive` of surface blocks emissive.  blocks: nx*nz*32768 bytes, chunk
+ * (cx,cz) at offset (cx*nz+cz)*32768, chunk-local index x*1024+y*32+z. */
+VRG_API vrg_status vrg_terrain_generate(uint64_t seed, uint32_t nx, uint32_t nz, float emissive,
+                                        uint8_t *blocks);
+/* Orbit camera of the benchmark path: frame f of n around the world centre. */
+VRG_API vrg_status vrg_orbit_camera(uint32_t nx, uint32_t nz, uint32_t frame, uint32_t n_frames,
+                                    uint32_t width, uint32_t height, vrg_camera *cam);
+/* PCG32 host stream for invocation seeds (replaces rand::rng()). */
+VRG_API uint32_t vrg_pcg32_next(uint64_t *state, uint64_t inc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VRG_H */

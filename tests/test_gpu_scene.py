@@ -1,0 +1,69 @@
+"""GPU chunk extraction (gen_mesh order + upload_object light prims) and the
+batched BLAS / top-level builds vs the oracle: counts, node arrays and prim
+order bit-exact."""
+import numpy as np
+import pytest
+
+import vrg
+from helpers import first_node_diff, nodes_equal, terrain_world
+
+pytestmark = pytest.mark.gpu
+
+
+def _worlds(gpu_ctx, orc, seed, nx, nz, emissive):
+    mats, n, world = terrain_world(seed, nx, nz, emissive)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    W = orc.build_world(mats, n, world)
+    return scene, objs, W
+
+
+@pytest.mark.parametrize("seed,nx,nz,em", [(1, 1, 1, 0.01), (2, 2, 3, 0.005), (5, 4, 4, 0.02)])
+def test_chunk_blas_bit_exact(gpu_ctx, orc, seed, nx, nz, em):
+    scene, objs, W = _worlds(gpu_ctx, orc, seed, nx, nz, em)
+    try:
+        for key, o in enumerate(objs):
+            gi = o.info()
+            oi = W.chunk_info(key)
+            assert gi["triangles"] == oi["triangles"]
+            assert gi["light_triangles"] == oi["light_triangles"]
+            assert gi["surface_blocks"] == oi["surface_blocks"]
+            for which in (0, 1):
+                gn, go = o.read_bvh(which)
+                on, oo = W.chunk_bvh(key, which)
+                assert nodes_equal(gn, on), (key, which, first_node_diff(gn, on))
+                assert np.array_equal(go, oo)
+        lt, gt = scene.get_tlas()
+        assert nodes_equal(lt, W.read_tl(0)), first_node_diff(lt, W.read_tl(0))
+        assert nodes_equal(gt, W.read_tl(1)), first_node_diff(gt, W.read_tl(1))
+    finally:
+        W.close()
+
+
+def test_no_lights_dummy_tl(gpu_ctx, orc):
+    scene, objs, W = _worlds(gpu_ctx, orc, 9, 2, 1, 0.0)
+    try:
+        lt, gt = scene.get_tlas()
+        assert len(lt) == 1 and lt[0]["left"] == 0xFFFFFFFF and lt[0]["right"] == 0xFFFFFFFF
+        assert nodes_equal(gt, W.read_tl(1))
+    finally:
+        W.close()
+
+
+def test_air_chunk_is_empty_object(gpu_ctx, vrglib):
+    mats, n = vrg.terrain_materials(1)
+    gpu_ctx.set_materials(mats, n)
+    up = vrg.SceneUploader(gpu_ctx)
+    o = up.upload_chunk(np.full(vrg.CHUNK_BLOCKS, 22, np.uint8))
+    assert o.info() == dict(faces=0, triangles=0, light_triangles=0, surface_blocks=0)
+    sc = vrg.Scene(gpu_ctx)
+    sc.add_object(1, o)
+    lt, gt = sc.get_tlas()
+    assert len(gt) == 0 and len(lt) == 1
+
+
+def test_update_missing_key_is_error(gpu_ctx):
+    sc = vrg.Scene(gpu_ctx)
+    with pytest.raises(vrg.VrgError) as e:
+        sc.update_object(12345, (0, 0, 0))
+    assert e.value.status == vrg.ERR_NOT_FOUND

@@ -1,0 +1,717 @@
+// C ABI of the path tracer: context, materials, chunk uploads, scene,
+// renderer orchestration (the frame graph of Renderer::render,
+// interactive_rendering.rs:952-1669, as one CUDA stream), debug readback and
+// the standalone batched SAH builds.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "vrg_frame.cuh"
+#include "vrg_internal.h"
+
+namespace vrg {
+
+vrg_status upload_frames(cudaStream_t s);
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int grid);
+vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
+vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
+int bounce_blocks_per_sm();
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+DevBuf::~DevBuf() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+}
+
+vrg_status dev_alloc(cudaStream_t s, size_t bytes, DevBufPtr &out) {
+    auto b = std::make_shared<DevBuf>();
+    b->stream = s;
+    b->bytes = bytes;
+    cudaError_t e = cudaMallocAsync(&b->ptr, bytes ? bytes : 16, s);
+    if (e != cudaSuccess) {
+        b->ptr = nullptr;
+        set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? VRG_ERR_OUT_OF_MEMORY : VRG_ERR_CUDA;
+    }
+    out = b;
+    return VRG_OK;
+}
+
+static void release_object(Object *o) {
+    if (o && --o->refs == 0) delete o;
+}
+
+}  // namespace vrg
+
+using namespace vrg;
+
+struct vrg_context : Context {};
+struct vrg_object : Object {};
+struct vrg_scene : Scene {};
+struct vrg_renderer : Renderer {};
+
+extern "C" {
+
+VRG_API const char *vrg_status_string(vrg_status s) {
+    switch (s) {
+    case VRG_OK: return "ok";
+    case VRG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case VRG_ERR_NOT_FOUND: return "not found";
+    case VRG_ERR_OUT_OF_MEMORY: return "out of memory";
+    case VRG_ERR_CUDA: return "cuda error";
+    case VRG_ERR_UNSUPPORTED: return "unsupported";
+    case VRG_ERR_OVERFLOW: return "device structure overflow";
+    case VRG_ERR_STATE: return "invalid state";
+    case VRG_ERR_NO_DEVICE: return "no cuda device";
+    default: return "unknown status";
+    }
+}
+
+VRG_API const char *vrg_last_error(void) { return g_err; }
+
+VRG_API vrg_status vrg_context_create(const vrg_context_desc *desc, vrg_context **out) {
+    if (!out) return VRG_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device visible");
+        return VRG_ERR_NO_DEVICE;
+    }
+    int dev = desc ? desc->device : 0;
+    if (dev < 0 || dev >= n) {
+        set_error("device %d out of range (%d devices)", dev, n);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    VRG_CUDA_TRY(cudaSetDevice(dev));
+    vrg_context *c = new vrg_context();
+    c->device = dev;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        set_error("cudaStreamCreate: %s", cudaGetErrorString(e));
+        return VRG_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    vrg_status st = upload_frames(c->stream);
+    if (st != VRG_OK) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_context_destroy(vrg_context *ctx) {
+    if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
+    for (Object *o : ctx->pending) release_object(o);
+    ctx->pending.clear();
+    ctx->d_mats.reset();
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_material_table_set(vrg_context *ctx, const vrg_material *mats, uint32_t n) {
+    if (!ctx || !mats || n == 0 || n % 6 || n / 6 > 255) {
+        set_error("material table needs a multiple of 6 entries, at most 6*255");
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->pending.empty()) {
+        set_error("material table changed with uploads pending");
+        return VRG_ERR_STATE;
+    }
+    ctx->mats.assign(mats, mats + n);
+    ctx->n_types = n / 6;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(ctx->stream, n * sizeof(vrg_material), b));
+    VRG_CUDA_TRY(cudaMemcpyAsync(b->ptr, mats, n * sizeof(vrg_material), cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->d_mats = b;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_upload_chunk(vrg_context *ctx, const uint8_t *blocks, const uint8_t *const neighbours[6],
+                                    vrg_object **out) {
+    if (!ctx || !blocks || !out) return VRG_ERR_INVALID_ARGUMENT;
+    if (ctx->n_types == 0) {
+        set_error("material table not set");
+        return VRG_ERR_STATE;
+    }
+    const uint32_t air = ctx->n_types;
+    for (uint32_t i = 0; i < VRG_CHUNK_BLOCKS; i++)
+        if (blocks[i] > air) {
+            set_error("block id %u at %u exceeds air id %u", blocks[i], i, air);
+            return VRG_ERR_INVALID_ARGUMENT;
+        }
+    vrg_object *o = new vrg_object();
+    o->ctx = ctx;
+    o->blocks.assign(blocks, blocks + VRG_CHUNK_BLOCKS);
+    o->slabs.assign(6 * 1024, (uint8_t)air);
+    for (int f = 0; f < 6; f++) {
+        const uint8_t *nb = neighbours ? neighbours[f] : nullptr;
+        if (!nb) continue;
+        o->slab_present |= 1u << f;
+        uint8_t *s = o->slabs.data() + f * 1024;
+        for (int a = 0; a < 32; a++)
+            for (int b = 0; b < 32; b++) {
+                uint32_t idx;
+                switch (f) {  // the neighbour's boundary plane facing this chunk
+                case 0: idx = 31 * 1024 + a * 32 + b; break;  // left: x=31, (y,z)
+                case 1: idx = 0 * 1024 + a * 32 + b; break;   // right: x=0
+                case 2: idx = a * 1024 + 31 * 32 + b; break;  // down: y=31, (x,z)
+                case 3: idx = a * 1024 + 0 * 32 + b; break;   // up: y=0
+                case 4: idx = a * 1024 + b * 32 + 31; break;  // back: z=31, (x,y)
+                default: idx = a * 1024 + b * 32 + 0; break;  // front: z=0
+                }
+                uint8_t v = nb[idx];
+                if (v > air) {
+                    delete o;
+                    set_error("neighbour %d block id %u exceeds air id %u", f, v, air);
+                    return VRG_ERR_INVALID_ARGUMENT;
+                }
+                s[a * 32 + b] = v;
+            }
+    }
+    o->refs = 2;  // caller + pending list
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->pending.push_back(o);
+    }
+    *out = o;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_flush_uploads(vrg_context *ctx) {
+    if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::vector<Object *> pend;
+    pend.swap(ctx->pending);
+    vrg_status st = extract_and_build(ctx, pend);
+    if (st != VRG_OK) {
+        ctx->pending.insert(ctx->pending.end(), pend.begin(), pend.end());
+        return st;
+    }
+    for (Object *o : pend) release_object(o);
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_object_release(vrg_object *obj) {
+    if (!obj) return VRG_ERR_INVALID_ARGUMENT;
+    release_object(obj);
+    return VRG_OK;
+}
+
+static vrg_status ensure_flushed(Object *o) {
+    if (o->flushed) return VRG_OK;
+    return vrg_flush_uploads(static_cast<vrg_context *>(o->ctx));
+}
+
+VRG_API vrg_status vrg_object_info(vrg_object *obj, uint32_t *n_faces, uint32_t *n_triangles,
+                                   uint32_t *n_light_triangles, uint32_t *n_surface_blocks) {
+    if (!obj) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_TRY(ensure_flushed(obj));
+    if (n_faces) *n_faces = obj->sum.n_faces;
+    if (n_triangles) *n_triangles = obj->sum.n_tris;
+    if (n_light_triangles) *n_light_triangles = obj->sum.n_light;
+    if (n_surface_blocks) *n_surface_blocks = obj->sum.n_geo;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_object_read_bvh(vrg_object *obj, uint32_t which, vrg_bvh_node *nodes, uint32_t cap_nodes,
+                                       uint32_t *n_nodes, uint32_t *prim_order, uint32_t cap_prims,
+                                       uint32_t *n_prims) {
+    if (!obj || which > 1) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_TRY(ensure_flushed(obj));
+    uint32_t np = which ? obj->sum.n_geo : obj->sum.n_light;
+    uint32_t nn = np ? 2 * np - 1 : 0;
+    if (n_nodes) *n_nodes = nn;
+    if (n_prims) *n_prims = np;
+    if (np == 0) return VRG_OK;
+    cudaStream_t s = obj->ctx->stream;
+    if (nodes) {
+        if (cap_nodes < nn) return VRG_ERR_INVALID_ARGUMENT;
+        VRG_CUDA_TRY(cudaMemcpyAsync(nodes, which ? obj->geo_nodes : obj->light_nodes, nn * sizeof(vrg_bvh_node),
+                                     cudaMemcpyDeviceToHost, s));
+    }
+    if (prim_order) {
+        if (cap_prims < np) return VRG_ERR_INVALID_ARGUMENT;
+        VRG_CUDA_TRY(cudaMemcpyAsync(prim_order, which ? obj->geo_perm : obj->light_perm, np * 4,
+                                     cudaMemcpyDeviceToHost, s));
+    }
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_create(vrg_context *ctx, vrg_scene **out) {
+    if (!ctx || !out) return VRG_ERR_INVALID_ARGUMENT;
+    vrg_scene *s = new vrg_scene();
+    s->ctx = ctx;
+    *out = s;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_destroy(vrg_scene *scene) {
+    if (!scene) return VRG_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(scene->ctx->stream);
+    for (auto &kv : scene->objects) release_object(kv.second.obj);
+    for (Object *o : scene->retired) release_object(o);
+    delete scene;
+    return VRG_OK;
+}
+
+static vrg_status parse_xform(const float *x, float off[3]) {
+    if (!x) {
+        off[0] = off[1] = off[2] = 0.0f;
+        return VRG_OK;
+    }
+    const float I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            if (x[4 * r + c] != I[r][c]) {
+                set_error("only translations are supported (chunks are translated, not rotated)");
+                return VRG_ERR_UNSUPPORTED;
+            }
+    off[0] = x[3];
+    off[1] = x[7];
+    off[2] = x[11];
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_add(vrg_scene *scene, uint64_t key, vrg_object *obj, const float xform3x4[12]) {
+    if (!scene || !obj) return VRG_ERR_INVALID_ARGUMENT;
+    float off[3];
+    VRG_TRY(parse_xform(xform3x4, off));
+    obj->refs++;
+    auto it = scene->objects.find(key);
+    if (it != scene->objects.end()) scene->retired.push_back(it->second.obj);
+    scene->objects[key] = SceneEntry{obj, {off[0], off[1], off[2]}};
+    scene->dirty = true;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_update(vrg_scene *scene, uint64_t key, const float xform3x4[12]) {
+    if (!scene) return VRG_ERR_INVALID_ARGUMENT;
+    auto it = scene->objects.find(key);
+    if (it == scene->objects.end()) {
+        set_error("object with key %llu does not exist", (unsigned long long)key);
+        return VRG_ERR_NOT_FOUND;  // reference panics (scene.rs:214)
+    }
+    float off[3];
+    VRG_TRY(parse_xform(xform3x4, off));
+    for (int a = 0; a < 3; a++) it->second.off[a] = off[a];
+    scene->dirty = true;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_remove(vrg_scene *scene, uint64_t key) {
+    if (!scene) return VRG_ERR_INVALID_ARGUMENT;
+    auto it = scene->objects.find(key);
+    if (it == scene->objects.end()) return VRG_OK;  // reference: removing a missing key is a no-op
+    scene->retired.push_back(it->second.obj);
+    scene->objects.erase(it);
+    scene->dirty = true;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_scene_commit(vrg_scene *scene) {
+    if (!scene) return VRG_ERR_INVALID_ARGUMENT;
+    return scene_commit(scene);
+}
+
+VRG_API vrg_status vrg_scene_read_tl(vrg_scene *scene, uint32_t which, vrg_bvh_node *nodes, uint32_t cap,
+                                     uint32_t *n_nodes) {
+    if (!scene || which > 1) return VRG_ERR_INVALID_ARGUMENT;
+    if (scene->dirty) {
+        set_error("scene not committed");
+        return VRG_ERR_STATE;
+    }
+    const auto &v = which ? scene->h_geo_tl : scene->h_light_tl;
+    if (n_nodes) *n_nodes = (uint32_t)v.size();
+    if (nodes) {
+        if (cap < v.size()) return VRG_ERR_INVALID_ARGUMENT;
+        memcpy(nodes, v.data(), v.size() * sizeof(vrg_bvh_node));
+    }
+    return VRG_OK;
+}
+
+// ---- renderer -------------------------------------------------------------
+
+static vrg_status renderer_alloc(vrg_renderer *r) {
+    const size_t P = (size_t)r->W * r->H;
+    const uint32_t nb = r->nb_max;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t o = 0;
+    size_t o_ro = o; o += al(P * 16);
+    size_t o_rd = o; o += al(P * 16);
+    size_t o_q0 = o; o += al(P * 4);
+    size_t o_q1 = o; o += al(P * 4);
+    size_t o_cnt = o; o += al(CNT_WORDS * 4);
+    size_t o_nl = o; o += al(P);
+    size_t o_rec = o; o += al(P * 32 * nb);
+    size_t o_xv = o; o += al(P * 16);
+    size_t o_nv = o; o += al(P * 16);
+    size_t o_xs = o; o += al(P * 16);
+    size_t o_ns = o; o += al(P * 16);
+    size_t o_pl = o; o += al(P * 16);
+    size_t o_sp = o; o += al(P * 80);
+    size_t o_ft = o; o += al(P * 16);
+    size_t o_bg = o; o += al(P * 4);
+    size_t o_rad = o; o += al(P * 12);
+    size_t o_acc = o; o += al(P * 24);
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(r->ctx->stream, o, b));
+    uint8_t *B = (uint8_t *)b->ptr;
+    r->ray_o = (float4 *)(B + o_ro);
+    r->ray_d = (float4 *)(B + o_rd);
+    r->queue[0] = (uint32_t *)(B + o_q0);
+    r->queue[1] = (uint32_t *)(B + o_q1);
+    r->counters = (uint32_t *)(B + o_cnt);
+    r->nlive = B + o_nl;
+    r->rec = (float4 *)(B + o_rec);
+    r->xv = (float4 *)(B + o_xv);
+    r->nv = (float4 *)(B + o_nv);
+    r->xs = (float4 *)(B + o_xs);
+    r->ns = (float4 *)(B + o_ns);
+    r->plain = (float4 *)(B + o_pl);
+    r->spatial = (float4 *)(B + o_sp);
+    r->final_t = (float4 *)(B + o_ft);
+    r->bgra = B + o_bg;
+    r->radiance = (float *)(B + o_rad);
+    r->accum = (double *)(B + o_acc);
+    VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, r->ctx->stream));
+    r->buf = b;
+    r->res = nullptr;
+    r->ring_slots = 0;
+    r->frame = 0;
+    r->accum_n = 0;
+    r->cap.reset();
+    r->captured = false;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_t height, uint32_t max_bounces,
+                                       vrg_renderer **out) {
+    if (!ctx || !out || width == 0 || height == 0 || max_bounces == 0 || max_bounces > MAX_BOUNCES - 1)
+        return VRG_ERR_INVALID_ARGUMENT;
+    if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
+    vrg_renderer *r = new vrg_renderer();
+    r->ctx = ctx;
+    r->W = width;
+    r->H = height;
+    r->nb_max = max_bounces;
+    vrg_status st = renderer_alloc(r);
+    if (st != VRG_OK) {
+        delete r;
+        return st;
+    }
+    for (auto &e : r->ev) cudaEventCreate(&e);
+    r->grid_bounce = ctx->num_sms * bounce_blocks_per_sm();
+    *out = r;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
+    if (!r) return VRG_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(r->ctx->stream);
+    for (auto &e : r->ev) cudaEventDestroy(e);
+    if (r->h_pinned) cudaFreeHost(r->h_pinned);
+    r->res_buf.reset();
+    delete r;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_resize(vrg_renderer *r, uint32_t width, uint32_t height) {
+    if (!r || width == 0 || height == 0) return VRG_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(r->ctx->stream);
+    r->W = width;
+    r->H = height;
+    r->res_buf.reset();
+    return renderer_alloc(r);
+}
+
+VRG_API vrg_status vrg_renderer_frame_index(vrg_renderer *r, uint32_t *frame_index) {
+    if (!r || !frame_index) return VRG_ERR_INVALID_ARGUMENT;
+    *frame_index = r->frame;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_reset_accumulation(vrg_renderer *r) {
+    if (!r) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_CUDA_TRY(cudaMemsetAsync(r->accum, 0, (size_t)r->W * r->H * 24, r->ctx->stream));
+    r->accum_n = 0;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_read_accumulation(vrg_renderer *r, float *rgb, uint32_t *n_frames) {
+    if (!r) return VRG_ERR_INVALID_ARGUMENT;
+    if (n_frames) *n_frames = r->accum_n;
+    if (!rgb) return VRG_OK;
+    size_t P = (size_t)r->W * r->H;
+    std::vector<double> h(P * 3);
+    VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), r->accum, P * 24, cudaMemcpyDeviceToHost, r->ctx->stream));
+    VRG_CUDA_TRY(cudaStreamSynchronize(r->ctx->stream));
+    double inv = r->accum_n ? 1.0 / (double)r->accum_n : 0.0;
+    for (size_t i = 0; i < P * 3; i++) rgb[i] = (float)(h[i] * inv);
+    return VRG_OK;
+}
+
+static vrg_status ensure_capture(vrg_renderer *r) {
+    if (r->cap) return VRG_OK;
+    const size_t P = (size_t)r->W * r->H, nb = r->nb_max;
+    size_t floats = (nb + 1) * P * 3 * 2 + nb * P * 3 * 4 + nb * P * 4 + nb * P * 4;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(r->ctx->stream, floats * 4, b));
+    float *f = (float *)b->ptr;
+    r->c_origin = f; f += (nb + 1) * P * 3;
+    r->c_dir = f; f += (nb + 1) * P * 3;
+    r->c_normal = f; f += nb * P * 3;
+    r->c_emis = f; f += nb * P * 3;
+    r->c_refl = f; f += nb * P * 3;
+    r->c_L = f; f += nb * P * 3;
+    r->c_mis = f; f += nb * P;
+    r->c_pdf = f; f += nb * P;
+    r->c_nee = f; f += nb * P;
+    r->c_q = f; f += nb * P;
+    r->c_hit = (uint32_t *)f;
+    VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, floats * 4, r->ctx->stream));
+    r->cap = b;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
+                              const vrg_render_params *pr, const vrg_frame_output *out, vrg_frame_stats *stats) {
+    if (!r || !scene || !cam || !pr) return VRG_ERR_INVALID_ARGUMENT;
+    if (cam->width != r->W || cam->height != r->H) {
+        set_error("camera extent %ux%u differs from the renderer's %ux%u (call vrg_renderer_resize)", cam->width,
+                  cam->height, r->W, r->H);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    if (pr->num_bounces == 0 || pr->num_bounces > r->nb_max || pr->spatial_iterations > 64 ||
+        pr->nee_type > 2 || pr->mode > 1) {
+        set_error("invalid render parameters");
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    if (scene->ctx != r->ctx) return VRG_ERR_INVALID_ARGUMENT;
+    Context *ctx = r->ctx;
+    cudaStream_t s = ctx->stream;
+    // Renderer::render starts with scene.get_tlas() (interactive_rendering.rs:961)
+    VRG_TRY(scene_commit(scene));
+    const size_t P = (size_t)r->W * r->H;
+    const uint32_t slots = pr->history_slots ? pr->history_slots : 3;
+    if (slots > 8) return VRG_ERR_INVALID_ARGUMENT;
+    if (slots != r->ring_slots) {
+        DevBufPtr b;
+        VRG_TRY(dev_alloc(s, (size_t)slots * 5 * P * 16, b));
+        VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, (size_t)slots * 5 * P * 16, s));
+        r->res_buf = b;
+        r->res = (float4 *)b->ptr;
+        r->ring_slots = slots;
+    }
+    const bool capture = (pr->flags & VRG_RENDER_CAPTURE) != 0;
+    if (capture) VRG_TRY(ensure_capture(r));
+    const uint32_t ring = r->frame % slots;
+    FrameArgs a;
+    memset(&a, 0, sizeof(a));
+    a.sc = scene->dev;
+    a.eye = f3{cam->eye[0], cam->eye[1], cam->eye[2]};
+    a.front = f3{cam->front[0], cam->front[1], cam->front[2]};
+    a.right = f3{cam->right[0], cam->right[1], cam->right[2]};
+    a.up = f3{cam->up[0], cam->up[1], cam->up[2]};
+    a.W = r->W;
+    a.H = r->H;
+    a.P = (uint32_t)P;
+    a.nb = pr->num_bounces;
+    a.nee_type = pr->nee_type;
+    a.frame = r->frame;
+    a.mode = pr->mode;
+    a.spatial_iters = pr->spatial_iterations;
+    a.temporal_seed = pr->temporal_seed;
+    a.spatial_seed = pr->spatial_seed;
+    a.spatial_radius = pr->spatial_radius;
+    a.m_cap = pr->m_cap;
+    a.debug_view = pr->debug_view;
+    a.accumulate = pr->accumulate;
+    a.pack = (pr->flags & VRG_RENDER_NO_PACK) ? 0u : 1u;
+    a.ray_o = r->ray_o;
+    a.ray_d = r->ray_d;
+    a.queue[0] = r->queue[0];
+    a.queue[1] = r->queue[1];
+    a.counters = r->counters;
+    a.nlive = r->nlive;
+    a.rec = r->rec;
+    a.xv = r->xv;
+    a.nv = r->nv;
+    a.xs = r->xs;
+    a.ns = r->ns;
+    a.plain = r->plain;
+    a.res = r->res + (size_t)ring * 5 * P;
+    a.spatial = r->spatial;
+    a.final_t = r->final_t;
+    a.bgra = r->bgra;
+    a.radiance = (out && out->radiance) ? r->radiance : nullptr;
+    a.accum = r->accum;
+    a.capture = capture ? 1u : 0u;
+    a.c_origin = r->c_origin;
+    a.c_dir = r->c_dir;
+    a.c_normal = r->c_normal;
+    a.c_emis = r->c_emis;
+    a.c_refl = r->c_refl;
+    a.c_mis = r->c_mis;
+    a.c_pdf = r->c_pdf;
+    a.c_nee = r->c_nee;
+    a.c_L = r->c_L;
+    a.c_q = r->c_q;
+    a.c_hit = r->c_hit;
+    if (out && !out->host && out->radiance) a.radiance = out->radiance;
+    if (out && !out->host && out->bgra8) a.bgra = out->bgra8;
+    VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
+    int ei = 0;
+    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    for (uint32_t b = 0; b < a.nb; b++) {
+        VRG_TRY(launch_bounce(s, a, b, r->grid_bounce));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    }
+    VRG_TRY(launch_resolve(s, a));
+    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    VRG_TRY(launch_spatial(s, a));
+    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    if (out && out->host) {
+        if (out->bgra8 && a.pack)
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->bgra8, a.bgra, P * 4, cudaMemcpyDeviceToHost, s));
+        if (out->radiance)
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, a.radiance, P * 12, cudaMemcpyDeviceToHost, s));
+    }
+    r->last_nb = a.nb;
+    r->last_ring = ring;
+    r->captured = capture;
+    if (pr->accumulate) r->accum_n++;
+    r->frame++;
+    if (stats || (out && out->host)) {
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, r->ev[0], r->ev[ei - 1]);
+        stats->ms_total = ms;
+        for (uint32_t b = 0; b < a.nb && b < 8; b++) {
+            cudaEventElapsedTime(&ms, r->ev[b], r->ev[b + 1]);
+            stats->ms_bounce[b] = ms;
+        }
+        cudaEventElapsedTime(&ms, r->ev[a.nb], r->ev[a.nb + 1]);
+        stats->ms_resolve = ms;
+        cudaEventElapsedTime(&ms, r->ev[a.nb + 1], r->ev[a.nb + 2]);
+        stats->ms_spatial = ms;
+        uint32_t cnt[CNT_WORDS];
+        VRG_CUDA_TRY(cudaMemcpy(cnt, r->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+        uint64_t rays, any;
+        memcpy(&rays, cnt + CNT_RAYS, 8);
+        memcpy(&any, cnt + CNT_ANY, 8);
+        stats->rays_closest = rays;
+        stats->rays_any = any;
+        stats->error_flags = cnt[CNT_ERROR];
+        if (cnt[CNT_ERROR]) {
+            set_error("device error flags 0x%x", cnt[CNT_ERROR]);
+            return VRG_ERR_OVERFLOW;
+        }
+    }
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes) {
+    if (!r || !dst || what >= VRG_DBG_COUNT) return VRG_ERR_INVALID_ARGUMENT;
+    if (!r->captured) {
+        set_error("last frame was not rendered with VRG_RENDER_CAPTURE");
+        return VRG_ERR_STATE;
+    }
+    cudaStream_t s = r->ctx->stream;
+    const size_t P = (size_t)r->W * r->H, nb = r->last_nb;
+    auto copy = [&](const void *src, size_t n) -> vrg_status {
+        if (bytes < n) return VRG_ERR_INVALID_ARGUMENT;
+        VRG_CUDA_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        return VRG_OK;
+    };
+    auto copy_res = [&](const float4 *planes) -> vrg_status {
+        if (bytes < P * 80) return VRG_ERR_INVALID_ARGUMENT;
+        std::vector<float4> h(5 * P);
+        VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), planes, 5 * P * 16, cudaMemcpyDeviceToHost, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        float *o = (float *)dst;
+        for (size_t p = 0; p < P; p++) {
+            float *d = o + 20 * p;
+            const float4 &a = h[p], &b = h[P + p], &c = h[2 * P + p], &e = h[3 * P + p], &l = h[4 * P + p];
+            d[0] = a.x; d[1] = a.y; d[2] = a.z;
+            d[3] = b.x; d[4] = b.y; d[5] = b.z;
+            d[6] = c.x; d[7] = c.y; d[8] = c.z;
+            d[9] = e.x; d[10] = e.y; d[11] = e.z;
+            d[12] = l.x; d[13] = l.y; d[14] = l.z;
+            d[15] = e.w;
+            d[16] = l.w;
+            d[17] = a.w;
+            d[18] = c.w;
+            d[19] = b.w;
+        }
+        return VRG_OK;
+    };
+    switch (what) {
+    case VRG_DBG_ORIGIN: return copy(r->c_origin, (nb + 1) * P * 12);
+    case VRG_DBG_DIRECTION: return copy(r->c_dir, (nb + 1) * P * 12);
+    case VRG_DBG_NORMAL: return copy(r->c_normal, nb * P * 12);
+    case VRG_DBG_EMISSIVITY: return copy(r->c_emis, nb * P * 12);
+    case VRG_DBG_REFLECTIVITY: return copy(r->c_refl, nb * P * 12);
+    case VRG_DBG_MIS: return copy(r->c_mis, nb * P * 4);
+    case VRG_DBG_BSDF_PDF: return copy(r->c_pdf, nb * P * 4);
+    case VRG_DBG_NEE_PDF: return copy(r->c_nee, nb * P * 4);
+    case VRG_DBG_RADIANCE: return copy(r->c_L, nb * P * 12);
+    case VRG_DBG_Q: return copy(r->c_q, nb * P * 4);
+    case VRG_DBG_HIT: return copy(r->c_hit, nb * P * 16);
+    case VRG_DBG_TEMPORAL: return copy_res(r->res + (size_t)r->last_ring * 5 * P);
+    case VRG_DBG_SPATIAL: return copy_res(r->spatial);
+    case VRG_DBG_FINAL: {
+        if (bytes < P * 12) return VRG_ERR_INVALID_ARGUMENT;
+        std::vector<float4> h(P);
+        VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), r->final_t, P * 16, cudaMemcpyDeviceToHost, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        float *o = (float *)dst;
+        for (size_t p = 0; p < P; p++) { o[3 * p] = h[p].x; o[3 * p + 1] = h[p].y; o[3 * p + 2] = h[p].z; }
+        return VRG_OK;
+    }
+    default: return VRG_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// ---- standalone batched builds --------------------------------------------
+
+VRG_API vrg_status vrg_build_tl_bvh_batched(vrg_context *ctx, uint32_t count, const uint32_t *n,
+                                            const uint32_t *prim_offset, const uint32_t *node_offset,
+                                            const float *translations, const float *aabbs, const float *power,
+                                            const uint32_t *ids, vrg_bvh_node *nodes_out,
+                                            uint32_t *prim_order_out) {
+    if (!ctx || !n || !prim_offset || !node_offset || !aabbs || !power || !ids) return VRG_ERR_INVALID_ARGUMENT;
+    return standalone_sah(ctx, false, count, n, prim_offset, node_offset, aabbs, translations, power, ids,
+                          nodes_out, prim_order_out);
+}
+
+VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, const uint32_t *n,
+                                            const uint32_t *prim_offset, const uint32_t *node_offset,
+                                            const float *luminance, const float *triangles, const uint32_t *ids,
+                                            vrg_bvh_node *nodes_out, uint32_t *prim_order_out) {
+    if (!ctx || !n || !prim_offset || !node_offset || !luminance || !triangles || !ids)
+        return VRG_ERR_INVALID_ARGUMENT;
+    return standalone_sah(ctx, true, count, n, prim_offset, node_offset, triangles, nullptr, luminance, ids,
+                          nodes_out, prim_order_out);
+}
+
+}  // extern "C"

@@ -1,0 +1,447 @@
+// Scene commit: the GB300 replacement of Scene::get_tlas (scene.rs:234-497).
+//
+// On change it rebuilds, on the GPU:
+//   * the light top-level BVH over objects with lights (build_tl_bvh over
+//     light root AABBs and powers, scene.rs:248-279) and the prim2node map
+//     (light_bvh_tl_idx, scene.rs:282-287);
+//   * the geometry top-level BVH over objects (same builder), replacing the
+//     driver TLAS (scene.rs:728-971);
+//   * the traversal layouts: one world-space BVH2 per structure in which
+//     each 64-byte node holds both children's boxes (translated to world
+//     space and widened by BOX_MARGIN, so culling is conservative) and child
+//     references (>= 0 node, < 0 ~record), with top-level leaves linked
+//     straight to the object's BLAS root; and 16-byte world-space records per
+//     surface block / light triangle.
+#include <algorithm>
+
+#include "vrg_internal.h"
+
+namespace vrg {
+
+namespace {
+
+struct InstBuild {
+    const vrg_bvh_node *bl;    // BLAS nodes (chunk-local)
+    const uint32_t *leaf;      // leaf -> local prim
+    const int2 *geo_local;     // geometry only
+    const uint32_t *light_tri; // light only
+    uint32_t n_prims;
+    uint32_t wbase, rbase;
+    float off[3];
+    int ioff[3];
+};
+
+__device__ __forceinline__ int bl_root_ref(const InstBuild &I) {
+    return I.bl[0].left_node_idx != INVALID ? (int)I.wbase : ~(int)(I.rbase + I.leaf[0]);
+}
+
+// one thread per node of the combined index space [TL nodes | BLAS nodes...]
+__global__ void k_wide(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *inst, uint32_t n_inst,
+                       uint32_t n_total, float4 *wide) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_total) return;
+    const vrg_bvh_node *node;
+    int k = -1;
+    uint32_t j;
+    if (g < n_tl) {
+        node = &tl[g];
+        j = g;
+    } else {
+        int lo = 0, hi = (int)n_inst - 1;
+        while (lo < hi) {  // last instance with wbase <= g
+            int mid = (lo + hi + 1) >> 1;
+            if (inst[mid].wbase <= g) lo = mid; else hi = mid - 1;
+        }
+        k = lo;
+        j = g - inst[k].wbase;
+        node = &inst[k].bl[j];
+    }
+    if (node->left_node_idx == INVALID) return;
+    uint32_t ch[2] = {node->left_node_idx, node->right_node_idx_or_prim_idx};
+    float box[2][6];
+    int ref[2];
+    for (int s = 0; s < 2; s++) {
+        const vrg_bvh_node *c;
+        float off[3] = {0.0f, 0.0f, 0.0f};
+        if (k < 0) {
+            c = &tl[ch[s]];
+            if (c->left_node_idx != INVALID) ref[s] = (int)ch[s];
+            else ref[s] = bl_root_ref(inst[c->right_node_idx_or_prim_idx]);
+        } else {
+            const InstBuild &I = inst[k];
+            c = &I.bl[ch[s]];
+            off[0] = I.off[0]; off[1] = I.off[1]; off[2] = I.off[2];
+            if (c->left_node_idx != INVALID) ref[s] = (int)(I.wbase + ch[s]);
+            else ref[s] = ~(int)(I.rbase + I.leaf[ch[s]]);
+        }
+        for (int a = 0; a < 3; a++) {
+            box[s][a] = (c->min[a] + off[a]) - BOX_MARGIN;
+            box[s][3 + a] = (c->max[a] + off[a]) + BOX_MARGIN;
+        }
+    }
+    float4 *w = wide + 4 * (size_t)g;
+    w[0] = make_float4(box[0][0], box[0][3], box[0][1], box[0][4]);
+    w[1] = make_float4(box[0][2], box[0][5], box[1][0], box[1][3]);
+    w[2] = make_float4(box[1][1], box[1][4], box[1][2], box[1][5]);
+    w[3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), 0.0f, 0.0f);
+}
+
+__global__ void k_geo_records(const InstBuild *inst, uint32_t k, int4 *rec) {
+    const InstBuild I = inst[k];
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < I.n_prims; p += gridDim.x * blockDim.x) {
+        int2 l = I.geo_local[p];
+        uint32_t blk = (uint32_t)l.x & 0x7FFFu;
+        int wx = (int)(blk >> 10) + I.ioff[0], wy = (int)((blk >> 5) & 31u) + I.ioff[1],
+            wz = (int)(blk & 31u) + I.ioff[2];
+        rec[I.rbase + p] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16), l.x, l.y);
+    }
+}
+
+__global__ void k_light_records(const InstBuild *inst, uint32_t k, int4 *rec) {
+    const InstBuild I = inst[k];
+    uint32_t n_nodes = 2 * I.n_prims - 1;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_nodes; j += gridDim.x * blockDim.x) {
+        uint32_t p = I.leaf[j];
+        if (p == INVALID) continue;
+        uint32_t t = I.light_tri[p];
+        int wx = (int)(t & 31u) + I.ioff[0], wy = (int)((t >> 5) & 31u) + I.ioff[1],
+            wz = (int)((t >> 10) & 31u) + I.ioff[2];
+        uint32_t f = (t >> 15) & 7u, h = (t >> 18) & 1u;
+        rec[I.rbase + p] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16), (int)(f | (h << 3)),
+                                     (int)j);
+    }
+}
+
+// top-level inputs: translated AABB (aabb.rs:75-92 for a translation) and
+// centroid (min+max)/2 (build.rs:391-400)
+__global__ void k_tl_inputs(const float *in /*[n][10]: lo3 hi3 off3 power*/, const uint32_t *ids, uint32_t n,
+                            float4 *lo, float4 *hi, float4 *cen, uint32_t *id_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *r = in + 10 * (size_t)i;
+    float l[3], h[3];
+    for (int a = 0; a < 3; a++) {
+        float x0 = r[a] + r[6 + a], x1 = r[3 + a] + r[6 + a];
+        l[a] = fminf(x0, x1);
+        h[a] = fmaxf(x0, x1);
+    }
+    lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+    hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
+    cen[i] = make_float4((l[0] + h[0]) / 2.0f, (l[1] + h[1]) / 2.0f, (l[2] + h[2]) / 2.0f, r[9]);
+    id_out[i] = ids[i];
+}
+
+// build_bl_bvh inputs (build.rs:262-270): AABB from the three points,
+// centroid (v0+v1+v2)/3, power = luminance
+__global__ void k_tri_inputs(const float *tris, const float *lum, uint32_t n, float4 *lo, float4 *hi, float4 *cen) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *t = tris + 9 * (size_t)i;
+    f3 v0 = f3{t[0], t[1], t[2]}, v1 = f3{t[3], t[4], t[5]}, v2 = f3{t[6], t[7], t[8]};
+    lo[i] = make_float4(fminf(fminf(fminf(v0.x, v0.x), v1.x), v2.x), fminf(fminf(fminf(v0.y, v0.y), v1.y), v2.y),
+                        fminf(fminf(fminf(v0.z, v0.z), v1.z), v2.z), 0.0f);
+    hi[i] = make_float4(fmaxf(fmaxf(fmaxf(v0.x, v0.x), v1.x), v2.x), fmaxf(fmaxf(fmaxf(v0.y, v0.y), v1.y), v2.y),
+                        fmaxf(fmaxf(fmaxf(v0.z, v0.z), v1.z), v2.z), 0.0f);
+    f3 s = add3(add3(v0, v1), v2);
+    cen[i] = make_float4(s.x / 3.0f, s.y / 3.0f, s.z / 3.0f, lum[i]);
+}
+
+}  // namespace
+
+vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t *n, const uint32_t *prim_offset,
+                          const uint32_t *node_offset, const float *prims, const float *translations,
+                          const float *power, const uint32_t *ids, vrg_bvh_node *nodes_out, uint32_t *order_out) {
+    cudaStream_t s = ctx->stream;
+    uint64_t total_prims = 0, total_nodes = 0;
+    std::vector<SahTree> trees(count);
+    for (uint32_t t = 0; t < count; t++) {
+        trees[t] = SahTree{n[t], prim_offset[t], node_offset[t], 0};
+        total_prims = std::max<uint64_t>(total_prims, (uint64_t)prim_offset[t] + n[t]);
+        if (n[t]) total_nodes = std::max<uint64_t>(total_nodes, (uint64_t)node_offset[t] + 2 * (uint64_t)n[t] - 1);
+    }
+    if (total_prims == 0) return VRG_OK;
+    if (total_prims > 0x3FFFFFFFull || total_nodes > 0x7FFFFFFFull) return VRG_ERR_UNSUPPORTED;
+    auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
+    const uint64_t in_floats = tri ? 9 : 10;
+    uint64_t o = 0;
+    uint64_t o_raw = o; o += al(total_prims * in_floats * 4);
+    uint64_t o_pw = o; o += al(total_prims * 4);
+    uint64_t o_lo = o; o += al(total_prims * 16);
+    uint64_t o_hi = o; o += al(total_prims * 16);
+    uint64_t o_cen = o; o += al(total_prims * 16);
+    uint64_t o_id = o; o += al(total_prims * 4);
+    uint64_t o_perm = o; o += al(total_prims * 4);
+    uint64_t o_nodes = o; o += al(total_nodes * sizeof(vrg_bvh_node));
+    uint64_t o_leaf = o; o += al(total_nodes * 4);
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(s, o, b));
+    uint8_t *B = (uint8_t *)b->ptr;
+    if (tri) {
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_raw, prims, total_prims * 36, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_pw, power, total_prims * 4, cudaMemcpyHostToDevice, s));
+        k_tri_inputs<<<(uint32_t)((total_prims + 255) / 256), 256, 0, s>>>(
+            (const float *)(B + o_raw), (const float *)(B + o_pw), (uint32_t)total_prims, (float4 *)(B + o_lo),
+            (float4 *)(B + o_hi), (float4 *)(B + o_cen));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_id, ids, total_prims * 4, cudaMemcpyHostToDevice, s));
+    } else {
+        std::vector<float> tin(10 * total_prims);
+        for (uint64_t i = 0; i < total_prims; i++) {
+            for (int a = 0; a < 3; a++) {
+                tin[10 * i + a] = prims[6 * i + a];
+                tin[10 * i + 3 + a] = prims[6 * i + 3 + a];
+                tin[10 * i + 6 + a] = translations ? translations[3 * i + a] : 0.0f;
+            }
+            tin[10 * i + 9] = power[i];
+        }
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_raw, tin.data(), total_prims * 40, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_pw, ids, total_prims * 4, cudaMemcpyHostToDevice, s));
+        k_tl_inputs<<<(uint32_t)((total_prims + 255) / 256), 256, 0, s>>>(
+            (const float *)(B + o_raw), (const uint32_t *)(B + o_pw), (uint32_t)total_prims, (float4 *)(B + o_lo),
+            (float4 *)(B + o_hi), (float4 *)(B + o_cen), (uint32_t *)(B + o_id));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));  // tin goes out of scope
+    }
+    VRG_CUDA_TRY(cudaGetLastError());
+    SahInputs in{(const float4 *)(B + o_lo), (const float4 *)(B + o_hi), (const float4 *)(B + o_cen),
+                 (const uint32_t *)(B + o_id)};
+    SahOutputs out{(vrg_bvh_node *)(B + o_nodes), (uint32_t *)(B + o_perm), (uint32_t *)(B + o_leaf)};
+    uint32_t levels = 0;
+    VRG_TRY(sah_build(s, trees, (uint32_t)total_prims, (uint32_t)total_nodes, in, out, &levels));
+    if (nodes_out)
+        VRG_CUDA_TRY(cudaMemcpyAsync(nodes_out, out.nodes, total_nodes * sizeof(vrg_bvh_node), cudaMemcpyDeviceToHost, s));
+    if (order_out) VRG_CUDA_TRY(cudaMemcpyAsync(order_out, out.perm, total_prims * 4, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+vrg_status scene_commit(Scene *sc) {
+    Context *ctx = sc->ctx;
+    cudaStream_t s = ctx->stream;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        std::vector<Object *> pend;
+        pend.swap(ctx->pending);
+        vrg_status st = extract_and_build(ctx, pend);
+        if (st != VRG_OK) {
+            ctx->pending.insert(ctx->pending.end(), pend.begin(), pend.end());
+            return st;
+        }
+        for (Object *o : pend)  // drop the pending list's reference
+            if (--o->refs == 0) delete o;
+    }
+    if (!sc->dirty) return VRG_OK;
+    // instances: non-empty objects in key order (scene.rs:245-260)
+    sc->inst_objs.clear();
+    sc->inst_off.clear();
+    for (auto &kv : sc->objects) {
+        Object *o = kv.second.obj;
+        if (!o->flushed) {
+            set_error("object not flushed");
+            return VRG_ERR_STATE;
+        }
+        if (o->sum.n_tris == 0) continue;
+        sc->inst_objs.push_back(o);
+        sc->inst_off.push_back({kv.second.off[0], kv.second.off[1], kv.second.off[2]});
+    }
+    const uint32_t ni = (uint32_t)sc->inst_objs.size();
+    if (ni > 65535) {
+        set_error("more than 65535 instances");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    // top-level inputs
+    std::vector<float> tl_in;
+    std::vector<uint32_t> tl_ids;
+    uint32_t n_light_inst = 0, n_geo_inst = 0;
+    for (uint32_t i = 0; i < ni; i++) {
+        const ChunkSummary &cs = sc->inst_objs[i]->sum;
+        if (cs.n_light == 0) continue;
+        const float *o = sc->inst_off[i].data();
+        float r[10] = {cs.light_lo[0], cs.light_lo[1], cs.light_lo[2], cs.light_hi[0], cs.light_hi[1],
+                       cs.light_hi[2], o[0], o[1], o[2], cs.light_power};
+        tl_in.insert(tl_in.end(), r, r + 10);
+        tl_ids.push_back(i);
+        n_light_inst++;
+    }
+    for (uint32_t i = 0; i < ni; i++) {
+        const ChunkSummary &cs = sc->inst_objs[i]->sum;
+        if (cs.n_geo == 0) continue;
+        const float *o = sc->inst_off[i].data();
+        float r[10] = {cs.geo_lo[0], cs.geo_lo[1], cs.geo_lo[2], cs.geo_hi[0], cs.geo_hi[1], cs.geo_hi[2],
+                       o[0], o[1], o[2], 0.0f};
+        tl_in.insert(tl_in.end(), r, r + 10);
+        tl_ids.push_back(i);
+        n_geo_inst++;
+    }
+    const uint32_t n_tl_prims = n_light_inst + n_geo_inst;
+    const uint32_t n_light_tl = n_light_inst ? 2 * n_light_inst - 1 : 1;
+    const uint32_t n_geo_tl = n_geo_inst ? 2 * n_geo_inst - 1 : 0;
+    // per-instance layout
+    uint64_t geo_nodes = 0, geo_recs = 0, light_nodes = 0, light_recs = 0;
+    std::vector<InstBuild> gb(ni), lb(ni);
+    uint32_t max_levels = 0;
+    for (uint32_t i = 0; i < ni; i++) {
+        Object *o = sc->inst_objs[i];
+        const ChunkSummary &cs = o->sum;
+        for (int a = 0; a < 3; a++) {
+            float t = sc->inst_off[i][a];
+            if (t != floorf(t) || fabsf(t) > 16384.0f) {
+                set_error("instance translation must be integral and within +-16384");
+                return VRG_ERR_UNSUPPORTED;
+            }
+            gb[i].off[a] = lb[i].off[a] = t;
+            gb[i].ioff[a] = lb[i].ioff[a] = (int)t;
+        }
+        gb[i].bl = o->geo_nodes;
+        gb[i].leaf = o->geo_leaf;
+        gb[i].geo_local = o->geo_local;
+        gb[i].light_tri = nullptr;
+        gb[i].n_prims = cs.n_geo;
+        gb[i].wbase = n_geo_tl + (uint32_t)geo_nodes;
+        gb[i].rbase = (uint32_t)geo_recs;
+        geo_nodes += cs.n_geo ? 2 * (uint64_t)cs.n_geo - 1 : 0;
+        geo_recs += cs.n_geo;
+        lb[i].bl = o->light_nodes;
+        lb[i].leaf = o->light_leaf;
+        lb[i].geo_local = nullptr;
+        lb[i].light_tri = o->light_tri;
+        lb[i].n_prims = cs.n_light;
+        lb[i].wbase = n_light_tl + (uint32_t)light_nodes;
+        lb[i].rbase = (uint32_t)light_recs;
+        light_nodes += cs.n_light ? 2 * (uint64_t)cs.n_light - 1 : 0;
+        light_recs += cs.n_light;
+        max_levels = std::max(max_levels, o->levels);
+    }
+    // instances without geometry/lights must not appear in the binary search
+    // of k_wide (wbase stays monotone: they own zero nodes), fine as is.
+    auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
+    uint64_t o = 0;
+    const uint64_t n_geo_wide = n_geo_tl + geo_nodes, n_light_wide = n_light_tl + light_nodes;
+    uint64_t o_gw = o; o += al(n_geo_wide * 64);
+    uint64_t o_gr = o; o += al(geo_recs * 16);
+    uint64_t o_lw = o; o += al(n_light_wide * 64);
+    uint64_t o_lr = o; o += al(light_recs * 16);
+    uint64_t o_tln = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * sizeof(vrg_bvh_node));
+    uint64_t o_inst = o; o += al((uint64_t)ni * sizeof(InstDev));
+    uint64_t o_gb = o; o += al((uint64_t)ni * sizeof(InstBuild));
+    uint64_t o_lb = o; o += al((uint64_t)ni * sizeof(InstBuild));
+    // TL build scratch
+    uint64_t o_tin = o; o += al((uint64_t)n_tl_prims * 40);
+    uint64_t o_tid = o; o += al((uint64_t)n_tl_prims * 4);
+    uint64_t o_tlo = o; o += al((uint64_t)n_tl_prims * 16);
+    uint64_t o_thi = o; o += al((uint64_t)n_tl_prims * 16);
+    uint64_t o_tcen = o; o += al((uint64_t)n_tl_prims * 16);
+    uint64_t o_tidd = o; o += al((uint64_t)n_tl_prims * 4);
+    uint64_t o_tperm = o; o += al((uint64_t)n_tl_prims * 4);
+    uint64_t o_tleaf = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * 4);
+    DevBufPtr buf;
+    VRG_TRY(dev_alloc(s, std::max<uint64_t>(o, 256), buf));
+    uint8_t *B = (uint8_t *)buf->ptr;
+    vrg_bvh_node *d_tl = (vrg_bvh_node *)(B + o_tln);  // [light TL | geometry TL]
+    uint32_t tl_levels = 0;
+    if (n_tl_prims) {
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_tin, tl_in.data(), tl_in.size() * 4, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_tid, tl_ids.data(), tl_ids.size() * 4, cudaMemcpyHostToDevice, s));
+        k_tl_inputs<<<(n_tl_prims + 127) / 128, 128, 0, s>>>((const float *)(B + o_tin), (const uint32_t *)(B + o_tid),
+                                                              n_tl_prims, (float4 *)(B + o_tlo), (float4 *)(B + o_thi),
+                                                              (float4 *)(B + o_tcen), (uint32_t *)(B + o_tidd));
+        VRG_CUDA_TRY(cudaGetLastError());
+        std::vector<SahTree> trees;
+        if (n_light_inst) trees.push_back(SahTree{n_light_inst, 0, 0, 0});
+        if (n_geo_inst) trees.push_back(SahTree{n_geo_inst, n_light_inst, n_light_tl, 0});
+        SahInputs in{(const float4 *)(B + o_tlo), (const float4 *)(B + o_thi), (const float4 *)(B + o_tcen),
+                     (const uint32_t *)(B + o_tidd)};
+        SahOutputs out{d_tl, (uint32_t *)(B + o_tperm), (uint32_t *)(B + o_tleaf)};
+        VRG_TRY(sah_build(s, trees, n_tl_prims, n_light_tl + n_geo_tl, in, out, &tl_levels));
+    }
+    if (!n_light_inst) {  // dummy node (BvhNode::default, bvh/mod.rs:27-38; scene.rs:276-277)
+        vrg_bvh_node d;
+        d.left_node_idx = d.right_node_idx_or_prim_idx = d.parent_idx = INVALID;
+        for (int a = 0; a < 3; a++) d.min[a] = d.max[a] = 0.0f;
+        d.power = 0.0f;
+        VRG_CUDA_TRY(cudaMemcpyAsync(d_tl, &d, sizeof(d), cudaMemcpyHostToDevice, s));
+    }
+    sc->h_light_tl.resize(n_light_tl);
+    sc->h_geo_tl.resize(n_geo_tl);
+    VRG_CUDA_TRY(cudaMemcpyAsync(sc->h_light_tl.data(), d_tl, n_light_tl * sizeof(vrg_bvh_node),
+                                 cudaMemcpyDeviceToHost, s));
+    if (n_geo_tl)
+        VRG_CUDA_TRY(cudaMemcpyAsync(sc->h_geo_tl.data(), d_tl + n_light_tl, n_geo_tl * sizeof(vrg_bvh_node),
+                                     cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    // instance table (prim2node)
+    std::vector<InstDev> idev(ni);
+    for (uint32_t i = 0; i < ni; i++) {
+        for (int a = 0; a < 3; a++) idev[i].off[a] = sc->inst_off[i][a];
+        idev[i].light_bvh_tl_idx = 0;
+        idev[i].light_bl = sc->inst_objs[i]->light_nodes;
+        idev[i].light_leaf_tri = sc->inst_objs[i]->light_leaf_tri;
+    }
+    if (n_light_inst)
+        for (uint32_t j = 0; j < n_light_tl; j++)
+            if (sc->h_light_tl[j].left_node_idx == INVALID) idev[sc->h_light_tl[j].right_node_idx_or_prim_idx].light_bvh_tl_idx = j;
+    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_inst, idev.data(), ni * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_gb, gb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_lb, lb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
+    const InstBuild *d_gb = (const InstBuild *)(B + o_gb), *d_lb = (const InstBuild *)(B + o_lb);
+    // wide layouts + records
+    if (n_geo_wide) {
+        k_wide<<<(uint32_t)((n_geo_wide + 255) / 256), 256, 0, s>>>(d_tl + n_light_tl, n_geo_tl, d_gb, ni,
+                                                                   (uint32_t)n_geo_wide, (float4 *)(B + o_gw));
+        VRG_CUDA_TRY(cudaGetLastError());
+    }
+    if (n_light_inst) {
+        k_wide<<<(uint32_t)((n_light_wide + 255) / 256), 256, 0, s>>>(d_tl, n_light_tl, d_lb, ni,
+                                                                     (uint32_t)n_light_wide, (float4 *)(B + o_lw));
+        VRG_CUDA_TRY(cudaGetLastError());
+    }
+    for (uint32_t i = 0; i < ni; i++) {
+        if (gb[i].n_prims) {
+            k_geo_records<<<std::min(64u, (gb[i].n_prims + 255) / 256), 256, 0, s>>>(d_gb, i, (int4 *)(B + o_gr));
+        }
+        if (lb[i].n_prims) {
+            k_light_records<<<std::min(64u, (2 * lb[i].n_prims + 254) / 256), 256, 0, s>>>(d_lb, i, (int4 *)(B + o_lr));
+        }
+    }
+    VRG_CUDA_TRY(cudaGetLastError());
+    // roots
+    DevScene &D = sc->dev;
+    D.geo_wide = (const float4 *)(B + o_gw);
+    D.geo_rec = (const int4 *)(B + o_gr);
+    D.light_wide = (const float4 *)(B + o_lw);
+    D.light_rec = (const int4 *)(B + o_lr);
+    D.light_tl = d_tl;
+    D.inst = (const InstDev *)(B + o_inst);
+    D.mats = (const vrg_material *)ctx->d_mats->ptr;
+    D.n_inst = ni;
+    auto root_of = [&](const std::vector<vrg_bvh_node> &tl, uint32_t n_tl, const std::vector<InstBuild> &ib,
+                       bool light) -> vrg_status {
+        int *dst = light ? &D.light_root : &D.geo_root;
+        if (n_tl == 0 || (light && !n_light_inst)) { *dst = EMPTY_ROOT; return VRG_OK; }
+        if (tl[0].left_node_idx != INVALID) { *dst = 0; return VRG_OK; }
+        // single object: the TL root is a leaf -> its BLAS root
+        uint32_t k = tl[0].right_node_idx_or_prim_idx;
+        vrg_bvh_node r;
+        VRG_CUDA_TRY(cudaMemcpy(&r, ib[k].bl, sizeof(r), cudaMemcpyDeviceToHost));
+        if (r.left_node_idx != INVALID) { *dst = (int)ib[k].wbase; return VRG_OK; }
+        uint32_t p0;
+        VRG_CUDA_TRY(cudaMemcpy(&p0, ib[k].leaf, 4, cudaMemcpyDeviceToHost));
+        *dst = ~(int)(ib[k].rbase + p0);
+        return VRG_OK;
+    };
+    VRG_TRY(root_of(sc->h_geo_tl, n_geo_tl, gb, false));
+    VRG_TRY(root_of(sc->h_light_tl, n_light_tl, lb, true));
+    sc->depth_bound = tl_levels + max_levels + 4;
+    if (sc->depth_bound >= (uint32_t)TRAV_STACK) {
+        set_error("BVH depth bound %u exceeds the traversal stack (%d)", sc->depth_bound, TRAV_STACK);
+        return VRG_ERR_UNSUPPORTED;
+    }
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    sc->d_buf = buf;
+    sc->dirty = false;
+    for (Object *r : sc->retired) {
+        if (--r->refs == 0) delete r;
+    }
+    sc->retired.clear();
+    return VRG_OK;
+}
+
+}  // namespace vrg

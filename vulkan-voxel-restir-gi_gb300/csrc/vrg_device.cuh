@@ -1,0 +1,232 @@
+// Device-side math shared by every kernel of the path tracer.
+//
+// Bit-exactness contract: every float expression here is a sequence of
+// single IEEE binary32 operations in source order.  The library is compiled
+// with -fmad=false (no FMA contraction), -prec-div=true and -prec-sqrt=true
+// (correctly rounded division and square root), so the same expression gives
+// the same bits on the GPU as on a host compiled with -ffp-contract=off.
+// GLSL built-ins follow the reference shader semantics with a fixed
+// evaluation order: dot(a,b) = (a.x*b.x + a.y*b.y) + a.z*b.z, normalize(v) =
+// v / length(v) per component, reflect(I,N) = I - (2*dot(N,I))*N.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/vrg.h"
+
+namespace vrg {
+
+struct f3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__host__ __device__ __forceinline__ f3 add3(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ __forceinline__ f3 sub3(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ __forceinline__ f3 scl3(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+__host__ __device__ __forceinline__ f3 lscl3(float s, f3 a) { return f3{s * a.x, s * a.y, s * a.z}; }
+__host__ __device__ __forceinline__ float dot3(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__host__ __device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+    return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+__host__ __device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
+__host__ __device__ __forceinline__ f3 norm3(f3 a) {
+    float l = len3(a);
+    return f3{a.x / l, a.y / l, a.z / l};
+}
+__host__ __device__ __forceinline__ bool zero3(f3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+__host__ __device__ __forceinline__ float cmp3(f3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ f3 ld3(float4 v) { return f3{v.x, v.y, v.z}; }
+
+constexpr float PI_F = 3.1415926535897932384626433832795f;          // raytrace.rs:12
+constexpr float TWO_PI_F = 6.283185307179586476925286766559f;
+constexpr float EPS_TRACE = 0.001f;                                   // raytrace.rs:13
+constexpr float EPS_NEE = 0.0001f;                                    // nee_pdf.rs:15
+constexpr float FACE_PAD = 1.0f / 4096.0f;                            // closed, overlapping faces
+constexpr float BOX_MARGIN = 1.0f / 128.0f;                           // conservative culling
+constexpr float COS25 = 0.906307787036649963f;                        // cos(radians(25))
+constexpr uint32_t INVALID = 0xFFFFFFFFu;
+constexpr uint32_t TERMINATED = 0xFFFFFFFEu;
+
+// murmur3 chaining (raygen.rs:48-78)
+__host__ __device__ __forceinline__ uint32_t mm_combine(uint32_t h, uint32_t k) {
+    k *= 0x1b873593u;
+    h ^= k;
+    h = (h << 13) | (h >> 19);
+    h = h * 5u + 0xe6546b64u;
+    return h;
+}
+__host__ __device__ __forceinline__ uint32_t mm_finalize(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+// floatConstruct (raygen.rs:37-46)
+__host__ __device__ __forceinline__ float float_construct(uint32_t m) {
+    m &= 0x007FFFFFu;
+    m |= 0x3F800000u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(m) - 1.0f;
+#else
+    float f;
+    __builtin_memcpy(&f, &m, 4);
+    return f - 1.0f;
+#endif
+}
+__host__ __device__ __forceinline__ float mm_rand(uint32_t h) { return float_construct(mm_finalize(h)); }
+
+// sin(2*pi*x), cos(2*pi*x), x in [0,1): exact quarter-turn reduction, then
+// the Taylor series of sin (to a^9) and cos (to a^10) on |a| <= pi/4.
+__host__ __device__ __forceinline__ void sincos_turns(float x, float *s, float *c) {
+    float q = rintf(x * 4.0f);
+    float r = x - q * 0.25f;
+    float a = r * TWO_PI_F;
+    float a2 = a * a;
+    float ps = (((2.75573192e-6f * a2 - 1.98412698e-4f) * a2 + 8.33333333e-3f) * a2 - 1.66666667e-1f) * a2;
+    float sn = a + a * ps;
+    float pc = ((((-2.75573192e-7f * a2 + 2.48015873e-5f) * a2 - 1.38888889e-3f) * a2 + 4.16666667e-2f) * a2 - 0.5f) * a2;
+    float cs = 1.0f + pc;
+    int k = ((int)q) & 3;
+    if (k == 0) { *s = sn; *c = cs; }
+    else if (k == 1) { *s = cs; *c = -sn; }
+    else if (k == 2) { *s = -sn; *c = -cs; }
+    else { *s = -cs; *c = sn; }
+}
+
+__host__ __device__ __forceinline__ float luminance3(f3 v) {  // restir_temporal_resampling.rs:248-250
+    return (0.2126f * v.x + 0.7152f * v.y) + 0.0722f * v.z;
+}
+
+// gen_mesh corner bits per (face, triangle, vertex): v{abc} = (x+a, y+b, z+c)
+// (chunk.rs:225-285, faces in the order left, right, down, up, back, front)
+__host__ __device__ __forceinline__ uint32_t face_corner(int f, int h, int j) {
+    // packed: 3 bits per vertex, 9 bits per triangle, 18 bits per face
+    constexpr uint64_t T[6] = {
+        (0b001ull | 0b010ull << 3 | 0b000ull << 6) | ((0b011ull | 0b010ull << 3 | 0b001ull << 6) << 9),
+        (0b110ull | 0b101ull << 3 | 0b100ull << 6) | ((0b110ull | 0b111ull << 3 | 0b101ull << 6) << 9),
+        (0b000ull | 0b100ull << 3 | 0b001ull << 6) | ((0b100ull | 0b101ull << 3 | 0b001ull << 6) << 9),
+        (0b011ull | 0b110ull << 3 | 0b010ull << 6) | ((0b011ull | 0b111ull << 3 | 0b110ull << 6) << 9),
+        (0b010ull | 0b100ull << 3 | 0b000ull << 6) | ((0b010ull | 0b110ull << 3 | 0b100ull << 6) << 9),
+        (0b001ull | 0b101ull << 3 | 0b011ull << 6) | ((0b101ull | 0b111ull << 3 | 0b011ull << 6) << 9),
+    };
+    return (uint32_t)((T[f] >> (9 * h + 3 * j)) & 7u);
+}
+__host__ __device__ __forceinline__ f3 corner_pos(int bx, int by, int bz, uint32_t bits) {
+    return f3{(float)(bx + (int)((bits >> 2) & 1u)), (float)(by + (int)((bits >> 1) & 1u)),
+              (float)(bz + (int)(bits & 1u))};
+}
+// in-plane axes of a face: a = normal axis, u/v = the other two ascending
+__host__ __device__ __forceinline__ void face_axes(int f, int &a, int &u, int &v) {
+    a = f >> 1;
+    u = (a == 0) ? 1 : 0;
+    v = (a == 2) ? 1 : 2;
+}
+__host__ __device__ __forceinline__ int bitsel(uint32_t bits, int axis) { return (int)((bits >> (2 - axis)) & 1u); }
+
+// barycentric weight of the triangle vertex at in-plane corner (cu, cv)
+__host__ __device__ __forceinline__ float corner_weight(int cu, int cv, int half, float lu, float lv) {
+    if (half == 0) {
+        if (cu == 0 && cv == 0) return (1.0f - lu) - lv;
+        if (cu == 1) return lu;
+        return lv;
+    }
+    if (cu == 1 && cv == 1) return (lu + lv) - 1.0f;
+    if (cu == 1) return 1.0f - lv;
+    return 1.0f - lu;
+}
+
+// Exact test of one exposed voxel face (the pair of gen_mesh triangles) —
+// the closest-hit and candidate semantics of the reference's ray query
+// restated for axis-aligned unit faces: plane hit t in [tmin, tmax], the
+// in-plane point inside the closed face rectangle padded by FACE_PAD, the
+// triangle half chosen by the face diagonal (on the diagonal: triangle 0).
+struct FaceHit {
+    float t;
+    int half;
+    float b1, b2;
+};
+__host__ __device__ __forceinline__ bool face_test(int bx, int by, int bz, int f, f3 o, f3 d, f3 inv, float tmin,
+                                                   float tmax, FaceHit &h) {
+    int a, u, v;
+    face_axes(f, a, u, v);
+    int bc[3] = {bx, by, bz};
+    float c = (float)(bc[a] + (f & 1));
+    float t = (c - cmp3(o, a)) * cmp3(inv, a);
+    if (!(t >= tmin && t <= tmax)) return false;
+    float pu = cmp3(o, u) + t * cmp3(d, u);
+    float pv = cmp3(o, v) + t * cmp3(d, v);
+    float lu = pu - (float)bc[u];
+    float lv = pv - (float)bc[v];
+    if (!(lu >= -FACE_PAD && lu <= 1.0f + FACE_PAD && lv >= -FACE_PAD && lv <= 1.0f + FACE_PAD)) return false;
+    int half = ((1.0f - lu) - lv >= 0.0f) ? 0 : 1;
+    uint32_t c1 = face_corner(f, half, 1), c2 = face_corner(f, half, 2);
+    h.t = t;
+    h.half = half;
+    h.b1 = corner_weight(bitsel(c1, u), bitsel(c1, v), half, lu, lv);
+    h.b2 = corner_weight(bitsel(c2, u), bitsel(c2, v), half, lu, lv);
+    return true;
+}
+
+// Shading frame of (face, half) (localCoordinateSystem, raytrace.rs:319-331).
+// The triangle edges are exact small integers, so the frame does not depend
+// on the block position; computed once on the host into constant memory.
+struct Frame {
+    f3 n, t, b;
+};
+__host__ __device__ inline Frame face_frame(int f, int h) {
+    f3 v0 = corner_pos(0, 0, 0, face_corner(f, h, 0));
+    f3 v1 = corner_pos(0, 0, 0, face_corner(f, h, 1));
+    f3 v2 = corner_pos(0, 0, 0, face_corner(f, h, 2));
+    f3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
+    f3 n = cross3(e1, e2);
+    f3 bt = cross3(n, e1);
+    return Frame{norm3(n), norm3(e1), norm3(bt)};
+}
+
+// ---------------------------------------------------------------------
+// device scene description (built by vrg_scene_commit)
+// ---------------------------------------------------------------------
+// Geometry prim record (one per surface block, world space), 16 bytes:
+//   x = (wx & 0xFFFF) | wz << 16      (signed 16-bit world block coords)
+//   y = (wy & 0xFFFF) | instance << 16
+//   z = chunk-local block index (15 bits) | face_mask << 15 | block id << 21
+//   w = first triangle index of the block in the chunk's gen_mesh order
+// Light record (one per light triangle), 16 bytes:
+//   x, y as above; z = face | half << 3; w = light BLAS leaf node index
+__host__ __device__ __forceinline__ int rec_wx(int4 r) { return (int)(short)(r.x & 0xFFFF); }
+__host__ __device__ __forceinline__ int rec_wz(int4 r) { return r.x >> 16; }
+__host__ __device__ __forceinline__ int rec_wy(int4 r) { return (int)(short)(r.y & 0xFFFF); }
+__host__ __device__ __forceinline__ uint32_t rec_inst(int4 r) { return ((uint32_t)r.y) >> 16; }
+
+struct InstDev {
+    float off[3];
+    uint32_t light_bvh_tl_idx;        // prim2node (scene.rs:282-287)
+    const vrg_bvh_node *light_bl;     // light BLAS nodes (chunk-local)
+    const uint32_t *light_leaf_tri;   // per light BLAS node: lx | ly<<5 | lz<<10 | face<<15 | half<<18
+};
+
+struct DevScene {
+    const float4 *geo_wide;   // 4 float4 per node: child boxes (world, +margin) and child refs
+    const int4 *geo_rec;
+    int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
+    const float4 *light_wide;
+    const int4 *light_rec;
+    int light_root;
+    const vrg_bvh_node *light_tl;  // reference-format light TL BVH (dummy node if no light)
+    const InstDev *inst;
+    const vrg_material *mats;
+    uint32_t n_inst;
+};
+
+constexpr int EMPTY_ROOT = (int)0x80000000;
+constexpr int TRAV_STACK = 64;
+constexpr uint32_t ERR_STACK = 1u;
+constexpr uint32_t ERR_LIGHT_LIST = 2u;
+constexpr uint32_t ERR_GUARD = 4u;
+constexpr uint32_t TRAV_GUARD = 1u << 22;  // iteration bound of every traversal loop
+
+}  // namespace vrg

@@ -1,0 +1,45 @@
+// Per-frame kernel arguments shared by the wavefront stages.
+#pragma once
+
+#include "vrg_device.cuh"
+
+namespace vrg {
+
+// counters[] layout (u32 words)
+constexpr int CNT_QUEUE = 0;     // [0..7]  rays queued for bounce b
+constexpr int CNT_FETCH = 8;     // [8..15] work-fetch cursor of bounce b
+constexpr int CNT_ERROR = 16;    // error word
+constexpr int CNT_RAYS = 18;     // u64 at words 18-19: closest-hit queries
+constexpr int CNT_ANY = 20;      // u64 at words 20-21: light any-hit queries
+constexpr int CNT_WORDS = 32;
+constexpr int MAX_BOUNCES = 8;
+
+struct FrameArgs {
+    DevScene sc;
+    f3 eye, front, right, up;
+    uint32_t W, H, P;
+    uint32_t nb, nee_type, frame;
+    uint32_t mode, spatial_iters, temporal_seed, spatial_seed;
+    float spatial_radius;
+    uint32_t m_cap, debug_view, accumulate, pack;
+    // wavefront state
+    float4 *ray_o, *ray_d;
+    uint32_t *queue[2];
+    uint32_t *counters;
+    uint8_t *nlive;
+    float4 *rec;                  // [nb][2][P]: (E.xyz, w), (R.xyz, q)
+    float4 *xv, *nv, *xs, *ns;
+    float4 *plain;                // L[0]
+    float4 *res;                  // temporal ring slot [5][P]
+    float4 *spatial;              // [5][P] (written when capture)
+    float4 *final_t;              // [P] (written when capture)
+    uint8_t *bgra;
+    float *radiance;
+    double *accum;
+    // capture (reference SoA layout, for parity readback)
+    uint32_t capture;
+    float *c_origin, *c_dir, *c_normal, *c_emis, *c_refl, *c_mis, *c_pdf, *c_nee, *c_L, *c_q;
+    uint32_t *c_hit;
+};
+
+}  // namespace vrg

@@ -1,0 +1,185 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/vrg.h"
+#include "vrg_device.cuh"
+
+namespace vrg {
+
+void set_error(const char *fmt, ...);
+
+#define VRG_CUDA_TRY(expr)                                                              \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            ::vrg::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__, \
+                             __LINE__);                                                 \
+            return VRG_ERR_CUDA;                                                        \
+        }                                                                               \
+    } while (0)
+
+#define VRG_TRY(expr)                   \
+    do {                                \
+        vrg_status _s = (expr);         \
+        if (_s != VRG_OK) return _s;    \
+    } while (0)
+
+// Stream-ordered device allocation owned by a shared_ptr: freed with
+// cudaFreeAsync on the owning stream, so a buffer retired while frames that
+// read it are still queued is released only after them (the reference keeps
+// retired objects alive in old_data for the same reason, scene.rs:58-70).
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    ~DevBuf();
+};
+using DevBufPtr = std::shared_ptr<DevBuf>;
+vrg_status dev_alloc(cudaStream_t s, size_t bytes, DevBufPtr &out);
+
+// ---- SAH builder ------------------------------------------------------
+struct SahTree {
+    uint32_t n;          // prims
+    uint32_t prim_off;   // into the prim arrays
+    uint32_t node_off;   // into the node array (2n-1 nodes)
+    uint32_t pad;
+};
+struct SahInputs {
+    const float4 *lo;    // prim AABB min (xyz)
+    const float4 *hi;    // prim AABB max (xyz)
+    const float4 *cen;   // centroid (xyz), w = power
+    const uint32_t *id;  // prim index id written into leaves
+};
+struct SahOutputs {
+    vrg_bvh_node *nodes;
+    uint32_t *perm;       // local prim order per tree (prim_off-relative)
+    uint32_t *leaf_prim;  // per node: local prim index of a leaf, INVALID for internal nodes
+};
+// Builds every tree; trees with n == 0 are skipped.  *levels receives the
+// number of level passes (an upper bound on depth - 2).
+vrg_status sah_build(cudaStream_t s, const std::vector<SahTree> &trees, uint32_t total_prims,
+                     uint32_t total_nodes, const SahInputs &in, const SahOutputs &out, uint32_t *levels);
+
+// ---- chunk extraction ---------------------------------------------------
+struct ChunkSummary {      // per chunk, copied to the host after a flush
+    uint32_t n_faces, n_tris, n_light, n_geo;
+    float light_lo[3], light_hi[3];
+    float light_power;
+    float geo_lo[3], geo_hi[3];
+    uint32_t pad;
+};
+
+struct Context;
+
+struct Object {
+    Context *ctx = nullptr;
+    std::vector<uint8_t> blocks;          // pending until flushed
+    std::vector<uint8_t> slabs;           // 6 x 1024 neighbour boundary planes
+    uint32_t slab_present = 0;            // bit i: neighbour i given
+    bool flushed = false;
+    ChunkSummary sum{};
+    DevBufPtr batch;                      // device arrays of the flush batch
+    // pointers into the batch (device)
+    const int2 *geo_local = nullptr;      // per geometry prim: (blk | mask<<15 | id<<21, first_tri)
+    const vrg_bvh_node *geo_nodes = nullptr;
+    const uint32_t *geo_perm = nullptr;
+    const uint32_t *geo_leaf = nullptr;
+    const vrg_bvh_node *light_nodes = nullptr;
+    const uint32_t *light_perm = nullptr;
+    const uint32_t *light_leaf = nullptr;
+    const uint32_t *light_tri = nullptr;  // per light prim: lx|ly<<5|lz<<10|face<<15|half<<18
+    const uint32_t *light_leaf_tri = nullptr;  // per light node (leaf payload, same packing)
+    uint32_t levels = 0;                  // SAH level passes of the batch (depth bound)
+    std::atomic<int> refs{1};
+    virtual ~Object() = default;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<vrg_material> mats;
+    DevBufPtr d_mats;
+    uint32_t n_types = 0;
+    std::mutex mu;                       // guards pending + stream use from upload threads
+    std::vector<Object *> pending;
+    int num_sms = 0;
+};
+
+vrg_status extract_and_build(Context *ctx, std::vector<Object *> &batch);
+
+// ---- scene -------------------------------------------------------------
+struct SceneEntry {
+    Object *obj;
+    float off[3];
+};
+
+struct Scene {
+    Context *ctx = nullptr;
+    std::map<uint64_t, SceneEntry> objects;
+    bool dirty = true;
+    // committed state
+    std::vector<Object *> inst_objs;      // instance order (key order, non-empty)
+    std::vector<std::array<float, 3>> inst_off;
+    DevBufPtr d_buf;                      // wide layouts, records, TLs, instance table
+    DevScene dev{};
+    std::vector<vrg_bvh_node> h_light_tl, h_geo_tl;
+    uint32_t depth_bound = 0;
+    std::vector<Object *> retired;        // released when the next commit completes
+};
+vrg_status scene_commit(Scene *sc);
+// Standalone batched builds of the C ABI: tri == false -> build_tl_bvh over
+// (aabb[6], translation[3]) prims, tri == true -> build_bl_bvh over triangles.
+vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t *n, const uint32_t *prim_offset,
+                          const uint32_t *node_offset, const float *prims, const float *translations,
+                          const float *power, const uint32_t *ids, vrg_bvh_node *nodes_out, uint32_t *order_out);
+
+// ---- renderer ------------------------------------------------------------
+struct Renderer {
+    Context *ctx = nullptr;
+    uint32_t W = 0, H = 0, nb_max = 0;
+    uint32_t frame = 0;
+    uint32_t ring_slots = 0;
+    uint32_t last_nb = 0;
+    uint32_t last_ring = 0;
+    bool captured = false;
+    DevBufPtr buf;
+    // device arrays (P = W*H)
+    float4 *ray_o = nullptr, *ray_d = nullptr;
+    uint32_t *queue[2] = {nullptr, nullptr};
+    uint32_t *counters = nullptr;         // [0..7] queue counts, [8] error word, [16..] ray counts (u64)
+    uint8_t *nlive = nullptr;
+    float4 *rec = nullptr;                // [nb][2][P]
+    float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
+    float4 *plain = nullptr;              // L[0] per pixel
+    float4 *res = nullptr;                // [ring][5][P] temporal reservoirs
+    DevBufPtr res_buf;
+    float4 *spatial = nullptr;            // [5][P] spatial reservoirs (capture)
+    float4 *final_t = nullptr;            // restir final target (capture)
+    uint8_t *bgra = nullptr;
+    float *radiance = nullptr;            // [P*3]
+    double *accum = nullptr;              // [P*3]
+    uint32_t accum_n = 0;
+    // capture arrays
+    DevBufPtr cap;
+    float *c_origin = nullptr, *c_dir = nullptr, *c_normal = nullptr, *c_emis = nullptr, *c_refl = nullptr;
+    float *c_mis = nullptr, *c_pdf = nullptr, *c_nee = nullptr, *c_L = nullptr, *c_q = nullptr;
+    uint32_t *c_hit = nullptr;
+    // host staging
+    uint8_t *h_pinned = nullptr;
+    size_t h_pinned_bytes = 0;
+    cudaEvent_t ev[16] = {};
+    int grid_bounce = 0;
+};
+
+}  // namespace vrg

@@ -1,0 +1,432 @@
+"""Python binding of libvrg.so (ctypes), mirroring the reference's render-system
+interface of pimpale/vulkan-voxel-restir-gi:
+
+    SceneUploader.upload_object   src/render_system/scene.rs:547  -> SceneUploader.upload_chunk
+    Scene.add_object / update_object / remove_object / get_tlas /
+          dispose_old_objects     src/render_system/scene.rs:150-234
+    Renderer.render(scene, eye, front, right, up, prefs)
+                                  src/render_system/interactive_rendering.rs:952
+    RenderingPreferences          src/camera.rs:38-56
+
+Every call goes to the CUDA library; there is no CPU path.  Loading fails
+loudly when libvrg.so has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvrg.so")
+
+CHUNK = 32
+CHUNK_BLOCKS = 32 * 32 * 32
+
+# status codes (include/vrg.h)
+OK, ERR_INVALID_ARGUMENT, ERR_NOT_FOUND, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_UNSUPPORTED, \
+    ERR_OVERFLOW, ERR_STATE, ERR_NO_DEVICE = range(9)
+
+MODE_PARITY, MODE_CONFIG = 0, 1
+RENDER_CAPTURE, RENDER_NO_PACK = 1, 2
+(DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
+ DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL) = range(14)
+
+
+class BvhNode(C.Structure):
+    """40-byte BvhNode (src/render_system/bvh/mod.rs:8-25)."""
+    _fields_ = [("left_node_idx", C.c_uint32), ("right_node_idx_or_prim_idx", C.c_uint32),
+                ("min", C.c_float * 3), ("power", C.c_float), ("max", C.c_float * 3),
+                ("parent_idx", C.c_uint32)]
+
+
+NODE_DTYPE = np.dtype([("left", "<u4"), ("right", "<u4"), ("min", "<f4", 3), ("power", "<f4"),
+                       ("max", "<f4", 3), ("parent", "<u4")])
+assert NODE_DTYPE.itemsize == C.sizeof(BvhNode) == 40
+
+
+class Material(C.Structure):
+    _fields_ = [("reflectivity", C.c_float * 3), ("alpha", C.c_float), ("emission", C.c_float * 3),
+                ("metallic", C.c_float), ("luminance", C.c_float), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
+
+
+class ContextDesc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("front", C.c_float * 3), ("right", C.c_float * 3),
+                ("up", C.c_float * 3), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("nee_type", C.c_uint32), ("debug_view", C.c_uint32), ("spatial_iterations", C.c_uint32),
+                ("num_bounces", C.c_uint32), ("mode", C.c_uint32), ("raygen_seed", C.c_uint32),
+                ("temporal_seed", C.c_uint32), ("spatial_seed", C.c_uint32), ("spatial_radius", C.c_float),
+                ("m_cap", C.c_uint32), ("history_slots", C.c_uint32), ("accumulate", C.c_uint32),
+                ("flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+class FrameOutput(C.Structure):
+    _fields_ = [("bgra8", C.c_void_p), ("radiance", C.c_void_p), ("host", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [("ms_total", C.c_float), ("ms_bounce", C.c_float * 8), ("ms_resolve", C.c_float),
+                ("ms_spatial", C.c_float), ("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
+                ("error_flags", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+_lib = None
+
+# (name, restype, argtypes) of every exported symbol of include/vrg.h
+_P = C.c_void_p
+SIGNATURES = [
+    ("vrg_context_create", C.c_int32, [C.POINTER(ContextDesc), C.POINTER(_P)]),
+    ("vrg_context_destroy", C.c_int32, [_P]),
+    ("vrg_status_string", C.c_char_p, [C.c_int32]),
+    ("vrg_last_error", C.c_char_p, []),
+    ("vrg_material_table_set", C.c_int32, [_P, C.POINTER(Material), C.c_uint32]),
+    ("vrg_upload_chunk", C.c_int32, [_P, _P, C.POINTER(_P), C.POINTER(_P)]),
+    ("vrg_flush_uploads", C.c_int32, [_P]),
+    ("vrg_object_release", C.c_int32, [_P]),
+    ("vrg_object_info", C.c_int32, [_P] + [C.POINTER(C.c_uint32)] * 4),
+    ("vrg_object_read_bvh", C.c_int32, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_uint32), _P, C.c_uint32,
+                                        C.POINTER(C.c_uint32)]),
+    ("vrg_scene_create", C.c_int32, [_P, C.POINTER(_P)]),
+    ("vrg_scene_destroy", C.c_int32, [_P]),
+    ("vrg_scene_add", C.c_int32, [_P, C.c_uint64, _P, C.POINTER(C.c_float)]),
+    ("vrg_scene_update", C.c_int32, [_P, C.c_uint64, C.POINTER(C.c_float)]),
+    ("vrg_scene_remove", C.c_int32, [_P, C.c_uint64]),
+    ("vrg_scene_commit", C.c_int32, [_P]),
+    ("vrg_scene_read_tl", C.c_int32, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    ("vrg_renderer_create", C.c_int32, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_P)]),
+    ("vrg_renderer_destroy", C.c_int32, [_P]),
+    ("vrg_renderer_resize", C.c_int32, [_P, C.c_uint32, C.c_uint32]),
+    ("vrg_render", C.c_int32, [_P, _P, C.POINTER(Camera), C.POINTER(RenderParams), C.POINTER(FrameOutput),
+                               C.POINTER(FrameStats)]),
+    ("vrg_renderer_frame_index", C.c_int32, [_P, C.POINTER(C.c_uint32)]),
+    ("vrg_renderer_reset_accumulation", C.c_int32, [_P]),
+    ("vrg_renderer_read_accumulation", C.c_int32, [_P, _P, C.POINTER(C.c_uint32)]),
+    ("vrg_debug_readback", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
+    ("vrg_build_tl_bvh_batched", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("vrg_build_bl_bvh_batched", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("vrg_terrain_materials", C.c_int32, [C.c_uint64, C.POINTER(Material), C.c_uint32, C.POINTER(C.c_uint32)]),
+    ("vrg_terrain_generate", C.c_int32, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P]),
+    ("vrg_orbit_camera", C.c_int32, [C.c_uint32] * 6 + [C.POINTER(Camera)]),
+    ("vrg_pcg32_next", C.c_uint32, [C.POINTER(C.c_uint64), C.c_uint64]),
+]
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libvrg.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libvrg.so not found at {path}: build it with __graft_entry__.build() "
+                           f"or python vulkan-voxel-restir-gi_gb300/build.py")
+    lib = C.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+class VrgError(RuntimeError):
+    def __init__(self, status, what):
+        lib = load_library()
+        msg = lib.vrg_last_error().decode(errors="replace")
+        super().__init__(f"{what}: {lib.vrg_status_string(status).decode()} ({status}) {msg}")
+        self.status = status
+
+
+def check(status, what=""):
+    if status != OK:
+        raise VrgError(status, what)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class RenderingPreferences:
+    """src/camera.rs:38-56."""
+    nee_type: int = 0
+    debug_view: int = 0
+    restir_spatial_iterations: int = 0
+
+
+def terrain_materials(seed: int):
+    lib = load_library()
+    mats = (Material * (6 * 22))()
+    n = C.c_uint32()
+    check(lib.vrg_terrain_materials(seed, mats, len(mats), C.byref(n)), "vrg_terrain_materials")
+    return mats, n.value
+
+
+def terrain_blocks(seed: int, nx: int, nz: int, emissive: float) -> np.ndarray:
+    lib = load_library()
+    out = np.empty(nx * nz * CHUNK_BLOCKS, dtype=np.uint8)
+    check(lib.vrg_terrain_generate(seed, nx, nz, emissive, _ptr(out)), "vrg_terrain_generate")
+    return out.reshape(nx, nz, CHUNK_BLOCKS)
+
+
+def chunk_neighbours(world: np.ndarray, cx: int, cz: int, solid_floor: np.ndarray):
+    """Six neighbour arrays (left, right, down, up, back, front) of chunk (cx, cz)
+    in a one-chunk-tall world; outside the world is air (None), below is solid."""
+    nx, nz = world.shape[:2]
+    left = world[cx - 1, cz] if cx > 0 else None
+    right = world[cx + 1, cz] if cx + 1 < nx else None
+    back = world[cx, cz - 1] if cz > 0 else None
+    front = world[cx, cz + 1] if cz + 1 < nz else None
+    return [left, right, solid_floor, None, back, front]
+
+
+def orbit_camera(nx, nz, frame, n_frames, width, height) -> Camera:
+    lib = load_library()
+    cam = Camera()
+    check(lib.vrg_orbit_camera(nx, nz, frame, n_frames, width, height, C.byref(cam)), "vrg_orbit_camera")
+    return cam
+
+
+class Pcg32:
+    """Host PCG32 stream for invocation seeds (replaces rand::rng())."""
+
+    def __init__(self, seed: int, stream: int = 54):
+        self.state = C.c_uint64(0)
+        self.inc = (stream << 1) | 1
+        self.next()
+        self.state.value = (self.state.value + seed) & (2 ** 64 - 1)
+        self.next()
+
+    def next(self) -> int:
+        return load_library().vrg_pcg32_next(C.byref(self.state), self.inc)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        desc = ContextDesc(device, 0)
+        check(self.lib.vrg_context_create(C.byref(desc), C.byref(self.h)), "vrg_context_create")
+
+    def set_materials(self, mats, n=None):
+        n = len(mats) if n is None else n
+        check(self.lib.vrg_material_table_set(self.h, mats, n), "vrg_material_table_set")
+
+    def flush(self):
+        check(self.lib.vrg_flush_uploads(self.h), "vrg_flush_uploads")
+
+    def close(self):
+        if self.h:
+            self.lib.vrg_context_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class UploadedObject:
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.h = handle
+
+    def info(self):
+        v = [C.c_uint32() for _ in range(4)]
+        check(self.ctx.lib.vrg_object_info(self.h, *[C.byref(x) for x in v]), "vrg_object_info")
+        return dict(faces=v[0].value, triangles=v[1].value, light_triangles=v[2].value,
+                    surface_blocks=v[3].value)
+
+    def read_bvh(self, which: int):
+        """which 0 = light BLAS (build_bl_bvh), 1 = geometry BLAS over block AABBs."""
+        nn, np_ = C.c_uint32(), C.c_uint32()
+        check(self.ctx.lib.vrg_object_read_bvh(self.h, which, None, 0, C.byref(nn), None, 0, C.byref(np_)),
+              "vrg_object_read_bvh")
+        nodes = np.zeros(nn.value, dtype=NODE_DTYPE)
+        order = np.zeros(np_.value, dtype=np.uint32)
+        if nn.value:
+            check(self.ctx.lib.vrg_object_read_bvh(self.h, which, _ptr(nodes), nn.value, C.byref(nn),
+                                                   _ptr(order), np_.value, C.byref(np_)), "vrg_object_read_bvh")
+        return nodes, order
+
+    def release(self):
+        if self.h:
+            self.ctx.lib.vrg_object_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class SceneUploader:
+    """SceneUploader (scene.rs:534-725): voxel chunks in, GPU-built BLAS out."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def upload_chunk(self, blocks: np.ndarray, neighbours=(None,) * 6) -> UploadedObject:
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1)
+        assert blocks.size == CHUNK_BLOCKS
+        keep = [None if n is None else np.ascontiguousarray(n, dtype=np.uint8).reshape(-1) for n in neighbours]
+        arr = (C.c_void_p * 6)(*[None if n is None else n.ctypes.data for n in keep])
+        h = C.c_void_p()
+        check(self.ctx.lib.vrg_upload_chunk(self.ctx.h, _ptr(blocks), arr, C.byref(h)), "vrg_upload_chunk")
+        return UploadedObject(self.ctx, h)
+
+
+def _xform(t):
+    x = (C.c_float * 12)(1, 0, 0, float(t[0]), 0, 1, 0, float(t[1]), 0, 0, 1, float(t[2]))
+    return x
+
+
+class Scene:
+    """Scene<K> (scene.rs:86-497) with u64 keys."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        check(ctx.lib.vrg_scene_create(ctx.h, C.byref(self.h)), "vrg_scene_create")
+        self._objs = {}
+
+    def add_object(self, key: int, obj: UploadedObject, translation=(0, 0, 0)):
+        check(self.ctx.lib.vrg_scene_add(self.h, key, obj.h, _xform(translation)), "vrg_scene_add")
+        self._objs[key] = obj
+
+    def update_object(self, key: int, translation):
+        check(self.ctx.lib.vrg_scene_update(self.h, key, _xform(translation)), "vrg_scene_update")
+
+    def remove_object(self, key: int):
+        check(self.ctx.lib.vrg_scene_remove(self.h, key), "vrg_scene_remove")
+        self._objs.pop(key, None)
+
+    def get_tlas(self):
+        """Commits the scene (top-level builds); returns (light TL, geometry TL) node arrays."""
+        check(self.ctx.lib.vrg_scene_commit(self.h), "vrg_scene_commit")
+        out = []
+        for which in (0, 1):
+            n = C.c_uint32()
+            check(self.ctx.lib.vrg_scene_read_tl(self.h, which, None, 0, C.byref(n)), "vrg_scene_read_tl")
+            nodes = np.zeros(n.value, dtype=NODE_DTYPE)
+            if n.value:
+                check(self.ctx.lib.vrg_scene_read_tl(self.h, which, _ptr(nodes), n.value, C.byref(n)),
+                      "vrg_scene_read_tl")
+            out.append(nodes)
+        return tuple(out)
+
+    commit = get_tlas
+
+    def dispose_old_objects(self):
+        """Retired objects are freed stream-ordered at the next commit."""
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.vrg_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Renderer:
+    """Renderer (interactive_rendering.rs:328-1669), headless."""
+
+    def __init__(self, ctx: Context, width: int, height: int, num_bounces: int = 3):
+        self.ctx = ctx
+        self.width, self.height, self.num_bounces = width, height, num_bounces
+        self.h = C.c_void_p()
+        check(ctx.lib.vrg_renderer_create(ctx.h, width, height, num_bounces, C.byref(self.h)),
+              "vrg_renderer_create")
+        self.seeds = Pcg32(0x5eed)
+        self.last_stats = FrameStats()
+
+    def params(self, prefs: RenderingPreferences, num_bounces=None, mode=MODE_PARITY, seeds=None,
+               spatial_radius=15.0, m_cap=0, history_slots=3, accumulate=0, flags=0) -> RenderParams:
+        if seeds is None:
+            seeds = (self.seeds.next(), self.seeds.next(), self.seeds.next())
+        return RenderParams(prefs.nee_type, prefs.debug_view, prefs.restir_spatial_iterations,
+                            self.num_bounces if num_bounces is None else num_bounces, mode, seeds[0], seeds[1],
+                            seeds[2], spatial_radius, m_cap, history_slots, accumulate, flags)
+
+    def render_params(self, scene: Scene, cam: Camera, params: RenderParams, want_image=True,
+                      want_radiance=False):
+        P = self.width * self.height
+        img = np.empty(P * 4, dtype=np.uint8) if want_image else None
+        rad = np.empty(P * 3, dtype=np.float32) if want_radiance else None
+        out = FrameOutput(None if img is None else img.ctypes.data, None if rad is None else rad.ctypes.data, 1, 0)
+        check(self.ctx.lib.vrg_render(self.h, scene.h, C.byref(cam), C.byref(params), C.byref(out),
+                                      C.byref(self.last_stats)), "vrg_render")
+        return (None if img is None else img.reshape(self.height, self.width, 4),
+                None if rad is None else rad.reshape(self.height, self.width, 3))
+
+    def render(self, scene: Scene, eye, front, right, up, prefs: RenderingPreferences, **kw):
+        """Renderer::render(scene, eye, front, right, up, prefs); returns the BGRA8 frame."""
+        cam = Camera((C.c_float * 3)(*eye), (C.c_float * 3)(*front), (C.c_float * 3)(*right),
+                     (C.c_float * 3)(*up), self.width, self.height)
+        img, _ = self.render_params(scene, cam, self.params(prefs, **kw))
+        return img
+
+    def readback(self, what: int, nb: int):
+        P = self.width * self.height
+        shapes = {DBG_ORIGIN: (nb + 1, P, 3), DBG_DIRECTION: (nb + 1, P, 3), DBG_NORMAL: (nb, P, 3),
+                  DBG_EMISSIVITY: (nb, P, 3), DBG_REFLECTIVITY: (nb, P, 3), DBG_MIS: (nb, P),
+                  DBG_BSDF_PDF: (nb, P), DBG_NEE_PDF: (nb, P), DBG_RADIANCE: (nb, P, 3), DBG_Q: (nb, P),
+                  DBG_HIT: (nb, P, 4), DBG_TEMPORAL: (P, 20), DBG_SPATIAL: (P, 20), DBG_FINAL: (P, 3)}
+        dt = np.uint32 if what == DBG_HIT else np.float32
+        a = np.zeros(shapes[what], dtype=dt)
+        check(self.ctx.lib.vrg_debug_readback(self.h, what, _ptr(a), a.nbytes), "vrg_debug_readback")
+        return a
+
+    def read_accumulation(self):
+        n = C.c_uint32()
+        a = np.zeros(self.width * self.height * 3, dtype=np.float32)
+        check(self.ctx.lib.vrg_renderer_read_accumulation(self.h, _ptr(a), C.byref(n)),
+              "vrg_renderer_read_accumulation")
+        return a.reshape(self.height, self.width, 3), n.value
+
+    def reset_accumulation(self):
+        check(self.ctx.lib.vrg_renderer_reset_accumulation(self.h), "vrg_renderer_reset_accumulation")
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.vrg_renderer_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def build_world(ctx: Context, world: np.ndarray):
+    """Uploads every chunk of a (nx, nz, 32768) world into a new Scene; key =
+    cx*nz + cz, translation (32cx, 0, 32cz).  Returns (scene, objects)."""
+    nx, nz = world.shape[:2]
+    floor = np.zeros(CHUNK_BLOCKS, dtype=np.uint8)  # solid ground below the world
+    up = SceneUploader(ctx)
+    scene = Scene(ctx)
+    objs = []
+    for cx in range(nx):
+        for cz in range(nz):
+            o = up.upload_chunk(world[cx, cz], chunk_neighbours(world, cx, cz, floor))
+            scene.add_object(cx * nz + cz, o, (32 * cx, 0, 32 * cz))
+            objs.append(o)
+    return scene, objs
