@@ -259,6 +259,25 @@ VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, co
                                             const uint32_t *ids, vrg_bvh_node *nodes_out,
                                             uint32_t *prim_order_out);
 
+/* Builds one tree with build_tl_bvh semantics (identity isometries) without
+ * allocating any memory.  No counterpart in the reference.  It is meant for
+ * callers that may not allocate device memory while they run: an engine
+ * that owns the whole device-memory budget, or a streaming worker building
+ * next to a frame in flight, where cudaMalloc/cudaFree can synchronize the
+ * device.  All pointers are device pointers owned by the caller: aabbs n x 6
+ * floats (min, max), power n floats, ids n u32; nodes receives 2n-1 nodes,
+ * prim_order n u32.  stream is a cudaStream_t (NULL = legacy default).
+ * n must be 1..32768; larger n returns VRG_ERR_INVALID_ARGUMENT.
+ * Scratch is one fixed device array of about 2.4 MiB inside the library,
+ * held by every GPU that loads it until the process exits.  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress),
+ * so make the first call on each device before any stream capture.  Every
+ * call shares the array: calls that overlap on the GPU (other threads or
+ * streams) race and must be serialized by the caller.  The call returns
+ * after the build has finished on `stream`. */
+VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const float *power, const uint32_t *ids,
+                                            uint32_t n, vrg_bvh_node *nodes, uint32_t *prim_order, void *stream);
+
 /* ---- synthetic scenes (no reference counterpart; the reference uses
  *      OpenSimplex worldgen, chunk.rs:56-109) -------------------------- */
 /* Fills mats (capacity >= 6*(6+16)) with 6 opaque Lambertian block types

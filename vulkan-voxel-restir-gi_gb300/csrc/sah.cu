@@ -22,6 +22,7 @@
 // swapped with the k-th predicate-true element from the right, the pairing
 // of the serial two-pointer partition.
 #include <cfloat>
+#include <mutex>
 
 #include "vrg_internal.h"
 
@@ -403,3 +404,145 @@ vrg_status sah_build(cudaStream_t s, const std::vector<SahTree> &trees, uint32_t
 }
 
 }  // namespace vrg
+
+namespace vrg {
+
+// ---------------------------------------------------------------------------
+// Build without allocating: vrg_build_tl_bvh_noalloc
+//
+// For callers that must not allocate device memory while they run: a game or
+// engine that owns the whole device-memory budget and hands this library
+// only the buffers it has set aside, or a chunk-streaming worker that builds
+// BVHs next to a frame in flight, where cudaMalloc/cudaFree may synchronize
+// the device and stall the frame.  The builder's scratch (work queues,
+// level counters, bottom-up arrival flags, prepared prim bounds) lives in
+// the fixed device array below instead of a cudaMallocAsync allocation.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_PRIMS = 32768;  // one chunk's worth of blocks
+constexpr size_t NOALLOC_QCAP = NOALLOC_MAX_PRIMS / 3 + 2;
+constexpr size_t NOALLOC_OFF_LO = 0;
+constexpr size_t NOALLOC_OFF_HI = NOALLOC_OFF_LO + (size_t)NOALLOC_MAX_PRIMS * 16;
+constexpr size_t NOALLOC_OFF_CEN = NOALLOC_OFF_HI + (size_t)NOALLOC_MAX_PRIMS * 16;
+constexpr size_t NOALLOC_OFF_Q0 = NOALLOC_OFF_CEN + (size_t)NOALLOC_MAX_PRIMS * 16;
+constexpr size_t NOALLOC_OFF_Q1 = NOALLOC_OFF_Q0 + NOALLOC_QCAP * sizeof(Item);
+constexpr size_t NOALLOC_OFF_CNT = (NOALLOC_OFF_Q1 + NOALLOC_QCAP * sizeof(Item) + 255) & ~(size_t)255;
+constexpr size_t NOALLOC_OFF_TREE = NOALLOC_OFF_CNT + 256;
+constexpr size_t NOALLOC_OFF_ARRIVE = NOALLOC_OFF_TREE + 256;
+constexpr size_t NOALLOC_OFF_LEAF = NOALLOC_OFF_ARRIVE + (size_t)2 * NOALLOC_MAX_PRIMS * 4;
+constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_LEAF + (size_t)2 * NOALLOC_MAX_PRIMS * 4;  // about 2.4 MiB
+
+// inputs of build_tl_bvh with identity isometries: AABB as given, centroid
+// (min+max)/2 (build.rs:391-400), w = power
+__global__ void k_noalloc_prep(const float *aabbs, const float *power, uint32_t n, float4 *lo, float4 *hi,
+                               float4 *cen) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *a = aabbs + 6 * (size_t)i;
+    float l[3], h[3];
+    for (int k = 0; k < 3; k++) {
+        float x0 = a[k] + 0.0f, x1 = a[3 + k] + 0.0f;  // translation by zero, as k_tl_inputs
+        l[k] = fminf(x0, x1);
+        h[k] = fmaxf(x0, x1);
+    }
+    lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+    hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
+    cen[i] = make_float4((l[0] + h[0]) / 2.0f, (l[1] + h[1]) / 2.0f, (l[2] + h[2]) / 2.0f, power[i]);
+}
+
+}  // namespace
+}  // namespace vrg
+
+// The scratch array every call of vrg_build_tl_bvh_noalloc shares.  Each GPU
+// that loads the library holds it until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[vrg::NOALLOC_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_dev_ptr[256] = {};  // device address of the array, per device ordinal
+}  // namespace
+
+extern "C" VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const float *power, const uint32_t *ids,
+                                                       uint32_t n, vrg_bvh_node *nodes, uint32_t *prim_order,
+                                                       void *stream) {
+    using namespace vrg;
+    if (!aabbs || !power || !ids || !nodes || !prim_order || n == 0) {
+        set_error("vrg_build_tl_bvh_noalloc: null pointer or n == 0");
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    if (n > NOALLOC_MAX_PRIMS) {
+        set_error("vrg_build_tl_bvh_noalloc: %u prims exceed the fixed scratch capacity of %u prims", n,
+                  NOALLOC_MAX_PRIMS);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0;
+    VRG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return VRG_ERR_UNSUPPORTED;
+    // set-up, once per device with that device current: the device address of
+    // the array (its name in host code is only a host-side stand-in)
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_dev_ptr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
+                return VRG_ERR_CUDA;
+            }
+            g_noalloc_dev_ptr[dev] = p;
+        }
+        base = g_noalloc_dev_ptr[dev];
+    }
+    uint8_t *B = (uint8_t *)base;
+    float4 *lo = (float4 *)(B + NOALLOC_OFF_LO), *hi = (float4 *)(B + NOALLOC_OFF_HI),
+           *cen = (float4 *)(B + NOALLOC_OFF_CEN);
+    Item *q0 = (Item *)(B + NOALLOC_OFF_Q0), *q1 = (Item *)(B + NOALLOC_OFF_Q1);
+    uint32_t *cnt = (uint32_t *)(B + NOALLOC_OFF_CNT);
+    SahTree *d_tree = (SahTree *)(B + NOALLOC_OFF_TREE);
+    uint32_t *arrive = (uint32_t *)(B + NOALLOC_OFF_ARRIVE);
+    uint32_t *leaf = (uint32_t *)(B + NOALLOC_OFF_LEAF);
+    const uint32_t n_nodes = 2 * n - 1;
+    // the array keeps the previous call's contents: reset what must start at zero
+    VRG_CUDA_TRY(cudaMemsetAsync(arrive, 0, (size_t)n_nodes * 4, s));
+    VRG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 256, s));
+    // tree descriptor and root work item: copies of host stack values
+    SahTree tree{n, 0, 0, 0};
+    Item root{0, 0, 1, 0, n, INVALID};
+    uint32_t one = 1;
+    VRG_CUDA_TRY(cudaMemcpyAsync(d_tree, &tree, sizeof(tree), cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(q0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(cnt, &one, 4, cudaMemcpyHostToDevice, s));
+    k_noalloc_prep<<<(n + 255) / 256, 256, 0, s>>>(aabbs, power, n, lo, hi, cen);
+    VRG_CUDA_TRY(cudaGetLastError());
+    SahInputs in{lo, hi, cen, ids};
+    SahOutputs out{nodes, prim_order, leaf};
+    k_perm_init<<<dim3(std::max(1u, (n + 255) / 256), 1), 256, 0, s>>>(d_tree, prim_order);
+    VRG_CUDA_TRY(cudaGetLastError());
+    uint32_t n_cur = 1, cur_slot = 0, lv = 0;
+    Item *cur = q0, *nxt = q1;
+    while (n_cur > 0) {
+        uint32_t next_slot = cur_slot ^ 1u;
+        VRG_CUDA_TRY(cudaMemsetAsync(cnt + next_slot, 0, 4, s));
+        uint32_t blocks = std::min<uint32_t>((n_cur + SAH_WARPS - 1) / SAH_WARPS, 152u * 16u);
+        k_sah_level<<<blocks, SAH_WARPS * 32, 0, s>>>(d_tree, in, out, cur, cnt + cur_slot, nxt, cnt + next_slot);
+        VRG_CUDA_TRY(cudaGetLastError());
+        uint32_t h_next = 0;
+        VRG_CUDA_TRY(cudaMemcpyAsync(&h_next, cnt + next_slot, 4, cudaMemcpyDeviceToHost, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        n_cur = h_next;
+        std::swap(cur, nxt);
+        cur_slot = next_slot;
+        if (++lv > 4 * NOALLOC_MAX_PRIMS) {
+            set_error("vrg_build_tl_bvh_noalloc: level loop did not terminate");
+            return VRG_ERR_STATE;
+        }
+    }
+    k_power_up<<<dim3(std::max(1u, (n_nodes + 255) / 256), 1), 256, 0, s>>>(d_tree, nodes, arrive);
+    VRG_CUDA_TRY(cudaGetLastError());
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
