@@ -93,3 +93,26 @@ def test_debug_views(gpu_ctx, orc):
             assert np.array_equal(img.reshape(-1), oimg.reshape(-1)), view
     finally:
         OW.close()
+
+
+def test_golden_tiny_frame_gpu(gpu_ctx):
+    """The CUDA path reproduces the committed golden frame (2 frames, ReSTIR)."""
+    import ctypes as C
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "frame_tiny.npz"))
+    mats, n = vrg.terrain_materials(77)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, g["blocks"])
+    lt, gt = scene.get_tlas()
+    assert lt.tobytes() == g["light_tl"].tobytes() and gt.tobytes() == g["geo_tl"].tobytes()
+    r = vrg.Renderer(gpu_ctx, 48, 32, 3)
+    for f in range(2):
+        v = g[f"f{f}_camera"]
+        cam = vrg.Camera((C.c_float * 3)(*v[0:3]), (C.c_float * 3)(*v[3:6]), (C.c_float * 3)(*v[6:9]),
+                         (C.c_float * 3)(*v[9:12]), 48, 32)
+        p = vrg.RenderParams(1, 1, 4, 3, vrg.MODE_PARITY, 0, 100 + f, 200 + f, 15.0, 0, 3, 0, vrg.RENDER_CAPTURE)
+        img, _ = r.render_params(scene, cam, p)
+        assert np.array_equal(img, g[f"f{f}_image"])
+        assert np.array_equal(r.readback(vrg.DBG_HIT, 3), g[f"f{f}_hit"])
+        for what, key in ((vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_FINAL, "final")):
+            assert r.readback(what, 3).tobytes() == g[f"f{f}_{key}"].tobytes(), (f, key)
