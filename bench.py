@@ -257,15 +257,14 @@ def run_ours(args, d):
     img = np.empty(W * H * 4, np.uint8)
     out_host = vrg.FrameOutput(img.ctypes.data, None, 1, 0)
     # pin the host image buffer for the device->host copy
-    cudart_pinned = False
     d.barrier()
     t0 = time.perf_counter()
     e2e_rays = 0
-    for s in range(args.steps):
+    for s in range(0 if args.no_e2e else args.steps):
         render(args.warmup + args.steps + s, out_host, stats)
         e2e_rays += stats.rays_closest + stats.rays_any
     e2e_s = d.max(time.perf_counter() - t0)
-    e2e_value = d.sum(e2e_rays) / e2e_s / 1e6
+    e2e_value = d.sum(e2e_rays) / e2e_s / 1e6 if e2e_rays else None
     if d.rank != 0:
         d.close()
         return
@@ -300,7 +299,7 @@ def run_ours(args, d):
                      "note": "traversal is L2-latency bound; stream kernels reported in stream_roofline"},
         "stream_roofline": {"kernels": "k_resolve+k_spatial", "achieved": round(stream_gbs, 2), "peak": hbm_peak,
                             "unit": "GB/s", "frac": round(stream_gbs / hbm_peak, 4), "bytes_per_px": 252},
-        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),
+        "e2e": {"value": None if e2e_value is None else round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),
                 "d2h_bytes_per_step": W * H * 4},
         "gpu_launches": (NB + 2) * args.steps,
         "clocks": clocks,
@@ -319,8 +318,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-rows", type=int, default=96, help="image rows the CPU baseline traces per frame")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")
     args = ap.parse_args()
+    global W, H
+    if args.resolution:
+        W, H = (int(x) for x in args.resolution.lower().split("x"))
     if args.warmup < 3:
         args.warmup = 3
     import vrg

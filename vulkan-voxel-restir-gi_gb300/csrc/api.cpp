@@ -357,6 +357,8 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     size_t o_q0 = o; o += al(P * 4);
     size_t o_q1 = o; o += al(P * 4);
     size_t o_cnt = o; o += al(CNT_WORDS * 4);
+    size_t o_aq = o; o += al(P * 4);
+    size_t o_hit = o; o += al(P * 16);
     size_t o_nl = o; o += al(P);
     size_t o_rec = o; o += al(P * 32 * nb);
     size_t o_xv = o; o += al(P * 16);
@@ -377,6 +379,8 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->queue[0] = (uint32_t *)(B + o_q0);
     r->queue[1] = (uint32_t *)(B + o_q1);
     r->counters = (uint32_t *)(B + o_cnt);
+    r->aqueue = (uint32_t *)(B + o_aq);
+    r->hits = (int4 *)(B + o_hit);
     r->nlive = B + o_nl;
     r->rec = (float4 *)(B + o_rec);
     r->xv = (float4 *)(B + o_xv);
@@ -547,6 +551,8 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.ray_d = r->ray_d;
     a.queue[0] = r->queue[0];
     a.queue[1] = r->queue[1];
+    a.aqueue = r->aqueue;
+    a.hits = r->hits;
     a.counters = r->counters;
     a.nlive = r->nlive;
     a.rec = r->rec;

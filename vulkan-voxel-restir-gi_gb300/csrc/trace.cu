@@ -54,81 +54,6 @@ __device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy,
     return tn <= tf;
 }
 
-struct Hit {
-    bool hit;
-    float t, b1, b2;
-    int face, half;
-    int4 rec;
-    uint32_t tri;
-};
-
-// Closest hit over the voxel faces; result independent of traversal order
-// (ties on t go to the smaller (instance, triangle) key, boxes are culled
-// only when strictly beyond the current best t).
-__device__ Hit closest_hit(const DevScene &sc, f3 o, f3 d, float tmin, float tmax, uint32_t *err) {
-    Hit h;
-    h.hit = false;
-    h.t = tmax;
-    uint64_t best_key = ~0ull;
-    int node = sc.geo_root;
-    if (node == EMPTY_ROOT) return h;
-    const f3 inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-    int stack[TRAV_STACK];
-    int sp = 0;
-    for (uint32_t guard = 0;; guard++) {
-        if (guard > TRAV_GUARD) {  // only reachable with a malformed layout
-            atomicOr(err, ERR_GUARD);
-            break;
-        }
-        if (node >= 0) {
-            const float4 *w = sc.geo_wide + 4 * (size_t)node;
-            float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
-            float tn0, tn1;
-            bool h0 = slab(A.x, A.y, A.z, A.w, B.x, B.y, o, inv, tmin, h.t, tn0);
-            bool h1 = slab(B.z, B.w, C.x, C.y, C.z, C.w, o, inv, tmin, h.t, tn1);
-            int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
-            if (h0 && h1) {
-                int nearr = r0, farr = r1;
-                if (tn1 < tn0) { nearr = r1; farr = r0; }
-                if (sp < TRAV_STACK) stack[sp++] = farr;
-                else atomicOr(err, ERR_STACK);
-                node = nearr;
-                continue;
-            }
-            if (h0) { node = r0; continue; }
-            if (h1) { node = r1; continue; }
-        } else {
-            const int4 r = __ldg(sc.geo_rec + (~node));
-            const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
-            const uint32_t mask = ((uint32_t)r.z >> 15) & 63u;
-            const uint64_t ikey = (uint64_t)rec_inst(r) << 32;
-            for (uint32_t m = mask; m; m &= m - 1u) {
-                int f = __ffs(m) - 1;
-                FaceHit fh;
-                if (face_test(wx, wy, wz, f, o, d, inv, tmin, h.t, fh)) {
-                    uint32_t rank = __popc(mask & ((1u << f) - 1u));
-                    uint32_t tri = (uint32_t)r.w + 2u * rank + (uint32_t)fh.half;
-                    uint64_t key = ikey | tri;
-                    if (fh.t < h.t || key < best_key) {
-                        h.hit = true;
-                        h.t = fh.t;
-                        best_key = key;
-                        h.b1 = fh.b1;
-                        h.b2 = fh.b2;
-                        h.face = f;
-                        h.half = fh.half;
-                        h.rec = r;
-                        h.tri = tri;
-                    }
-                }
-            }
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
-    }
-    return h;
-}
-
 // nodeImportance (raytrace.rs:181-208: uint visibility, EPS 1e-3;
 // nee_pdf.rs:125-152: float visibility, EPS 1e-4); translation transforms
 template <bool NEE>
@@ -268,64 +193,8 @@ __device__ float nee_pdf_of(const DevScene &sc, f3 point, f3 normal, f3 dir, uin
 }
 
 constexpr int LIGHT_LIST = 32;
-
-// Sum of the light-sampling pdf over every light triangle the ray crosses in
-// [1e-4, 1000] (nee_pdf.rs:302-336), added in ascending (instance, leaf) order.
-__device__ float nee_any_hit(const DevScene &sc, f3 o, f3 d, f3 normal, uint32_t *err) {
-    const float tmin = EPS_NEE, tmax = 1000.0f;
-    int node = sc.light_root;
-    if (node == EMPTY_ROOT) return 0.0f;
-    const f3 inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-    uint64_t keys[LIGHT_LIST];
-    float vals[LIGHT_LIST];
-    int n = 0;
-    int stack[TRAV_STACK];
-    int sp = 0;
-    for (uint32_t guard = 0;; guard++) {
-        if (guard > TRAV_GUARD) {
-            atomicOr(err, ERR_GUARD);
-            break;
-        }
-        if (node >= 0) {
-            const float4 *w = sc.light_wide + 4 * (size_t)node;
-            float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
-            float tn0, tn1;
-            bool h0 = slab(A.x, A.y, A.z, A.w, B.x, B.y, o, inv, tmin, tmax, tn0);
-            bool h1 = slab(B.z, B.w, C.x, C.y, C.z, C.w, o, inv, tmin, tmax, tn1);
-            int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
-            if (h0 && h1) {
-                if (sp < TRAV_STACK) stack[sp++] = r1;
-                else atomicOr(err, ERR_STACK);
-                node = r0;
-                continue;
-            }
-            if (h0) { node = r0; continue; }
-            if (h1) { node = r1; continue; }
-        } else {
-            const int4 r = __ldg(sc.light_rec + (~node));
-            int f = r.z & 7, hh = (r.z >> 3) & 1;
-            FaceHit fh;
-            if (face_test(rec_wx(r), rec_wy(r), rec_wz(r), f, o, d, inv, tmin, tmax, fh) && fh.half == hh) {
-                uint32_t ii = rec_inst(r), leaf = (uint32_t)r.w;
-                float v = nee_pdf_of(sc, o, normal, d, ii, leaf, fh.b1, fh.b2);
-                uint64_t key = ((uint64_t)ii << 32) | leaf;
-                if (n < LIGHT_LIST) {
-                    int j = n++;
-                    while (j > 0 && keys[j - 1] > key) { keys[j] = keys[j - 1]; vals[j] = vals[j - 1]; j--; }
-                    keys[j] = key;
-                    vals[j] = v;
-                } else {
-                    atomicOr(err, ERR_LIGHT_LIST);
-                }
-            }
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
-    }
-    float pdf = 0.0f;
-    for (int j = 0; j < n; j++) pdf += vals[j];
-    return pdf;
-}
+constexpr int REFILL_MIN = 8;  // refill a warp once this many lanes are idle
+constexpr uint32_t FULL = 0xffffffffu;
 
 __device__ __forceinline__ void st3(float *a, size_t i, f3 v) {
     a[3 * i] = v.x;
@@ -333,36 +202,176 @@ __device__ __forceinline__ void st3(float *a, size_t i, f3 v) {
     a[3 * i + 2] = v.z;
 }
 
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// raygen (raygen.rs:84-111): pixel corner, jitter multiplied by 0.00
+__device__ __forceinline__ void raygen(const FrameArgs &a, uint32_t p, f3 &o, f3 &d) {
+    uint32_t x = p % a.W, y = p / a.W;
+    float u = 2.0f * (float)x / (float)a.W - 1.0f;
+    float v = 2.0f * (float)y / (float)a.H - 1.0f;
+    float aspect = (float)a.W / (float)a.H;
+    o = a.eye;
+    d = norm3(add3(add3(scl3(lscl3(u, a.right), aspect), lscl3(v, a.up)), a.front));
+}
+
+// Conservative slab test of a traversal box (boxes carry BOX_MARGIN, so the
+// rounding of the FMA form never culls a box that holds a candidate face).
+__device__ __forceinline__ bool slab_fma(float lox, float hix, float loy, float hiy, float loz, float hiz, f3 inv,
+                                         f3 oi, float tmin, float tmax, float &tn) {
+    float t0x = __fmaf_rn(lox, inv.x, oi.x), t1x = __fmaf_rn(hix, inv.x, oi.x);
+    float t0y = __fmaf_rn(loy, inv.y, oi.y), t1y = __fmaf_rn(hiy, inv.y, oi.y);
+    float t0z = __fmaf_rn(loz, inv.z, oi.z), t1z = __fmaf_rn(hiz, inv.z, oi.z);
+    tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+    return tn <= tf;
+}
+
+// ---------------------------------------------------------------------------
+// k_trace: closest hit over the voxel faces (replaces getIntersectionInfo,
+// raytrace.rs:354-388).  Persistent warps; each lane owns one ray and, when
+// its traversal ends, takes a new ray from the bounce queue (warp-aggregated
+// fetch once REFILL_MIN lanes are idle), so a warp does not wait for its
+// longest ray.  The result is independent of traversal order: ties on t go
+// to the smaller (instance, triangle) key and boxes are culled only when
+// strictly beyond the current best t.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_in = (b == 0) ? a.P : a.counters[CNT_QUEUE + b];
+    const uint32_t *qin = a.queue[(b + 1) & 1];
+    uint32_t *err = a.counters + CNT_ERROR;
+    const float4 *wide = a.sc.geo_wide;
+    const int4 *recs = a.sc.geo_rec;
+    const int root = a.sc.geo_root;
+    bool has = false, exhausted = false;
+    uint32_t p = 0, steps = 0, traced = 0;
+    f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0};
+    float best_t = 0.0f, hb1 = 0.0f, hb2 = 0.0f;
+    uint64_t best_key = 0;
+    int node = 0, sp = 0, hrec = -1;
+    uint32_t hfh = 0;
+    int stack[TRAV_STACK];
+    while (true) {
+        const uint32_t need = __ballot_sync(FULL, !has);
+        if (!exhausted && need && (__popc(need) >= REFILL_MIN || need == FULL)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&a.counters[CNT_FETCH + b], (uint32_t)__popc(need));
+            base = __shfl_sync(FULL, base, 0);
+            if (base + (uint32_t)__popc(need) >= n_in) exhausted = true;
+            if (!has) {
+                const uint32_t idx = base + (uint32_t)__popc(need & lanemask_lt());
+                if (idx < n_in) {
+                    has = true;
+                    traced++;
+                    p = (b == 0) ? idx : qin[idx];
+                    if (b == 0) raygen(a, p, o, d);
+                    else { o = ld3(a.ray_o[p]); d = ld3(a.ray_d[p]); }
+                    inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                    oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+                    best_t = 1000.0f;
+                    best_key = ~0ull;
+                    node = root;
+                    sp = 0;
+                    hrec = -1;
+                    steps = 0;
+                }
+            }
+        }
+        if (!__any_sync(FULL, has)) break;
+        if (has) {
+            bool done = (node == EMPTY_ROOT);
+            // descend through inner nodes to the next leaf
+            while (!done && node >= 0) {
+                const float4 *w = wide + 4 * (size_t)node;
+                const float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+                float tn0, tn1;
+                const bool h0 = slab_fma(A.x, A.y, A.z, A.w, B.x, B.y, inv, oi, EPS_TRACE, best_t, tn0);
+                const bool h1 = slab_fma(B.z, B.w, C.x, C.y, C.z, C.w, inv, oi, EPS_TRACE, best_t, tn1);
+                const int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
+                if (h0 && h1) {
+                    const bool swap = tn1 < tn0;
+                    if (sp < TRAV_STACK) stack[sp++] = swap ? r0 : r1;
+                    else atomicOr(err, ERR_STACK);
+                    node = swap ? r1 : r0;
+                } else if (h0) {
+                    node = r0;
+                } else if (h1) {
+                    node = r1;
+                } else if (sp == 0) {
+                    done = true;
+                } else {
+                    node = stack[--sp];
+                }
+                if (++steps > TRAV_GUARD) {  // only reachable with a malformed layout
+                    atomicOr(err, ERR_GUARD);
+                    done = true;
+                }
+            }
+            if (!done) {  // leaf: the exposed faces of one surface block
+                const int4 r = __ldg(recs + (~node));
+                const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
+                const uint32_t mask = ((uint32_t)r.z >> 15) & 63u;
+                const uint64_t ikey = (uint64_t)rec_inst(r) << 32;
+                for (uint32_t m = mask; m; m &= m - 1u) {
+                    const int f = __ffs(m) - 1;
+                    FaceHit fh;
+                    if (face_test(wx, wy, wz, f, o, d, inv, EPS_TRACE, best_t, fh)) {
+                        const uint32_t rank = __popc(mask & ((1u << f) - 1u));
+                        const uint64_t key = ikey | ((uint32_t)r.w + 2u * rank + (uint32_t)fh.half);
+                        if (fh.t < best_t || key < best_key) {
+                            best_t = fh.t;
+                            best_key = key;
+                            hrec = ~node;
+                            hfh = (uint32_t)f | ((uint32_t)fh.half << 3);
+                            hb1 = fh.b1;
+                            hb2 = fh.b2;
+                        }
+                    }
+                }
+                if (sp == 0) done = true;
+                else node = stack[--sp];
+            }
+            if (done) {
+                a.hits[p] = make_int4(hrec, (int)hfh, __float_as_int(hb1), __float_as_int(hb2));
+                has = false;
+            }
+        }
+    }
+    for (int off = 16; off; off >>= 1) traced += __shfl_xor_sync(FULL, traced, off);
+    if (lane == 0 && traced)
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_RAYS), (unsigned long long)traced);
+}
+
+// ---------------------------------------------------------------------------
+// k_shade: shading of the hit, light-BVH descent and direction sampling
+// (raytrace.rs:405-577).  Rays whose light pdf is needed are queued for
+// k_anyhit; the others get their (E, w) (R, q) record here.
+// ---------------------------------------------------------------------------
 template <bool CAPTURE>
-__global__ void __launch_bounds__(128) k_bounce(FrameArgs a, uint32_t b) {
+__global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
     const uint32_t n_in = (b == 0) ? P : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *qout = a.queue[b & 1];
-    uint32_t *err = a.counters + CNT_ERROR;
     const uint32_t inv_seed = a.frame * nb + b;  // interactive_rendering.rs:1189
     const float inv2pi = 1.0f / (2.0f * PI_F);
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&a.counters[CNT_FETCH + b], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n_in) break;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (uint32_t base = wid * 32; base < n_in; base += warps * 32) {
         const uint32_t i = base + lane;
         const bool active = i < n_in;
-        bool cont = false, traced_any = false;
+        bool cont = false, anyj = false;
         uint32_t p = 0;
         if (active) {
             p = (b == 0) ? i : qin[i];
             f3 o, d;
             if (b == 0) {
-                // raygen (raygen.rs:84-111): pixel corner, jitter x0.00
-                uint32_t x = p % a.W, y = p / a.W;
-                float u = 2.0f * (float)x / (float)a.W - 1.0f;
-                float v = 2.0f * (float)y / (float)a.H - 1.0f;
-                float aspect = (float)a.W / (float)a.H;
-                o = a.eye;
-                d = norm3(add3(add3(scl3(lscl3(u, a.right), aspect), lscl3(v, a.up)), a.front));
+                raygen(a, p, o, d);
                 if (CAPTURE) {
                     st3(a.c_origin, p, o);
                     st3(a.c_dir, p, d);
@@ -372,28 +381,33 @@ __global__ void __launch_bounds__(128) k_bounce(FrameArgs a, uint32_t b) {
                 d = ld3(a.ray_d[p]);
             }
             const uint32_t seed = mm_combine(inv_seed, p);
-            Hit hit = closest_hit(a.sc, o, d, EPS_TRACE, 1000.0f, err);
+            const int4 hv = a.hits[p];
             f3 new_o, new_d, n, E, R;
-            float mis = 0.0f, pdf = 1.0f, nee = 0.0f;
-            if (!hit.hit) {
+            float mis = 0.0f, pdf = 1.0f;
+            int face = 0, half = 0;
+            int4 rc = make_int4(0, 0, 0, 0);
+            if (hv.x < 0) {
                 new_o = add3(o, scl3(d, 5000.0f));
                 new_d = f3{0.0f, 0.0f, 0.0f};
                 n = f3{0.0f, 0.0f, 0.0f};
-                float sky = (dot3(d, f3{0.0f, 1.0f, 0.0f}) > 0.9f) ? 50.0f : 0.0f;
+                const float sky = (dot3(d, f3{0.0f, 1.0f, 0.0f}) > 0.9f) ? 50.0f : 0.0f;
                 E = f3{sky, sky, sky};
                 R = f3{0.0f, 0.0f, 0.0f};
             } else {
-                const int f = hit.face, hh = hit.half;
-                const int wx = rec_wx(hit.rec), wy = rec_wy(hit.rec), wz = rec_wz(hit.rec);
-                f3 t0 = corner_pos(wx, wy, wz, face_corner(f, hh, 0));
-                f3 t1 = corner_pos(wx, wy, wz, face_corner(f, hh, 1));
-                f3 t2 = corner_pos(wx, wy, wz, face_corner(f, hh, 2));
-                const Frame fr = c_frames[2 * f + hh];
+                rc = __ldg(a.sc.geo_rec + hv.x);
+                face = hv.y & 7;
+                half = (hv.y >> 3) & 1;
+                const float b1 = __int_as_float(hv.z), b2 = __int_as_float(hv.w);
+                const int wx = rec_wx(rc), wy = rec_wy(rc), wz = rec_wz(rc);
+                const f3 t0 = corner_pos(wx, wy, wz, face_corner(face, half, 0));
+                const f3 t1 = corner_pos(wx, wy, wz, face_corner(face, half, 1));
+                const f3 t2 = corner_pos(wx, wy, wz, face_corner(face, half, 2));
+                const Frame fr = c_frames[2 * face + half];
                 n = fr.n;
-                const uint32_t blk_id = ((uint32_t)hit.rec.z >> 21) & 0xFFu;
-                const vrg_material &m = a.sc.mats[6u * blk_id + (uint32_t)f];
-                float b0 = (1.0f - hit.b1) - hit.b2;
-                new_o = add3(add3(scl3(t0, b0), scl3(t1, hit.b1)), scl3(t2, hit.b2));
+                const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
+                const vrg_material &m = a.sc.mats[6u * blk_id + (uint32_t)face];
+                const float b0 = (1.0f - b1) - b2;
+                new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
                 R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
                 const float alpha = __ldg(&m.alpha), metal = __ldg(&m.metallic);
                 const float ndd = -dot3(d, n);
@@ -421,29 +435,31 @@ __global__ void __launch_bounds__(128) k_bounce(FrameArgs a, uint32_t b) {
                         f3 lt[3];
                         light_tri_world(a.sc, res.inst, res.leaf, lt);
                         if (ux + uy > 1.0f) { ux = 1.0f - ux; uy = 1.0f - uy; }  // triangleSample
-                        float bx = (1.0f - ux) - uy;
-                        f3 sp = add3(add3(lscl3(bx, lt[0]), lscl3(ux, lt[1])), lscl3(uy, lt[2]));
+                        const float bx = (1.0f - ux) - uy;
+                        const f3 sp = add3(add3(lscl3(bx, lt[0]), lscl3(ux, lt[1])), lscl3(uy, lt[2]));
                         new_d = norm3(sub3(sp, new_o));
                     } else {
                         float s, c;
                         sincos_turns(ux, &s, &c);
-                        float vv = sqrtf(fmaxf(0.0f, 1.0f - uy * uy));
-                        f3 hs = f3{vv * c, uy, vv * s};
+                        const float vv = sqrtf(fmaxf(0.0f, 1.0f - uy * uy));
+                        const f3 hs = f3{vv * c, uy, vv * s};
                         new_d = norm3(add3(add3(lscl3(hs.x, fr.t), lscl3(hs.y, fr.n)), lscl3(hs.z, fr.b)));
                     }
                     pdf = dot3(new_d, n) / PI_F;
                 }
-                // light pdf of the chosen direction (nee_pdf pass; bounce nb-1 is never computed)
-                if (b + 1 < nb && mis != 0.0f && len3(new_d) != 0.0f) {
-                    nee = nee_any_hit(a.sc, new_o, new_d, n, err);
-                    traced_any = true;
-                }
+                // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
+                anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
             }
-            const float q = nee * mis + (1.0f - mis) * inv2pi;
-            const float w = pdf / q;
             const size_t rb = (size_t)b * 2 * P;
-            a.rec[rb + p] = make_float4(E.x, E.y, E.z, w);
-            a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, q);
+            if (anyj) {
+                a.rec[rb + p] = make_float4(E.x, E.y, E.z, 0.0f);
+                a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, 0.0f);
+            } else {
+                const float q = 0.0f * mis + (1.0f - mis) * inv2pi;
+                const float w = pdf / q;
+                a.rec[rb + p] = make_float4(E.x, E.y, E.z, w);
+                a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, q);
+            }
             if (b == 0) {
                 a.xv[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
                 a.nv[p] = make_float4(n.x, n.y, n.z, 0.0f);
@@ -453,8 +469,9 @@ __global__ void __launch_bounds__(128) k_bounce(FrameArgs a, uint32_t b) {
             }
             cont = !zero3(new_d) && (b + 1 < nb);
             if (cont) {
-                a.ray_o[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
-                a.ray_d[p] = make_float4(new_d.x, new_d.y, new_d.z, 0.0f);
+                // .w of the ray carries the face and the bsdf pdf to k_anyhit
+                a.ray_o[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+                a.ray_d[p] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
             } else {
                 a.nlive[p] = (uint8_t)(b + 1);
             }
@@ -467,31 +484,151 @@ __global__ void __launch_bounds__(128) k_bounce(FrameArgs a, uint32_t b) {
                 st3(a.c_refl, s0, R);
                 a.c_mis[s0] = mis;
                 a.c_pdf[s0] = pdf;
-                a.c_nee[s0] = nee;
-                uint4 hv;
-                if (hit.hit) {
-                    hv.x = rec_inst(hit.rec);
-                    hv.y = hit.tri;
-                    hv.z = (uint32_t)hit.rec.z & 0x7FFFu;
-                    hv.w = (uint32_t)hit.face | ((uint32_t)hit.half << 8);
+                a.c_nee[s0] = 0.0f;
+                uint4 hw;
+                if (hv.x >= 0) {
+                    const uint32_t mask = ((uint32_t)rc.z >> 15) & 63u;
+                    hw.x = rec_inst(rc);
+                    hw.y = (uint32_t)rc.w + 2u * __popc(mask & ((1u << face) - 1u)) + (uint32_t)half;
+                    hw.z = (uint32_t)rc.z & 0x7FFFu;
+                    hw.w = (uint32_t)face | ((uint32_t)half << 8);
                 } else {
-                    hv = make_uint4(INVALID, INVALID, INVALID, INVALID);
+                    hw = make_uint4(INVALID, INVALID, INVALID, INVALID);
                 }
-                reinterpret_cast<uint4 *>(a.c_hit)[s0] = hv;
+                reinterpret_cast<uint4 *>(a.c_hit)[s0] = hw;
             }
         }
-        // compaction of continuing rays into the next queue
-        const uint32_t cm = __ballot_sync(0xffffffffu, cont);
-        const uint32_t am = __ballot_sync(0xffffffffu, active);
-        const uint32_t hm = __ballot_sync(0xffffffffu, traced_any);
-        uint32_t qbase = 0;
+        // compaction: continuing rays into the next bounce queue, light-pdf jobs
+        // into the any-hit queue (one ballot + one atomic per warp each)
+        const uint32_t cm = __ballot_sync(FULL, cont);
+        const uint32_t am = __ballot_sync(FULL, anyj);
+        uint32_t qb = 0, ab = 0;
         if (lane == 0) {
-            if (cm) qbase = atomicAdd(&a.counters[CNT_QUEUE + b + 1], (uint32_t)__popc(cm));
-            atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_RAYS), (unsigned long long)__popc(am));
-            if (hm) atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANY), (unsigned long long)__popc(hm));
+            if (cm) qb = atomicAdd(&a.counters[CNT_QUEUE + b + 1], (uint32_t)__popc(cm));
+            if (am) ab = atomicAdd(&a.counters[CNT_AQUEUE + b], (uint32_t)__popc(am));
         }
-        qbase = __shfl_sync(0xffffffffu, qbase, 0);
-        if (cont) qout[qbase + __popc(cm & ((1u << lane) - 1u))] = p;
+        qb = __shfl_sync(FULL, qb, 0);
+        ab = __shfl_sync(FULL, ab, 0);
+        if (cont) qout[qb + __popc(cm & lanemask_lt())] = p;
+        if (anyj) a.aqueue[ab + __popc(am & lanemask_lt())] = p;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_anyhit: the nee_pdf pass (nee_pdf.rs:281-337) for the queued rays: every
+// light triangle the ray crosses in [1e-4, 1000] adds its light-sampling pdf
+// (computeNeePdf, nee_pdf.rs:240-279), summed in ascending (instance, leaf)
+// order; then q and w = bsdf_pdf / q complete the bounce record.  Persistent
+// warps with per-lane job replacement, as k_trace.
+// ---------------------------------------------------------------------------
+template <bool CAPTURE>
+__global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t P = a.P;
+    const uint32_t n_in = a.counters[CNT_AQUEUE + b];
+    uint32_t *err = a.counters + CNT_ERROR;
+    const float4 *wide = a.sc.light_wide;
+    const int4 *recs = a.sc.light_rec;
+    const int root = a.sc.light_root;
+    const float inv2pi = 1.0f / (2.0f * PI_F);
+    const float tmin = EPS_NEE, tmax = 1000.0f;
+    bool has = false, exhausted = false;
+    uint32_t p = 0, steps = 0;
+    f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0}, n = f3{0, 0, 0};
+    float pdf = 0.0f;
+    int node = 0, sp = 0, nh = 0;
+    int stack[TRAV_STACK];
+    uint64_t keys[LIGHT_LIST];
+    float vals[LIGHT_LIST];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n_in)
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANY), (unsigned long long)n_in);
+    while (true) {
+        const uint32_t need = __ballot_sync(FULL, !has);
+        if (!exhausted && need && (__popc(need) >= REFILL_MIN || need == FULL)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&a.counters[CNT_AFETCH + b], (uint32_t)__popc(need));
+            base = __shfl_sync(FULL, base, 0);
+            if (base + (uint32_t)__popc(need) >= n_in) exhausted = true;
+            if (!has) {
+                const uint32_t idx = base + (uint32_t)__popc(need & lanemask_lt());
+                if (idx < n_in) {
+                    has = true;
+                    p = a.aqueue[idx];
+                    const float4 ro = a.ray_o[p], rd = a.ray_d[p];
+                    o = ld3(ro);
+                    d = ld3(rd);
+                    pdf = rd.w;
+                    n = c_frames[2 * __float_as_int(ro.w)].n;
+                    inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                    oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+                    node = root;
+                    sp = 0;
+                    nh = 0;
+                    steps = 0;
+                }
+            }
+        }
+        if (!__any_sync(FULL, has)) break;
+        if (has) {
+            bool done = (node == EMPTY_ROOT);
+            while (!done && node >= 0) {
+                const float4 *w = wide + 4 * (size_t)node;
+                const float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+                float tn0, tn1;
+                const bool h0 = slab_fma(A.x, A.y, A.z, A.w, B.x, B.y, inv, oi, tmin, tmax, tn0);
+                const bool h1 = slab_fma(B.z, B.w, C.x, C.y, C.z, C.w, inv, oi, tmin, tmax, tn1);
+                const int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
+                if (h0 && h1) {
+                    if (sp < TRAV_STACK) stack[sp++] = r1;
+                    else atomicOr(err, ERR_STACK);
+                    node = r0;
+                } else if (h0) {
+                    node = r0;
+                } else if (h1) {
+                    node = r1;
+                } else if (sp == 0) {
+                    done = true;
+                } else {
+                    node = stack[--sp];
+                }
+                if (++steps > TRAV_GUARD) {
+                    atomicOr(err, ERR_GUARD);
+                    done = true;
+                }
+            }
+            if (!done) {  // leaf: one light triangle
+                const int4 r = __ldg(recs + (~node));
+                const int f = r.z & 7, hh = (r.z >> 3) & 1;
+                FaceHit fh;
+                if (face_test(rec_wx(r), rec_wy(r), rec_wz(r), f, o, d, inv, tmin, tmax, fh) && fh.half == hh) {
+                    const uint32_t ii = rec_inst(r), leaf = (uint32_t)r.w;
+                    const float v = nee_pdf_of(a.sc, o, n, d, ii, leaf, fh.b1, fh.b2);
+                    const uint64_t key = ((uint64_t)ii << 32) | leaf;
+                    if (nh < LIGHT_LIST) {
+                        int j = nh++;
+                        while (j > 0 && keys[j - 1] > key) { keys[j] = keys[j - 1]; vals[j] = vals[j - 1]; j--; }
+                        keys[j] = key;
+                        vals[j] = v;
+                    } else {
+                        atomicOr(err, ERR_LIGHT_LIST);
+                    }
+                }
+                if (sp == 0) done = true;
+                else node = stack[--sp];
+            }
+            if (done) {
+                float nee = 0.0f;
+                for (int j = 0; j < nh; j++) nee += vals[j];
+                const float mis = 0.3f;
+                const float q = nee * mis + (1.0f - mis) * inv2pi;
+                const float w = pdf / q;
+                const size_t rb = (size_t)b * 2 * P;
+                reinterpret_cast<float *>(a.rec + rb + p)[3] = w;
+                reinterpret_cast<float *>(a.rec + rb + P + p)[3] = q;
+                if (CAPTURE) a.c_nee[(size_t)b * P + p] = nee;
+                has = false;
+            }
+        }
     }
 }
 
@@ -505,17 +642,33 @@ vrg_status upload_frames(cudaStream_t s) {
     return VRG_OK;
 }
 
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int grid) {
-    if (a.capture) k_bounce<true><<<grid, 128, 0, s>>>(a, b);
-    else k_bounce<false><<<grid, 128, 0, s>>>(a, b);
+static int occupancy_grid(const void *fn, int threads) {
+    int dev = 0, sms = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, 0);
+    return std::max(1, sms) * std::max(1, n);
+}
+
+// One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int /*grid*/) {
+    static int g_trace = 0, g_shade = 0, g_any = 0;
+    if (!g_trace) {
+        g_trace = occupancy_grid((const void *)k_trace, 128);
+        g_shade = occupancy_grid((const void *)k_shade<false>, 128);
+        g_any = occupancy_grid((const void *)k_anyhit<false>, 128);
+    }
+    k_trace<<<g_trace, 128, 0, s>>>(a, b);
+    if (a.capture) k_shade<true><<<g_shade, 128, 0, s>>>(a, b);
+    else k_shade<false><<<g_shade, 128, 0, s>>>(a, b);
+    if (b + 1 < a.nb) {
+        if (a.capture) k_anyhit<true><<<g_any, 128, 0, s>>>(a, b);
+        else k_anyhit<false><<<g_any, 128, 0, s>>>(a, b);
+    }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }
 
-int bounce_blocks_per_sm() {
-    int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bounce<false>, 128, 0);
-    return n > 0 ? n : 1;
-}
+int bounce_blocks_per_sm() { return 1; }
 
 }  // namespace vrg

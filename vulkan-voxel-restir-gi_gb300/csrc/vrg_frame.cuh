@@ -7,11 +7,14 @@ namespace vrg {
 
 // counters[] layout (u32 words)
 constexpr int CNT_QUEUE = 0;     // [0..7]  rays queued for bounce b
-constexpr int CNT_FETCH = 8;     // [8..15] work-fetch cursor of bounce b
+constexpr int CNT_FETCH = 8;     // [8..15] closest-hit work-fetch cursor of bounce b
 constexpr int CNT_ERROR = 16;    // error word
 constexpr int CNT_RAYS = 18;     // u64 at words 18-19: closest-hit queries
 constexpr int CNT_ANY = 20;      // u64 at words 20-21: light any-hit queries
-constexpr int CNT_WORDS = 32;
+constexpr int CNT_AQUEUE = 24;   // [24..31] any-hit jobs queued by bounce b
+constexpr int CNT_AFETCH = 32;   // [32..39] any-hit work-fetch cursor of bounce b
+constexpr int CNT_SFETCH = 40;   // [40..47] shading work-fetch cursor of bounce b
+constexpr int CNT_WORDS = 64;
 constexpr int MAX_BOUNCES = 8;
 
 struct FrameArgs {
@@ -25,6 +28,8 @@ struct FrameArgs {
     // wavefront state
     float4 *ray_o, *ray_d;
     uint32_t *queue[2];
+    uint32_t *aqueue;             // any-hit jobs of the current bounce
+    int4 *hits;                   // closest hit per pixel: (~record or -1, face|half<<3, b1, b2)
     uint32_t *counters;
     uint8_t *nlive;
     float4 *rec;                  // [nb][2][P]: (E.xyz, w), (R.xyz, q)

@@ -157,7 +157,9 @@ struct Renderer {
     // device arrays (P = W*H)
     float4 *ray_o = nullptr, *ray_d = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};
-    uint32_t *counters = nullptr;         // [0..7] queue counts, [8] error word, [16..] ray counts (u64)
+    uint32_t *counters = nullptr;         // CNT_* words of vrg_frame.cuh
+    uint32_t *aqueue = nullptr;           // any-hit job queue
+    int4 *hits = nullptr;                 // closest hit per pixel
     uint8_t *nlive = nullptr;
     float4 *rec = nullptr;                // [nb][2][P]
     float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
