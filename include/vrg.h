@@ -54,7 +54,7 @@ enum {
 /* Block faces in gen_mesh emission order (block.rs:9-17, chunk.rs:225-285). */
 enum { VRG_FACE_LEFT = 0, VRG_FACE_RIGHT, VRG_FACE_DOWN, VRG_FACE_UP, VRG_FACE_BACK, VRG_FACE_FRONT };
 
-/* 32-byte BVH node, the reference's wire format (bvh/mod.rs:8-25).
+/* 40-byte BVH node, the reference's wire format (bvh/mod.rs:8-25).
  * left_node_idx == 0xFFFFFFFF marks a leaf; both indices 0xFFFFFFFF marks
  * the dummy node of an empty light BVH. */
 typedef struct vrg_bvh_node {
@@ -124,11 +124,16 @@ typedef struct vrg_render_params {
     uint32_t history_slots;       /* reservoir ring length; reference: 3 (frame % 3) */
     uint32_t accumulate;          /* 1 = add this frame's radiance to the accumulator */
     uint32_t flags;               /* VRG_RENDER_* */
-    uint32_t reserved[3];
+    uint32_t cache_train_bounces; /* extra bounces of the cache's training paths (4) */
+    uint32_t reserved[2];
 } vrg_render_params;
 
 #define VRG_RENDER_CAPTURE 1u      /* keep the full per-bounce SoA for vrg_debug_readback */
 #define VRG_RENDER_NO_PACK 2u      /* skip the u8 pack (radiance output only) */
+#define VRG_RENDER_CACHE 4u        /* terminate paths into the attached radiance cache after the
+                                      first bounce; 1/16 of the paths trace cache_train_bounces
+                                      more bounces and train the cache (no ReSTIR) */
+#define VRG_RENDER_PLAIN_ONLY 8u   /* skip the ReSTIR stages (plain path tracer, view 0) */
 
 /* Where the frame goes.  Pointers may be NULL (not written).  host != 0 means
  * the pointers are host memory and the library copies the frame back before
@@ -277,6 +282,44 @@ VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, co
  * after the build has finished on `stream`. */
 VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const float *power, const uint32_t *ids,
                                             uint32_t n, vrg_bvh_node *nodes, uint32_t *prim_order, void *stream);
+
+/* ---- neural radiance cache (no reference counterpart) ----------------
+ * Multiresolution hash-grid encoding of the position (levels x 2 features,
+ * 2^log2_table entries per level, resolutions base..max geometric) plus
+ * octahedral normal and view direction, 5 hidden ReLU layers of width 64 and
+ * a linear RGB output; BF16 weights/activations on the tensor cores with
+ * FP32 accumulation; relative L2 loss; Adam (beta1 0.9, beta2 0.99). */
+typedef struct vrg_nrc vrg_nrc;
+typedef struct vrg_nrc_desc {
+    uint32_t levels;           /* 16 */
+    uint32_t log2_table;       /* 19 */
+    uint32_t features;         /* 2 */
+    uint32_t base_resolution;  /* 16 */
+    uint32_t max_resolution;   /* 2048 */
+    uint32_t batch;            /* training samples per frame, 65536 */
+    float learning_rate;       /* 1e-2 */
+    uint32_t seed;
+    float scene_min[3];        /* box mapped to the unit cube */
+    float scene_max[3];
+} vrg_nrc_desc;
+enum { VRG_NRC_WEIGHTS = 0, VRG_NRC_WEIGHT_GRADS, VRG_NRC_TABLE, VRG_NRC_TABLE_GRADS, VRG_NRC_ZERO_GRADS };
+VRG_API vrg_status vrg_nrc_create(vrg_context *ctx, const vrg_nrc_desc *desc, vrg_nrc **out);
+VRG_API vrg_status vrg_nrc_destroy(vrg_nrc *nrc);
+/* Host arrays: pos/normal/dir n x 3 floats (dir = the incoming ray direction;
+ * the network sees -dir), rgb n x 3 out. */
+VRG_API vrg_status vrg_nrc_query(vrg_nrc *nrc, uint32_t n, const float *pos, const float *normal, const float *dir,
+                                 float *rgb);
+/* One training batch: gradients accumulate; update != 0 applies an Adam step
+ * (and clears the gradients). *loss = mean relative L2 loss of the batch. */
+VRG_API vrg_status vrg_nrc_train(vrg_nrc *nrc, uint32_t n, const float *pos, const float *normal, const float *dir,
+                                 const float *target, uint32_t update, float *loss);
+/* Parameter / gradient access (fp32): weights = 5 x 64x64 then 16x64
+ * (rows 0..2 used), [out][in]; table = levels x 2^log2_table x 2. */
+VRG_API vrg_status vrg_nrc_read(vrg_nrc *nrc, uint32_t what, void *dst, uint64_t bytes);
+VRG_API vrg_status vrg_nrc_write(vrg_nrc *nrc, uint32_t what, const void *src, uint64_t bytes);
+VRG_API vrg_status vrg_nrc_layout(vrg_nrc *nrc, uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1);
+/* Attaches a cache to a renderer for VRG_RENDER_CACHE frames (NULL detaches). */
+VRG_API vrg_status vrg_renderer_set_cache(vrg_renderer *r, vrg_nrc *nrc);
 
 /* ---- synthetic scenes (no reference counterpart; the reference uses
  *      OpenSimplex worldgen, chunk.rs:56-109) -------------------------- */

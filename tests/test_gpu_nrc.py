@@ -1,0 +1,87 @@
+"""Neural radiance cache: the CUDA forward and gradients against the PyTorch
+CPU oracle (tests/nrc_ref.py), and training convergence."""
+import numpy as np
+import pytest
+
+import vrg
+from nrc_ref import Model, corners
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = (0.0, 0.0, 0.0), (64.0, 32.0, 64.0)
+
+
+def _samples(rng, n):
+    pos = (rng.random((n, 3)) * np.array(HI)).astype(np.float32)
+    face = rng.integers(0, 6, n)
+    nrm = np.zeros((n, 3), np.float32)
+    nrm[np.arange(n), face // 2] = np.where(face % 2, 1.0, -1.0)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    target = (np.abs(np.sin(pos[:, :1] * 0.2)) * np.array([[2.0, 1.0, 0.5]]) + 0.1).astype(np.float32)
+    return pos, nrm, d.astype(np.float32), target
+
+
+def _cache(gpu_ctx, levels=8, log2_t=12, seed=3):
+    return vrg.RadianceCache(gpu_ctx, LO, HI, levels=levels, log2_table=log2_t, base_resolution=4,
+                             max_resolution=128, batch=4096, learning_rate=1e-2, seed=seed)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_forward_matches_oracle(gpu_ctx):
+    rng = np.random.default_rng(1)
+    c = _cache(gpu_ctx)
+    pos, nrm, d, _ = _samples(rng, 777)
+    # non-trivial table values
+    tab = (rng.normal(size=c.levels * (1 << c.log2_table) * 2) * 0.5).astype(np.float32)
+    c.write(vrg.NRC_TABLE, tab)
+    y = c.query(pos, nrm, d)
+    sc, dn, r1 = c.layout()
+    m = Model(c.read(vrg.NRC_WEIGHTS), c.read(vrg.NRC_TABLE), c.levels, c.log2_table)
+    yr = m.forward(corners(pos, LO, HI, sc, dn, r1, c.log2_table), nrm, d).detach().numpy()
+    assert _rel(y, yr) < 2e-2
+    c.close()
+
+
+def test_gradients_match_oracle(gpu_ctx):
+    rng = np.random.default_rng(2)
+    c = _cache(gpu_ctx)
+    tab = (rng.normal(size=c.levels * (1 << c.log2_table) * 2) * 0.5).astype(np.float32)
+    c.write(vrg.NRC_TABLE, tab)
+    pos, nrm, d, target = _samples(rng, 1500)
+    c.write(vrg.NRC_ZERO_GRADS)
+    loss = c.train(pos, nrm, d, target, update=False)
+    gw = c.read(vrg.NRC_WEIGHT_GRADS)
+    gt = c.read(vrg.NRC_TABLE_GRADS)
+    sc, dn, r1 = c.layout()
+    m = Model(c.read(vrg.NRC_WEIGHTS), c.read(vrg.NRC_TABLE), c.levels, c.log2_table)
+    y = m.forward(corners(pos, LO, HI, sc, dn, r1, c.log2_table), nrm, d)
+    L = m.loss(y, target)
+    L.backward()
+    assert abs(loss - float(L)) / float(L) < 2e-2
+    for l in range(5):
+        ref = m.Ws[l].grad.numpy().reshape(-1)
+        got = gw[l * 4096:(l + 1) * 4096]
+        assert _rel(got, ref) < 5e-2, (l, _rel(got, ref))
+    ref5 = m.W5.grad.numpy().reshape(-1)
+    assert _rel(gw[5 * 4096:5 * 4096 + 192], ref5) < 5e-2
+    assert np.all(gw[5 * 4096 + 192:] == 0)
+    reft = m.table.grad.numpy().reshape(-1)
+    assert _rel(gt, reft) < 5e-2
+    c.close()
+
+
+def test_training_converges(gpu_ctx):
+    rng = np.random.default_rng(4)
+    c = _cache(gpu_ctx, levels=12, log2_t=14)
+    pos, nrm, d, target = _samples(rng, 8192)
+    first = c.train(pos, nrm, d, target)
+    for _ in range(200):
+        last = c.train(pos, nrm, d, target)
+    assert last < 0.1 * first, (first, last)
+    y = c.query(pos, nrm, d)
+    assert np.mean(np.abs(y - target) / (np.abs(target) + 0.1)) < 0.2
+    c.close()

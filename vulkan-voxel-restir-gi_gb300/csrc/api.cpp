@@ -720,4 +720,51 @@ VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, co
                           nodes_out, prim_order_out);
 }
 
+// ---- neural radiance cache ------------------------------------------------
+
+static Nrc *NR(vrg_nrc *p) { return reinterpret_cast<Nrc *>(p); }
+
+VRG_API vrg_status vrg_nrc_create(vrg_context *ctx, const vrg_nrc_desc *desc, vrg_nrc **out) {
+    if (!ctx || !desc || !out) return VRG_ERR_INVALID_ARGUMENT;
+    Nrc *n = nullptr;
+    VRG_TRY(nrc_create(ctx, desc, &n));
+    *out = reinterpret_cast<vrg_nrc *>(n);
+    return VRG_OK;
+}
+VRG_API vrg_status vrg_nrc_destroy(vrg_nrc *nrc) {
+    if (!nrc) return VRG_ERR_INVALID_ARGUMENT;
+    nrc_destroy(NR(nrc));
+    return VRG_OK;
+}
+VRG_API vrg_status vrg_nrc_query(vrg_nrc *nrc, uint32_t n, const float *pos, const float *normal, const float *dir,
+                                 float *rgb) {
+    if (!nrc || !pos || !normal || !dir || !rgb) return VRG_ERR_INVALID_ARGUMENT;
+    if (n == 0) return VRG_OK;
+    return nrc_query_host(NR(nrc), n, pos, normal, dir, rgb);
+}
+VRG_API vrg_status vrg_nrc_train(vrg_nrc *nrc, uint32_t n, const float *pos, const float *normal, const float *dir,
+                                 const float *target, uint32_t update, float *loss) {
+    if (!nrc || !pos || !normal || !dir || !target) return VRG_ERR_INVALID_ARGUMENT;
+    if (n == 0) return VRG_OK;
+    return nrc_train_host(NR(nrc), n, pos, normal, dir, target, update, loss);
+}
+VRG_API vrg_status vrg_nrc_read(vrg_nrc *nrc, uint32_t what, void *dst, uint64_t bytes) {
+    if (!nrc || !dst) return VRG_ERR_INVALID_ARGUMENT;
+    return nrc_read(NR(nrc), what, dst, bytes);
+}
+VRG_API vrg_status vrg_nrc_write(vrg_nrc *nrc, uint32_t what, const void *src, uint64_t bytes) {
+    if (!nrc || (!src && what != VRG_NRC_ZERO_GRADS)) return VRG_ERR_INVALID_ARGUMENT;
+    return nrc_write(NR(nrc), what, src, bytes);
+}
+VRG_API vrg_status vrg_nrc_layout(vrg_nrc *nrc, uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1) {
+    if (!nrc || !levels || !scales || !dense || !res1) return VRG_ERR_INVALID_ARGUMENT;
+    nrc_layout(levels, scales, dense, res1, NR(nrc));
+    return VRG_OK;
+}
+VRG_API vrg_status vrg_renderer_set_cache(vrg_renderer *r, vrg_nrc *nrc) {
+    if (!r) return VRG_ERR_INVALID_ARGUMENT;
+    r->cache = NR(nrc);
+    return VRG_OK;
+}
+
 }  // extern "C"

@@ -1,0 +1,893 @@
+// Neural radiance cache (no reference counterpart): a multiresolution hash
+// grid encoding (Müller et al. 2022, "Instant Neural Graphics Primitives")
+// of the query position plus octahedral normal and view direction, followed
+// by a 5 x 64 ReLU MLP with a linear RGB output, trained online on radiance
+// the path tracer produces (Müller et al. 2021, "Real-time Neural Radiance
+// Caching") with a relative L2 loss and Adam.
+//
+// GB300 mapping: BF16 weights and activations on the tensor cores
+// (mma m16n8k16, FP32 accumulate) in fully fused per-warp tiles: a warp
+// encodes 32 queries into shared memory, then runs the whole MLP with the
+// activations in registers (the f32 C fragment of layer l is repacked as the
+// bf16 A fragment of layer l+1 without shuffles) and the weights resident in
+// shared memory (row stride padded to 72 bf16: conflict-free fragment loads).
+// Training fuses encode, forward, loss, backward through the layers and the
+// hash-grid gradient scatter; weight gradients are a split-K tensor-core
+// reduction over the batch; Adam runs over FP32 master copies and refreshes
+// the BF16 / FP16 working copies.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "vrg_internal.h"
+
+namespace vrg {
+
+constexpr int NRC_W = 64;            // hidden width
+constexpr int NRC_LAYERS = 6;        // 5 hidden (64) + output (16 padded, 3 used)
+constexpr int NRC_OUT = 16;
+constexpr int NRC_STRIDE = 72;       // padded bf16 row stride of weights and tiles
+constexpr int NRC_TSTRIDE5 = 24;     // padded row stride of the transposed output layer
+constexpr int NRC_MAX_LEVELS = 16;
+
+struct NrcParams {
+    int levels, log2_t, base_res, features;
+    float scale[NRC_MAX_LEVELS];      // per-level resolution
+    uint32_t dense[NRC_MAX_LEVELS];   // 1 = dense indexing
+    uint32_t res1[NRC_MAX_LEVELS];    // resolution + 1 (dense stride)
+    float lo[3], inv_ext[3];          // scene box -> [0,1]^3
+};
+
+// weight pack in shared-memory layout (bf16): W_l [out][72], then WT_l [in][72 or 24]
+__host__ __device__ constexpr size_t w_off(int l) { return (size_t)l * NRC_W * NRC_STRIDE; }  // l < 5
+constexpr size_t W5_OFF = 5 * (size_t)NRC_W * NRC_STRIDE;
+constexpr size_t WT_OFF = W5_OFF + (size_t)NRC_OUT * NRC_STRIDE;
+__host__ __device__ constexpr size_t wt_off(int l) { return WT_OFF + (size_t)l * NRC_W * NRC_STRIDE; }
+constexpr size_t WT5_OFF = WT_OFF + 5 * (size_t)NRC_W * NRC_STRIDE;
+constexpr size_t WPACK_ELEMS = WT5_OFF + (size_t)NRC_W * NRC_TSTRIDE5;
+constexpr size_t WFWD_ELEMS = WT_OFF;  // forward needs W only
+// fp32 master weights: layer l has out(l) x 64
+__host__ __device__ constexpr int out_dim(int l) { return l < 5 ? NRC_W : NRC_OUT; }
+__host__ __device__ constexpr size_t m_off(int l) { return (size_t)l * NRC_W * NRC_W; }
+constexpr size_t MASTER_ELEMS = 5 * (size_t)NRC_W * NRC_W + (size_t)NRC_OUT * NRC_W;
+
+namespace {
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+// octahedral map of a unit vector to [0,1]^2
+__device__ __forceinline__ void oct_encode(f3 v, float &u, float &w) {
+    float s = fabsf(v.x) + fabsf(v.y) + fabsf(v.z);
+    float px = v.x / s, py = v.y / s;
+    if (v.z < 0.0f) {
+        float tx = (1.0f - fabsf(py)) * (px >= 0.0f ? 1.0f : -1.0f);
+        float ty = (1.0f - fabsf(px)) * (py >= 0.0f ? 1.0f : -1.0f);
+        px = tx;
+        py = ty;
+    }
+    u = px * 0.5f + 0.5f;
+    w = py * 0.5f + 0.5f;
+}
+
+__device__ __forceinline__ uint32_t grid_index(const NrcParams &P, int l, int x, int y, int z) {
+    const uint32_t mask = (1u << P.log2_t) - 1u;
+    if (P.dense[l]) {
+        const uint32_t r = P.res1[l];
+        return ((uint32_t)x + (uint32_t)y * r + (uint32_t)z * r * r) & mask;
+    }
+    return ((uint32_t)x ^ ((uint32_t)y * 2654435761u) ^ ((uint32_t)z * 805459861u)) & mask;
+}
+
+struct Corner {
+    uint32_t idx[8];
+    float w[8];
+};
+
+__device__ __forceinline__ void level_corners(const NrcParams &P, int l, f3 p, Corner &c) {
+    const float s = P.scale[l];
+    const float gx = p.x * s, gy = p.y * s, gz = p.z * s;
+    const float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    const float tx = gx - fx, ty = gy - fy, tz = gz - fz;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int dx = (k >> 2) & 1, dy = (k >> 1) & 1, dz = k & 1;
+        c.idx[k] = grid_index(P, l, ix + dx, iy + dy, iz + dz);
+        c.w[k] = (dx ? tx : 1.0f - tx) * (dy ? ty : 1.0f - ty) * (dz ? tz : 1.0f - tz);
+    }
+}
+
+__device__ __forceinline__ f3 normalize_pos(const NrcParams &P, f3 x) {
+    f3 p = f3{(x.x - P.lo[0]) * P.inv_ext[0], (x.y - P.lo[1]) * P.inv_ext[1], (x.z - P.lo[2]) * P.inv_ext[2]};
+    p.x = fminf(fmaxf(p.x, 0.0f), 1.0f);
+    p.y = fminf(fmaxf(p.y, 0.0f), 1.0f);
+    p.z = fminf(fmaxf(p.z, 0.0f), 1.0f);
+    return p;
+}
+
+// encodes one query into a bf16 row of 64: 2*levels hash features, oct
+// normal, oct view direction, zeros
+__device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 nrm, f3 dir,
+                           __nv_bfloat16 *row) {
+    const f3 p = normalize_pos(P, pos);
+    const size_t T = (size_t)1 << P.log2_t;
+    for (int l = 0; l < P.levels; l++) {
+        Corner c;
+        level_corners(P, l, p, c);
+        float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float2 v = __half22float2(table[(size_t)l * T + c.idx[k]]);
+            f0 += c.w[k] * v.x;
+            f1 += c.w[k] * v.y;
+        }
+        row[2 * l] = __float2bfloat16_rn(f0);
+        row[2 * l + 1] = __float2bfloat16_rn(f1);
+    }
+    float a, b;
+    oct_encode(nrm, a, b);
+    row[2 * P.levels] = __float2bfloat16_rn(a);
+    row[2 * P.levels + 1] = __float2bfloat16_rn(b);
+    oct_encode(dir, a, b);
+    row[2 * P.levels + 2] = __float2bfloat16_rn(a);
+    row[2 * P.levels + 3] = __float2bfloat16_rn(b);
+    for (int k = 2 * P.levels + 4; k < NRC_W; k++) row[k] = __float2bfloat16_rn(0.0f);
+}
+
+// A fragments of a 16-row tile held row-major in shared memory
+__device__ __forceinline__ void load_a(const __nv_bfloat16 *tile, int g, int q, uint32_t a[4][4]) {
+#pragma unroll
+    for (int kc = 0; kc < 4; kc++) {
+        a[kc][0] = ld32(tile + g * NRC_STRIDE + kc * 16 + 2 * q);
+        a[kc][1] = ld32(tile + (g + 8) * NRC_STRIDE + kc * 16 + 2 * q);
+        a[kc][2] = ld32(tile + g * NRC_STRIDE + kc * 16 + 8 + 2 * q);
+        a[kc][3] = ld32(tile + (g + 8) * NRC_STRIDE + kc * 16 + 8 + 2 * q);
+    }
+}
+
+// one 64 -> 64 layer: C = A * W^T
+__device__ __forceinline__ void layer64(const __nv_bfloat16 *W, const uint32_t a[4][4], int g, int q, float c[8][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+        const __nv_bfloat16 *wr = W + (nt * 8 + g) * NRC_STRIDE;
+#pragma unroll
+        for (int kc = 0; kc < 4; kc++) mma16816(c[nt], a[kc], ld32(wr + kc * 16 + 2 * q), ld32(wr + kc * 16 + 8 + 2 * q));
+    }
+}
+
+// ReLU + bf16 repack of the C fragments as the next layer's A fragments;
+// returns the ReLU mask (bit 4*nt + i)
+__device__ __forceinline__ uint32_t relu_pack(float c[8][4], uint32_t a[4][4]) {
+    uint32_t mask = 0;
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            if (c[nt][i] > 0.0f) mask |= 1u << (4 * nt + i);
+            else c[nt][i] = 0.0f;
+        }
+#pragma unroll
+    for (int kc = 0; kc < 4; kc++) {
+        a[kc][0] = pack_bf16(c[2 * kc][0], c[2 * kc][1]);
+        a[kc][1] = pack_bf16(c[2 * kc][2], c[2 * kc][3]);
+        a[kc][2] = pack_bf16(c[2 * kc + 1][0], c[2 * kc + 1][1]);
+        a[kc][3] = pack_bf16(c[2 * kc + 1][2], c[2 * kc + 1][3]);
+    }
+    return mask;
+}
+
+// output layer (16 padded outputs): y[2][4] fragments
+__device__ __forceinline__ void layer_out(const __nv_bfloat16 *W5, const uint32_t a[4][4], int g, int q, float y[2][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 2; nt++) {
+        y[nt][0] = y[nt][1] = y[nt][2] = y[nt][3] = 0.0f;
+        const __nv_bfloat16 *wr = W5 + (nt * 8 + g) * NRC_STRIDE;
+#pragma unroll
+        for (int kc = 0; kc < 4; kc++) mma16816(y[nt], a[kc], ld32(wr + kc * 16 + 2 * q), ld32(wr + kc * 16 + 8 + 2 * q));
+    }
+}
+
+// stores the A fragments of a tile (the bf16 activations) to a [16][64] global block
+__device__ __forceinline__ void store_a(__nv_bfloat16 *dst, const uint32_t a[4][4], int g, int q) {
+#pragma unroll
+    for (int kc = 0; kc < 4; kc++) {
+        *reinterpret_cast<uint32_t *>(dst + g * NRC_W + kc * 16 + 2 * q) = a[kc][0];
+        *reinterpret_cast<uint32_t *>(dst + (g + 8) * NRC_W + kc * 16 + 2 * q) = a[kc][1];
+        *reinterpret_cast<uint32_t *>(dst + g * NRC_W + kc * 16 + 8 + 2 * q) = a[kc][2];
+        *reinterpret_cast<uint32_t *>(dst + (g + 8) * NRC_W + kc * 16 + 8 + 2 * q) = a[kc][3];
+    }
+}
+
+constexpr int NRC_WARPS = 4;
+
+struct InferArgs {
+    NrcParams P;
+    const __half2 *table;
+    const __nv_bfloat16 *wpack;
+    uint32_t n;
+    const uint32_t *list;      // optional pixel list (NULL: direct indexing)
+    const float4 *pos;         // (x, y, z, face) per pixel / query
+    const float4 *dir;
+    const float4 *nrm;         // optional explicit normals (NULL: from the face in pos.w)
+    float4 *out;               // rgb per pixel / query
+};
+
+__device__ __forceinline__ f3 face_normal(int f) {
+    f3 n = f3{0.0f, 0.0f, 0.0f};
+    const float s = (f & 1) ? 1.0f : -1.0f;
+    if ((f >> 1) == 0) n.x = s;
+    else if ((f >> 1) == 1) n.y = s;
+    else n.z = s;
+    return n;
+}
+
+// inference: per warp 32 queries per iteration (2 tiles of 16)
+__global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_infer(InferArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
+    __nv_bfloat16 *tiles = W + WFWD_ELEMS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack);
+        uint4 *dst = reinterpret_cast<uint4 *>(W);
+        for (size_t i = threadIdx.x; i < WFWD_ELEMS * 2 / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
+    const uint32_t warps = gridDim.x * NRC_WARPS;
+    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < a.n; base += warps * 32) {
+        const uint32_t i = base + lane;
+        uint32_t id = 0;
+        if (i < a.n) {
+            id = a.list ? a.list[i] : i;
+            const float4 pp = a.pos[id], dd = a.dir[id];
+            const f3 nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
+            encode_row(a.P, a.table, ld3(pp), nrm, f3{-dd.x, -dd.y, -dd.z}, tile + lane * NRC_STRIDE);
+        } else {
+            for (int k = 0; k < NRC_W; k++) tile[lane * NRC_STRIDE + k] = __float2bfloat16_rn(0.0f);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int t = 0; t < 2; t++) {
+            uint32_t act[4][4];
+            float c[8][4];
+            load_a(tile + t * 16 * NRC_STRIDE, g, q, act);
+#pragma unroll 1
+            for (int l = 0; l < 5; l++) {
+                layer64(W + w_off(l), act, g, q, c);
+                relu_pack(c, act);
+            }
+            float y[2][4];
+            layer_out(W + W5_OFF, act, g, q, y);
+            // outputs 0..2 live in n-tile 0, columns 2q, 2q+1 (q = 0, 1)
+            float *ys = reinterpret_cast<float *>(tile + t * 16 * NRC_STRIDE);  // reuse: 16 rows x 4 floats
+            __syncwarp();
+            if (q < 2) {
+                ys[g * 4 + 2 * q] = y[0][0];
+                ys[g * 4 + 2 * q + 1] = y[0][1];
+                ys[(g + 8) * 4 + 2 * q] = y[0][2];
+                ys[(g + 8) * 4 + 2 * q + 1] = y[0][3];
+            }
+            __syncwarp();
+            if (lane >= 16 * t && lane < 16 * t + 16 && i < a.n) {
+                const float *r = ys + (lane - 16 * t) * 4;
+                a.out[id] = make_float4(r[0], r[1], r[2], 0.0f);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+struct TrainArgs {
+    NrcParams P;
+    const __half2 *table;
+    const __nv_bfloat16 *wpack;
+    uint32_t n;                 // batch (multiple of 32 not required)
+    const uint32_t *list;
+    const float4 *pos, *dir, *nrm;  // nrm optional
+    const float4 *target;
+    __nv_bfloat16 *H;           // [6][n_pad][64] layer inputs (H0 = encoding)
+    __nv_bfloat16 *dZ;          // [6][n_pad][64] pre-activation gradients (layer 5: 16 used)
+    float2 *gtable;             // hash-grid gradients (fp32)
+    float *loss;                // summed loss
+    float inv_n;
+};
+
+__global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
+    __nv_bfloat16 *tiles = W + WPACK_ELEMS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack);
+        uint4 *dst = reinterpret_cast<uint4 *>(W);
+        for (size_t i = threadIdx.x; i < WPACK_ELEMS * 2 / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
+    float *ybuf = reinterpret_cast<float *>(tiles + (size_t)NRC_WARPS * 32 * NRC_STRIDE) + (size_t)w * 32 * NRC_OUT;
+    const size_t n_pad = ((size_t)a.n + 31) & ~(size_t)31;
+    const uint32_t warps = gridDim.x * NRC_WARPS;
+    float loss_acc = 0.0f;
+    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < a.n; base += warps * 32) {
+        const uint32_t i = base + lane;
+        uint32_t id = 0;
+        f3 pos = f3{0, 0, 0}, nrm = f3{0, 0, 1}, vdir = f3{0, 0, 1};
+        float4 tg = make_float4(0, 0, 0, 0);
+        if (i < a.n) {
+            id = a.list ? a.list[i] : i;
+            const float4 pp = a.pos[id], dd = a.dir[id];
+            pos = ld3(pp);
+            nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
+            vdir = f3{-dd.x, -dd.y, -dd.z};
+            tg = a.target[id];
+            encode_row(a.P, a.table, pos, nrm, vdir, tile + lane * NRC_STRIDE);
+        } else {
+            for (int k = 0; k < NRC_W; k++) tile[lane * NRC_STRIDE + k] = __float2bfloat16_rn(0.0f);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int t = 0; t < 2; t++) {
+            const size_t row0 = (size_t)base + 16 * t;
+            uint32_t act[4][4];
+            float c[8][4];
+            uint32_t masks[5];
+            load_a(tile + t * 16 * NRC_STRIDE, g, q, act);
+            store_a(a.H + row0 * NRC_W, act, g, q);
+#pragma unroll 1
+            for (int l = 0; l < 5; l++) {
+                layer64(W + w_off(l), act, g, q, c);
+                masks[l] = relu_pack(c, act);
+                store_a(a.H + ((size_t)(l + 1) * n_pad + row0) * NRC_W, act, g, q);
+            }
+            float y[2][4];
+            layer_out(W + W5_OFF, act, g, q, y);
+            float *yt = ybuf + t * 16 * NRC_OUT;
+#pragma unroll
+            for (int nt = 0; nt < 2; nt++) {
+                yt[g * NRC_OUT + nt * 8 + 2 * q] = y[nt][0];
+                yt[g * NRC_OUT + nt * 8 + 2 * q + 1] = y[nt][1];
+                yt[(g + 8) * NRC_OUT + nt * 8 + 2 * q] = y[nt][2];
+                yt[(g + 8) * NRC_OUT + nt * 8 + 2 * q + 1] = y[nt][3];
+            }
+            __syncwarp();
+            // relative L2 loss (NRC): sum_c (y_c - t_c)^2 / (sg(mean y)^2 + 0.01), mean over the batch
+            if (lane >= 16 * t && lane < 16 * t + 16) {
+                float *yr = yt + (lane - 16 * t) * NRC_OUT;
+                if (i < a.n) {
+                    const float m = (yr[0] + yr[1] + yr[2]) * (1.0f / 3.0f);
+                    const float den = m * m + 0.01f;
+                    const float e0 = yr[0] - tg.x, e1 = yr[1] - tg.y, e2 = yr[2] - tg.z;
+                    loss_acc += (e0 * e0 + e1 * e1 + e2 * e2) / den * a.inv_n;
+                    yr[0] = 2.0f * e0 / den * a.inv_n;
+                    yr[1] = 2.0f * e1 / den * a.inv_n;
+                    yr[2] = 2.0f * e2 / den * a.inv_n;
+                } else {
+                    yr[0] = yr[1] = yr[2] = 0.0f;
+                }
+                for (int k = 3; k < NRC_OUT; k++) yr[k] = 0.0f;
+            }
+            __syncwarp();
+            // dZ6 (16 wide) as A fragments: one k-chunk
+            uint32_t ad[4];
+            ad[0] = pack_bf16(yt[g * NRC_OUT + 2 * q], yt[g * NRC_OUT + 2 * q + 1]);
+            ad[1] = pack_bf16(yt[(g + 8) * NRC_OUT + 2 * q], yt[(g + 8) * NRC_OUT + 2 * q + 1]);
+            ad[2] = pack_bf16(yt[g * NRC_OUT + 8 + 2 * q], yt[g * NRC_OUT + 8 + 2 * q + 1]);
+            ad[3] = pack_bf16(yt[(g + 8) * NRC_OUT + 8 + 2 * q], yt[(g + 8) * NRC_OUT + 8 + 2 * q + 1]);
+            {
+                __nv_bfloat16 *d5 = a.dZ + ((size_t)5 * n_pad + row0) * NRC_W;
+                *reinterpret_cast<uint32_t *>(d5 + g * NRC_W + 2 * q) = ad[0];
+                *reinterpret_cast<uint32_t *>(d5 + (g + 8) * NRC_W + 2 * q) = ad[1];
+                *reinterpret_cast<uint32_t *>(d5 + g * NRC_W + 8 + 2 * q) = ad[2];
+                *reinterpret_cast<uint32_t *>(d5 + (g + 8) * NRC_W + 8 + 2 * q) = ad[3];
+            }
+            // dH5 = dZ6 * W5 (K = 16): b from WT5 [in][24]
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+                const __nv_bfloat16 *wr = W + WT5_OFF + (nt * 8 + g) * NRC_TSTRIDE5;
+                mma16816(c[nt], ad, ld32(wr + 2 * q), ld32(wr + 8 + 2 * q));
+            }
+            // backward through the hidden layers: dZ_l = dH_l * relu'(Z_l), dH_{l-1} = dZ_l * W_{l-1}
+#pragma unroll 1
+            for (int l = 4; l >= 0; l--) {
+                const uint32_t m = masks[l];
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (!((m >> (4 * nt + k)) & 1u)) c[nt][k] = 0.0f;
+                uint32_t dz[4][4];
+#pragma unroll
+                for (int kc = 0; kc < 4; kc++) {
+                    dz[kc][0] = pack_bf16(c[2 * kc][0], c[2 * kc][1]);
+                    dz[kc][1] = pack_bf16(c[2 * kc][2], c[2 * kc][3]);
+                    dz[kc][2] = pack_bf16(c[2 * kc + 1][0], c[2 * kc + 1][1]);
+                    dz[kc][3] = pack_bf16(c[2 * kc + 1][2], c[2 * kc + 1][3]);
+                }
+                store_a(a.dZ + ((size_t)l * n_pad + row0) * NRC_W, dz, g, q);
+                // dH_{l} (input of layer l) = dZ_{l+1} * W_l  (b from WT_l)
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++) {
+                    c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+                    const __nv_bfloat16 *wr = W + wt_off(l) + (nt * 8 + g) * NRC_STRIDE;
+#pragma unroll
+                    for (int kc = 0; kc < 4; kc++)
+                        mma16816(c[nt], dz[kc], ld32(wr + kc * 16 + 2 * q), ld32(wr + kc * 16 + 8 + 2 * q));
+                }
+            }
+            // c now holds dX, the gradient of the encoding; the hash features are
+            // columns 0 .. 2*levels-1 (n-tiles 0..3), staged as floats for the scatter
+            __syncwarp();
+            float *dx = ybuf;  // 16 rows x 32 floats (yt of this tile is no longer needed)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                dx[g * 32 + j * 8 + 2 * q] = c[j][0];
+                dx[g * 32 + j * 8 + 2 * q + 1] = c[j][1];
+                dx[(g + 8) * 32 + j * 8 + 2 * q] = c[j][2];
+                dx[(g + 8) * 32 + j * 8 + 2 * q + 1] = c[j][3];
+            }
+            __syncwarp();
+            if (lane >= 16 * t && lane < 16 * t + 16 && i < a.n) {
+                const float *dr = dx + (lane - 16 * t) * 32;
+                const f3 p = normalize_pos(a.P, pos);
+                const size_t T = (size_t)1 << a.P.log2_t;
+                for (int l = 0; l < a.P.levels; l++) {
+                    Corner cr;
+                    level_corners(a.P, l, p, cr);
+                    const float g0 = dr[2 * l], g1 = dr[2 * l + 1];
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        atomicAdd(&a.gtable[(size_t)l * T + cr.idx[k]], make_float2(cr.w[k] * g0, cr.w[k] * g1));
+                }
+            }
+            __syncwarp();
+        }
+    }
+    for (int o = 16; o; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+    if (lane == 0 && loss_acc != 0.0f) atomicAdd(a.loss, loss_acc);
+}
+
+// dW_l[n][k] += sum_b dZ_l[b][n] * H_l[b][k]: split-K over the batch, one warp per
+// 16-row block of n, atomics into the fp32 gradient
+__global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __nv_bfloat16 *dZ, size_t n_pad,
+                                                uint32_t n, float *dW, uint32_t rows_per_cta) {
+    const int l = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
+    const int mdim = out_dim(l);
+    if (w * 16 >= mdim) return;
+    __shared__ __align__(16) __nv_bfloat16 sz[4][16][NRC_STRIDE];
+    __shared__ __align__(16) __nv_bfloat16 sh[4][16][NRC_STRIDE];
+    const __nv_bfloat16 *Hl = H + (size_t)l * n_pad * NRC_W;
+    const __nv_bfloat16 *Zl = dZ + (size_t)l * n_pad * NRC_W;
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    const size_t r0 = (size_t)blockIdx.x * rows_per_cta;
+    const size_t r1 = min((size_t)n, r0 + rows_per_cta);
+    for (size_t s0 = r0; s0 < r1; s0 += 16) {
+        // stage 16 samples of dZ and H (each warp its own copy: no block barrier)
+        for (int e = lane; e < 16 * 8; e += 32) {
+            const int r = e >> 3, cc = (e & 7) * 8;
+            const size_t row = s0 + r;
+            uint4 vz = make_uint4(0, 0, 0, 0), vh = make_uint4(0, 0, 0, 0);
+            if (row < r1) {
+                vz = *reinterpret_cast<const uint4 *>(Zl + row * NRC_W + cc);
+                vh = *reinterpret_cast<const uint4 *>(Hl + row * NRC_W + cc);
+            }
+            *reinterpret_cast<uint4 *>(&sz[w][r][cc]) = vz;
+            *reinterpret_cast<uint4 *>(&sh[w][r][cc]) = vh;
+        }
+        __syncwarp();
+        // A[m = n-index][k = sample] = dZ[sample][n]; B[k = sample][col = k-index] = H[sample][k]
+        uint32_t af[4];
+        const int m0 = w * 16;
+        auto lo_hi = [](__nv_bfloat16 lo, __nv_bfloat16 hi) {
+            return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+        };
+        af[0] = lo_hi(sz[w][2 * q][m0 + g], sz[w][2 * q + 1][m0 + g]);
+        af[1] = lo_hi(sz[w][2 * q][m0 + g + 8], sz[w][2 * q + 1][m0 + g + 8]);
+        af[2] = lo_hi(sz[w][2 * q + 8][m0 + g], sz[w][2 * q + 9][m0 + g]);
+        af[3] = lo_hi(sz[w][2 * q + 8][m0 + g + 8], sz[w][2 * q + 9][m0 + g + 8]);
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const uint32_t b0 = lo_hi(sh[w][2 * q][nt * 8 + g], sh[w][2 * q + 1][nt * 8 + g]);
+            const uint32_t b1 = lo_hi(sh[w][2 * q + 8][nt * 8 + g], sh[w][2 * q + 9][nt * 8 + g]);
+            mma16816(acc[nt], af, b0, b1);
+        }
+        __syncwarp();
+    }
+    float *dWl = dW + m_off(l);
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const int m = w * 16 + g, k = nt * 8 + 2 * q;
+        atomicAdd(&dWl[m * NRC_W + k], acc[nt][0]);
+        atomicAdd(&dWl[m * NRC_W + k + 1], acc[nt][1]);
+        atomicAdd(&dWl[(m + 8) * NRC_W + k], acc[nt][2]);
+        atomicAdd(&dWl[(m + 8) * NRC_W + k + 1], acc[nt][3]);
+    }
+}
+
+struct AdamArgs {
+    float lr, b1, b2, eps, c1, c2;  // c1 = 1/(1-b1^t), c2 = 1/(1-b2^t)
+};
+
+__global__ void k_adam_weights(float *master, float *m, float *v, float *grad, AdamArgs A) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= MASTER_ELEMS) return;
+    // the padded output rows 3..15 stay zero
+    if (i >= 5 * (size_t)NRC_W * NRC_W && (i - 5 * (size_t)NRC_W * NRC_W) / NRC_W >= 3) {
+        grad[i] = 0.0f;
+        return;
+    }
+    const float gr = grad[i];
+    const float mi = A.b1 * m[i] + (1.0f - A.b1) * gr;
+    const float vi = A.b2 * v[i] + (1.0f - A.b2) * gr * gr;
+    m[i] = mi;
+    v[i] = vi;
+    master[i] -= A.lr * (mi * A.c1) / (sqrtf(vi * A.c2) + A.eps);
+    grad[i] = 0.0f;
+}
+
+// master weights -> bf16 pack (W and W^T in the padded shared-memory layout)
+__global__ void k_pack_weights(const float *master, __nv_bfloat16 *pack) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= WPACK_ELEMS) return;
+    float v = 0.0f;
+    if (i < W5_OFF) {
+        const int l = (int)(i / (NRC_W * NRC_STRIDE)), r = (int)(i % (NRC_W * NRC_STRIDE));
+        const int o = r / NRC_STRIDE, k = r % NRC_STRIDE;
+        if (k < NRC_W) v = master[m_off(l) + o * NRC_W + k];
+    } else if (i < WT_OFF) {
+        const int r = (int)(i - W5_OFF), o = r / NRC_STRIDE, k = r % NRC_STRIDE;
+        if (k < NRC_W) v = master[m_off(5) + o * NRC_W + k];
+    } else if (i < WT5_OFF) {
+        const int r = (int)(i - WT_OFF), l = r / (NRC_W * NRC_STRIDE), rr = r % (NRC_W * NRC_STRIDE);
+        const int k = rr / NRC_STRIDE, o = rr % NRC_STRIDE;
+        if (o < NRC_W) v = master[m_off(l) + o * NRC_W + k];
+    } else {
+        const int r = (int)(i - WT5_OFF), k = r / NRC_TSTRIDE5, o = r % NRC_TSTRIDE5;
+        if (o < NRC_OUT) v = master[m_off(5) + o * NRC_W + k];
+    }
+    pack[i] = __float2bfloat16_rn(v);
+}
+
+__global__ void k_adam_table(float2 *master, float2 *m, float2 *v, float2 *grad, __half2 *table, size_t n,
+                             AdamArgs A) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 gr = grad[i];
+    if (gr.x == 0.0f && gr.y == 0.0f) return;  // untouched entries keep their moments
+    float2 mi = m[i], vi = v[i], p = master[i];
+    mi.x = A.b1 * mi.x + (1.0f - A.b1) * gr.x;
+    mi.y = A.b1 * mi.y + (1.0f - A.b1) * gr.y;
+    vi.x = A.b2 * vi.x + (1.0f - A.b2) * gr.x * gr.x;
+    vi.y = A.b2 * vi.y + (1.0f - A.b2) * gr.y * gr.y;
+    p.x -= A.lr * (mi.x * A.c1) / (sqrtf(vi.x * A.c2) + A.eps);
+    p.y -= A.lr * (mi.y * A.c1) / (sqrtf(vi.y * A.c2) + A.eps);
+    m[i] = mi;
+    v[i] = vi;
+    master[i] = p;
+    table[i] = __floats2half2_rn(p.x, p.y);
+    grad[i] = make_float2(0.0f, 0.0f);
+}
+
+__global__ void k_init_table(float2 *master, __half2 *table, size_t n, uint64_t seed) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto u = [&](uint64_t k) {
+        uint64_t x = seed ^ (k * 0x9E3779B97F4A7C15ull);
+        x ^= x >> 31; x *= 0x7fb5d329728ea185ull; x ^= x >> 27; x *= 0x81dadef4bc2dd44dull; x ^= x >> 33;
+        return (float)((x >> 40) * (1.0 / 16777216.0)) * 2.0f - 1.0f;
+    };
+    const float2 p = make_float2(1e-4f * u(2 * i), 1e-4f * u(2 * i + 1));
+    master[i] = p;
+    table[i] = __floats2half2_rn(p.x, p.y);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------
+struct Nrc {
+    Context *ctx = nullptr;
+    vrg_nrc_desc desc{};
+    NrcParams P{};
+    size_t T = 0, table_entries = 0;
+    DevBufPtr buf;
+    float2 *t_master = nullptr, *t_m = nullptr, *t_v = nullptr, *t_grad = nullptr;
+    __half2 *table = nullptr;
+    float *w_master = nullptr, *w_m = nullptr, *w_v = nullptr, *w_grad = nullptr;
+    __nv_bfloat16 *wpack = nullptr;
+    float *loss = nullptr;
+    DevBufPtr act;  // training activations
+    size_t act_rows = 0;
+    __nv_bfloat16 *H = nullptr, *dZ = nullptr;
+    uint32_t step = 0;
+    int grid_infer = 0, grid_train = 0;
+};
+
+static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2; }
+static size_t train_smem() {
+    return WPACK_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2 + (size_t)NRC_WARPS * 32 * NRC_OUT * 4;
+}
+
+vrg_status nrc_set_bounds(Nrc *N, const float lo[3], const float hi[3]) {
+    for (int k = 0; k < 3; k++) {
+        N->P.lo[k] = lo[k];
+        float e = hi[k] - lo[k];
+        N->P.inv_ext[k] = e > 0.0f ? 1.0f / e : 1.0f;
+    }
+    return VRG_OK;
+}
+
+vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
+    Nrc *N = new Nrc();
+    N->ctx = ctx;
+    N->desc = *d;
+    NrcParams &P = N->P;
+    P.levels = (int)d->levels;
+    P.log2_t = (int)d->log2_table;
+    P.base_res = (int)d->base_resolution;
+    P.features = 2;
+    if (P.levels < 1 || P.levels > NRC_MAX_LEVELS || 2 * P.levels + 4 > NRC_W || P.log2_t < 4 || P.log2_t > 24 ||
+        d->features != 2) {
+        delete N;
+        set_error("nrc: levels 1..16, log2_table 4..24, features 2");
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    N->T = (size_t)1 << P.log2_t;
+    const double b = P.levels > 1 ? std::exp((std::log((double)d->max_resolution) - std::log((double)d->base_resolution)) /
+                                             (double)(P.levels - 1))
+                                  : 1.0;
+    for (int l = 0; l < P.levels; l++) {
+        const double res = std::floor((double)d->base_resolution * std::pow(b, (double)l));
+        P.scale[l] = (float)res;
+        const double cells = (res + 1.0) * (res + 1.0) * (res + 1.0);
+        P.dense[l] = cells <= (double)N->T ? 1u : 0u;
+        P.res1[l] = (uint32_t)(res + 1.0);
+    }
+    nrc_set_bounds(N, d->scene_min, d->scene_max);
+    N->table_entries = N->T * (size_t)P.levels;
+    const size_t te = N->table_entries;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t o = 0;
+    size_t o_tm = o; o += al(te * 8);
+    size_t o_t1 = o; o += al(te * 8);
+    size_t o_t2 = o; o += al(te * 8);
+    size_t o_tg = o; o += al(te * 8);
+    size_t o_th = o; o += al(te * 4);
+    size_t o_wm = o; o += al(MASTER_ELEMS * 4);
+    size_t o_w1 = o; o += al(MASTER_ELEMS * 4);
+    size_t o_w2 = o; o += al(MASTER_ELEMS * 4);
+    size_t o_wg = o; o += al(MASTER_ELEMS * 4);
+    size_t o_wp = o; o += al(WPACK_ELEMS * 2);
+    size_t o_ls = o; o += 256;
+    cudaStream_t s = ctx->stream;
+    vrg_status st = dev_alloc(s, o, N->buf);
+    if (st != VRG_OK) {
+        delete N;
+        return st;
+    }
+    uint8_t *B = (uint8_t *)N->buf->ptr;
+    N->t_master = (float2 *)(B + o_tm);
+    N->t_m = (float2 *)(B + o_t1);
+    N->t_v = (float2 *)(B + o_t2);
+    N->t_grad = (float2 *)(B + o_tg);
+    N->table = (__half2 *)(B + o_th);
+    N->w_master = (float *)(B + o_wm);
+    N->w_m = (float *)(B + o_w1);
+    N->w_v = (float *)(B + o_w2);
+    N->w_grad = (float *)(B + o_wg);
+    N->wpack = (__nv_bfloat16 *)(B + o_wp);
+    N->loss = (float *)(B + o_ls);
+    VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, s));
+    k_init_table<<<(uint32_t)((te + 255) / 256), 256, 0, s>>>(N->t_master, N->table, te, d->seed ^ 0x7ab1eull);
+    // He-uniform hidden layers, Xavier-uniform output layer (rows 0..2)
+    std::vector<float> wm(MASTER_ELEMS, 0.0f);
+    uint64_t x = d->seed * 0x9E3779B97F4A7C15ull + 1;
+    auto rnd = [&]() {
+        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+        return (float)((x >> 40) * (1.0 / 16777216.0)) * 2.0f - 1.0f;
+    };
+    for (int l = 0; l < 5; l++) {
+        const float a = std::sqrt(6.0f / (float)NRC_W);
+        for (int i = 0; i < NRC_W * NRC_W; i++) wm[m_off(l) + i] = a * rnd();
+    }
+    const float a5 = std::sqrt(6.0f / (float)(NRC_W + 3));
+    for (int o5 = 0; o5 < 3; o5++)
+        for (int k = 0; k < NRC_W; k++) wm[m_off(5) + o5 * NRC_W + k] = a5 * rnd();
+    VRG_CUDA_TRY(cudaMemcpyAsync(N->w_master, wm.data(), MASTER_ELEMS * 4, cudaMemcpyHostToDevice, s));
+    k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
+    VRG_CUDA_TRY(cudaGetLastError());
+    VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+    VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+    int bi = 0, bt = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bi, k_nrc_infer, NRC_WARPS * 32, infer_smem());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_nrc_train, NRC_WARPS * 32, train_smem());
+    N->grid_infer = std::max(1, ctx->num_sms * std::max(1, bi));
+    N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = N;
+    return VRG_OK;
+}
+
+vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
+                     const float4 *nrm, float4 *out) {
+    if (n == 0) return VRG_OK;
+    InferArgs a{N->P, N->table, N->wpack, n, list, pos, dir, nrm, out};
+    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
+    k_nrc_infer<<<blocks, NRC_WARPS * 32, infer_smem(), s>>>(a);
+    VRG_CUDA_TRY(cudaGetLastError());
+    return VRG_OK;
+}
+
+static vrg_status ensure_act(Nrc *N, size_t rows) {
+    const size_t n_pad = (rows + 31) & ~(size_t)31;
+    if (N->act && N->act_rows >= n_pad) return VRG_OK;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(N->ctx->stream, 2 * 6 * n_pad * NRC_W * 2, b));
+    VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, 2 * 6 * n_pad * NRC_W * 2, N->ctx->stream));
+    N->act = b;
+    N->act_rows = n_pad;
+    N->H = (__nv_bfloat16 *)b->ptr;
+    N->dZ = N->H + 6 * n_pad * NRC_W;
+    return VRG_OK;
+}
+
+// gradients of one batch (accumulated into w_grad / t_grad); update == true
+// also runs the Adam step
+vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
+                     const float4 *nrm, const float4 *target, bool update) {
+    if (n == 0) return VRG_OK;
+    VRG_TRY(ensure_act(N, n));
+    const size_t n_pad = N->act_rows;
+    TrainArgs a{N->P, N->table, N->wpack, n, list, pos, dir, nrm, target, N->H, N->dZ, N->t_grad, N->loss,
+                1.0f / (float)n};
+    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
+    k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
+    VRG_CUDA_TRY(cudaGetLastError());
+    const uint32_t rows_per_cta = 512;
+    dim3 g((n + rows_per_cta - 1) / rows_per_cta, NRC_LAYERS);
+    k_nrc_dw<<<g, 128, 0, s>>>(N->H, N->dZ, n_pad, n, N->w_grad, rows_per_cta);
+    VRG_CUDA_TRY(cudaGetLastError());
+    if (update) {
+        N->step++;
+        AdamArgs A;
+        A.lr = N->desc.learning_rate;
+        A.b1 = 0.9f;
+        A.b2 = 0.99f;
+        A.eps = 1e-8f;
+        A.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)N->step)));
+        A.c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)N->step)));
+        k_adam_weights<<<(uint32_t)((MASTER_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->w_m, N->w_v, N->w_grad, A);
+        k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
+        k_adam_table<<<(uint32_t)((N->table_entries + 255) / 256), 256, 0, s>>>(N->t_master, N->t_m, N->t_v, N->t_grad,
+                                                                               N->table, N->table_entries, A);
+        VRG_CUDA_TRY(cudaGetLastError());
+    }
+    return VRG_OK;
+}
+
+void nrc_destroy(Nrc *N) {
+    if (!N) return;
+    cudaStreamSynchronize(N->ctx->stream);
+    delete N;
+}
+
+// ---- host-array entry points (tests and tools) ------------------------------
+
+static vrg_status stage4(cudaStream_t s, const float *src, uint32_t n, int comps, float4 *dst) {
+    std::vector<float4> h(n);
+    for (uint32_t i = 0; i < n; i++)
+        h[i] = make_float4(src[comps * i], src[comps * i + 1], src[comps * i + 2], comps > 3 ? src[comps * i + 3] : 0.0f);
+    VRG_CUDA_TRY(cudaMemcpyAsync(dst, h.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb) {
+    cudaStream_t s = N->ctx->stream;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(s, (size_t)n * 16 * 4 + 64, b));
+    float4 *dp = (float4 *)b->ptr, *dd = dp + n, *dn = dd + n, *dout = dn + n;
+    VRG_TRY(stage4(s, pos, n, 3, dp));
+    VRG_TRY(stage4(s, dir, n, 3, dd));
+    VRG_TRY(stage4(s, nrm, n, 3, dn));
+    VRG_TRY(nrc_infer(N, s, n, nullptr, dp, dd, dn, dout));
+    std::vector<float4> h(n);
+    VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), dout, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < n; i++) { rgb[3 * i] = h[i].x; rgb[3 * i + 1] = h[i].y; rgb[3 * i + 2] = h[i].z; }
+    return VRG_OK;
+}
+
+vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
+                          uint32_t update, float *loss_out) {
+    cudaStream_t s = N->ctx->stream;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(s, (size_t)n * 16 * 4 + 64, b));
+    float4 *dp = (float4 *)b->ptr, *dd = dp + n, *dn = dd + n, *dt = dn + n;
+    VRG_TRY(stage4(s, pos, n, 3, dp));
+    VRG_TRY(stage4(s, dir, n, 3, dd));
+    VRG_TRY(stage4(s, nrm, n, 3, dn));
+    VRG_TRY(stage4(s, target, n, 3, dt));
+    VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 4, s));
+    VRG_TRY(nrc_train(N, s, n, nullptr, dp, dd, dn, dt, update != 0));
+    float l = 0.0f;
+    VRG_CUDA_TRY(cudaMemcpyAsync(&l, N->loss, 4, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (loss_out) *loss_out = l;
+    return VRG_OK;
+}
+
+vrg_status nrc_read(Nrc *N, uint32_t what, void *dst, uint64_t bytes) {
+    cudaStream_t s = N->ctx->stream;
+    const void *src = nullptr;
+    size_t nb = 0;
+    switch (what) {
+    case VRG_NRC_WEIGHTS: src = N->w_master; nb = MASTER_ELEMS * 4; break;
+    case VRG_NRC_WEIGHT_GRADS: src = N->w_grad; nb = MASTER_ELEMS * 4; break;
+    case VRG_NRC_TABLE: src = N->t_master; nb = N->table_entries * 8; break;
+    case VRG_NRC_TABLE_GRADS: src = N->t_grad; nb = N->table_entries * 8; break;
+    default: return VRG_ERR_INVALID_ARGUMENT;
+    }
+    if (bytes < nb) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_CUDA_TRY(cudaMemcpyAsync(dst, src, nb, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+vrg_status nrc_write(Nrc *N, uint32_t what, const void *src, uint64_t bytes) {
+    cudaStream_t s = N->ctx->stream;
+    if (what == VRG_NRC_WEIGHTS) {
+        if (bytes < MASTER_ELEMS * 4) return VRG_ERR_INVALID_ARGUMENT;
+        VRG_CUDA_TRY(cudaMemcpyAsync(N->w_master, src, MASTER_ELEMS * 4, cudaMemcpyHostToDevice, s));
+        k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
+    } else if (what == VRG_NRC_TABLE) {
+        if (bytes < N->table_entries * 8) return VRG_ERR_INVALID_ARGUMENT;
+        std::vector<float2> h(N->table_entries);
+        memcpy(h.data(), src, N->table_entries * 8);
+        std::vector<__half2> hh(N->table_entries);
+        for (size_t i = 0; i < h.size(); i++) hh[i] = __floats2half2_rn(h[i].x, h[i].y);
+        VRG_CUDA_TRY(cudaMemcpyAsync(N->t_master, h.data(), N->table_entries * 8, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(N->table, hh.data(), N->table_entries * 4, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    } else if (what == VRG_NRC_ZERO_GRADS) {
+        VRG_CUDA_TRY(cudaMemsetAsync(N->w_grad, 0, MASTER_ELEMS * 4, s));
+        VRG_CUDA_TRY(cudaMemsetAsync(N->t_grad, 0, N->table_entries * 8, s));
+    } else {
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    VRG_CUDA_TRY(cudaGetLastError());
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+void nrc_layout(uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1, const Nrc *N) {
+    *levels = (uint32_t)N->P.levels;
+    for (int l = 0; l < N->P.levels; l++) {
+        scales[l] = N->P.scale[l];
+        dense[l] = N->P.dense[l];
+        res1[l] = N->P.res1[l];
+    }
+}
+
+}  // namespace vrg

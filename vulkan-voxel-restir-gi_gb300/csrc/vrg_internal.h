@@ -144,6 +144,22 @@ vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t
                           const uint32_t *node_offset, const float *prims, const float *translations,
                           const float *power, const uint32_t *ids, vrg_bvh_node *nodes_out, uint32_t *order_out);
 
+// ---- neural radiance cache (nrc.cu) ---------------------------------------
+struct Nrc;
+vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out);
+void nrc_destroy(Nrc *N);
+vrg_status nrc_set_bounds(Nrc *N, const float lo[3], const float hi[3]);
+vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
+                     const float4 *nrm, float4 *out);
+vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
+                     const float4 *nrm, const float4 *target, bool update);
+vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb);
+vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
+                          uint32_t update, float *loss_out);
+vrg_status nrc_read(Nrc *N, uint32_t what, void *dst, uint64_t bytes);
+vrg_status nrc_write(Nrc *N, uint32_t what, const void *src, uint64_t bytes);
+void nrc_layout(uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1, const Nrc *N);
+
 // ---- renderer ------------------------------------------------------------
 struct Renderer {
     Context *ctx = nullptr;
@@ -181,6 +197,7 @@ struct Renderer {
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
     cudaEvent_t ev[16] = {};
+    Nrc *cache = nullptr;                 // attached radiance cache (not owned)
     int grid_bounce = 0;
 };
 

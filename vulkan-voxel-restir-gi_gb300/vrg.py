@@ -30,7 +30,8 @@ OK, ERR_INVALID_ARGUMENT, ERR_NOT_FOUND, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_UNSUPP
     ERR_OVERFLOW, ERR_STATE, ERR_NO_DEVICE = range(9)
 
 MODE_PARITY, MODE_CONFIG = 0, 1
-RENDER_CAPTURE, RENDER_NO_PACK = 1, 2
+RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY = 1, 2, 4, 8
+NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS = range(5)
 (DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
  DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL) = range(14)
 
@@ -67,7 +68,14 @@ class RenderParams(C.Structure):
                 ("num_bounces", C.c_uint32), ("mode", C.c_uint32), ("raygen_seed", C.c_uint32),
                 ("temporal_seed", C.c_uint32), ("spatial_seed", C.c_uint32), ("spatial_radius", C.c_float),
                 ("m_cap", C.c_uint32), ("history_slots", C.c_uint32), ("accumulate", C.c_uint32),
-                ("flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("flags", C.c_uint32), ("cache_train_bounces", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
+class NrcDesc(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("log2_table", C.c_uint32), ("features", C.c_uint32),
+                ("base_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("batch", C.c_uint32),
+                ("learning_rate", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
+                ("scene_max", C.c_float * 3)]
 
 
 class FrameOutput(C.Structure):
@@ -119,6 +127,14 @@ SIGNATURES = [
     ("vrg_terrain_generate", C.c_int32, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P]),
     ("vrg_orbit_camera", C.c_int32, [C.c_uint32] * 6 + [C.POINTER(Camera)]),
     ("vrg_pcg32_next", C.c_uint32, [C.POINTER(C.c_uint64), C.c_uint64]),
+    ("vrg_nrc_create", C.c_int32, [_P, C.POINTER(NrcDesc), C.POINTER(_P)]),
+    ("vrg_nrc_destroy", C.c_int32, [_P]),
+    ("vrg_nrc_query", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P]),
+    ("vrg_nrc_train", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, C.c_uint32, C.POINTER(C.c_float)]),
+    ("vrg_nrc_read", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
+    ("vrg_nrc_write", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
+    ("vrg_nrc_layout", C.c_int32, [_P, C.POINTER(C.c_uint32), _P, _P, _P]),
+    ("vrg_renderer_set_cache", C.c_int32, [_P, _P]),
 ]
 
 
@@ -358,12 +374,17 @@ class Renderer:
         self.last_stats = FrameStats()
 
     def params(self, prefs: RenderingPreferences, num_bounces=None, mode=MODE_PARITY, seeds=None,
-               spatial_radius=15.0, m_cap=0, history_slots=3, accumulate=0, flags=0) -> RenderParams:
+               spatial_radius=15.0, m_cap=0, history_slots=3, accumulate=0, flags=0,
+               cache_train_bounces=4) -> RenderParams:
         if seeds is None:
             seeds = (self.seeds.next(), self.seeds.next(), self.seeds.next())
         return RenderParams(prefs.nee_type, prefs.debug_view, prefs.restir_spatial_iterations,
                             self.num_bounces if num_bounces is None else num_bounces, mode, seeds[0], seeds[1],
-                            seeds[2], spatial_radius, m_cap, history_slots, accumulate, flags)
+                            seeds[2], spatial_radius, m_cap, history_slots, accumulate, flags, cache_train_bounces)
+
+    def set_cache(self, cache):
+        check(self.ctx.lib.vrg_renderer_set_cache(self.h, None if cache is None else cache.h),
+              "vrg_renderer_set_cache")
 
     def render_params(self, scene: Scene, cam: Camera, params: RenderParams, want_image=True,
                       want_radiance=False):
@@ -407,6 +428,70 @@ class Renderer:
     def close(self):
         if self.h:
             self.ctx.lib.vrg_renderer_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+NRC_MASTER = 5 * 64 * 64 + 16 * 64
+
+
+class RadianceCache:
+    """Neural radiance cache (no reference counterpart): hash grid + 5x64 MLP."""
+
+    def __init__(self, ctx: Context, scene_min, scene_max, levels=16, log2_table=19, base_resolution=16,
+                 max_resolution=2048, batch=65536, learning_rate=1e-2, seed=1):
+        self.ctx = ctx
+        self.levels, self.log2_table = levels, log2_table
+        d = NrcDesc(levels, log2_table, 2, base_resolution, max_resolution, batch, learning_rate, seed,
+                    (C.c_float * 3)(*scene_min), (C.c_float * 3)(*scene_max))
+        self.h = C.c_void_p()
+        check(ctx.lib.vrg_nrc_create(ctx.h, C.byref(d), C.byref(self.h)), "vrg_nrc_create")
+
+    def query(self, pos, normal, direction):
+        pos, normal, direction = (np.ascontiguousarray(a, np.float32) for a in (pos, normal, direction))
+        out = np.zeros((len(pos), 3), np.float32)
+        check(self.ctx.lib.vrg_nrc_query(self.h, len(pos), _ptr(pos), _ptr(normal), _ptr(direction), _ptr(out)),
+              "vrg_nrc_query")
+        return out
+
+    def train(self, pos, normal, direction, target, update=True):
+        pos, normal, direction, target = (np.ascontiguousarray(a, np.float32)
+                                          for a in (pos, normal, direction, target))
+        loss = C.c_float()
+        check(self.ctx.lib.vrg_nrc_train(self.h, len(pos), _ptr(pos), _ptr(normal), _ptr(direction), _ptr(target),
+                                         1 if update else 0, C.byref(loss)), "vrg_nrc_train")
+        return loss.value
+
+    def read(self, what):
+        n = NRC_MASTER if what in (NRC_WEIGHTS, NRC_WEIGHT_GRADS) else self.levels * (1 << self.log2_table) * 2
+        a = np.zeros(n, np.float32)
+        check(self.ctx.lib.vrg_nrc_read(self.h, what, _ptr(a), a.nbytes), "vrg_nrc_read")
+        return a
+
+    def write(self, what, a=None):
+        if a is None:
+            check(self.ctx.lib.vrg_nrc_write(self.h, what, None, 0), "vrg_nrc_write")
+        else:
+            a = np.ascontiguousarray(a, np.float32)
+            check(self.ctx.lib.vrg_nrc_write(self.h, what, _ptr(a), a.nbytes), "vrg_nrc_write")
+
+    def layout(self):
+        lv = C.c_uint32()
+        sc = np.zeros(16, np.float32)
+        dn = np.zeros(16, np.uint32)
+        r1 = np.zeros(16, np.uint32)
+        check(self.ctx.lib.vrg_nrc_layout(self.h, C.byref(lv), _ptr(sc), _ptr(dn), _ptr(r1)), "vrg_nrc_layout")
+        n = lv.value
+        return sc[:n], dn[:n], r1[:n]
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.vrg_nrc_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):
