@@ -1300,7 +1300,7 @@ static void render_frame(ORenderer &R, const OWorld &W, const vrg_camera &cam, c
         R.image[4 * p + 1] = to_u8(c.y);
         R.image[4 * p + 2] = to_u8(c.x);
         R.image[4 * p + 3] = 255;
-        if (pr.accumulate) {
+        if (pr.accumulate && std::isfinite(c.x) && std::isfinite(c.y) && std::isfinite(c.z)) {
             R.accum[3 * p + 0] += (double)c.x;
             R.accum[3 * p + 1] += (double)c.y;
             R.accum[3 * p + 2] += (double)c.z;

@@ -1,0 +1,49 @@
+"""Cache-terminated tracing vs the plain tracer against an FP64 ground truth
+(relMSE), and the FP64 accumulation itself."""
+import numpy as np
+import pytest
+
+import quality
+import vrg
+from helpers import terrain_world
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(gpu_ctx, seed=5, nx=2, nz=2, em=0.01):
+    mats, n, world = terrain_world(seed, nx, nz, em)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    lt, gt = scene.get_tlas()
+    return scene, objs, gt[0]["min"], gt[0]["max"]
+
+
+def test_fp64_accumulation_is_the_frame_mean(gpu_ctx):
+    scene, objs, lo, hi = _scene(gpu_ctx)
+    W, H = 64, 48
+    r = vrg.Renderer(gpu_ctx, W, H, 8)
+    cam = vrg.orbit_camera(2, 2, 0, 64, W, H)
+    frames = []
+    r.reset_accumulation()
+    for f in range(6):
+        _, rad = r.render_params(scene, cam, quality._params(4, vrg.RENDER_PLAIN_ONLY, f), want_image=False,
+                                 want_radiance=True)
+        frames.append(rad.astype(np.float64))
+    acc, n = r.read_accumulation()
+    assert n == 6
+    np.testing.assert_allclose(acc, np.mean(frames, axis=0), rtol=1e-6, atol=1e-6)
+
+
+def test_cache_beats_plain_at_equal_time(gpu_ctx):
+    scene, objs, lo, hi = _scene(gpu_ctx)
+    W, H = 160, 96
+    r = vrg.Renderer(gpu_ctx, W, H, 8)
+    cam = vrg.orbit_camera(2, 2, 5, 64, W, H)
+    gt = quality.ground_truth(r, scene, cam, spp=1024, bounces=8)
+    res = quality.equal_time_study(gpu_ctx, scene, r, cam, gt, lo, hi, frames=8, cache_warmup=96)
+    # what the trained cache gains over the method without it: lower error per
+    # frame and per accumulated run (the 2x target of the workload is measured
+    # and reported by bench.py at full size, not asserted here)
+    assert res["cache"]["relmse_1spp"] < res["plain"]["relmse_1spp"], res
+    assert res["cache"]["relmse_mean_of_frames"] < res["plain"]["relmse_mean_of_frames"], res
+    assert res["cache"]["nonfinite"] == 0.0 and np.isfinite(res["restir"]["relmse_1spp"])

@@ -15,6 +15,7 @@ vrg_status upload_frames(cudaStream_t s);
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int grid);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
+vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a);
 int bounce_blocks_per_sm();
 
 static thread_local char g_err[512] = "";
@@ -406,7 +407,7 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
 
 VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_t height, uint32_t max_bounces,
                                        vrg_renderer **out) {
-    if (!ctx || !out || width == 0 || height == 0 || max_bounces == 0 || max_bounces > MAX_BOUNCES - 1)
+    if (!ctx || !out || width == 0 || height == 0 || max_bounces == 0 || max_bounces > MAX_BOUNCES)
         return VRG_ERR_INVALID_ARGUMENT;
     if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
     vrg_renderer *r = new vrg_renderer();
@@ -501,7 +502,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
                   cam->height, r->W, r->H);
         return VRG_ERR_INVALID_ARGUMENT;
     }
-    if (pr->num_bounces == 0 || pr->num_bounces > r->nb_max || pr->spatial_iterations > 64 ||
+    if (pr->num_bounces == 0 || pr->spatial_iterations > 64 ||
         pr->nee_type > 2 || pr->mode > 1) {
         set_error("invalid render parameters");
         return VRG_ERR_INVALID_ARGUMENT;
@@ -524,6 +525,46 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     }
     const bool capture = (pr->flags & VRG_RENDER_CAPTURE) != 0;
     if (capture) VRG_TRY(ensure_capture(r));
+    const bool cache = (pr->flags & VRG_RENDER_CACHE) != 0;
+    const uint32_t nb_total = cache ? pr->num_bounces + pr->cache_train_bounces : pr->num_bounces;
+    if (cache) {
+        if (!r->cache) {
+            set_error("VRG_RENDER_CACHE without an attached radiance cache");
+            return VRG_ERR_STATE;
+        }
+        if (pr->num_bounces < 2 || nb_total > r->nb_max) {
+            set_error("cache mode needs num_bounces >= 2 and num_bounces + cache_train_bounces <= %u", r->nb_max);
+            return VRG_ERR_INVALID_ARGUMENT;
+        }
+        if (!r->cache_buf) {
+            const uint32_t cap = nrc_batch(r->cache);
+            auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+            size_t o = 0;
+            size_t o_qp = o; o += al(P * 16);
+            size_t o_qd = o; o += al(P * 16);
+            size_t o_pr = o; o += al(P * 16);
+            size_t o_tg = o; o += al(P * 16);
+            size_t o_il = o; o += al(P * 4);
+            size_t o_tl = o; o += al((size_t)cap * 4);
+            size_t o_qf = o; o += al(P);
+            DevBufPtr b;
+            VRG_TRY(dev_alloc(s, o, b));
+            VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, o, s));
+            uint8_t *B = (uint8_t *)b->ptr;
+            r->q_pos = (float4 *)(B + o_qp);
+            r->q_dir = (float4 *)(B + o_qd);
+            r->pred = (float4 *)(B + o_pr);
+            r->target = (float4 *)(B + o_tg);
+            r->infer_list = (uint32_t *)(B + o_il);
+            r->train_list = (uint32_t *)(B + o_tl);
+            r->qflag = B + o_qf;
+            r->cache_buf = b;
+        }
+        if (!scene->h_geo_tl.empty())
+            nrc_set_bounds(r->cache, scene->h_geo_tl[0].min, scene->h_geo_tl[0].max);
+    } else if (nb_total > r->nb_max) {
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
     const uint32_t ring = r->frame % slots;
     FrameArgs a;
     memset(&a, 0, sizeof(a));
@@ -535,7 +576,18 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.W = r->W;
     a.H = r->H;
     a.P = (uint32_t)P;
-    a.nb = pr->num_bounces;
+    a.nb = nb_total;
+    a.nb_render = pr->num_bounces;
+    a.cache = cache ? 1u : 0u;
+    a.train_cap = cache ? nrc_batch(r->cache) : 0u;
+    a.restir = (cache || (pr->flags & VRG_RENDER_PLAIN_ONLY)) ? 0u : 1u;
+    a.q_pos = r->q_pos;
+    a.q_dir = r->q_dir;
+    a.pred = r->pred;
+    a.target = r->target;
+    a.infer_list = r->infer_list;
+    a.train_list = r->train_list;
+    a.qflag = r->qflag;
     a.nee_type = pr->nee_type;
     a.frame = r->frame;
     a.mode = pr->mode;
@@ -588,7 +640,15 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         VRG_TRY(launch_bounce(s, a, b, r->grid_bounce));
         VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     }
+    if (cache)  // radiance-cache queries of every path that ends into the cache
+        VRG_TRY(nrc_infer(r->cache, s, (uint32_t)P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir,
+                          nullptr, r->pred));
     VRG_TRY(launch_resolve(s, a));
+    if (cache) {  // one training step on this frame's long paths
+        VRG_TRY(launch_train_targets(s, a));
+        VRG_TRY(nrc_train(r->cache, s, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
+                          nullptr, r->target, true));
+    }
     VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     VRG_TRY(launch_spatial(s, a));
     VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));

@@ -220,7 +220,8 @@ struct InferArgs {
     NrcParams P;
     const __half2 *table;
     const __nv_bfloat16 *wpack;
-    uint32_t n;
+    uint32_t n;                // capacity (and count when n_dev is NULL)
+    const uint32_t *n_dev;     // optional device-side count
     const uint32_t *list;      // optional pixel list (NULL: direct indexing)
     const float4 *pos;         // (x, y, z, face) per pixel / query
     const float4 *dir;
@@ -251,10 +252,11 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_infer(InferArgs a) {
     __syncthreads();
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
     const uint32_t warps = gridDim.x * NRC_WARPS;
-    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < a.n; base += warps * 32) {
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < n; base += warps * 32) {
         const uint32_t i = base + lane;
         uint32_t id = 0;
-        if (i < a.n) {
+        if (i < n) {
             id = a.list ? a.list[i] : i;
             const float4 pp = a.pos[id], dd = a.dir[id];
             const f3 nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_infer(InferArgs a) {
                 ys[(g + 8) * 4 + 2 * q + 1] = y[0][3];
             }
             __syncwarp();
-            if (lane >= 16 * t && lane < 16 * t + 16 && i < a.n) {
+            if (lane >= 16 * t && lane < 16 * t + 16 && i < n) {
                 const float *r = ys + (lane - 16 * t) * 4;
                 a.out[id] = make_float4(r[0], r[1], r[2], 0.0f);
             }
@@ -298,7 +300,8 @@ struct TrainArgs {
     NrcParams P;
     const __half2 *table;
     const __nv_bfloat16 *wpack;
-    uint32_t n;                 // batch (multiple of 32 not required)
+    uint32_t n;                 // capacity (and batch when n_dev is NULL)
+    const uint32_t *n_dev;      // optional device-side batch size
     const uint32_t *list;
     const float4 *pos, *dir, *nrm;  // nrm optional
     const float4 *target;
@@ -306,7 +309,6 @@ struct TrainArgs {
     __nv_bfloat16 *dZ;          // [6][n_pad][64] pre-activation gradients (layer 5: 16 used)
     float2 *gtable;             // hash-grid gradients (fp32)
     float *loss;                // summed loss
-    float inv_n;
 };
 
 __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
@@ -324,13 +326,15 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
     float *ybuf = reinterpret_cast<float *>(tiles + (size_t)NRC_WARPS * 32 * NRC_STRIDE) + (size_t)w * 32 * NRC_OUT;
     const size_t n_pad = ((size_t)a.n + 31) & ~(size_t)31;
     const uint32_t warps = gridDim.x * NRC_WARPS;
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const float inv_n = n ? 1.0f / (float)n : 0.0f;
     float loss_acc = 0.0f;
-    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < a.n; base += warps * 32) {
+    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < n; base += warps * 32) {
         const uint32_t i = base + lane;
         uint32_t id = 0;
         f3 pos = f3{0, 0, 0}, nrm = f3{0, 0, 1}, vdir = f3{0, 0, 1};
         float4 tg = make_float4(0, 0, 0, 0);
-        if (i < a.n) {
+        if (i < n) {
             id = a.list ? a.list[i] : i;
             const float4 pp = a.pos[id], dd = a.dir[id];
             pos = ld3(pp);
@@ -370,14 +374,14 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
             // relative L2 loss (NRC): sum_c (y_c - t_c)^2 / (sg(mean y)^2 + 0.01), mean over the batch
             if (lane >= 16 * t && lane < 16 * t + 16) {
                 float *yr = yt + (lane - 16 * t) * NRC_OUT;
-                if (i < a.n) {
+                if (i < n) {
                     const float m = (yr[0] + yr[1] + yr[2]) * (1.0f / 3.0f);
                     const float den = m * m + 0.01f;
                     const float e0 = yr[0] - tg.x, e1 = yr[1] - tg.y, e2 = yr[2] - tg.z;
-                    loss_acc += (e0 * e0 + e1 * e1 + e2 * e2) / den * a.inv_n;
-                    yr[0] = 2.0f * e0 / den * a.inv_n;
-                    yr[1] = 2.0f * e1 / den * a.inv_n;
-                    yr[2] = 2.0f * e2 / den * a.inv_n;
+                    loss_acc += (e0 * e0 + e1 * e1 + e2 * e2) / den * inv_n;
+                    yr[0] = 2.0f * e0 / den * inv_n;
+                    yr[1] = 2.0f * e1 / den * inv_n;
+                    yr[2] = 2.0f * e2 / den * inv_n;
                 } else {
                     yr[0] = yr[1] = yr[2] = 0.0f;
                 }
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
                 dx[(g + 8) * 32 + j * 8 + 2 * q + 1] = c[j][3];
             }
             __syncwarp();
-            if (lane >= 16 * t && lane < 16 * t + 16 && i < a.n) {
+            if (lane >= 16 * t && lane < 16 * t + 16 && i < n) {
                 const float *dr = dx + (lane - 16 * t) * 32;
                 const f3 p = normalize_pos(a.P, pos);
                 const size_t T = (size_t)1 << a.P.log2_t;
@@ -467,8 +471,10 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
 // dW_l[n][k] += sum_b dZ_l[b][n] * H_l[b][k]: split-K over the batch, one warp per
 // 16-row block of n, atomics into the fp32 gradient
 __global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __nv_bfloat16 *dZ, size_t n_pad,
-                                                uint32_t n, float *dW, uint32_t rows_per_cta) {
+                                                uint32_t n_cap, const uint32_t *n_dev, float *dW,
+                                                uint32_t rows_per_cta) {
     const int l = blockIdx.y;
+    const uint32_t n = n_dev ? min(*n_dev, n_cap) : n_cap;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
     const int mdim = out_dim(l);
     if (w * 16 >= mdim) return;
@@ -480,6 +486,7 @@ __global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
     const size_t r0 = (size_t)blockIdx.x * rows_per_cta;
+    if (r0 >= n) return;
     const size_t r1 = min((size_t)n, r0 + rows_per_cta);
     for (size_t s0 = r0; s0 < r1; s0 += 16) {
         // stage 16 samples of dZ and H (each warp its own copy: no block barrier)
@@ -729,10 +736,10 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     return VRG_OK;
 }
 
-vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
-                     const float4 *nrm, float4 *out) {
+vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
+                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out) {
     if (n == 0) return VRG_OK;
-    InferArgs a{N->P, N->table, N->wpack, n, list, pos, dir, nrm, out};
+    InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out};
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
     k_nrc_infer<<<blocks, NRC_WARPS * 32, infer_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
@@ -754,19 +761,18 @@ static vrg_status ensure_act(Nrc *N, size_t rows) {
 
 // gradients of one batch (accumulated into w_grad / t_grad); update == true
 // also runs the Adam step
-vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
-                     const float4 *nrm, const float4 *target, bool update) {
+vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
+                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update) {
     if (n == 0) return VRG_OK;
     VRG_TRY(ensure_act(N, n));
     const size_t n_pad = N->act_rows;
-    TrainArgs a{N->P, N->table, N->wpack, n, list, pos, dir, nrm, target, N->H, N->dZ, N->t_grad, N->loss,
-                1.0f / (float)n};
+    TrainArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, target, N->H, N->dZ, N->t_grad, N->loss};
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
     k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     const uint32_t rows_per_cta = 512;
     dim3 g((n + rows_per_cta - 1) / rows_per_cta, NRC_LAYERS);
-    k_nrc_dw<<<g, 128, 0, s>>>(N->H, N->dZ, n_pad, n, N->w_grad, rows_per_cta);
+    k_nrc_dw<<<g, 128, 0, s>>>(N->H, N->dZ, n_pad, n, n_dev, N->w_grad, rows_per_cta);
     VRG_CUDA_TRY(cudaGetLastError());
     if (update) {
         N->step++;
@@ -785,6 +791,8 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, c
     }
     return VRG_OK;
 }
+
+uint32_t nrc_batch(const Nrc *N) { return N->desc.batch ? N->desc.batch : 65536u; }
 
 void nrc_destroy(Nrc *N) {
     if (!N) return;
@@ -811,7 +819,7 @@ vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, pos, n, 3, dp));
     VRG_TRY(stage4(s, dir, n, 3, dd));
     VRG_TRY(stage4(s, nrm, n, 3, dn));
-    VRG_TRY(nrc_infer(N, s, n, nullptr, dp, dd, dn, dout));
+    VRG_TRY(nrc_infer(N, s, n, nullptr, nullptr, dp, dd, dn, dout));
     std::vector<float4> h(n);
     VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), dout, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -830,7 +838,7 @@ vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, nrm, n, 3, dn));
     VRG_TRY(stage4(s, target, n, 3, dt));
     VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 4, s));
-    VRG_TRY(nrc_train(N, s, n, nullptr, dp, dd, dn, dt, update != 0));
+    VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0));
     float l = 0.0f;
     VRG_CUDA_TRY(cudaMemcpyAsync(&l, N->loss, 4, cudaMemcpyDeviceToHost, s));
     VRG_CUDA_TRY(cudaStreamSynchronize(s));

@@ -80,7 +80,23 @@ __global__ void __launch_bounds__(256) k_resolve(FrameArgs a) {
             a.c_q[s0] = inv2pi;
         }
     }
-    for (int b = (int)nl - 1; b >= 0; b--) {
+    int top = (int)nl - 1;
+    if (a.cache && nl >= a.nb_render) {
+        // the path ends into the radiance cache at vertex nb_render-1: its
+        // outgoing radiance is the cache's prediction when the ray hit geometry,
+        // the record's emission (sky) when it missed
+        const int qb = (int)a.nb_render - 1;
+        if (a.qflag[p]) {
+            const float4 pr = a.pred[p];
+            L = f3{pr.x, pr.y, pr.z};
+        } else {
+            const float4 e = a.rec[(size_t)qb * 2 * P + p];
+            L = f3{e.x, e.y, e.z};
+        }
+        if (qb == 1) L1 = L;
+        top = qb - 1;
+    }
+    for (int b = top; b >= 0; b--) {
         const size_t rb = (size_t)b * 2 * P;
         const float4 e = a.rec[rb + p], r = a.rec[rb + P + p];
         // L = E + R * L * (bsdf_pdf / q) * valid, valid = 1 for traced rays
@@ -93,7 +109,7 @@ __global__ void __launch_bounds__(256) k_resolve(FrameArgs a) {
         }
     }
     a.plain[p] = make_float4(L.x, L.y, L.z, 0.0f);
-    if (nb < 2) return;
+    if (nb < 2 || !a.restir) return;
     // initial sample (interactive_rendering.rs:1359-1414)
     Res S;
     S.x_v = ld3(a.xv[p]);
@@ -145,7 +161,7 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs a) {
     if (p >= P) return;
     f3 fin = f3{0.0f, 0.0f, 0.0f};
     float ucw_view = 0.0f;
-    if (a.nb >= 2) {
+    if (a.nb >= 2 && a.restir) {
         const uint32_t qx = p % a.W, qy = p / a.W;
         const uint32_t ps = mm_combine(a.spatial_seed, p);
         Res Rs = load_res(a.res, P, p);
@@ -214,14 +230,38 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs a) {
         reinterpret_cast<uchar4 *>(a.bgra)[p] = px;
     }
     if (a.radiance) st3(a.radiance, p, c);
-    if (a.accumulate) {
+    if (a.accumulate && isfinite(c.x) && isfinite(c.y) && isfinite(c.z)) {
+        // non-finite samples (the estimator's 0*inf cases) are left out of the sum
         a.accum[3 * (size_t)p] += (double)c.x;
         a.accum[3 * (size_t)p + 1] += (double)c.y;
         a.accum[3 * (size_t)p + 2] += (double)c.z;
     }
 }
 
+// training targets of the radiance cache: the outgoing radiance at vertex
+// nb_render-1 of each long training path (its full backward recurrence)
+__global__ void __launch_bounds__(256) k_train_targets(FrameArgs a) {
+    const uint32_t n = min(a.counters[CNT_TRAIN], a.train_cap);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t P = a.P, p = a.train_list[i];
+    const int nl = a.nlive[p], qb = (int)a.nb_render - 1;
+    f3 L = f3{0.0f, 0.0f, 0.0f};
+    for (int b = nl - 1; b >= qb; b--) {
+        const size_t rb = (size_t)b * 2 * P;
+        const float4 e = a.rec[rb + p], r = a.rec[rb + P + p];
+        L = f3{e.x + (r.x * L.x) * e.w, e.y + (r.y * L.y) * e.w, e.z + (r.z * L.z) * e.w};
+    }
+    a.target[p] = make_float4(L.x, L.y, L.z, 0.0f);
+}
+
 }  // namespace
+
+vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a) {
+    k_train_targets<<<(a.train_cap + 255) / 256, 256, 0, s>>>(a);
+    VRG_CUDA_TRY(cudaGetLastError());
+    return VRG_OK;
+}
 
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a) {
     dim3 g((a.P + 255) / 256);

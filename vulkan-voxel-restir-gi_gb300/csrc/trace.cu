@@ -365,8 +365,16 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
     for (uint32_t base = wid * 32; base < n_in; base += warps * 32) {
         const uint32_t i = base + lane;
         const bool active = i < n_in;
-        bool cont = false, anyj = false;
+        bool cont = false, anyj = false, qhit = false, want_train = false;
+        const bool at_query = a.cache && b + 1 == a.nb_render;
+        f3 stash_E = f3{0, 0, 0}, stash_R = f3{0, 0, 0}, stash_n = f3{0, 0, 0};
+        float stash_mis = 0.0f;
+        int4 stash_hit = make_int4(-1, 0, 0, 0), stash_rc = make_int4(0, 0, 0, 0);
+        int stash_half = 0;
         uint32_t p = 0;
+        f3 new_o = f3{0, 0, 0}, new_d = f3{0, 0, 0};
+        float pdf = 1.0f;
+        int face = 0;
         if (active) {
             p = (b == 0) ? i : qin[i];
             f3 o, d;
@@ -382,9 +390,9 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
             }
             const uint32_t seed = mm_combine(inv_seed, p);
             const int4 hv = a.hits[p];
-            f3 new_o, new_d, n, E, R;
-            float mis = 0.0f, pdf = 1.0f;
-            int face = 0, half = 0;
+            f3 n, E, R;
+            float mis = 0.0f;
+            int half = 0;
             int4 rc = make_int4(0, 0, 0, 0);
             if (hv.x < 0) {
                 new_o = add3(o, scl3(d, 5000.0f));
@@ -450,6 +458,52 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
                 anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
             }
+            // radiance cache: the vertex where rendered paths end into the cache
+            if (at_query) {
+                qhit = hv.x >= 0;
+                a.qflag[p] = qhit ? 1 : 0;
+                if (qhit) {
+                    a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+                    a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
+                    want_train = (mm_finalize(mm_combine(a.frame * 0x9E3779B9u + 0x7a11u, p)) & 15u) == 0u;
+                }
+            }
+            // stash for the second half (after the warp-level training-slot grant)
+            stash_E = E;
+            stash_R = R;
+            stash_n = n;
+            stash_mis = mis;
+            stash_hit = hv;
+            stash_rc = rc;
+            stash_half = half;
+        }
+        // training paths: up to train_cap per frame, granted per warp
+        bool is_train = false;
+        if (at_query) {
+            const uint32_t tm = __ballot_sync(FULL, active && qhit && want_train);
+            const uint32_t im = __ballot_sync(FULL, active && qhit);
+            uint32_t tb = 0, ib = 0;
+            if (lane == 0) {
+                if (tm) tb = atomicAdd(&a.counters[CNT_TRAIN], (uint32_t)__popc(tm));
+                if (im) ib = atomicAdd(&a.counters[CNT_INFER], (uint32_t)__popc(im));
+            }
+            tb = __shfl_sync(FULL, tb, 0);
+            ib = __shfl_sync(FULL, ib, 0);
+            if (active && qhit) a.infer_list[ib + __popc(im & lanemask_lt())] = p;
+            if (active && qhit && want_train) {
+                const uint32_t slot = tb + __popc(tm & lanemask_lt());
+                if (slot < a.train_cap) {
+                    a.train_list[slot] = p;
+                    is_train = true;
+                }
+            }
+            if (!is_train) anyj = false;  // the record of this bounce is replaced by the cache
+        }
+        if (active) {
+            const f3 E = stash_E, R = stash_R, n = stash_n;
+            const float mis = stash_mis;
+            const int4 hv = stash_hit, rc = stash_rc;
+            const int half = stash_half;
             const size_t rb = (size_t)b * 2 * P;
             if (anyj) {
                 a.rec[rb + p] = make_float4(E.x, E.y, E.z, 0.0f);
@@ -467,7 +521,7 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 a.xs[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
                 a.ns[p] = make_float4(n.x, n.y, n.z, 0.0f);
             }
-            cont = !zero3(new_d) && (b + 1 < nb);
+            cont = !zero3(new_d) && (b + 1 < nb) && (!at_query || is_train);
             if (cont) {
                 // .w of the ray carries the face and the bsdf pdf to k_anyhit
                 a.ray_o[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));

@@ -14,6 +14,8 @@ constexpr int CNT_ANY = 20;      // u64 at words 20-21: light any-hit queries
 constexpr int CNT_AQUEUE = 24;   // [24..31] any-hit jobs queued by bounce b
 constexpr int CNT_AFETCH = 32;   // [32..39] any-hit work-fetch cursor of bounce b
 constexpr int CNT_SFETCH = 40;   // [40..47] shading work-fetch cursor of bounce b
+constexpr int CNT_INFER = 48;    // radiance-cache queries of the frame
+constexpr int CNT_TRAIN = 49;    // radiance-cache training paths of the frame
 constexpr int CNT_WORDS = 64;
 constexpr int MAX_BOUNCES = 8;
 
@@ -41,6 +43,12 @@ struct FrameArgs {
     uint8_t *bgra;
     float *radiance;
     double *accum;
+    // radiance cache (VRG_RENDER_CACHE): paths end into the cache after
+    // nb_render bounces; 1/16 of them (up to train_cap) trace to nb and train it
+    uint32_t nb_render, cache, train_cap, restir;
+    float4 *q_pos, *q_dir, *pred, *target;
+    uint32_t *infer_list, *train_list;
+    uint8_t *qflag;
     // capture (reference SoA layout, for parity readback)
     uint32_t capture;
     float *c_origin, *c_dir, *c_normal, *c_emis, *c_refl, *c_mis, *c_pdf, *c_nee, *c_L, *c_q;

@@ -149,10 +149,11 @@ struct Nrc;
 vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out);
 void nrc_destroy(Nrc *N);
 vrg_status nrc_set_bounds(Nrc *N, const float lo[3], const float hi[3]);
-vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
-                     const float4 *nrm, float4 *out);
-vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *list, const float4 *pos, const float4 *dir,
-                     const float4 *nrm, const float4 *target, bool update);
+vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
+                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out);
+vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
+                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update);
+uint32_t nrc_batch(const Nrc *N);
 vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb);
 vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
                           uint32_t update, float *loss_out);
@@ -198,6 +199,10 @@ struct Renderer {
     size_t h_pinned_bytes = 0;
     cudaEvent_t ev[16] = {};
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
+    DevBufPtr cache_buf;                  // per-pixel cache queries / predictions / targets
+    float4 *q_pos = nullptr, *q_dir = nullptr, *pred = nullptr, *target = nullptr;
+    uint32_t *infer_list = nullptr, *train_list = nullptr;
+    uint8_t *qflag = nullptr;
     int grid_bounce = 0;
 };
 

@@ -1,0 +1,99 @@
+"""Image-quality measurement of the renderer: an FP64-accumulated ground truth
+of the plain path tracer and the relative MSE of other estimators against it,
+with the cache-terminated tracer compared to the plain one at equal frame
+time (none of this has a reference counterpart: the reference renders 1 spp
+per frame with no error metric).
+
+relMSE(x, gt) = mean over pixels and channels of (x - gt)^2 / (gt^2 + 0.01).
+"""
+import time
+
+import numpy as np
+
+import vrg
+
+EPS = 0.01
+
+
+def relmse(x, gt):
+    """Non-finite estimates (the estimator's 0*inf cases) count as 0."""
+    x = np.nan_to_num(np.asarray(x, np.float64), nan=0.0, posinf=0.0, neginf=0.0)
+    gt = np.asarray(gt, np.float64)
+    return float(np.mean((x - gt) ** 2 / (gt * gt + EPS)))
+
+
+def nonfinite_fraction(x):
+    return float(np.mean(~np.isfinite(np.asarray(x))))
+
+
+def _params(nb, flags, seed, accumulate=1, train_bounces=4):
+    return vrg.RenderParams(1, 0, 0, nb, vrg.MODE_CONFIG, seed, seed + 1, seed + 2, 30.0, 20, 1, accumulate,
+                            flags | vrg.RENDER_NO_PACK, train_bounces)
+
+
+def ground_truth(renderer, scene, cam, spp=4096, bounces=8):
+    """Plain path tracer, `bounces` bounces, `spp` frames accumulated in FP64 on the GPU."""
+    renderer.reset_accumulation()
+    for f in range(spp):
+        renderer.render_params(scene, cam, _params(bounces, vrg.RENDER_PLAIN_ONLY, f), want_image=False)
+    acc, n = renderer.read_accumulation()
+    assert n == spp
+    return acc
+
+
+def frame_ms(renderer):
+    return float(renderer.last_stats.ms_total)
+
+
+def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=None):
+    """Renders `frames` 1-spp frames of `method` at a fixed camera; returns
+    (mean image, list of single-frame radiance images, mean device ms/frame).
+    method: 'plain' (3 bounces), 'restir' (3 bounces + ReSTIR view), 'cache'
+    (2 bounces ending into the radiance cache, 4 more for 1/16 training paths)."""
+    if method == "cache":
+        renderer.set_cache(cache)
+    singles, ms = [], []
+    for f in range(warmup + frames):
+        if method == "plain":
+            p = _params(3, vrg.RENDER_PLAIN_ONLY, seed0 + f, accumulate=0)
+        elif method == "restir":
+            p = _params(3, 0, seed0 + f, accumulate=0)
+            p.debug_view = 1
+            p.spatial_iterations = 3
+        else:
+            p = _params(2, vrg.RENDER_CACHE, seed0 + f, accumulate=0)
+        _, rad = renderer.render_params(scene, cam, p, want_image=False, want_radiance=True)
+        if f >= warmup:
+            singles.append(rad.astype(np.float32))
+            ms.append(frame_ms(renderer))
+    clean = [np.nan_to_num(s, nan=0.0, posinf=0.0, neginf=0.0) for s in singles]
+    return np.mean(clean, axis=0), singles, float(np.mean(ms))
+
+
+def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames=16, cache_warmup=64, seed=7):
+    """Single-frame and equal-time relMSE of plain, ReSTIR and cache-terminated
+    tracing against `gt`.  The cache is trained online for `cache_warmup`
+    frames at this camera before the measured frames (it keeps training)."""
+    cache = vrg.RadianceCache(ctx, scene_min, scene_max, seed=seed)
+    out = {}
+    for method in ("plain", "restir", "cache"):
+        warm = cache_warmup if method == "cache" else 2
+        mean_img, singles, ms = run_method(renderer, scene, cam, method, frames, seed0=1000, warmup=warm,
+                                           cache=cache)
+        out[method] = {"ms_per_frame": round(ms, 4),
+                       "relmse_1spp": round(float(np.mean([relmse(s, gt) for s in singles])), 6),
+                       "nonfinite": round(float(np.mean([nonfinite_fraction(s) for s in singles])), 8),
+                       "relmse_mean_of_frames": round(relmse(mean_img, gt), 6), "frames": frames}
+    renderer.set_cache(None)
+    # equal time: how many 1-spp plain frames fit in one cache frame's budget
+    t_plain, t_cache = out["plain"]["ms_per_frame"], out["cache"]["ms_per_frame"]
+    out["plain_frames_per_cache_frame"] = round(t_cache / t_plain, 3) if t_plain > 0 else None
+    # plain accumulated over the same device time as one cache frame
+    k = max(1, int(round(t_cache / t_plain))) if t_plain > 0 else 1
+    acc_img, _, _ = run_method(renderer, scene, cam, "plain", k, seed0=5000)
+    out["equal_time"] = {"plain_frames": k, "relmse_plain": round(relmse(acc_img, gt), 6),
+                         "relmse_cache_1spp": out["cache"]["relmse_1spp"]}
+    out["equal_time"]["cache_gain"] = round(out["equal_time"]["relmse_plain"] /
+                                            max(out["equal_time"]["relmse_cache_1spp"], 1e-12), 3)
+    cache.close()
+    return out
