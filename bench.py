@@ -237,14 +237,22 @@ def run_ours(args, d):
     clk = ClockSampler(d.local)
     clk.start()
     ms, rays, ms_b, ms_res, ms_sp = [], 0, [0.0] * NB, 0.0, 0.0
+    ms_tr, ms_sh, ms_ah = [0.0] * NB, [0.0] * NB, [0.0] * NB
+    closest, nodes, leaves = 0, 0, 0
     for s in range(args.steps):
         render(args.warmup + s, out_dev, stats)
         if stats.error_flags:
             raise RuntimeError(f"device error flags {stats.error_flags:#x}")
         ms.append(stats.ms_total)
         rays += stats.rays_closest + stats.rays_any
+        closest += stats.rays_closest
+        nodes += stats.nodes_visited
+        leaves += stats.leaves_visited
         for b in range(NB):
             ms_b[b] += stats.ms_bounce[b]
+            ms_tr[b] += stats.ms_trace[b]
+            ms_sh[b] += stats.ms_shade[b]
+            ms_ah[b] += stats.ms_anyhit[b]
         ms_res += stats.ms_resolve
         ms_sp += stats.ms_spatial
     clocks = clk.stop()
@@ -268,16 +276,35 @@ def run_ours(args, d):
     if d.rank != 0:
         d.close()
         return
-    # roofline of the dominant kernel (the bounce kernel): compulsory HBM bytes
-    # per ray-bounce (ray in/out, queue, per-bounce record, sample geometry)
+    # roofline of the dominant kernel, k_trace (closest hit): its compulsory HBM
+    # bytes are 16 B of hit record per ray plus 36 B of queue index and ray
+    # (origin, direction) for every ray after the primary one; the BVH nodes it
+    # walks stay in L1/L2 and are reported separately as traversal bytes
     hbm_peak = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm_peak else "fallback"
     hbm_peak = hbm_peak or 6800.0
-    bounce_ms = sum(ms_b)
-    bytes_per_ray = 36 + 32 + 36 + 16  # ray+queue in, record out, ray+queue out, sample geometry (avg)
-    achieved = (rays - 0) * bytes_per_ray / (bounce_ms / 1000.0) / 1e9 if bounce_ms > 0 else 0.0
+    trace_s = sum(ms_tr) / 1000.0
+    P = W * H
+    trace_bytes = 16 * closest + 36 * (closest - P * args.steps)
+    achieved = trace_bytes / trace_s / 1e9 if trace_s > 0 else 0.0
+    trav_bytes = 64 * nodes + 16 * leaves
     stream_bytes = W * H * 252  # ReSTIR compulsory stream bytes per frame (reservoirs + radiance)
     stream_gbs = stream_bytes * args.steps / ((ms_res + ms_sp) / 1000.0) / 1e9 if ms_res + ms_sp > 0 else 0.0
+    quality_block = None
+    if not args.no_quality:
+        import quality
+        qr = vrg.Renderer(ctx, W, H, 8)
+        cam = vrg.orbit_camera(NX, NZ, 0, ORBIT, W, H)
+        lt, gtl = scene.get_tlas()
+        t0 = time.perf_counter()
+        gt = quality.ground_truth(qr, scene, cam, spp=args.gt_spp, bounces=8)
+        gt_s = time.perf_counter() - t0
+        study = quality.equal_time_study(ctx, scene, qr, cam, gt, gtl[0]["min"], gtl[0]["max"], frames=16,
+                                         cache_warmup=128)
+        quality_block = {"ground_truth": {"spp": args.gt_spp, "bounces": 8, "accumulation": "fp64 on the GPU",
+                                          "seconds": round(gt_s, 2), "camera": "orbit frame 0"},
+                         "relmse_eps": quality.EPS, **study}
+        qr.close()
     cpu_mr, cpu_dt, cpu_rays = oracle_sample(world, mats, n, args.ref_rows, 1, 0) if not args.no_cpu else (None, 0, 0)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
@@ -289,19 +316,29 @@ def run_ours(args, d):
                    "m_cap": 20, "emissive_fraction": EMISSIVE, "orbit_frames": ORBIT,
                    "l2": "per-frame state (~1.2 GB of rays, records, reservoirs) exceeds L2; BVH L2-resident",
                    "parallelism": f"replicas{args.gpus}"},
-        "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b], "resolve_temporal": round(ms_res / args.steps, 4),
+        "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b],
+                         "k_trace": [round(x / args.steps, 4) for x in ms_tr],
+                         "k_shade": [round(x / args.steps, 4) for x in ms_sh],
+                         "k_anyhit": [round(x / args.steps, 4) for x in ms_ah],
+                         "resolve_temporal": round(ms_res / args.steps, 4),
                          "spatial_finalize_pack": round(ms_sp / args.steps, 4)},
         "rays_per_frame": rays // max(args.steps, 1),
         "scene_build_ms": round(build_s * 1000, 2),
-        "roofline": {"bound": "hbm", "kernel": "k_bounce", "achieved": round(achieved, 2), "peak": hbm_peak,
+        "roofline": {"bound": "hbm", "kernel": "k_trace", "achieved": round(achieved, 2), "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
-                     "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
-                     "note": "traversal is L2-latency bound; stream kernels reported in stream_roofline"},
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
+                     "algorithmic_bytes": "16 B hit per ray + 36 B ray/queue per secondary ray",
+                     "note": "k_trace is issue/latency bound: its BVH walk is served from L1/L2 (see traversal)"},
+        "traversal": {"kernel": "k_trace", "nodes_per_ray": round(nodes / max(closest, 1), 2),
+                      "leaves_per_ray": round(leaves / max(closest, 1), 2),
+                      "l1_l2_bytes_per_s_gbs": round(trav_bytes / trace_s / 1e9, 1) if trace_s > 0 else None,
+                      "grays_per_s": round(closest / trace_s / 1e9, 3) if trace_s > 0 else None},
         "stream_roofline": {"kernels": "k_resolve+k_spatial", "achieved": round(stream_gbs, 2), "peak": hbm_peak,
                             "unit": "GB/s", "frac": round(stream_gbs / hbm_peak, 4), "bytes_per_px": 252},
         "e2e": {"value": None if e2e_value is None else round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),
                 "d2h_bytes_per_step": W * H * 4},
-        "gpu_launches": (NB + 2) * args.steps,
+        "gpu_launches": (3 * NB - 1 + 2) * args.steps,
+        "quality": quality_block,
         "clocks": clocks,
         "cpu_baseline": None if cpu_mr is None else {
             "value": round(cpu_mr, 4), "unit": "Mrays/s", "cores": cpu_threads(), "kind": "port",
@@ -321,6 +358,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")
+    ap.add_argument("--no-quality", action="store_true", help="skip the FP64 ground truth / relMSE study")
+    ap.add_argument("--gt-spp", type=int, default=4096, help="ground-truth samples per pixel")
     args = ap.parse_args()
     global W, H
     if args.resolution:

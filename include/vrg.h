@@ -148,13 +148,18 @@ typedef struct vrg_frame_output {
 
 typedef struct vrg_frame_stats {
     float ms_total;            /* device time of the whole frame (CUDA events) */
-    float ms_bounce[8];        /* per bounce kernel */
-    float ms_resolve;          /* outgoing radiance + temporal */
+    float ms_bounce[8];        /* per bounce: closest hit + shading + light-pdf walk */
+    float ms_resolve;          /* outgoing radiance + temporal (+ cache inference/training) */
     float ms_spatial;          /* spatial + finalize + pack */
     uint64_t rays_closest;     /* closest-hit queries issued */
     uint64_t rays_any;         /* light any-hit queries issued */
     uint32_t error_flags;      /* device-side error word (stack overflow etc.) */
     uint32_t reserved;
+    float ms_trace[8];         /* per bounce: k_trace alone */
+    float ms_shade[8];         /* per bounce: k_shade alone */
+    float ms_anyhit[8];        /* per bounce: k_anyhit alone */
+    uint64_t nodes_visited;    /* closest-hit traversal: inner nodes fetched (64 B each) */
+    uint64_t leaves_visited;   /* closest-hit traversal: surface-block records tested (16 B each) */
 } vrg_frame_stats;
 
 typedef struct vrg_context vrg_context;

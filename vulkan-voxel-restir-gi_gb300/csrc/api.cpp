@@ -12,7 +12,7 @@
 namespace vrg {
 
 vrg_status upload_frames(cudaStream_t s);
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int grid);
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a);
@@ -360,6 +360,9 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     size_t o_cnt = o; o += al(CNT_WORDS * 4);
     size_t o_aq = o; o += al(P * 4);
     size_t o_hit = o; o += al(P * 16);
+    size_t o_hb = o; o += al(P * 2 * 32);
+    size_t o_hv = o; o += al(P * 2 * 4);
+    size_t o_jm = o; o += al(P * 8);
     size_t o_nl = o; o += al(P);
     size_t o_rec = o; o += al(P * 32 * nb);
     size_t o_xv = o; o += al(P * 16);
@@ -382,6 +385,9 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->counters = (uint32_t *)(B + o_cnt);
     r->aqueue = (uint32_t *)(B + o_aq);
     r->hits = (int4 *)(B + o_hit);
+    r->hitbuf = (uint4 *)(B + o_hb);
+    r->hitval = (float *)(B + o_hv);
+    r->jmeta = (uint2 *)(B + o_jm);
     r->nlive = B + o_nl;
     r->rec = (float4 *)(B + o_rec);
     r->xv = (float4 *)(B + o_xv);
@@ -421,6 +427,8 @@ VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_
         return st;
     }
     for (auto &e : r->ev) cudaEventCreate(&e);
+    for (auto &row : r->ev_k)
+        for (auto &e : row) cudaEventCreate(&e);
     r->grid_bounce = ctx->num_sms * bounce_blocks_per_sm();
     *out = r;
     return VRG_OK;
@@ -430,6 +438,8 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
     if (!r) return VRG_ERR_INVALID_ARGUMENT;
     cudaStreamSynchronize(r->ctx->stream);
     for (auto &e : r->ev) cudaEventDestroy(e);
+    for (auto &row : r->ev_k)
+        for (auto &e : row) cudaEventDestroy(e);
     if (r->h_pinned) cudaFreeHost(r->h_pinned);
     r->res_buf.reset();
     delete r;
@@ -605,6 +615,10 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.queue[1] = r->queue[1];
     a.aqueue = r->aqueue;
     a.hits = r->hits;
+    a.hitbuf = r->hitbuf;
+    a.hitval = r->hitval;
+    a.jmeta = r->jmeta;
+    a.hit_cap = (uint32_t)std::min<size_t>(2 * P, 0xFFFFFFF0u);
     a.counters = r->counters;
     a.nlive = r->nlive;
     a.rec = r->rec;
@@ -637,7 +651,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     int ei = 0;
     VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     for (uint32_t b = 0; b < a.nb; b++) {
-        VRG_TRY(launch_bounce(s, a, b, r->grid_bounce));
+        VRG_TRY(launch_bounce(s, a, b, r->ev_k[0][b], r->ev_k[1][b]));
         VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     }
     if (cache)  // radiance-cache queries of every path that ends into the cache
@@ -674,6 +688,12 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         for (uint32_t b = 0; b < a.nb && b < 8; b++) {
             cudaEventElapsedTime(&ms, r->ev[b], r->ev[b + 1]);
             stats->ms_bounce[b] = ms;
+            cudaEventElapsedTime(&ms, r->ev[b], r->ev_k[0][b]);
+            stats->ms_trace[b] = ms;
+            cudaEventElapsedTime(&ms, r->ev_k[0][b], r->ev_k[1][b]);
+            stats->ms_shade[b] = ms;
+            cudaEventElapsedTime(&ms, r->ev_k[1][b], r->ev[b + 1]);
+            stats->ms_anyhit[b] = ms;
         }
         cudaEventElapsedTime(&ms, r->ev[a.nb], r->ev[a.nb + 1]);
         stats->ms_resolve = ms;
@@ -686,6 +706,11 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         memcpy(&any, cnt + CNT_ANY, 8);
         stats->rays_closest = rays;
         stats->rays_any = any;
+        uint64_t nn, nlv;
+        memcpy(&nn, cnt + CNT_NODES, 8);
+        memcpy(&nlv, cnt + CNT_LEAVES, 8);
+        stats->nodes_visited = nn;
+        stats->leaves_visited = nlv;
         stats->error_flags = cnt[CNT_ERROR];
         if (cnt[CNT_ERROR]) {
             set_error("device error flags 0x%x", cnt[CNT_ERROR]);

@@ -374,7 +374,9 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
             // relative L2 loss (NRC): sum_c (y_c - t_c)^2 / (sg(mean y)^2 + 0.01), mean over the batch
             if (lane >= 16 * t && lane < 16 * t + 16) {
                 float *yr = yt + (lane - 16 * t) * NRC_OUT;
-                if (i < n) {
+                // a non-finite target (the path estimator's 0*inf cases) carries no gradient
+                const bool finite_target = isfinite(tg.x) && isfinite(tg.y) && isfinite(tg.z);
+                if (i < n && finite_target) {
                     const float m = (yr[0] + yr[1] + yr[2]) * (1.0f / 3.0f);
                     const float den = m * m + 0.01f;
                     const float e0 = yr[0] - tg.x, e1 = yr[1] - tg.y, e2 = yr[2] - tg.z;

@@ -146,7 +146,168 @@ __global__ void k_tri_inputs(const float *tris, const float *lum, uint32_t n, fl
     cen[i] = make_float4(s.x / 3.0f, s.y / 3.0f, s.z / 3.0f, lum[i]);
 }
 
+// ---- lamp-block layout of the light any-hit walk ------------------------
+// Light triangles of one block are consecutive in the light records (gen_mesh
+// order: block, face, half), so a block boundary is a change of coordinates.
+__global__ void k_lamp_flags(const int4 *rec, uint32_t n, uint32_t *flag) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 r = rec[i];
+    bool start = (i == 0);
+    if (!start) {
+        const int4 q = rec[i - 1];
+        start = (r.x != q.x) || (r.y != q.y);
+    }
+    flag[i] = start ? 1u : 0u;
+}
+
+// single-CTA inclusive scan in place; *total = sum
+__global__ void __launch_bounds__(1024) k_scan_inclusive(uint32_t *v, uint32_t n, uint32_t *total) {
+    __shared__ uint32_t sh[32];
+    __shared__ uint32_t s_carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t x = i < n ? v[i] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        if (lane == 31) sh[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t y = sh[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
+                if (lane >= o) y += t;
+            }
+            sh[lane] = y;
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        const uint32_t incl = carry + x + (w ? sh[w - 1] : 0u);
+        if (i < n) v[i] = incl;
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry = incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = s_carry;
+}
+
+__global__ void k_lamp_fill(const int4 *rec, const uint32_t *grp, uint32_t n, int4 *lamp, uint32_t *table,
+                            float4 *lo, float4 *hi, float4 *cen, uint32_t *id) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 r = rec[i];
+    const uint32_t g = grp[i] - 1u;
+    const int f = r.z & 7, h = (r.z >> 3) & 1;
+    table[12u * g + 2u * (uint32_t)f + (uint32_t)h] = (uint32_t)r.w;
+    atomicOr(&lamp[g].z, 1 << f);
+    if (i == 0 || grp[i - 1] != grp[i]) {
+        lamp[g].x = r.x;
+        lamp[g].y = r.y;
+        lamp[g].w = (int)(12u * g);
+        const float x = (float)rec_wx(r), y = (float)rec_wy(r), z = (float)rec_wz(r);
+        lo[g] = make_float4(x, y, z, 0.0f);
+        hi[g] = make_float4(x + 1.0f, y + 1.0f, z + 1.0f, 0.0f);
+        cen[g] = make_float4(x + 0.5f, y + 0.5f, z + 0.5f, 0.0f);
+        id[g] = g;
+    }
+}
+
+// traversal layout of a single-level tree whose leaf prim p is record p
+__global__ void k_wide_single(const vrg_bvh_node *nodes, const uint32_t *leaf, uint32_t n_nodes, float4 *wide) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_nodes) return;
+    const vrg_bvh_node &nd = nodes[g];
+    if (nd.left_node_idx == INVALID) return;
+    const uint32_t ch[2] = {nd.left_node_idx, nd.right_node_idx_or_prim_idx};
+    float box[2][6];
+    int ref[2];
+    for (int s = 0; s < 2; s++) {
+        const vrg_bvh_node &c = nodes[ch[s]];
+        ref[s] = c.left_node_idx != INVALID ? (int)ch[s] : ~(int)leaf[ch[s]];
+        for (int a = 0; a < 3; a++) {
+            box[s][a] = c.min[a] - BOX_MARGIN;
+            box[s][3 + a] = c.max[a] + BOX_MARGIN;
+        }
+    }
+    float4 *w = wide + 4 * (size_t)g;
+    w[0] = make_float4(box[0][0], box[0][3], box[0][1], box[0][4]);
+    w[1] = make_float4(box[0][2], box[0][5], box[1][0], box[1][3]);
+    w[2] = make_float4(box[1][1], box[1][4], box[1][2], box[1][5]);
+    w[3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), 0.0f, 0.0f);
+}
+
 }  // namespace
+
+// The light any-hit walk (nee_pdf's candidate enumeration) runs over a
+// world-space SAH BVH of the lamp blocks: a leaf tests the block's emissive
+// faces and maps the hit (face, half) to its light-BLAS leaf, so the set of
+// light triangles found is the same as walking the triangle light BVH.
+static vrg_status build_lamp_layout(Scene *sc, const int4 *light_rec, uint32_t n_light, uint32_t *depth) {
+    cudaStream_t s = sc->ctx->stream;
+    DevScene &D = sc->dev;
+    D.lamp_root = EMPTY_ROOT;
+    *depth = 0;
+    if (n_light == 0) return VRG_OK;
+    auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
+    const uint64_t n = n_light;
+    uint64_t o = 0;
+    uint64_t o_flag = o; o += al(n * 4);
+    uint64_t o_tot = o; o += 256;
+    uint64_t o_lo = o; o += al(n * 16);
+    uint64_t o_hi = o; o += al(n * 16);
+    uint64_t o_cen = o; o += al(n * 16);
+    uint64_t o_id = o; o += al(n * 4);
+    uint64_t o_perm = o; o += al(n * 4);
+    uint64_t o_nodes = o; o += al(2 * n * sizeof(vrg_bvh_node));
+    uint64_t o_leaf = o; o += al(2 * n * 4);
+    uint64_t o_rec = o; o += al(n * 16);
+    uint64_t o_tab = o; o += al(n * 12 * 4);
+    uint64_t o_wide = o; o += al(2 * n * 64);
+    DevBufPtr buf;
+    VRG_TRY(dev_alloc(s, o, buf));
+    uint8_t *B = (uint8_t *)buf->ptr;
+    uint32_t *flag = (uint32_t *)(B + o_flag), *tot = (uint32_t *)(B + o_tot);
+    int4 *lamp = (int4 *)(B + o_rec);
+    uint32_t *table = (uint32_t *)(B + o_tab);
+    VRG_CUDA_TRY(cudaMemsetAsync(lamp, 0, n * 16, s));
+    VRG_CUDA_TRY(cudaMemsetAsync(table, 0xFF, n * 48, s));
+    k_lamp_flags<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, n_light, flag);
+    k_scan_inclusive<<<1, 1024, 0, s>>>(flag, n_light, tot);
+    k_lamp_fill<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, flag, n_light, lamp, table,
+                                                           (float4 *)(B + o_lo), (float4 *)(B + o_hi),
+                                                           (float4 *)(B + o_cen), (uint32_t *)(B + o_id));
+    VRG_CUDA_TRY(cudaGetLastError());
+    uint32_t n_lamps = 0;
+    VRG_CUDA_TRY(cudaMemcpyAsync(&n_lamps, tot, 4, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<SahTree> trees{SahTree{n_lamps, 0, 0, 0}};
+    SahInputs in{(const float4 *)(B + o_lo), (const float4 *)(B + o_hi), (const float4 *)(B + o_cen),
+                 (const uint32_t *)(B + o_id)};
+    vrg_bvh_node *nodes = (vrg_bvh_node *)(B + o_nodes);
+    uint32_t *leaf = (uint32_t *)(B + o_leaf);
+    SahOutputs out{nodes, (uint32_t *)(B + o_perm), leaf};
+    uint32_t levels = 0;
+    VRG_TRY(sah_build(s, trees, n_lamps, 2 * n_lamps - 1, in, out, &levels));
+    float4 *wide = (float4 *)(B + o_wide);
+    if (n_lamps > 1) {
+        k_wide_single<<<(2 * n_lamps - 1 + 255) / 256, 256, 0, s>>>(nodes, leaf, 2 * n_lamps - 1, wide);
+        VRG_CUDA_TRY(cudaGetLastError());
+        D.lamp_root = 0;
+    } else {
+        D.lamp_root = ~0;
+    }
+    D.lamp_wide = wide;
+    D.lamp_rec = lamp;
+    D.lamp_table = table;
+    sc->lamp_buf = buf;
+    *depth = levels + 2;
+    return VRG_OK;
+}
 
 vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t *n, const uint32_t *prim_offset,
                           const uint32_t *node_offset, const float *prims, const float *translations,
@@ -314,10 +475,9 @@ vrg_status scene_commit(Scene *sc) {
     // of k_wide (wbase stays monotone: they own zero nodes), fine as is.
     auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
     uint64_t o = 0;
-    const uint64_t n_geo_wide = n_geo_tl + geo_nodes, n_light_wide = n_light_tl + light_nodes;
+    const uint64_t n_geo_wide = n_geo_tl + geo_nodes;
     uint64_t o_gw = o; o += al(n_geo_wide * 64);
     uint64_t o_gr = o; o += al(geo_recs * 16);
-    uint64_t o_lw = o; o += al(n_light_wide * 64);
     uint64_t o_lr = o; o += al(light_recs * 16);
     uint64_t o_tln = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * sizeof(vrg_bvh_node));
     uint64_t o_inst = o; o += al((uint64_t)ni * sizeof(InstDev));
@@ -388,11 +548,6 @@ vrg_status scene_commit(Scene *sc) {
                                                                    (uint32_t)n_geo_wide, (float4 *)(B + o_gw));
         VRG_CUDA_TRY(cudaGetLastError());
     }
-    if (n_light_inst) {
-        k_wide<<<(uint32_t)((n_light_wide + 255) / 256), 256, 0, s>>>(d_tl, n_light_tl, d_lb, ni,
-                                                                     (uint32_t)n_light_wide, (float4 *)(B + o_lw));
-        VRG_CUDA_TRY(cudaGetLastError());
-    }
     for (uint32_t i = 0; i < ni; i++) {
         if (gb[i].n_prims) {
             k_geo_records<<<std::min(64u, (gb[i].n_prims + 255) / 256), 256, 0, s>>>(d_gb, i, (int4 *)(B + o_gr));
@@ -406,16 +561,16 @@ vrg_status scene_commit(Scene *sc) {
     DevScene &D = sc->dev;
     D.geo_wide = (const float4 *)(B + o_gw);
     D.geo_rec = (const int4 *)(B + o_gr);
-    D.light_wide = (const float4 *)(B + o_lw);
-    D.light_rec = (const int4 *)(B + o_lr);
+
     D.light_tl = d_tl;
     D.inst = (const InstDev *)(B + o_inst);
     D.mats = (const vrg_material *)ctx->d_mats->ptr;
     D.n_inst = ni;
     auto root_of = [&](const std::vector<vrg_bvh_node> &tl, uint32_t n_tl, const std::vector<InstBuild> &ib,
                        bool light) -> vrg_status {
-        int *dst = light ? &D.light_root : &D.geo_root;
-        if (n_tl == 0 || (light && !n_light_inst)) { *dst = EMPTY_ROOT; return VRG_OK; }
+        (void)light;
+        int *dst = &D.geo_root;
+        if (n_tl == 0) { *dst = EMPTY_ROOT; return VRG_OK; }
         if (tl[0].left_node_idx != INVALID) { *dst = 0; return VRG_OK; }
         // single object: the TL root is a leaf -> its BLAS root
         uint32_t k = tl[0].right_node_idx_or_prim_idx;
@@ -428,8 +583,9 @@ vrg_status scene_commit(Scene *sc) {
         return VRG_OK;
     };
     VRG_TRY(root_of(sc->h_geo_tl, n_geo_tl, gb, false));
-    VRG_TRY(root_of(sc->h_light_tl, n_light_tl, lb, true));
-    sc->depth_bound = tl_levels + max_levels + 4;
+    uint32_t lamp_depth = 0;
+    VRG_TRY(build_lamp_layout(sc, (const int4 *)(B + o_lr), (uint32_t)light_recs, &lamp_depth));
+    sc->depth_bound = std::max(tl_levels + max_levels + 4, lamp_depth);
     if (sc->depth_bound >= (uint32_t)TRAV_STACK) {
         set_error("BVH depth bound %u exceeds the traversal stack (%d)", sc->depth_bound, TRAV_STACK);
         return VRG_ERR_UNSUPPORTED;

@@ -64,6 +64,21 @@ __device__ __forceinline__ float node_importance(f3 point, f3 normal, const floa
     f3 cc = sub3(lscl3(0.5f, add3(v000, v111)), point);
     float dist_sq = fmaxf(dot3(e, e), dot3(cc, cc));
     const float eps = NEE ? EPS_NEE : EPS_TRACE;
+    // Voxel-face normals are one of +-x, +-y, +-z: then dot(c - p, n) is
+    // exactly +-(c_a - p_a) (the other two products are +-0), so the 8 corners
+    // reduce to the box's min and max along the normal axis, 4 corners each.
+    const bool nx = normal.x != 0.0f, ny = normal.y != 0.0f, nz = normal.z != 0.0f;
+    if ((int)nx + (int)ny + (int)nz == 1) {
+        const int ax = nx ? 0 : (ny ? 1 : 2);
+        const float na = cmp3(normal, ax);
+        if (na == 1.0f || na == -1.0f) {
+            float dlo = cmp3(v000, ax) - cmp3(point, ax), dhi = cmp3(v111, ax) - cmp3(point, ax);
+            if (na < 0.0f) { dlo = -dlo; dhi = -dhi; }
+            const uint32_t visible = (dlo >= eps ? 4u : 0u) + (dhi >= eps ? 4u : 0u);
+            if (!NEE) return n.power / dist_sq * ((float)visible / 8.0f);
+            return n.power / dist_sq * ((float)visible * 0.125f);  // = the sum of 0.125 terms, exact
+        }
+    }
     f3 c[8] = {v000, f3{v000.x, v000.y, v111.z}, f3{v000.x, v111.y, v000.z}, f3{v000.x, v111.y, v111.z},
                f3{v111.x, v000.y, v000.z}, f3{v111.x, v000.y, v111.z}, f3{v111.x, v111.y, v000.z}, v111};
     if (!NEE) {
@@ -248,7 +263,7 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
     const int4 *recs = a.sc.geo_rec;
     const int root = a.sc.geo_root;
     bool has = false, exhausted = false;
-    uint32_t p = 0, steps = 0, traced = 0;
+    uint32_t p = 0, steps = 0, traced = 0, n_nodes = 0, n_leaves = 0;
     f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0};
     float best_t = 0.0f, hb1 = 0.0f, hb2 = 0.0f;
     uint64_t best_key = 0;
@@ -288,6 +303,7 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
             while (!done && node >= 0) {
                 const float4 *w = wide + 4 * (size_t)node;
                 const float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+                n_nodes++;
                 float tn0, tn1;
                 const bool h0 = slab_fma(A.x, A.y, A.z, A.w, B.x, B.y, inv, oi, EPS_TRACE, best_t, tn0);
                 const bool h1 = slab_fma(B.z, B.w, C.x, C.y, C.z, C.w, inv, oi, EPS_TRACE, best_t, tn1);
@@ -313,6 +329,7 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
             }
             if (!done) {  // leaf: the exposed faces of one surface block
                 const int4 r = __ldg(recs + (~node));
+                n_leaves++;
                 const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
                 const uint32_t mask = ((uint32_t)r.z >> 15) & 63u;
                 const uint64_t ikey = (uint64_t)rec_inst(r) << 32;
@@ -341,9 +358,16 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
             }
         }
     }
-    for (int off = 16; off; off >>= 1) traced += __shfl_xor_sync(FULL, traced, off);
-    if (lane == 0 && traced)
+    for (int off = 16; off; off >>= 1) {
+        traced += __shfl_xor_sync(FULL, traced, off);
+        n_nodes += __shfl_xor_sync(FULL, n_nodes, off);
+        n_leaves += __shfl_xor_sync(FULL, n_leaves, off);
+    }
+    if (lane == 0 && traced) {
         atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_RAYS), (unsigned long long)traced);
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_NODES), (unsigned long long)n_nodes);
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_LEAVES), (unsigned long long)n_leaves);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -569,31 +593,45 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
 }
 
 // ---------------------------------------------------------------------------
-// k_anyhit: the nee_pdf pass (nee_pdf.rs:281-337) for the queued rays: every
-// light triangle the ray crosses in [1e-4, 1000] adds its light-sampling pdf
-// (computeNeePdf, nee_pdf.rs:240-279), summed in ascending (instance, leaf)
-// order; then q and w = bsdf_pdf / q complete the bounce record.  Persistent
-// warps with per-lane job replacement, as k_trace.
+// The nee_pdf pass (nee_pdf.rs:281-337) for the queued rays, in three passes
+// so that each runs with coherent lanes:
+//   k_anyhit     every light triangle the ray crosses in [1e-4, 1000] is
+//                collected (persistent warps, per-lane job replacement), in
+//                ascending (instance, leaf) order; rays that cross none get
+//                their record here;
+//   k_hit_eval   one thread per hit: computeNeePdf (nee_pdf.rs:240-279) with
+//                its reverse walk up the light BVH;
+//   k_hit_sum    one thread per job: the sum in key order, then q and
+//                w = bsdf_pdf / q complete the bounce record.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void finish_job(const FrameArgs &a, uint32_t b, uint32_t p, float pdf, float nee) {
+    const float inv2pi = 1.0f / (2.0f * PI_F);
+    const float mis = 0.3f;
+    const float q = nee * mis + (1.0f - mis) * inv2pi;
+    const float w = pdf / q;
+    const size_t rb = (size_t)b * 2 * a.P;
+    reinterpret_cast<float *>(a.rec + rb + p)[3] = w;
+    reinterpret_cast<float *>(a.rec + rb + a.P + p)[3] = q;
+}
+
 template <bool CAPTURE>
 __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
-    const uint32_t P = a.P;
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
     uint32_t *err = a.counters + CNT_ERROR;
-    const float4 *wide = a.sc.light_wide;
-    const int4 *recs = a.sc.light_rec;
-    const int root = a.sc.light_root;
-    const float inv2pi = 1.0f / (2.0f * PI_F);
+    const float4 *wide = a.sc.lamp_wide;
+    const int4 *recs = a.sc.lamp_rec;
+    const uint32_t *table = a.sc.lamp_table;
+    const int root = a.sc.lamp_root;
     const float tmin = EPS_NEE, tmax = 1000.0f;
     bool has = false, exhausted = false;
-    uint32_t p = 0, steps = 0;
-    f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0}, n = f3{0, 0, 0};
+    uint32_t p = 0, idx = 0, steps = 0;
+    f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0};
     float pdf = 0.0f;
     int node = 0, sp = 0, nh = 0;
     int stack[TRAV_STACK];
     uint64_t keys[LIGHT_LIST];
-    float vals[LIGHT_LIST];
+    float b1s[LIGHT_LIST], b2s[LIGHT_LIST];
     if (blockIdx.x == 0 && threadIdx.x == 0 && n_in)
         atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANY), (unsigned long long)n_in);
     while (true) {
@@ -604,7 +642,7 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
             base = __shfl_sync(FULL, base, 0);
             if (base + (uint32_t)__popc(need) >= n_in) exhausted = true;
             if (!has) {
-                const uint32_t idx = base + (uint32_t)__popc(need & lanemask_lt());
+                idx = base + (uint32_t)__popc(need & lanemask_lt());
                 if (idx < n_in) {
                     has = true;
                     p = a.aqueue[idx];
@@ -612,7 +650,6 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
                     o = ld3(ro);
                     d = ld3(rd);
                     pdf = rd.w;
-                    n = c_frames[2 * __float_as_int(ro.w)].n;
                     inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
                     node = root;
@@ -650,19 +687,28 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
                     done = true;
                 }
             }
-            if (!done) {  // leaf: one light triangle
+            if (!done) {  // leaf: one lamp block; each emissive face hit names one light triangle
                 const int4 r = __ldg(recs + (~node));
-                const int f = r.z & 7, hh = (r.z >> 3) & 1;
-                FaceHit fh;
-                if (face_test(rec_wx(r), rec_wy(r), rec_wz(r), f, o, d, inv, tmin, tmax, fh) && fh.half == hh) {
-                    const uint32_t ii = rec_inst(r), leaf = (uint32_t)r.w;
-                    const float v = nee_pdf_of(a.sc, o, n, d, ii, leaf, fh.b1, fh.b2);
+                const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
+                const uint32_t ii = rec_inst(r);
+                for (uint32_t fm = (uint32_t)r.z; fm; fm &= fm - 1u) {
+                    const int f = __ffs(fm) - 1;
+                    FaceHit fh;
+                    if (!face_test(wx, wy, wz, f, o, d, inv, tmin, tmax, fh)) continue;
+                    const uint32_t leaf = __ldg(table + r.w + 2 * f + fh.half);
+                    if (leaf == INVALID) continue;
                     const uint64_t key = ((uint64_t)ii << 32) | leaf;
                     if (nh < LIGHT_LIST) {
                         int j = nh++;
-                        while (j > 0 && keys[j - 1] > key) { keys[j] = keys[j - 1]; vals[j] = vals[j - 1]; j--; }
+                        while (j > 0 && keys[j - 1] > key) {
+                            keys[j] = keys[j - 1];
+                            b1s[j] = b1s[j - 1];
+                            b2s[j] = b2s[j - 1];
+                            j--;
+                        }
                         keys[j] = key;
-                        vals[j] = v;
+                        b1s[j] = fh.b1;
+                        b2s[j] = fh.b2;
                     } else {
                         atomicOr(err, ERR_LIGHT_LIST);
                     }
@@ -671,18 +717,53 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
                 else node = stack[--sp];
             }
             if (done) {
-                float nee = 0.0f;
-                for (int j = 0; j < nh; j++) nee += vals[j];
-                const float mis = 0.3f;
-                const float q = nee * mis + (1.0f - mis) * inv2pi;
-                const float w = pdf / q;
-                const size_t rb = (size_t)b * 2 * P;
-                reinterpret_cast<float *>(a.rec + rb + p)[3] = w;
-                reinterpret_cast<float *>(a.rec + rb + P + p)[3] = q;
-                if (CAPTURE) a.c_nee[(size_t)b * P + p] = nee;
+                uint32_t hb = 0;
+                if (nh > 0) {
+                    hb = atomicAdd(&a.counters[CNT_HITS], (uint32_t)nh);
+                    if (hb + (uint32_t)nh > a.hit_cap) {
+                        atomicOr(err, ERR_LIGHT_LIST);
+                        nh = 0;
+                    }
+                }
+                if (nh == 0) {
+                    finish_job(a, b, p, pdf, 0.0f);
+                    if (CAPTURE) a.c_nee[(size_t)b * a.P + p] = 0.0f;
+                } else {
+                    for (int j = 0; j < nh; j++) {
+                        a.hitbuf[2 * (size_t)(hb + j)] =
+                            make_uint4(p, (uint32_t)(keys[j] >> 32), (uint32_t)keys[j], __float_as_uint(b1s[j]));
+                        a.hitbuf[2 * (size_t)(hb + j) + 1] = make_uint4(__float_as_uint(b2s[j]), 0u, 0u, 0u);
+                    }
+                }
+                a.jmeta[idx] = make_uint2(hb, (uint32_t)nh);
                 has = false;
             }
         }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_hit_eval(FrameArgs a) {
+    const uint32_t n = min(a.counters[CNT_HITS], a.hit_cap);
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
+        const uint4 A = a.hitbuf[2 * (size_t)h], B = a.hitbuf[2 * (size_t)h + 1];
+        const uint32_t p = A.x;
+        const float4 ro = a.ray_o[p], rd = a.ray_d[p];
+        const f3 n3 = c_frames[2 * __float_as_int(ro.w)].n;
+        a.hitval[h] = nee_pdf_of(a.sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
+    }
+}
+
+template <bool CAPTURE>
+__global__ void __launch_bounds__(128) k_hit_sum(FrameArgs a, uint32_t b) {
+    const uint32_t n_in = a.counters[CNT_AQUEUE + b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += gridDim.x * blockDim.x) {
+        const uint2 m = a.jmeta[i];
+        if (m.y == 0) continue;
+        const uint32_t p = a.aqueue[i];
+        float nee = 0.0f;
+        for (uint32_t j = 0; j < m.y; j++) nee += a.hitval[m.x + j];
+        finish_job(a, b, p, a.ray_d[p].w, nee);
+        if (CAPTURE) a.c_nee[(size_t)b * a.P + p] = nee;
     }
 }
 
@@ -705,7 +786,7 @@ static int occupancy_grid(const void *fn, int threads) {
 }
 
 // One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int /*grid*/) {
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade) {
     static int g_trace = 0, g_shade = 0, g_any = 0;
     if (!g_trace) {
         g_trace = occupancy_grid((const void *)k_trace, 128);
@@ -713,11 +794,17 @@ vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, int /*g
         g_any = occupancy_grid((const void *)k_anyhit<false>, 128);
     }
     k_trace<<<g_trace, 128, 0, s>>>(a, b);
+    if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
     if (a.capture) k_shade<true><<<g_shade, 128, 0, s>>>(a, b);
     else k_shade<false><<<g_shade, 128, 0, s>>>(a, b);
+    if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
     if (b + 1 < a.nb) {
         if (a.capture) k_anyhit<true><<<g_any, 128, 0, s>>>(a, b);
         else k_anyhit<false><<<g_any, 128, 0, s>>>(a, b);
+        k_hit_eval<<<g_shade, 128, 0, s>>>(a);
+        if (a.capture) k_hit_sum<true><<<g_shade, 128, 0, s>>>(a, b);
+        else k_hit_sum<false><<<g_shade, 128, 0, s>>>(a, b);
+        VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
     }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;

@@ -195,7 +195,7 @@ __host__ __device__ inline Frame face_frame(int f, int h) {
 //   y = (wy & 0xFFFF) | instance << 16
 //   z = chunk-local block index (15 bits) | face_mask << 15 | block id << 21
 //   w = first triangle index of the block in the chunk's gen_mesh order
-// Light record (one per light triangle), 16 bytes:
+// Light record (one per light triangle, scene build only), 16 bytes:
 //   x, y as above; z = face | half << 3; w = light BLAS leaf node index
 __host__ __device__ __forceinline__ int rec_wx(int4 r) { return (int)(short)(r.x & 0xFFFF); }
 __host__ __device__ __forceinline__ int rec_wz(int4 r) { return r.x >> 16; }
@@ -213,9 +213,10 @@ struct DevScene {
     const float4 *geo_wide;   // 4 float4 per node: child boxes (world, +margin) and child refs
     const int4 *geo_rec;
     int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
-    const float4 *light_wide;
-    const int4 *light_rec;
-    int light_root;
+    const float4 *lamp_wide;  // any-hit layout over lamp blocks (world space, +margin)
+    const int4 *lamp_rec;     // per lamp block: x/y packed coords + instance, z emissive face mask, w table base
+    const uint32_t *lamp_table;  // 12 per lamp block: light-BLAS leaf of (face, half), INVALID if none
+    int lamp_root;
     const vrg_bvh_node *light_tl;  // reference-format light TL BVH (dummy node if no light)
     const InstDev *inst;
     const vrg_material *mats;

@@ -14,6 +14,9 @@ constexpr int CNT_ANY = 20;      // u64 at words 20-21: light any-hit queries
 constexpr int CNT_AQUEUE = 24;   // [24..31] any-hit jobs queued by bounce b
 constexpr int CNT_AFETCH = 32;   // [32..39] any-hit work-fetch cursor of bounce b
 constexpr int CNT_SFETCH = 40;   // [40..47] shading work-fetch cursor of bounce b
+constexpr int CNT_NODES = 50;    // u64 at words 50-51: inner nodes fetched by k_trace
+constexpr int CNT_LEAVES = 52;   // u64 at words 52-53: leaf records tested by k_trace
+constexpr int CNT_HITS = 54;     // light hits collected by k_anyhit for the current bounce
 constexpr int CNT_INFER = 48;    // radiance-cache queries of the frame
 constexpr int CNT_TRAIN = 49;    // radiance-cache training paths of the frame
 constexpr int CNT_WORDS = 64;
@@ -31,6 +34,10 @@ struct FrameArgs {
     float4 *ray_o, *ray_d;
     uint32_t *queue[2];
     uint32_t *aqueue;             // any-hit jobs of the current bounce
+    uint4 *hitbuf;                // light hits: (pixel, instance, leaf, b1 bits), then (b2 bits, 0, 0, 0)
+    float *hitval;                // light-sampling pdf of each hit
+    uint2 *jmeta;                 // per any-hit job: (first hit, hit count)
+    uint32_t hit_cap;
     int4 *hits;                   // closest hit per pixel: (~record or -1, face|half<<3, b1, b2)
     uint32_t *counters;
     uint8_t *nlive;

@@ -132,6 +132,7 @@ struct Scene {
     std::vector<Object *> inst_objs;      // instance order (key order, non-empty)
     std::vector<std::array<float, 3>> inst_off;
     DevBufPtr d_buf;                      // wide layouts, records, TLs, instance table
+    DevBufPtr lamp_buf;                   // lamp-block any-hit layout
     DevScene dev{};
     std::vector<vrg_bvh_node> h_light_tl, h_geo_tl;
     uint32_t depth_bound = 0;
@@ -177,6 +178,9 @@ struct Renderer {
     uint32_t *counters = nullptr;         // CNT_* words of vrg_frame.cuh
     uint32_t *aqueue = nullptr;           // any-hit job queue
     int4 *hits = nullptr;                 // closest hit per pixel
+    uint4 *hitbuf = nullptr;              // light hits of the any-hit pass
+    float *hitval = nullptr;
+    uint2 *jmeta = nullptr;
     uint8_t *nlive = nullptr;
     float4 *rec = nullptr;                // [nb][2][P]
     float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
@@ -198,6 +202,7 @@ struct Renderer {
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
     cudaEvent_t ev[16] = {};
+    cudaEvent_t ev_k[2][8] = {};          // after k_trace / after k_shade, per bounce
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
     DevBufPtr cache_buf;                  // per-pixel cache queries / predictions / targets
     float4 *q_pos = nullptr, *q_dir = nullptr, *pred = nullptr, *target = nullptr;

@@ -86,7 +86,9 @@ class FrameOutput(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("ms_total", C.c_float), ("ms_bounce", C.c_float * 8), ("ms_resolve", C.c_float),
                 ("ms_spatial", C.c_float), ("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
-                ("error_flags", C.c_uint32), ("reserved", C.c_uint32)]
+                ("error_flags", C.c_uint32), ("reserved", C.c_uint32), ("ms_trace", C.c_float * 8),
+                ("ms_shade", C.c_float * 8), ("ms_anyhit", C.c_float * 8), ("nodes_visited", C.c_uint64),
+                ("leaves_visited", C.c_uint64)]
 
 
 _lib = None
