@@ -287,7 +287,7 @@ def run_ours(args, d):
     P = W * H
     trace_bytes = 16 * closest + 36 * (closest - P * args.steps)
     achieved = trace_bytes / trace_s / 1e9 if trace_s > 0 else 0.0
-    trav_bytes = 64 * nodes + 16 * leaves
+    trav_bytes = 128 * nodes + 16 * leaves  # 4-wide nodes (128 B) and surface-block records (16 B)
     stream_bytes = W * H * 252  # ReSTIR compulsory stream bytes per frame (reservoirs + radiance)
     stream_gbs = stream_bytes * args.steps / ((ms_res + ms_sp) / 1000.0) / 1e9 if ms_res + ms_sp > 0 else 0.0
     quality_block = None

@@ -130,9 +130,10 @@ typedef struct vrg_render_params {
 
 #define VRG_RENDER_CAPTURE 1u      /* keep the full per-bounce SoA for vrg_debug_readback */
 #define VRG_RENDER_NO_PACK 2u      /* skip the u8 pack (radiance output only) */
-#define VRG_RENDER_CACHE 4u        /* terminate paths into the attached radiance cache after the
-                                      first bounce; 1/16 of the paths trace cache_train_bounces
-                                      more bounces and train the cache (no ReSTIR) */
+#define VRG_RENDER_CACHE 4u        /* terminate paths into the attached radiance cache after
+                                      num_bounces-1 bounces; 1/16 of the paths trace
+                                      cache_train_bounces more bounces and train the cache; ReSTIR
+                                      then resamples the cache-terminated samples */
 #define VRG_RENDER_PLAIN_ONLY 8u   /* skip the ReSTIR stages (plain path tracer, view 0) */
 
 /* Where the frame goes.  Pointers may be NULL (not written).  host != 0 means

@@ -590,7 +590,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.nb_render = pr->num_bounces;
     a.cache = cache ? 1u : 0u;
     a.train_cap = cache ? nrc_batch(r->cache) : 0u;
-    a.restir = (cache || (pr->flags & VRG_RENDER_PLAIN_ONLY)) ? 0u : 1u;
+    a.restir = (pr->flags & VRG_RENDER_PLAIN_ONLY) ? 0u : 1u;
     a.q_pos = r->q_pos;
     a.q_dir = r->q_dir;
     a.pred = r->pred;

@@ -86,6 +86,115 @@ __global__ void k_wide(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *i
     w[3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), 0.0f, 0.0f);
 }
 
+// 4-wide traversal node for every inner node g of the combined index space:
+// g's children, with each inner child replaced by its own two children
+// (so inner children of a 4-wide node are nodes two levels down).  Layout
+// (8 float4): lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], refs[4], pad.
+// Unused slots hold ref EMPTY_ROOT (skipped by the walk) and a box at +inf.
+struct ChildRef {
+    const vrg_bvh_node *node;
+    float off[3];
+    int ref;        // node / ~record
+    int inner;      // combined index of an inner child (to expand), -1 otherwise
+    int k;          // instance of a BLAS child, -1 for top level
+};
+
+__device__ __forceinline__ void child_of(const vrg_bvh_node *tl, const InstBuild *inst, int k, uint32_t c,
+                                         ChildRef &out) {
+    out.off[0] = out.off[1] = out.off[2] = 0.0f;
+    if (k < 0) {
+        const vrg_bvh_node *n = &tl[c];
+        if (n->left_node_idx != INVALID) {
+            out.node = n;
+            out.ref = (int)c;
+            out.inner = (int)c;
+            out.k = -1;
+            return;
+        }
+        // a top-level leaf stands for its object's BLAS root (translated)
+        const int kk = (int)n->right_node_idx_or_prim_idx;
+        const InstBuild &I = inst[kk];
+        out.node = &I.bl[0];
+        out.off[0] = I.off[0]; out.off[1] = I.off[1]; out.off[2] = I.off[2];
+        out.k = kk;
+        if (I.bl[0].left_node_idx != INVALID) {
+            out.ref = (int)I.wbase;
+            out.inner = (int)I.wbase;
+        } else {
+            out.ref = ~(int)(I.rbase + I.leaf[0]);
+            out.inner = -1;
+        }
+        return;
+    }
+    const InstBuild &I = inst[k];
+    out.node = &I.bl[c];
+    out.off[0] = I.off[0]; out.off[1] = I.off[1]; out.off[2] = I.off[2];
+    out.k = k;
+    if (out.node->left_node_idx != INVALID) {
+        out.ref = (int)(I.wbase + c);
+        out.inner = (int)(I.wbase + c);
+    } else {
+        out.ref = ~(int)(I.rbase + I.leaf[c]);
+        out.inner = -1;
+    }
+}
+
+__global__ void k_wide4(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *inst, uint32_t n_inst,
+                        uint32_t n_total, float4 *wide4) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_total) return;
+    int k = -1;
+    const vrg_bvh_node *node;
+    if (g < n_tl) {
+        node = &tl[g];
+    } else {
+        int lo = 0, hi = (int)n_inst - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (inst[mid].wbase <= g) lo = mid; else hi = mid - 1;
+        }
+        k = lo;
+        node = &inst[k].bl[g - inst[k].wbase];
+    }
+    if (node->left_node_idx == INVALID) return;
+    ChildRef lv1[2], out[4];
+    child_of(tl, inst, k, node->left_node_idx, lv1[0]);
+    child_of(tl, inst, k, node->right_node_idx_or_prim_idx, lv1[1]);
+    int n = 0;
+    for (int s = 0; s < 2; s++) {
+        if (lv1[s].inner >= 0) {
+            const vrg_bvh_node *c = lv1[s].node;
+            child_of(tl, inst, lv1[s].k, c->left_node_idx, out[n++]);
+            child_of(tl, inst, lv1[s].k, c->right_node_idx_or_prim_idx, out[n++]);
+        } else {
+            out[n++] = lv1[s];
+        }
+    }
+    float b[6][4];
+    int refs[4];
+    for (int i = 0; i < 4; i++) {
+        if (i < n) {
+            const vrg_bvh_node *c = out[i].node;
+            for (int a = 0; a < 3; a++) {
+                b[2 * a][i] = (c->min[a] + out[i].off[a]) - BOX_MARGIN;
+                b[2 * a + 1][i] = (c->max[a] + out[i].off[a]) + BOX_MARGIN;
+            }
+            refs[i] = out[i].ref;
+        } else {
+            for (int a = 0; a < 3; a++) {
+                b[2 * a][i] = INFINITY;
+                b[2 * a + 1][i] = INFINITY;
+            }
+            refs[i] = EMPTY_ROOT;
+        }
+    }
+    float4 *w = wide4 + 8 * (size_t)g;
+    for (int r = 0; r < 6; r++) w[r] = make_float4(b[r][0], b[r][1], b[r][2], b[r][3]);
+    w[6] = make_float4(__int_as_float(refs[0]), __int_as_float(refs[1]), __int_as_float(refs[2]),
+                       __int_as_float(refs[3]));
+    w[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void k_geo_records(const InstBuild *inst, uint32_t k, int4 *rec) {
     const InstBuild I = inst[k];
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < I.n_prims; p += gridDim.x * blockDim.x) {
@@ -476,7 +585,7 @@ vrg_status scene_commit(Scene *sc) {
     auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
     uint64_t o = 0;
     const uint64_t n_geo_wide = n_geo_tl + geo_nodes;
-    uint64_t o_gw = o; o += al(n_geo_wide * 64);
+    uint64_t o_gw = o; o += al(n_geo_wide * 128);
     uint64_t o_gr = o; o += al(geo_recs * 16);
     uint64_t o_lr = o; o += al(light_recs * 16);
     uint64_t o_tln = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * sizeof(vrg_bvh_node));
@@ -544,8 +653,8 @@ vrg_status scene_commit(Scene *sc) {
     const InstBuild *d_gb = (const InstBuild *)(B + o_gb), *d_lb = (const InstBuild *)(B + o_lb);
     // wide layouts + records
     if (n_geo_wide) {
-        k_wide<<<(uint32_t)((n_geo_wide + 255) / 256), 256, 0, s>>>(d_tl + n_light_tl, n_geo_tl, d_gb, ni,
-                                                                   (uint32_t)n_geo_wide, (float4 *)(B + o_gw));
+        k_wide4<<<(uint32_t)((n_geo_wide + 255) / 256), 256, 0, s>>>(d_tl + n_light_tl, n_geo_tl, d_gb, ni,
+                                                                    (uint32_t)n_geo_wide, (float4 *)(B + o_gw));
         VRG_CUDA_TRY(cudaGetLastError());
     }
     for (uint32_t i = 0; i < ni; i++) {
@@ -585,7 +694,8 @@ vrg_status scene_commit(Scene *sc) {
     VRG_TRY(root_of(sc->h_geo_tl, n_geo_tl, gb, false));
     uint32_t lamp_depth = 0;
     VRG_TRY(build_lamp_layout(sc, (const int4 *)(B + o_lr), (uint32_t)light_recs, &lamp_depth));
-    sc->depth_bound = std::max(tl_levels + max_levels + 4, lamp_depth);
+    // the 4-wide walk pushes up to 3 refs per 4-wide level (half the binary depth)
+    sc->depth_bound = std::max(3 * ((tl_levels + max_levels + 4 + 1) / 2) + 1, lamp_depth);
     if (sc->depth_bound >= (uint32_t)TRAV_STACK) {
         set_error("BVH depth bound %u exceeds the traversal stack (%d)", sc->depth_bound, TRAV_STACK);
         return VRG_ERR_UNSUPPORTED;

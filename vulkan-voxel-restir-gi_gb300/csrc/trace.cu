@@ -245,6 +245,36 @@ __device__ __forceinline__ bool slab_fma(float lox, float hix, float loy, float 
     return tn <= tf;
 }
 
+__device__ __forceinline__ void cswap(float &ta, int &ra, float &tb, int &rb) {
+    if (tb < ta) {
+        const float t = ta; ta = tb; tb = t;
+        const int r = ra; ra = rb; rb = r;
+    }
+}
+
+// slab test of the 4 children of a 4-wide node; returns the entry distances
+// sorted ascending (+inf for a miss) with their refs
+__device__ __forceinline__ void slab4(float4 LX, float4 HX, float4 LY, float4 HY, float4 LZ, float4 HZ, float4 RF,
+                                      f3 inv, f3 oi, float tmin, float tmax, float tk[4], int rk[4]) {
+    const float lx[4] = {LX.x, LX.y, LX.z, LX.w}, hx[4] = {HX.x, HX.y, HX.z, HX.w};
+    const float ly[4] = {LY.x, LY.y, LY.z, LY.w}, hy[4] = {HY.x, HY.y, HY.z, HY.w};
+    const float lz[4] = {LZ.x, LZ.y, LZ.z, LZ.w}, hz[4] = {HZ.x, HZ.y, HZ.z, HZ.w};
+    const int rf[4] = {__float_as_int(RF.x), __float_as_int(RF.y), __float_as_int(RF.z), __float_as_int(RF.w)};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float tn;
+        const bool h = slab_fma(lx[i], hx[i], ly[i], hy[i], lz[i], hz[i], inv, oi, tmin, tmax, tn);
+        tk[i] = (h && rf[i] != EMPTY_ROOT) ? tn : INFINITY;  // unused slots never enter the walk
+        rk[i] = rf[i];
+    }
+    // sorting network for 4
+    cswap(tk[0], rk[0], tk[1], rk[1]);
+    cswap(tk[2], rk[2], tk[3], rk[3]);
+    cswap(tk[0], rk[0], tk[2], rk[2]);
+    cswap(tk[1], rk[1], tk[3], rk[3]);
+    cswap(tk[1], rk[1], tk[2], rk[2]);
+}
+
 // ---------------------------------------------------------------------------
 // k_trace: closest hit over the voxel faces (replaces getIntersectionInfo,
 // raytrace.rs:354-388).  Persistent warps; each lane owns one ray and, when
@@ -299,28 +329,28 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
         if (!__any_sync(FULL, has)) break;
         if (has) {
             bool done = (node == EMPTY_ROOT);
-            // descend through inner nodes to the next leaf
+            // descend through 4-wide inner nodes to the next leaf
             while (!done && node >= 0) {
-                const float4 *w = wide + 4 * (size_t)node;
-                const float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+                const float4 *w = wide + 8 * (size_t)node;
+                const float4 LX = __ldg(w), HX = __ldg(w + 1), LY = __ldg(w + 2), HY = __ldg(w + 3);
+                const float4 LZ = __ldg(w + 4), HZ = __ldg(w + 5), RF = __ldg(w + 6);
                 n_nodes++;
-                float tn0, tn1;
-                const bool h0 = slab_fma(A.x, A.y, A.z, A.w, B.x, B.y, inv, oi, EPS_TRACE, best_t, tn0);
-                const bool h1 = slab_fma(B.z, B.w, C.x, C.y, C.z, C.w, inv, oi, EPS_TRACE, best_t, tn1);
-                const int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
-                if (h0 && h1) {
-                    const bool swap = tn1 < tn0;
-                    if (sp < TRAV_STACK) stack[sp++] = swap ? r0 : r1;
-                    else atomicOr(err, ERR_STACK);
-                    node = swap ? r1 : r0;
-                } else if (h0) {
-                    node = r0;
-                } else if (h1) {
-                    node = r1;
-                } else if (sp == 0) {
-                    done = true;
+                float tk[4];
+                int rk[4];
+                slab4(LX, HX, LY, HY, LZ, HZ, RF, inv, oi, EPS_TRACE, best_t, tk, rk);
+                // tk sorted ascending (misses at +inf)
+                if (tk[0] == INFINITY) {
+                    if (sp == 0) done = true;
+                    else node = stack[--sp];
                 } else {
-                    node = stack[--sp];
+                    node = rk[0];
+                    if (sp + 3 <= TRAV_STACK) {
+                        if (tk[3] != INFINITY) stack[sp++] = rk[3];
+                        if (tk[2] != INFINITY) stack[sp++] = rk[2];
+                        if (tk[1] != INFINITY) stack[sp++] = rk[1];
+                    } else {
+                        atomicOr(err, ERR_STACK);
+                    }
                 }
                 if (++steps > TRAV_GUARD) {  // only reachable with a malformed layout
                     atomicOr(err, ERR_GUARD);

@@ -210,7 +210,7 @@ struct InstDev {
 };
 
 struct DevScene {
-    const float4 *geo_wide;   // 4 float4 per node: child boxes (world, +margin) and child refs
+    const float4 *geo_wide;   // 8 float4 per node: 4-wide child boxes (world, +margin, SoA) and refs
     const int4 *geo_rec;
     int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
     const float4 *lamp_wide;  // any-hit layout over lamp blocks (world space, +margin)
@@ -224,7 +224,7 @@ struct DevScene {
 };
 
 constexpr int EMPTY_ROOT = (int)0x80000000;
-constexpr int TRAV_STACK = 64;
+constexpr int TRAV_STACK = 96;
 constexpr uint32_t ERR_STACK = 1u;
 constexpr uint32_t ERR_LIGHT_LIST = 2u;
 constexpr uint32_t ERR_GUARD = 4u;

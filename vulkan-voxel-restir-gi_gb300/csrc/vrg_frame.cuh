@@ -52,7 +52,7 @@ struct FrameArgs {
     double *accum;
     // radiance cache (VRG_RENDER_CACHE): paths end into the cache after
     // nb_render bounces; 1/16 of them (up to train_cap) trace to nb and train it
-    uint32_t nb_render, cache, train_cap, restir;
+    uint32_t nb_render, cache, train_cap, restir;  // restir: run the ReSTIR stages
     float4 *q_pos, *q_dir, *pred, *target;
     uint32_t *infer_list, *train_list;
     uint8_t *qflag;
