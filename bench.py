@@ -166,6 +166,75 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
     return rays / dt / 1e6, dt, rays
 
 
+C2_SEED = 20240602
+C2_SCENES = 64
+C2_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
+
+
+def batched_block(ctx, steps, warmup):
+    """Batched workload: 64 independent scenes, chunk grids drawn from 1x1..8x8
+    and resolutions from {256^2, 640x480, 1280x720, 1920x1080}, each with its
+    own terrain seed and orbit camera, 2 bounces + ReSTIR (1 temporal, 3
+    spatial, 30 px, M-cap 20).  All chunks of all scenes are built by one
+    batched BLAS build; one step = one frame of every view, replayed from a
+    CUDA graph (device time from events around the graph launch), next to the
+    same frames issued as plain launches."""
+    import vrg
+    rng = np.random.default_rng(C2_SEED)
+    grids = rng.integers(1, 9, size=(C2_SCENES, 2))
+    res = [C2_RES[i] for i in rng.integers(0, len(C2_RES), size=C2_SCENES)]
+    scenes, keep = [], []
+    t0 = time.perf_counter()
+    for i in range(C2_SCENES):
+        nx, nz = int(grids[i, 0]), int(grids[i, 1])
+        blocks = vrg.terrain_blocks(C2_SEED + 1 + i, nx, nz, EMISSIVE)
+        sc, objs = vrg.build_world(ctx, blocks)
+        scenes.append(sc)
+        keep.append(objs)
+    t_upload = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.flush()  # every chunk of every scene: one batched extraction + BLAS build
+    t_blas = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for sc in scenes:
+        sc.commit()
+    t_tl = time.perf_counter() - t0
+    br = vrg.BatchRenderer(ctx, res, 2)
+    seeds = vrg.Pcg32(C2_SEED)
+
+    def step(f, flags):
+        cams = [vrg.orbit_camera(int(grids[i, 0]), int(grids[i, 1]), f % ORBIT, ORBIT, w, h)
+                for i, (w, h) in enumerate(res)]
+        p = vrg.RenderParams(1, 1, 3, 2, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, 0, flags | vrg.RENDER_NO_PACK, 4)
+        br.render(scenes, cams, p, [(seeds.next(), seeds.next()) for _ in res])
+        st = br.last_stats
+        if st.error_flags:
+            raise RuntimeError(f"device error flags {st.error_flags:#x}")
+        return st.ms_total, st.rays_closest + st.rays_any
+
+    out = {"workload": "batched-64-scenes", "scenes": C2_SCENES, "pixels": br.pixels,
+           "chunks": int((grids[:, 0] * grids[:, 1]).sum()), "bounces": 2,
+           "resolutions": {f"{w}x{h}": sum(1 for r in res if r == (w, h)) for w, h in C2_RES},
+           "upload_s": round(t_upload, 3), "blas_build_ms": round(1000 * t_blas, 2),
+           "tl_commit_ms": round(1000 * t_tl, 2)}
+    for name, flags in (("graph", vrg.RENDER_GRAPH), ("launches", 0)):
+        for f in range(warmup):
+            step(f, flags)
+        ms, rays = 0.0, 0
+        t0 = time.perf_counter()
+        for s_ in range(steps):
+            m, r_ = step(warmup + s_, flags)
+            ms += m
+            rays += r_
+        wall = time.perf_counter() - t0
+        out[name] = {"mrays_s": round(rays / (ms / 1000.0) / 1e6, 3), "ms_per_step": round(ms / steps, 4),
+                     "wall_ms_per_step": round(1000 * wall / steps, 3), "rays_per_step": rays // steps}
+    br.close()
+    for sc in scenes:
+        sc.close()
+    return out
+
+
 def run_reference(args, d):
     import vrg
     if d.rank != 0:
@@ -305,6 +374,10 @@ def run_ours(args, d):
                                           "seconds": round(gt_s, 2), "camera": "orbit frame 0"},
                          "relmse_eps": quality.EPS, **study}
         qr.close()
+    batched = None
+    if not args.no_batched:
+        r.close()  # the batch needs the memory of the 1080p renderer
+        batched = batched_block(ctx, steps=16, warmup=3)
     cpu_mr, cpu_dt, cpu_rays = oracle_sample(world, mats, n, args.ref_rows, 1, 0) if not args.no_cpu else (None, 0, 0)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
@@ -339,6 +412,7 @@ def run_ours(args, d):
                 "d2h_bytes_per_step": W * H * 4},
         "gpu_launches": (3 * NB - 1 + 2) * args.steps,
         "quality": quality_block,
+        "batched": batched,
         "clocks": clocks,
         "cpu_baseline": None if cpu_mr is None else {
             "value": round(cpu_mr, 4), "unit": "Mrays/s", "cores": cpu_threads(), "kind": "port",
@@ -360,6 +434,7 @@ def main():
     ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")
     ap.add_argument("--no-quality", action="store_true", help="skip the FP64 ground truth / relMSE study")
     ap.add_argument("--gt-spp", type=int, default=4096, help="ground-truth samples per pixel")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched workload")
     args = ap.parse_args()
     global W, H
     if args.resolution:

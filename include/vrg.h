@@ -135,6 +135,8 @@ typedef struct vrg_render_params {
                                       cache_train_bounces more bounces and train the cache; ReSTIR
                                       then resamples the cache-terminated samples */
 #define VRG_RENDER_PLAIN_ONLY 8u   /* skip the ReSTIR stages (plain path tracer, view 0) */
+#define VRG_RENDER_GRAPH 16u       /* batched frames: record the frame's launch sequence once
+                                      in a CUDA graph and replay it (see vrg_render_batched) */
 
 /* Where the frame goes.  Pointers may be NULL (not written).  host != 0 means
  * the pointers are host memory and the library copies the frame back before
@@ -159,7 +161,7 @@ typedef struct vrg_frame_stats {
     float ms_trace[8];         /* per bounce: k_trace alone */
     float ms_shade[8];         /* per bounce: k_shade alone */
     float ms_anyhit[8];        /* per bounce: k_anyhit alone */
-    uint64_t nodes_visited;    /* closest-hit traversal: inner nodes fetched (64 B each) */
+    uint64_t nodes_visited;    /* closest-hit traversal: 4-wide inner nodes fetched (128 B each) */
     uint64_t leaves_visited;   /* closest-hit traversal: surface-block records tested (16 B each) */
 } vrg_frame_stats;
 
@@ -251,6 +253,44 @@ enum {
     VRG_DBG_FINAL, VRG_DBG_COUNT
 };
 VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes);
+
+/* ---- batched views (no reference counterpart: the reference renders one
+ * swapchain view per Renderer::render) ------------------------------------
+ * A batched renderer owns n_views views of independent extents; one
+ * vrg_render_batched call renders every view, each of its own scene and
+ * camera, through ONE wavefront launch sequence: the views' pixels are
+ * numbered view after view (view v starts at pixel_offset(v)), every kernel
+ * looks up its pixel's view, and the queues are shared, so small views do
+ * not leave the GPU idle.  A view renders exactly the image that a
+ * single-view renderer of its extent renders with the same scene, camera,
+ * seeds and frame index.  Per-view data (scene BVHs, cameras, seeds, frame
+ * index) lives in a device table refreshed at the start of every call, so
+ * with VRG_RENDER_GRAPH the launch sequence is recorded once in a CUDA graph
+ * (one per history-ring slot and parameter set; a change of num_bounces,
+ * flags or the other parameters records a new one) and replayed.
+ * VRG_RENDER_GRAPH cannot be combined with VRG_RENDER_CACHE or
+ * VRG_RENDER_CAPTURE (VRG_ERR_UNSUPPORTED); the stats of a graph frame carry
+ * ms_total and the counters, not the per-kernel times. */
+typedef struct vrg_view {
+    vrg_scene *scene;          /* committed by the call if dirty (all views' scenes
+                                  are committed before any view renders) */
+    vrg_camera camera;         /* width/height must equal the view's extent */
+    uint32_t temporal_seed;    /* this view's ReSTIR seeds (the params' seeds are unused) */
+    uint32_t spatial_seed;
+} vrg_view;
+
+VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_views, const uint32_t *widths,
+                                               const uint32_t *heights, uint32_t max_bounces,
+                                               vrg_renderer **out);
+/* Pixel offset of a view in the batch's pixel numbering (0 for a single-view renderer). */
+VRG_API vrg_status vrg_renderer_view_offset(vrg_renderer *r, uint32_t view, uint64_t *pixel_offset);
+/* Renders all views.  outs: NULL or n_views entries (per view, like
+ * vrg_render's out; host or device pointers).  vrg_renderer_read_accumulation
+ * and vrg_debug_readback of a batched renderer cover all views' pixels in
+ * batch order. */
+VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, uint32_t n_views,
+                                      const vrg_render_params *params, const vrg_frame_output *outs,
+                                      vrg_frame_stats *stats);
 
 /* ---- standalone SAH builds (build.rs:249,374), batched, device-side --- */
 /* Builds `count` independent trees in one launch sequence.  Tree i owns

@@ -1,0 +1,135 @@
+"""Batched views (vrg_render_batched): several scenes of uneven chunk grids and
+view extents rendered by one launch sequence must give, view by view, the
+bit-identical frames of single-view renderers fed the same scene, camera,
+seeds and frame index — with and without the CUDA-graph replay.  This is the
+parity contract of the batched path: the batch changes only how the work is
+scheduled, never a pixel's arithmetic."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import vrg
+
+pytestmark = pytest.mark.gpu
+
+MAT_SEED = 20240601
+# (terrain seed, chunks x, chunks z, width, height): uneven grids and extents,
+# including views whose pixel counts are not multiples of the 256-pixel lookup
+# group and one smaller than a group
+SCENES = [(11, 1, 1, 64, 48), (12, 2, 1, 97, 61), (13, 1, 2, 12, 10), (14, 1, 1, 40, 40)]
+FRAMES = 3
+
+
+def _params(flags=0, accumulate=0):
+    return vrg.RenderParams(1, 1, 3, 2, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, accumulate, flags, 4)
+
+
+def _seeds(v, f):
+    return (1000 + 17 * v + 101 * f, 2000 + 31 * v + 103 * f)
+
+
+@pytest.fixture(scope="module")
+def world(gpu_ctx):
+    mats, n = vrg.terrain_materials(MAT_SEED)
+    gpu_ctx.set_materials(mats, n)
+    scenes, keep, cams = [], [], []
+    for seed, nx, nz, w, h in SCENES:
+        blocks = vrg.terrain_blocks(seed, nx, nz, 0.01)
+        sc, objs = vrg.build_world(gpu_ctx, blocks)
+        scenes.append(sc)
+        keep.append(objs)
+        cams.append([vrg.orbit_camera(nx, nz, f, 64, w, h) for f in range(FRAMES)])
+    yield scenes, cams, keep
+    for sc in scenes:
+        sc.close()
+    for objs in keep:
+        for o in objs:
+            o.release()
+
+
+def _single(gpu_ctx, scenes, cams, accumulate=0):
+    """Each view through its own single-view renderer."""
+    out, rays = [], 0
+    for v, (seed, nx, nz, w, h) in enumerate(SCENES):
+        r = vrg.Renderer(gpu_ctx, w, h, 2)
+        frames = []
+        for f in range(FRAMES):
+            p = _params(accumulate=accumulate)
+            p.temporal_seed, p.spatial_seed = _seeds(v, f)
+            img, rad = r.render_params(scenes[v], cams[v][f], p, want_image=True, want_radiance=True)
+            frames.append((img.copy(), rad.copy()))
+            rays += r.last_stats.rays_closest + r.last_stats.rays_any
+        acc = r.read_accumulation() if accumulate else None
+        out.append((frames, acc))
+        r.close()
+    return out, rays
+
+
+def _batched(gpu_ctx, scenes, cams, flags, accumulate=0):
+    br = vrg.BatchRenderer(gpu_ctx, [(w, h) for *_, w, h in SCENES], 2)
+    frames, rays = [], []
+    for f in range(FRAMES):
+        imgs, rads = br.render(scenes, [cams[v][f] for v in range(len(SCENES))], _params(flags, accumulate),
+                               [_seeds(v, f) for v in range(len(SCENES))], want_image=True, want_radiance=True)
+        frames.append([(i.copy(), r.copy()) for i, r in zip(imgs, rads)])
+        rays.append(br.last_stats.rays_closest + br.last_stats.rays_any)
+        assert br.last_stats.error_flags == 0
+    acc = br.read_accumulation() if accumulate else None
+    br.close()
+    return frames, rays, acc
+
+
+def _same_bits(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("flags", [0, vrg.RENDER_GRAPH], ids=["launches", "graph"])
+def test_batched_views_match_single_view_renders(gpu_ctx, world, flags):
+    scenes, cams, _ = world
+    single, rays_single = _single(gpu_ctx, scenes, cams)
+    frames, rays, _ = _batched(gpu_ctx, scenes, cams, flags)
+    for f in range(FRAMES):
+        for v in range(len(SCENES)):
+            img_s, rad_s = single[v][0][f]
+            img_b, rad_b = frames[f][v]
+            assert _same_bits(rad_s, rad_b), (f, v)
+            assert np.array_equal(img_s, img_b), (f, v)
+    assert sum(rays) == rays_single
+
+
+def test_batched_accumulation_and_offsets(gpu_ctx, world):
+    scenes, cams, _ = world
+    single, _ = _single(gpu_ctx, scenes, cams, accumulate=1)
+    _, _, (acc, n) = _batched(gpu_ctx, scenes, cams, vrg.RENDER_GRAPH, accumulate=1)
+    assert n == FRAMES
+    for v in range(len(SCENES)):
+        a_s, n_s = single[v][1]
+        assert n_s == FRAMES
+        assert _same_bits(a_s, acc[v]), v
+
+
+def test_batched_rejects_mismatched_views(gpu_ctx, world):
+    scenes, cams, _ = world
+    br = vrg.BatchRenderer(gpu_ctx, [(w, h) for *_, w, h in SCENES], 2)
+    lib = gpu_ctx.lib
+    n = len(SCENES)
+    views = (vrg.View * n)()
+    for v in range(n):
+        views[v] = vrg.View(scenes[v].h, cams[v][0], 1, 2)
+    p = _params()
+    assert lib.vrg_render_batched(br.h, views, n - 1, C.byref(p), None, None) == vrg.ERR_INVALID_ARGUMENT
+    views[1].camera.width += 1
+    assert lib.vrg_render_batched(br.h, views, n, C.byref(p), None, None) == vrg.ERR_INVALID_ARGUMENT
+    views[1].camera.width -= 1
+    p.flags = vrg.RENDER_CAPTURE
+    assert lib.vrg_render_batched(br.h, views, n, C.byref(p), None, None) == vrg.ERR_UNSUPPORTED
+    p.flags = vrg.RENDER_GRAPH | vrg.RENDER_CACHE
+    assert lib.vrg_render_batched(br.h, views, n, C.byref(p), None, None) == vrg.ERR_UNSUPPORTED
+    # a single-view renderer refuses the batched call and the reverse
+    r = vrg.Renderer(gpu_ctx, 8, 8, 2)
+    assert lib.vrg_render_batched(r.h, views, n, C.byref(_params()), None, None) == vrg.ERR_STATE
+    cam = vrg.orbit_camera(1, 1, 0, 64, SCENES[0][3], SCENES[0][4])
+    assert lib.vrg_render(br.h, scenes[0].h, C.byref(cam), C.byref(_params()), None, None) == vrg.ERR_STATE
+    r.close()
+    br.close()

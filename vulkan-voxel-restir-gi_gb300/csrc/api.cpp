@@ -2,6 +2,8 @@
 // renderer orchestration (the frame graph of Renderer::render,
 // interactive_rendering.rs:952-1669, as one CUDA stream), debug readback and
 // the standalone batched SAH builds.
+#include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -348,8 +350,13 @@ VRG_API vrg_status vrg_scene_read_tl(vrg_scene *scene, uint32_t which, vrg_bvh_n
 
 // ---- renderer -------------------------------------------------------------
 
+static void drop_graphs(vrg_renderer *r) {
+    for (auto &g : r->graphs) cudaGraphExecDestroy(g.exec);
+    r->graphs.clear();
+}
+
 static vrg_status renderer_alloc(vrg_renderer *r) {
-    const size_t P = (size_t)r->W * r->H;
+    const size_t P = (size_t)r->P;
     const uint32_t nb = r->nb_max;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     size_t o = 0;
@@ -401,13 +408,24 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->radiance = (float *)(B + o_rad);
     r->accum = (double *)(B + o_acc);
     VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, r->ctx->stream));
+    drop_graphs(r);
     r->buf = b;
     r->res = nullptr;
+    r->res_buf.reset();
     r->ring_slots = 0;
     r->frame = 0;
     r->accum_n = 0;
     r->cap.reset();
+    r->cache_buf.reset();
     r->captured = false;
+    return VRG_OK;
+}
+
+static vrg_status renderer_events(vrg_renderer *r) {
+    for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
+    for (auto &row : r->ev_k)
+        for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
+    r->grid_bounce = r->ctx->num_sms * bounce_blocks_per_sm();
     return VRG_OK;
 }
 
@@ -420,27 +438,107 @@ VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_
     r->ctx = ctx;
     r->W = width;
     r->H = height;
+    r->P = (uint64_t)width * height;
     r->nb_max = max_bounces;
     vrg_status st = renderer_alloc(r);
+    if (st == VRG_OK) st = renderer_events(r);
     if (st != VRG_OK) {
-        delete r;
+        vrg_renderer_destroy(r);
         return st;
     }
-    for (auto &e : r->ev) cudaEventCreate(&e);
-    for (auto &row : r->ev_k)
-        for (auto &e : row) cudaEventCreate(&e);
-    r->grid_bounce = ctx->num_sms * bounce_blocks_per_sm();
     *out = r;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_views, const uint32_t *widths,
+                                               const uint32_t *heights, uint32_t max_bounces,
+                                               vrg_renderer **out) {
+    if (!ctx || !out || !widths || !heights || n_views == 0 || n_views > 65535 || max_bounces == 0 ||
+        max_bounces > MAX_BOUNCES)
+        return VRG_ERR_INVALID_ARGUMENT;
+    uint64_t P = 0;
+    std::vector<uint64_t> off(n_views);
+    for (uint32_t v = 0; v < n_views; v++) {
+        if (widths[v] == 0 || heights[v] == 0) return VRG_ERR_INVALID_ARGUMENT;
+        off[v] = P;
+        P += (uint64_t)widths[v] * heights[v];
+    }
+    if (P >= (1ull << 31)) {
+        set_error("a batch holds fewer than 2^31 pixels (asked for %llu)", (unsigned long long)P);
+        return VRG_ERR_UNSUPPORTED;
+    }
+    vrg_renderer *r = new vrg_renderer();
+    r->ctx = ctx;
+    r->W = widths[0];
+    r->H = heights[0];
+    r->P = P;
+    r->nb_max = max_bounces;
+    r->n_views = n_views;
+    r->vw.assign(widths, widths + n_views);
+    r->vh.assign(heights, heights + n_views);
+    r->voff = off;
+    auto fail = [&](vrg_status st) {
+        vrg_renderer_destroy(r);
+        return st;
+    };
+    vrg_status st = renderer_alloc(r);
+    if (st == VRG_OK) st = renderer_events(r);
+    if (st != VRG_OK) return fail(st);
+    // view table + pixel-group lookup (the view of each group's first pixel)
+    const size_t n_groups = (size_t)((P + (1u << VIEW_SHIFT) - 1) >> VIEW_SHIFT);
+    const size_t tab_off = ((size_t)n_views * sizeof(ViewDev) + 255) & ~(size_t)255;
+    DevBufPtr vb;
+    st = dev_alloc(ctx->stream, tab_off + n_groups * 2, vb);
+    if (st != VRG_OK) return fail(st);
+    r->view_buf = vb;
+    r->d_views = (ViewDev *)vb->ptr;
+    r->d_vtab = (uint16_t *)((uint8_t *)vb->ptr + tab_off);
+    std::vector<uint16_t> vtab(n_groups);
+    uint32_t v = 0;
+    for (size_t g = 0; g < n_groups; g++) {
+        const uint64_t p = (uint64_t)g << VIEW_SHIFT;
+        while (v + 1 < n_views && p >= off[v + 1]) v++;
+        vtab[g] = (uint16_t)v;
+    }
+    if (cudaMemcpyAsync(r->d_vtab, vtab.data(), n_groups * 2, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+        cudaHostAlloc((void **)&r->h_views, 2 * (size_t)n_views * sizeof(ViewDev), cudaHostAllocDefault) !=
+            cudaSuccess) {
+        set_error("batched renderer set-up failed");
+        return fail(VRG_ERR_CUDA);
+    }
+    memset(r->h_views, 0, 2 * (size_t)n_views * sizeof(ViewDev));
+    for (auto &e : r->ev_stage)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(VRG_ERR_CUDA);
+    *out = r;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_view_offset(vrg_renderer *r, uint32_t view, uint64_t *pixel_offset) {
+    if (!r || !pixel_offset) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views == 0) {
+        if (view != 0) return VRG_ERR_INVALID_ARGUMENT;
+        *pixel_offset = 0;
+        return VRG_OK;
+    }
+    if (view >= r->n_views) return VRG_ERR_INVALID_ARGUMENT;
+    *pixel_offset = r->voff[view];
     return VRG_OK;
 }
 
 VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
     if (!r) return VRG_ERR_INVALID_ARGUMENT;
     cudaStreamSynchronize(r->ctx->stream);
-    for (auto &e : r->ev) cudaEventDestroy(e);
+    drop_graphs(r);
+    for (auto &e : r->ev)
+        if (e) cudaEventDestroy(e);
     for (auto &row : r->ev_k)
-        for (auto &e : row) cudaEventDestroy(e);
+        for (auto &e : row)
+            if (e) cudaEventDestroy(e);
+    for (auto &e : r->ev_stage)
+        if (e) cudaEventDestroy(e);
     if (r->h_pinned) cudaFreeHost(r->h_pinned);
+    if (r->h_views) cudaFreeHost(r->h_views);
     r->res_buf.reset();
     delete r;
     return VRG_OK;
@@ -448,10 +546,15 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
 
 VRG_API vrg_status vrg_renderer_resize(vrg_renderer *r, uint32_t width, uint32_t height) {
     if (!r || width == 0 || height == 0) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views) {
+        set_error("a batched renderer has fixed view extents");
+        return VRG_ERR_STATE;
+    }
+    if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
     cudaStreamSynchronize(r->ctx->stream);
     r->W = width;
     r->H = height;
-    r->res_buf.reset();
+    r->P = (uint64_t)width * height;
     return renderer_alloc(r);
 }
 
@@ -463,7 +566,7 @@ VRG_API vrg_status vrg_renderer_frame_index(vrg_renderer *r, uint32_t *frame_ind
 
 VRG_API vrg_status vrg_renderer_reset_accumulation(vrg_renderer *r) {
     if (!r) return VRG_ERR_INVALID_ARGUMENT;
-    VRG_CUDA_TRY(cudaMemsetAsync(r->accum, 0, (size_t)r->W * r->H * 24, r->ctx->stream));
+    VRG_CUDA_TRY(cudaMemsetAsync(r->accum, 0, (size_t)r->P * 24, r->ctx->stream));
     r->accum_n = 0;
     return VRG_OK;
 }
@@ -472,7 +575,7 @@ VRG_API vrg_status vrg_renderer_read_accumulation(vrg_renderer *r, float *rgb, u
     if (!r) return VRG_ERR_INVALID_ARGUMENT;
     if (n_frames) *n_frames = r->accum_n;
     if (!rgb) return VRG_OK;
-    size_t P = (size_t)r->W * r->H;
+    const size_t P = (size_t)r->P;
     std::vector<double> h(P * 3);
     VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), r->accum, P * 24, cudaMemcpyDeviceToHost, r->ctx->stream));
     VRG_CUDA_TRY(cudaStreamSynchronize(r->ctx->stream));
@@ -483,7 +586,7 @@ VRG_API vrg_status vrg_renderer_read_accumulation(vrg_renderer *r, float *rgb, u
 
 static vrg_status ensure_capture(vrg_renderer *r) {
     if (r->cap) return VRG_OK;
-    const size_t P = (size_t)r->W * r->H, nb = r->nb_max;
+    const size_t P = (size_t)r->P, nb = r->nb_max;
     size_t floats = (nb + 1) * P * 3 * 2 + nb * P * 3 * 4 + nb * P * 4 + nb * P * 4;
     DevBufPtr b;
     VRG_TRY(dev_alloc(r->ctx->stream, floats * 4, b));
@@ -504,31 +607,23 @@ static vrg_status ensure_capture(vrg_renderer *r) {
     return VRG_OK;
 }
 
-VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
-                              const vrg_render_params *pr, const vrg_frame_output *out, vrg_frame_stats *stats) {
-    if (!r || !scene || !cam || !pr) return VRG_ERR_INVALID_ARGUMENT;
-    if (cam->width != r->W || cam->height != r->H) {
-        set_error("camera extent %ux%u differs from the renderer's %ux%u (call vrg_renderer_resize)", cam->width,
-                  cam->height, r->W, r->H);
-        return VRG_ERR_INVALID_ARGUMENT;
-    }
-    if (pr->num_bounces == 0 || pr->spatial_iterations > 64 ||
-        pr->nee_type > 2 || pr->mode > 1) {
+// Frame set-up shared by vrg_render and vrg_render_batched: parameter checks,
+// the reservoir ring, capture and cache buffers, and every FrameArgs field but
+// the view ones.
+static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool want_radiance, FrameArgs &a) {
+    if (pr->num_bounces == 0 || pr->spatial_iterations > 64 || pr->nee_type > 2 || pr->mode > 1) {
         set_error("invalid render parameters");
         return VRG_ERR_INVALID_ARGUMENT;
     }
-    if (scene->ctx != r->ctx) return VRG_ERR_INVALID_ARGUMENT;
-    Context *ctx = r->ctx;
-    cudaStream_t s = ctx->stream;
-    // Renderer::render starts with scene.get_tlas() (interactive_rendering.rs:961)
-    VRG_TRY(scene_commit(scene));
-    const size_t P = (size_t)r->W * r->H;
+    cudaStream_t s = r->ctx->stream;
+    const size_t P = (size_t)r->P;
     const uint32_t slots = pr->history_slots ? pr->history_slots : 3;
     if (slots > 8) return VRG_ERR_INVALID_ARGUMENT;
     if (slots != r->ring_slots) {
         DevBufPtr b;
         VRG_TRY(dev_alloc(s, (size_t)slots * 5 * P * 16, b));
         VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, (size_t)slots * 5 * P * 16, s));
+        drop_graphs(r);
         r->res_buf = b;
         r->res = (float4 *)b->ptr;
         r->ring_slots = slots;
@@ -570,21 +665,11 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
             r->qflag = B + o_qf;
             r->cache_buf = b;
         }
-        if (!scene->h_geo_tl.empty())
-            nrc_set_bounds(r->cache, scene->h_geo_tl[0].min, scene->h_geo_tl[0].max);
     } else if (nb_total > r->nb_max) {
         return VRG_ERR_INVALID_ARGUMENT;
     }
     const uint32_t ring = r->frame % slots;
-    FrameArgs a;
     memset(&a, 0, sizeof(a));
-    a.sc = scene->dev;
-    a.eye = f3{cam->eye[0], cam->eye[1], cam->eye[2]};
-    a.front = f3{cam->front[0], cam->front[1], cam->front[2]};
-    a.right = f3{cam->right[0], cam->right[1], cam->right[2]};
-    a.up = f3{cam->up[0], cam->up[1], cam->up[2]};
-    a.W = r->W;
-    a.H = r->H;
     a.P = (uint32_t)P;
     a.nb = nb_total;
     a.nb_render = pr->num_bounces;
@@ -599,11 +684,8 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.train_list = r->train_list;
     a.qflag = r->qflag;
     a.nee_type = pr->nee_type;
-    a.frame = r->frame;
     a.mode = pr->mode;
     a.spatial_iters = pr->spatial_iterations;
-    a.temporal_seed = pr->temporal_seed;
-    a.spatial_seed = pr->spatial_seed;
     a.spatial_radius = pr->spatial_radius;
     a.m_cap = pr->m_cap;
     a.debug_view = pr->debug_view;
@@ -631,7 +713,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.spatial = r->spatial;
     a.final_t = r->final_t;
     a.bgra = r->bgra;
-    a.radiance = (out && out->radiance) ? r->radiance : nullptr;
+    a.radiance = want_radiance ? r->radiance : nullptr;
     a.accum = r->accum;
     a.capture = capture ? 1u : 0u;
     a.c_origin = r->c_origin;
@@ -645,45 +727,46 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.c_L = r->c_L;
     a.c_q = r->c_q;
     a.c_hit = r->c_hit;
-    if (out && !out->host && out->radiance) a.radiance = out->radiance;
-    if (out && !out->host && out->bgra8) a.bgra = out->bgra8;
-    VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
+    r->last_ring = ring;
+    return VRG_OK;
+}
+
+// The frame's launch sequence on the context stream.  timed: CUDA events
+// around every stage (r->ev: frame start, after each bounce, after resolve,
+// after spatial; r->ev_k: after k_trace / k_shade of each bounce); a graph
+// recording passes false.
+static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) {
+    cudaStream_t s = r->ctx->stream;
     int ei = 0;
-    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     for (uint32_t b = 0; b < a.nb; b++) {
-        VRG_TRY(launch_bounce(s, a, b, r->ev_k[0][b], r->ev_k[1][b]));
-        VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+        VRG_TRY(launch_bounce(s, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr));
+        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     }
-    if (cache)  // radiance-cache queries of every path that ends into the cache
-        VRG_TRY(nrc_infer(r->cache, s, (uint32_t)P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir,
-                          nullptr, r->pred));
+    if (a.cache)  // radiance-cache queries of every path that ends into the cache
+        VRG_TRY(nrc_infer(r->cache, s, a.P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
+                          r->pred));
     VRG_TRY(launch_resolve(s, a));
-    if (cache) {  // one training step on this frame's long paths
+    if (a.cache) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));
         VRG_TRY(nrc_train(r->cache, s, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
                           nullptr, r->target, true));
     }
-    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
     VRG_TRY(launch_spatial(s, a));
-    VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
-    if (out && out->host) {
-        if (out->bgra8 && a.pack)
-            VRG_CUDA_TRY(cudaMemcpyAsync(out->bgra8, a.bgra, P * 4, cudaMemcpyDeviceToHost, s));
-        if (out->radiance)
-            VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, a.radiance, P * 12, cudaMemcpyDeviceToHost, s));
-    }
-    r->last_nb = a.nb;
-    r->last_ring = ring;
-    r->captured = capture;
-    if (pr->accumulate) r->accum_n++;
-    r->frame++;
-    if (stats || (out && out->host)) {
-        VRG_CUDA_TRY(cudaStreamSynchronize(s));
-    }
-    if (stats) {
-        memset(stats, 0, sizeof(*stats));
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, r->ev[0], r->ev[ei - 1]);
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    return VRG_OK;
+}
+
+// Stats of the frame just launched (synchronizes).  per_kernel: the frame was
+// launched with timed == true; otherwise ev[0]/ev[1] bracket a graph launch.
+static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kernel, vrg_frame_stats *stats) {
+    VRG_CUDA_TRY(cudaStreamSynchronize(r->ctx->stream));
+    memset(stats, 0, sizeof(*stats));
+    float ms = 0.0f;
+    if (per_kernel) {
+        cudaEventElapsedTime(&ms, r->ev[0], r->ev[a.nb + 2]);
         stats->ms_total = ms;
         for (uint32_t b = 0; b < a.nb && b < 8; b++) {
             cudaEventElapsedTime(&ms, r->ev[b], r->ev[b + 1]);
@@ -699,24 +782,204 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         stats->ms_resolve = ms;
         cudaEventElapsedTime(&ms, r->ev[a.nb + 1], r->ev[a.nb + 2]);
         stats->ms_spatial = ms;
-        uint32_t cnt[CNT_WORDS];
-        VRG_CUDA_TRY(cudaMemcpy(cnt, r->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
-        uint64_t rays, any;
-        memcpy(&rays, cnt + CNT_RAYS, 8);
-        memcpy(&any, cnt + CNT_ANY, 8);
-        stats->rays_closest = rays;
-        stats->rays_any = any;
-        uint64_t nn, nlv;
-        memcpy(&nn, cnt + CNT_NODES, 8);
-        memcpy(&nlv, cnt + CNT_LEAVES, 8);
-        stats->nodes_visited = nn;
-        stats->leaves_visited = nlv;
-        stats->error_flags = cnt[CNT_ERROR];
-        if (cnt[CNT_ERROR]) {
-            set_error("device error flags 0x%x", cnt[CNT_ERROR]);
-            return VRG_ERR_OVERFLOW;
+    } else {
+        cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+        stats->ms_total = ms;
+    }
+    uint32_t cnt[CNT_WORDS];
+    VRG_CUDA_TRY(cudaMemcpy(cnt, r->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    uint64_t rays, any, nn, nlv;
+    memcpy(&rays, cnt + CNT_RAYS, 8);
+    memcpy(&any, cnt + CNT_ANY, 8);
+    memcpy(&nn, cnt + CNT_NODES, 8);
+    memcpy(&nlv, cnt + CNT_LEAVES, 8);
+    stats->rays_closest = rays;
+    stats->rays_any = any;
+    stats->nodes_visited = nn;
+    stats->leaves_visited = nlv;
+    stats->error_flags = cnt[CNT_ERROR];
+    if (cnt[CNT_ERROR]) {
+        set_error("device error flags 0x%x", cnt[CNT_ERROR]);
+        return VRG_ERR_OVERFLOW;
+    }
+    return VRG_OK;
+}
+
+static void frame_done(vrg_renderer *r, const FrameArgs &a, const vrg_render_params *pr) {
+    r->last_nb = a.nb;
+    r->captured = a.capture != 0;
+    if (pr->accumulate) r->accum_n++;
+    r->frame++;
+}
+
+VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
+                              const vrg_render_params *pr, const vrg_frame_output *out, vrg_frame_stats *stats) {
+    if (!r || !scene || !cam || !pr) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views) {
+        set_error("a batched renderer renders with vrg_render_batched");
+        return VRG_ERR_STATE;
+    }
+    if (cam->width != r->W || cam->height != r->H) {
+        set_error("camera extent %ux%u differs from the renderer's %ux%u (call vrg_renderer_resize)", cam->width,
+                  cam->height, r->W, r->H);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    if (pr->flags & VRG_RENDER_GRAPH) {
+        set_error("VRG_RENDER_GRAPH is a flag of vrg_render_batched");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    if (scene->ctx != r->ctx) return VRG_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = r->ctx->stream;
+    // Renderer::render starts with scene.get_tlas() (interactive_rendering.rs:961)
+    VRG_TRY(scene_commit(scene));
+    const size_t P = (size_t)r->P;
+    FrameArgs a;
+    VRG_TRY(frame_setup(r, pr, out && out->radiance, a));
+    if (a.cache && !scene->h_geo_tl.empty())
+        nrc_set_bounds(r->cache, scene->h_geo_tl[0].min, scene->h_geo_tl[0].max);
+    a.v0.sc = scene->dev;
+    a.v0.eye = f3{cam->eye[0], cam->eye[1], cam->eye[2]};
+    a.v0.front = f3{cam->front[0], cam->front[1], cam->front[2]};
+    a.v0.right = f3{cam->right[0], cam->right[1], cam->right[2]};
+    a.v0.up = f3{cam->up[0], cam->up[1], cam->up[2]};
+    a.v0.W = r->W;
+    a.v0.H = r->H;
+    a.v0.pix_off = 0;
+    a.v0.pix_end = (uint32_t)P;
+    a.v0.frame = r->frame;
+    a.v0.temporal_seed = pr->temporal_seed;
+    a.v0.spatial_seed = pr->spatial_seed;
+    if (out && !out->host && out->radiance) a.radiance = out->radiance;
+    if (out && !out->host && out->bgra8) a.bgra = out->bgra8;
+    VRG_TRY(frame_launch(r, a, true));
+    if (out && out->host) {
+        if (out->bgra8 && a.pack)
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->bgra8, a.bgra, P * 4, cudaMemcpyDeviceToHost, s));
+        if (out->radiance)
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, a.radiance, P * 12, cudaMemcpyDeviceToHost, s));
+    }
+    frame_done(r, a, pr);
+    if (stats) return frame_stats(r, a, true, stats);
+    if (out && out->host) VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, uint32_t n_views,
+                                      const vrg_render_params *pr, const vrg_frame_output *outs,
+                                      vrg_frame_stats *stats) {
+    if (!r || !views || !pr) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views == 0) {
+        set_error("vrg_render_batched needs a renderer made by vrg_renderer_create_batched");
+        return VRG_ERR_STATE;
+    }
+    if (n_views != r->n_views) {
+        set_error("%u views given, the renderer has %u", n_views, r->n_views);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    const bool graph = (pr->flags & VRG_RENDER_GRAPH) != 0;
+    if ((pr->flags & VRG_RENDER_CAPTURE) || (graph && (pr->flags & VRG_RENDER_CACHE))) {
+        set_error("batched frames take neither VRG_RENDER_CAPTURE nor VRG_RENDER_GRAPH with VRG_RENDER_CACHE");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    for (uint32_t v = 0; v < n_views; v++) {
+        const vrg_view &w = views[v];
+        if (!w.scene || w.scene->ctx != r->ctx) return VRG_ERR_INVALID_ARGUMENT;
+        if (w.camera.width != r->vw[v] || w.camera.height != r->vh[v]) {
+            set_error("view %u: camera extent %ux%u differs from the view's %ux%u", v, w.camera.width,
+                      w.camera.height, r->vw[v], r->vh[v]);
+            return VRG_ERR_INVALID_ARGUMENT;
         }
     }
+    cudaStream_t s = r->ctx->stream;
+    for (uint32_t v = 0; v < n_views; v++) VRG_TRY(scene_commit(views[v].scene));
+    bool want_rad = false;
+    if (outs)
+        for (uint32_t v = 0; v < n_views; v++) want_rad |= outs[v].radiance != nullptr;
+    FrameArgs a;
+    VRG_TRY(frame_setup(r, pr, want_rad, a));
+    if (a.cache) {  // the cache spans every view's scene
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t v = 0; v < n_views; v++) {
+            const auto &tl = views[v].scene->h_geo_tl;
+            if (tl.empty()) continue;
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::min(lo[k], tl[0].min[k]);
+                hi[k] = std::max(hi[k], tl[0].max[k]);
+            }
+        }
+        if (lo[0] <= hi[0]) nrc_set_bounds(r->cache, lo, hi);
+    }
+    // per-view table: staged in pinned memory (two halves, so that the next
+    // call does not overwrite a half whose copy has not run yet)
+    ViewDev *hv = r->h_views + (size_t)r->stage * n_views;
+    VRG_CUDA_TRY(cudaEventSynchronize(r->ev_stage[r->stage]));
+    for (uint32_t v = 0; v < n_views; v++) {
+        const vrg_view &w = views[v];
+        ViewDev &d = hv[v];
+        memset(&d, 0, sizeof(d));
+        d.sc = w.scene->dev;
+        d.eye = f3{w.camera.eye[0], w.camera.eye[1], w.camera.eye[2]};
+        d.front = f3{w.camera.front[0], w.camera.front[1], w.camera.front[2]};
+        d.right = f3{w.camera.right[0], w.camera.right[1], w.camera.right[2]};
+        d.up = f3{w.camera.up[0], w.camera.up[1], w.camera.up[2]};
+        d.W = r->vw[v];
+        d.H = r->vh[v];
+        d.pix_off = (uint32_t)r->voff[v];
+        d.pix_end = (uint32_t)(r->voff[v] + (uint64_t)r->vw[v] * r->vh[v]);
+        d.frame = r->frame;
+        d.temporal_seed = w.temporal_seed;
+        d.spatial_seed = w.spatial_seed;
+    }
+    VRG_CUDA_TRY(cudaMemcpyAsync(r->d_views, hv, (size_t)n_views * sizeof(ViewDev), cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaEventRecord(r->ev_stage[r->stage], s));
+    r->stage ^= 1u;
+    a.views = r->d_views;
+    a.vtab = r->d_vtab;
+    a.n_views = n_views;
+    if (graph) {
+        // the FrameArgs bytes name the recording: buffers, ring slot and parameters
+        std::vector<uint8_t> key((const uint8_t *)&a, (const uint8_t *)&a + sizeof(a));
+        Renderer::GraphEntry *ge = nullptr;
+        for (auto &g : r->graphs)
+            if (g.key == key) ge = &g;
+        if (!ge) {
+            if (r->graphs.size() >= 8) drop_graphs(r);
+            cudaGraph_t g = nullptr;
+            VRG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            vrg_status st = frame_launch(r, a, false);
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (st != VRG_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            VRG_CUDA_TRY(ce);
+            cudaGraphExec_t ex = nullptr;
+            ce = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            VRG_CUDA_TRY(ce);
+            r->graphs.push_back(Renderer::GraphEntry{key, ex});
+            ge = &r->graphs.back();
+        }
+        VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
+        VRG_CUDA_TRY(cudaGraphLaunch(ge->exec, s));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev[1], s));
+    } else {
+        VRG_TRY(frame_launch(r, a, true));
+    }
+    bool host_out = false;
+    if (outs) {
+        for (uint32_t v = 0; v < n_views; v++) {
+            const vrg_frame_output &o = outs[v];
+            const size_t off = (size_t)r->voff[v], n = (size_t)r->vw[v] * r->vh[v];
+            const cudaMemcpyKind k = o.host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+            if (o.bgra8 && a.pack) VRG_CUDA_TRY(cudaMemcpyAsync(o.bgra8, r->bgra + 4 * off, n * 4, k, s));
+            if (o.radiance) VRG_CUDA_TRY(cudaMemcpyAsync(o.radiance, r->radiance + 3 * off, n * 12, k, s));
+            host_out |= o.host && (o.bgra8 || o.radiance);
+        }
+    }
+    frame_done(r, a, pr);
+    if (stats) return frame_stats(r, a, !graph, stats);
+    if (host_out) VRG_CUDA_TRY(cudaStreamSynchronize(s));
     return VRG_OK;
 }
 
@@ -727,7 +990,7 @@ VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst,
         return VRG_ERR_STATE;
     }
     cudaStream_t s = r->ctx->stream;
-    const size_t P = (size_t)r->W * r->H, nb = r->last_nb;
+    const size_t P = (size_t)r->P, nb = r->last_nb;
     auto copy = [&](const void *src, size_t n) -> vrg_status {
         if (bytes < n) return VRG_ERR_INVALID_ARGUMENT;
         VRG_CUDA_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s));

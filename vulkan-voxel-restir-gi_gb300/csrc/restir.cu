@@ -51,8 +51,8 @@ __device__ __forceinline__ void st3(float *a, size_t i, f3 v) {
     a[3 * i + 2] = v.z;
 }
 
-template <bool CAPTURE>
-__global__ void __launch_bounds__(256) k_resolve(FrameArgs a) {
+template <bool CAPTURE, bool BATCH>
+__global__ void __launch_bounds__(256) k_resolve(const __grid_constant__ FrameArgs a) {
     const uint32_t P = a.P;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
@@ -125,7 +125,8 @@ __global__ void __launch_bounds__(256) k_resolve(FrameArgs a) {
     S.p_omega = q0;
     S.seed = 0;
     // temporal resampling (restir_temporal_resampling.rs:256-301)
-    const uint32_t ps = mm_combine(a.temporal_seed, p);
+    const ViewDev &V = view_of<BATCH>(a, p);
+    const uint32_t ps = mm_combine(V.temporal_seed, p - V.pix_off);
     Res R = load_res(a.res, P, p);
     if (mm_rand(mm_combine(ps, 0)) < 0.4f) {
         R.w_sum = 0.0f;
@@ -154,16 +155,19 @@ __device__ __forceinline__ uint8_t to_u8(float x) {
     return (uint8_t)(int)v;
 }
 
-template <bool CAPTURE>
-__global__ void __launch_bounds__(256) k_spatial(FrameArgs a) {
+template <bool CAPTURE, bool BATCH>
+__global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameArgs a) {
     const uint32_t P = a.P;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     f3 fin = f3{0.0f, 0.0f, 0.0f};
     float ucw_view = 0.0f;
     if (a.nb >= 2 && a.restir) {
-        const uint32_t qx = p % a.W, qy = p / a.W;
-        const uint32_t ps = mm_combine(a.spatial_seed, p);
+        // neighbours are taken within the pixel's own view
+        const ViewDev &V = view_of<BATCH>(a, p);
+        const uint32_t lp = p - V.pix_off;
+        const uint32_t qx = lp % V.W, qy = lp / V.W;
+        const uint32_t ps = mm_combine(V.spatial_seed, lp);
         Res Rs = load_res(a.res, P, p);
         const f3 Sx_v = Rs.x_v, Sn_v = Rs.n_v;
         uint32_t Z = (luminance3(Rs.l) > 0.0f) ? Rs.m : 0u;
@@ -173,9 +177,9 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs a) {
             const float jy = a.spatial_radius * (mm_rand(mm_combine(is, 1)) - 0.5f);
             int nx = (int)(((float)qx + 0.5f) + jx);
             int ny = (int)(((float)qy + 0.5f) + jy);
-            nx = min(max(nx, 0), (int)a.W - 1);
-            ny = min(max(ny, 0), (int)a.H - 1);
-            const uint32_t np = (uint32_t)nx + (uint32_t)ny * a.W;
+            nx = min(max(nx, 0), (int)V.W - 1);
+            ny = min(max(ny, 0), (int)V.H - 1);
+            const uint32_t np = V.pix_off + (uint32_t)nx + (uint32_t)ny * V.W;
             // geometricallySimilar (restir_spatial_resampling.rs:277-288)
             const float4 nvn = a.res[P + np];
             const f3 nn = ld3(nvn);
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs a) {
 
 // training targets of the radiance cache: the outgoing radiance at vertex
 // nb_render-1 of each long training path (its full backward recurrence)
-__global__ void __launch_bounds__(256) k_train_targets(FrameArgs a) {
+__global__ void __launch_bounds__(256) k_train_targets(const __grid_constant__ FrameArgs a) {
     const uint32_t n = min(a.counters[CNT_TRAIN], a.train_cap);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -265,16 +269,18 @@ vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a) {
 
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a) {
     dim3 g((a.P + 255) / 256);
-    if (a.capture) k_resolve<true><<<g, 256, 0, s>>>(a);
-    else k_resolve<false><<<g, 256, 0, s>>>(a);
+    if (a.views) k_resolve<false, true><<<g, 256, 0, s>>>(a);
+    else if (a.capture) k_resolve<true, false><<<g, 256, 0, s>>>(a);
+    else k_resolve<false, false><<<g, 256, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }
 
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a) {
     dim3 g((a.P + 255) / 256);
-    if (a.capture) k_spatial<true><<<g, 256, 0, s>>>(a);
-    else k_spatial<false><<<g, 256, 0, s>>>(a);
+    if (a.views) k_spatial<false, true><<<g, 256, 0, s>>>(a);
+    else if (a.capture) k_spatial<true, false><<<g, 256, 0, s>>>(a);
+    else k_spatial<false, false><<<g, 256, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

@@ -224,13 +224,14 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 // raygen (raygen.rs:84-111): pixel corner, jitter multiplied by 0.00
-__device__ __forceinline__ void raygen(const FrameArgs &a, uint32_t p, f3 &o, f3 &d) {
-    uint32_t x = p % a.W, y = p / a.W;
-    float u = 2.0f * (float)x / (float)a.W - 1.0f;
-    float v = 2.0f * (float)y / (float)a.H - 1.0f;
-    float aspect = (float)a.W / (float)a.H;
-    o = a.eye;
-    d = norm3(add3(add3(scl3(lscl3(u, a.right), aspect), lscl3(v, a.up)), a.front));
+// lp: the pixel's index within its view
+__device__ __forceinline__ void raygen(const ViewDev &V, uint32_t lp, f3 &o, f3 &d) {
+    uint32_t x = lp % V.W, y = lp / V.W;
+    float u = 2.0f * (float)x / (float)V.W - 1.0f;
+    float v = 2.0f * (float)y / (float)V.H - 1.0f;
+    float aspect = (float)V.W / (float)V.H;
+    o = V.eye;
+    d = norm3(add3(add3(scl3(lscl3(u, V.right), aspect), lscl3(v, V.up)), V.front));
 }
 
 // Conservative slab test of a traversal box (boxes carry BOX_MARGIN, so the
@@ -282,16 +283,18 @@ __device__ __forceinline__ void slab4(float4 LX, float4 HX, float4 LY, float4 HY
 // fetch once REFILL_MIN lanes are idle), so a warp does not wait for its
 // longest ray.  The result is independent of traversal order: ties on t go
 // to the smaller (instance, triangle) key and boxes are culled only when
-// strictly beyond the current best t.
+// strictly beyond the current best t.  In a batched frame each lane reads the
+// scene of its ray's view when it takes the ray.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t n_in = (b == 0) ? a.P : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *err = a.counters + CNT_ERROR;
-    const float4 *wide = a.sc.geo_wide;
-    const int4 *recs = a.sc.geo_rec;
-    const int root = a.sc.geo_root;
+    const float4 *wide = a.v0.sc.geo_wide;
+    const int4 *recs = a.v0.sc.geo_rec;
+    int root = a.v0.sc.geo_root;
     bool has = false, exhausted = false;
     uint32_t p = 0, steps = 0, traced = 0, n_nodes = 0, n_leaves = 0;
     f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0};
@@ -313,7 +316,13 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
                     has = true;
                     traced++;
                     p = (b == 0) ? idx : qin[idx];
-                    if (b == 0) raygen(a, p, o, d);
+                    const ViewDev &V = view_of<BATCH>(a, p);
+                    if constexpr (BATCH) {
+                        wide = V.sc.geo_wide;
+                        recs = V.sc.geo_rec;
+                        root = V.sc.geo_root;
+                    }
+                    if (b == 0) raygen(V, p - V.pix_off, o, d);
                     else { o = ld3(a.ray_o[p]); d = ld3(a.ray_d[p]); }
                     inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
@@ -405,14 +414,13 @@ __global__ void __launch_bounds__(128) k_trace(FrameArgs a, uint32_t b) {
 // (raytrace.rs:405-577).  Rays whose light pdf is needed are queued for
 // k_anyhit; the others get their (E, w) (R, q) record here.
 // ---------------------------------------------------------------------------
-template <bool CAPTURE>
-__global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
+template <bool CAPTURE, bool BATCH>
+__global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
     const uint32_t n_in = (b == 0) ? P : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *qout = a.queue[b & 1];
-    const uint32_t inv_seed = a.frame * nb + b;  // interactive_rendering.rs:1189
     const float inv2pi = 1.0f / (2.0f * PI_F);
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -431,9 +439,11 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
         int face = 0;
         if (active) {
             p = (b == 0) ? i : qin[i];
+            const ViewDev &V = view_of<BATCH>(a, p);
+            const uint32_t lp = p - V.pix_off;
             f3 o, d;
             if (b == 0) {
-                raygen(a, p, o, d);
+                raygen(V, lp, o, d);
                 if (CAPTURE) {
                     st3(a.c_origin, p, o);
                     st3(a.c_dir, p, d);
@@ -442,7 +452,7 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 o = ld3(a.ray_o[p]);
                 d = ld3(a.ray_d[p]);
             }
-            const uint32_t seed = mm_combine(inv_seed, p);
+            const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
             const int4 hv = a.hits[p];
             f3 n, E, R;
             float mis = 0.0f;
@@ -456,7 +466,7 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 E = f3{sky, sky, sky};
                 R = f3{0.0f, 0.0f, 0.0f};
             } else {
-                rc = __ldg(a.sc.geo_rec + hv.x);
+                rc = __ldg(V.sc.geo_rec + hv.x);
                 face = hv.y & 7;
                 half = (hv.y >> 3) & 1;
                 const float b1 = __int_as_float(hv.z), b2 = __int_as_float(hv.w);
@@ -467,7 +477,7 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 const Frame fr = c_frames[2 * face + half];
                 n = fr.n;
                 const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
-                const vrg_material &m = a.sc.mats[6u * blk_id + (uint32_t)face];
+                const vrg_material &m = V.sc.mats[6u * blk_id + (uint32_t)face];
                 const float b0 = (1.0f - b1) - b2;
                 new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
                 R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
@@ -489,13 +499,13 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                     res.success = false;
                     res.importance = 0.0f;
                     if (a.nee_type == 1 || (a.nee_type == 2 && b == 1))
-                        res = light_descent(a.sc, new_o, n, mm_combine(seed, 2));
+                        res = light_descent(V.sc, new_o, n, mm_combine(seed, 2));
                     if (res.success && res.importance > 0.0f) mis = 0.3f;
                     const float mis_rand = mm_rand(mm_combine(seed, 3));
                     float ux = mm_rand(mm_combine(seed, 4)), uy = mm_rand(mm_combine(seed, 5));
                     if (mis_rand < mis) {
                         f3 lt[3];
-                        light_tri_world(a.sc, res.inst, res.leaf, lt);
+                        light_tri_world(V.sc, res.inst, res.leaf, lt);
                         if (ux + uy > 1.0f) { ux = 1.0f - ux; uy = 1.0f - uy; }  // triangleSample
                         const float bx = (1.0f - ux) - uy;
                         const f3 sp = add3(add3(lscl3(bx, lt[0]), lscl3(ux, lt[1])), lscl3(uy, lt[2]));
@@ -519,7 +529,7 @@ __global__ void __launch_bounds__(128) k_shade(FrameArgs a, uint32_t b) {
                 if (qhit) {
                     a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
                     a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
-                    want_train = (mm_finalize(mm_combine(a.frame * 0x9E3779B9u + 0x7a11u, p)) & 15u) == 0u;
+                    want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
                 }
             }
             // stash for the second half (after the warp-level training-slot grant)
@@ -644,15 +654,15 @@ __device__ __forceinline__ void finish_job(const FrameArgs &a, uint32_t b, uint3
     reinterpret_cast<float *>(a.rec + rb + a.P + p)[3] = q;
 }
 
-template <bool CAPTURE>
-__global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
+template <bool CAPTURE, bool BATCH>
+__global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
     uint32_t *err = a.counters + CNT_ERROR;
-    const float4 *wide = a.sc.lamp_wide;
-    const int4 *recs = a.sc.lamp_rec;
-    const uint32_t *table = a.sc.lamp_table;
-    const int root = a.sc.lamp_root;
+    const float4 *wide = a.v0.sc.lamp_wide;
+    const int4 *recs = a.v0.sc.lamp_rec;
+    const uint32_t *table = a.v0.sc.lamp_table;
+    int root = a.v0.sc.lamp_root;
     const float tmin = EPS_NEE, tmax = 1000.0f;
     bool has = false, exhausted = false;
     uint32_t p = 0, idx = 0, steps = 0;
@@ -676,6 +686,13 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
                 if (idx < n_in) {
                     has = true;
                     p = a.aqueue[idx];
+                    if constexpr (BATCH) {
+                        const ViewDev &V = view_of<BATCH>(a, p);
+                        wide = V.sc.lamp_wide;
+                        recs = V.sc.lamp_rec;
+                        table = V.sc.lamp_table;
+                        root = V.sc.lamp_root;
+                    }
                     const float4 ro = a.ray_o[p], rd = a.ray_d[p];
                     o = ld3(ro);
                     d = ld3(rd);
@@ -772,19 +789,20 @@ __global__ void __launch_bounds__(128) k_anyhit(FrameArgs a, uint32_t b) {
     }
 }
 
-__global__ void __launch_bounds__(128) k_hit_eval(FrameArgs a) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_hit_eval(const __grid_constant__ FrameArgs a) {
     const uint32_t n = min(a.counters[CNT_HITS], a.hit_cap);
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
         const uint4 A = a.hitbuf[2 * (size_t)h], B = a.hitbuf[2 * (size_t)h + 1];
         const uint32_t p = A.x;
         const float4 ro = a.ray_o[p], rd = a.ray_d[p];
         const f3 n3 = c_frames[2 * __float_as_int(ro.w)].n;
-        a.hitval[h] = nee_pdf_of(a.sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
+        a.hitval[h] = nee_pdf_of(view_of<BATCH>(a, p).sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
     }
 }
 
 template <bool CAPTURE>
-__global__ void __launch_bounds__(128) k_hit_sum(FrameArgs a, uint32_t b) {
+__global__ void __launch_bounds__(128) k_hit_sum(const __grid_constant__ FrameArgs a, uint32_t b) {
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += gridDim.x * blockDim.x) {
         const uint2 m = a.jmeta[i];
@@ -816,22 +834,37 @@ static int occupancy_grid(const void *fn, int threads) {
 }
 
 // One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
+// A batched frame (a.views set) runs the variants that look up each pixel's view.
+static int g_trace = 0, g_shade = 0, g_any = 0;
+
+// grids of the persistent bounce kernels (set once, before any stream capture)
+static void init_grids() {
+    if (g_trace) return;
+    g_shade = occupancy_grid((const void *)k_shade<false, false>, 128);
+    g_any = occupancy_grid((const void *)k_anyhit<false, false>, 128);
+    g_trace = occupancy_grid((const void *)k_trace<false>, 128);
+}
+
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade) {
-    static int g_trace = 0, g_shade = 0, g_any = 0;
-    if (!g_trace) {
-        g_trace = occupancy_grid((const void *)k_trace, 128);
-        g_shade = occupancy_grid((const void *)k_shade<false>, 128);
-        g_any = occupancy_grid((const void *)k_anyhit<false>, 128);
+    init_grids();
+    const bool batch = a.views != nullptr;
+    if (batch && a.capture) {
+        set_error("capture is not available for batched frames");
+        return VRG_ERR_UNSUPPORTED;
     }
-    k_trace<<<g_trace, 128, 0, s>>>(a, b);
+    if (batch) k_trace<true><<<g_trace, 128, 0, s>>>(a, b);
+    else k_trace<false><<<g_trace, 128, 0, s>>>(a, b);
     if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
-    if (a.capture) k_shade<true><<<g_shade, 128, 0, s>>>(a, b);
-    else k_shade<false><<<g_shade, 128, 0, s>>>(a, b);
+    if (batch) k_shade<false, true><<<g_shade, 128, 0, s>>>(a, b);
+    else if (a.capture) k_shade<true, false><<<g_shade, 128, 0, s>>>(a, b);
+    else k_shade<false, false><<<g_shade, 128, 0, s>>>(a, b);
     if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
     if (b + 1 < a.nb) {
-        if (a.capture) k_anyhit<true><<<g_any, 128, 0, s>>>(a, b);
-        else k_anyhit<false><<<g_any, 128, 0, s>>>(a, b);
-        k_hit_eval<<<g_shade, 128, 0, s>>>(a);
+        if (batch) k_anyhit<false, true><<<g_any, 128, 0, s>>>(a, b);
+        else if (a.capture) k_anyhit<true, false><<<g_any, 128, 0, s>>>(a, b);
+        else k_anyhit<false, false><<<g_any, 128, 0, s>>>(a, b);
+        if (batch) k_hit_eval<true><<<g_shade, 128, 0, s>>>(a);
+        else k_hit_eval<false><<<g_shade, 128, 0, s>>>(a);
         if (a.capture) k_hit_sum<true><<<g_shade, 128, 0, s>>>(a, b);
         else k_hit_sum<false><<<g_shade, 128, 0, s>>>(a, b);
         VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
@@ -840,6 +873,9 @@ vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEve
     return VRG_OK;
 }
 
-int bounce_blocks_per_sm() { return 1; }
+int bounce_blocks_per_sm() {
+    init_grids();
+    return 1;
+}
 
 }  // namespace vrg

@@ -22,12 +22,29 @@ constexpr int CNT_TRAIN = 49;    // radiance-cache training paths of the frame
 constexpr int CNT_WORDS = 64;
 constexpr int MAX_BOUNCES = 8;
 
-struct FrameArgs {
+// One camera view of one scene.  A frame renders either one view (the
+// FrameArgs::v0 fields, passed as kernel parameters) or a batch of views whose
+// pixels are numbered view after view in one pixel space (FrameArgs::views in
+// device memory, so that a captured launch sequence reads each frame's
+// cameras, seeds and scenes from there).  Pixel streams and reservoir
+// neighbourhoods use the view-local pixel index p - pix_off, so a view renders
+// the same image alone or inside a batch.
+struct ViewDev {
     DevScene sc;
     f3 eye, front, right, up;
-    uint32_t W, H, P;
-    uint32_t nb, nee_type, frame;
-    uint32_t mode, spatial_iters, temporal_seed, spatial_seed;
+    uint32_t W, H, pix_off, pix_end;
+    uint32_t frame, temporal_seed, spatial_seed, pad;
+};
+constexpr int VIEW_SHIFT = 8;  // vtab entry per 256 pixels: the view of the group's first pixel
+
+struct FrameArgs {
+    ViewDev v0;                   // the view of a single-view frame
+    const ViewDev *views;         // batched frame: the views (device), else null
+    const uint16_t *vtab;         // batched frame: view of pixel group p >> VIEW_SHIFT
+    uint32_t n_views;
+    uint32_t P;                   // pixels of the frame (all views)
+    uint32_t nb, nee_type;
+    uint32_t mode, spatial_iters;
     float spatial_radius;
     uint32_t m_cap, debug_view, accumulate, pack;
     // wavefront state
@@ -61,5 +78,18 @@ struct FrameArgs {
     float *c_origin, *c_dir, *c_normal, *c_emis, *c_refl, *c_mis, *c_pdf, *c_nee, *c_L, *c_q;
     uint32_t *c_hit;
 };
+
+// The view that owns pixel p of the frame.
+template <bool BATCH>
+__device__ __forceinline__ const ViewDev &view_of(const FrameArgs &a, uint32_t p) {
+    if constexpr (BATCH) {
+        uint32_t v = a.vtab[p >> VIEW_SHIFT];
+        while (p >= a.views[v].pix_end) v++;  // views smaller than a pixel group
+        return a.views[v];
+    } else {
+        (void)p;
+        return a.v0;
+    }
+}
 
 }  // namespace vrg

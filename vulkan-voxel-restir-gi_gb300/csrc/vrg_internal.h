@@ -14,6 +14,7 @@
 
 #include "../../include/vrg.h"
 #include "vrg_device.cuh"
+#include "vrg_frame.cuh"
 
 namespace vrg {
 
@@ -166,6 +167,22 @@ void nrc_layout(uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1
 struct Renderer {
     Context *ctx = nullptr;
     uint32_t W = 0, H = 0, nb_max = 0;
+    uint64_t P = 0;                       // pixels of a frame (all views of a batched renderer)
+    // batched views (n_views == 0: single-view renderer)
+    uint32_t n_views = 0;
+    std::vector<uint32_t> vw, vh;         // view extents
+    std::vector<uint64_t> voff;           // first pixel of each view
+    DevBufPtr view_buf;                   // ViewDev[n_views] + vtab
+    ViewDev *d_views = nullptr;
+    uint16_t *d_vtab = nullptr;
+    ViewDev *h_views = nullptr;           // pinned staging, 2 x n_views
+    cudaEvent_t ev_stage[2] = {};         // after the copy out of each staging half
+    uint32_t stage = 0;
+    struct GraphEntry {
+        std::vector<uint8_t> key;         // the frame's FrameArgs bytes
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
     uint32_t frame = 0;
     uint32_t ring_slots = 0;
     uint32_t last_nb = 0;

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -30,7 +31,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_NOT_FOUND, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_UNSUPP
     ERR_OVERFLOW, ERR_STATE, ERR_NO_DEVICE = range(9)
 
 MODE_PARITY, MODE_CONFIG = 0, 1
-RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY = 1, 2, 4, 8
+RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY, RENDER_GRAPH = 1, 2, 4, 8, 16
 NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS = range(5)
 (DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
  DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL) = range(14)
@@ -76,6 +77,11 @@ class NrcDesc(C.Structure):
                 ("base_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("batch", C.c_uint32),
                 ("learning_rate", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
                 ("scene_max", C.c_float * 3)]
+
+
+class View(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("temporal_seed", C.c_uint32),
+                ("spatial_seed", C.c_uint32)]
 
 
 class FrameOutput(C.Structure):
@@ -137,6 +143,10 @@ SIGNATURES = [
     ("vrg_nrc_write", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
     ("vrg_nrc_layout", C.c_int32, [_P, C.POINTER(C.c_uint32), _P, _P, _P]),
     ("vrg_renderer_set_cache", C.c_int32, [_P, _P]),
+    ("vrg_renderer_create_batched", C.c_int32, [_P, C.c_uint32, _P, _P, C.c_uint32, C.POINTER(_P)]),
+    ("vrg_renderer_view_offset", C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_uint64)]),
+    ("vrg_render_batched", C.c_int32, [_P, C.POINTER(View), C.c_uint32, C.POINTER(RenderParams), _P,
+                                       C.POINTER(FrameStats)]),
 ]
 
 
@@ -236,6 +246,13 @@ class Context:
         self.h = C.c_void_p()
         desc = ContextDesc(device, 0)
         check(self.lib.vrg_context_create(C.byref(desc), C.byref(self.h)), "vrg_context_create")
+        # handles made from this context; closed before it, whatever the
+        # order in which Python collects them
+        self._children = weakref.WeakSet()
+
+    def adopt(self, obj):
+        self._children.add(obj)
+        return obj
 
     def set_materials(self, mats, n=None):
         n = len(mats) if n is None else n
@@ -246,6 +263,8 @@ class Context:
 
     def close(self):
         if self.h:
+            for c in list(self._children):
+                c.close()
             self.lib.vrg_context_destroy(self.h)
             self.h = C.c_void_p()
 
@@ -260,6 +279,7 @@ class UploadedObject:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self.h = handle
+        ctx.adopt(self)
 
     def info(self):
         v = [C.c_uint32() for _ in range(4)]
@@ -283,6 +303,8 @@ class UploadedObject:
         if self.h:
             self.ctx.lib.vrg_object_release(self.h)
             self.h = None
+
+    close = release
 
     def __del__(self):
         try:
@@ -320,6 +342,7 @@ class Scene:
         self.h = C.c_void_p()
         check(ctx.lib.vrg_scene_create(ctx.h, C.byref(self.h)), "vrg_scene_create")
         self._objs = {}
+        ctx.adopt(self)
 
     def add_object(self, key: int, obj: UploadedObject, translation=(0, 0, 0)):
         check(self.ctx.lib.vrg_scene_add(self.h, key, obj.h, _xform(translation)), "vrg_scene_add")
@@ -372,6 +395,7 @@ class Renderer:
         self.h = C.c_void_p()
         check(ctx.lib.vrg_renderer_create(ctx.h, width, height, num_bounces, C.byref(self.h)),
               "vrg_renderer_create")
+        ctx.adopt(self)
         self.seeds = Pcg32(0x5eed)
         self.last_stats = FrameStats()
 
@@ -439,6 +463,72 @@ class Renderer:
             pass
 
 
+class BatchRenderer:
+    """Many views of independent scenes and extents rendered by one launch
+    sequence (vrg_render_batched); no reference counterpart."""
+
+    def __init__(self, ctx: Context, extents, num_bounces: int = 2):
+        self.ctx = ctx
+        self.extents = [(int(w), int(h)) for w, h in extents]
+        self.num_bounces = num_bounces
+        n = len(self.extents)
+        ws = np.array([w for w, _ in self.extents], np.uint32)
+        hs = np.array([h for _, h in self.extents], np.uint32)
+        self.h = C.c_void_p()
+        check(ctx.lib.vrg_renderer_create_batched(ctx.h, n, _ptr(ws), _ptr(hs), num_bounces, C.byref(self.h)),
+              "vrg_renderer_create_batched")
+        ctx.adopt(self)
+        self.offsets = []
+        for v in range(n):
+            o = C.c_uint64()
+            check(ctx.lib.vrg_renderer_view_offset(self.h, v, C.byref(o)), "vrg_renderer_view_offset")
+            self.offsets.append(o.value)
+        self.pixels = sum(w * h for w, h in self.extents)
+        self.last_stats = FrameStats()
+
+    def render(self, scenes, cameras, params: RenderParams, seeds, want_image=False, want_radiance=False):
+        """scenes/cameras/seeds: one per view (seeds = (temporal, spatial)).
+        Returns per-view lists of images / radiance (None when not asked for)."""
+        n = len(self.extents)
+        views = (View * n)()
+        for v in range(n):
+            views[v] = View(scenes[v].h, cameras[v], seeds[v][0], seeds[v][1])
+        imgs, rads = [], []
+        outs = (FrameOutput * n)()
+        for v, (w, h) in enumerate(self.extents):
+            img = np.empty((h, w, 4), np.uint8) if want_image else None
+            rad = np.empty((h, w, 3), np.float32) if want_radiance else None
+            outs[v] = FrameOutput(None if img is None else img.ctypes.data, None if rad is None else rad.ctypes.data,
+                                  1, 0)
+            imgs.append(img)
+            rads.append(rad)
+        check(self.ctx.lib.vrg_render_batched(self.h, views, n, C.byref(params),
+                                              C.cast(outs, C.c_void_p) if (want_image or want_radiance) else None,
+                                              C.byref(self.last_stats)), "vrg_render_batched")
+        return imgs, rads
+
+    def read_accumulation(self):
+        n = C.c_uint32()
+        a = np.zeros(self.pixels * 3, dtype=np.float32)
+        check(self.ctx.lib.vrg_renderer_read_accumulation(self.h, _ptr(a), C.byref(n)),
+              "vrg_renderer_read_accumulation")
+        out = []
+        for (w, h), o in zip(self.extents, self.offsets):
+            out.append(a[3 * o:3 * (o + w * h)].reshape(h, w, 3))
+        return out, n.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.vrg_renderer_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 NRC_MASTER = 5 * 64 * 64 + 16 * 64
 
 
@@ -453,6 +543,7 @@ class RadianceCache:
                     (C.c_float * 3)(*scene_min), (C.c_float * 3)(*scene_max))
         self.h = C.c_void_p()
         check(ctx.lib.vrg_nrc_create(ctx.h, C.byref(d), C.byref(self.h)), "vrg_nrc_create")
+        ctx.adopt(self)
 
     def query(self, pos, normal, direction):
         pos, normal, direction = (np.ascontiguousarray(a, np.float32) for a in (pos, normal, direction))
