@@ -143,26 +143,44 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
-    """The oracle on the same workload, only `rows` image rows traced per frame.
-    Returns (Mrays/s, seconds, rays)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    import vrg
-    ow = oracle.build_world(mats, n, world)
-    orr = oracle.Renderer(W, H, NB)
-    rays = 0
-    t0 = time.perf_counter()
-    for f in range(frames):
-        cam = vrg.orbit_camera(NX, NZ, (start_frame + f) % ORBIT, ORBIT, W, H)
+class OracleSampler:
+    """The oracle (CPU restatement of the reference's path, OpenMP over pixels)
+    on the same workload: world built once, then frames of the orbit rendered
+    with `rows` image rows around the centre traced per frame."""
+
+    def __init__(self, world, mats, n, rows):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        self.ow = oracle.build_world(mats, n, world)
+        self.orr = oracle.Renderer(W, H, NB)
+        self.rows = min(rows, H)
+
+    def frame(self, f):
+        """Renders orbit frame f; returns (seconds, rays)."""
+        import vrg
+        cam = vrg.orbit_camera(NX, NZ, f % ORBIT, ORBIT, W, H)
         p = vrg.RenderParams(1, 1, 3, NB, vrg.MODE_CONFIG, f, 1000 + f, 2000 + f, 30.0, 20, 1, 0, 0)
-        y0 = (H // 2 - rows // 2)
-        orr.render(ow, cam, p, (y0 * W, (y0 + rows) * W))
-        a, b = orr.ray_counts()
-        rays += a + b
-    dt = time.perf_counter() - t0
-    orr.close()
-    ow.close()
+        y0 = H // 2 - self.rows // 2
+        t0 = time.perf_counter()
+        self.orr.render(self.ow, cam, p, (y0 * W, (y0 + self.rows) * W))
+        dt = time.perf_counter() - t0
+        a, b = self.orr.ray_counts()
+        return dt, a + b
+
+    def close(self):
+        self.orr.close()
+        self.ow.close()
+
+
+def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
+    """Returns (Mrays/s, seconds, rays) of `frames` oracle frames."""
+    smp = OracleSampler(world, mats, n, rows)
+    dt, rays = 0.0, 0
+    for f in range(frames):
+        t, r_ = smp.frame(start_frame + f)
+        dt += t
+        rays += r_
+    smp.close()
     return rays / dt / 1e6, dt, rays
 
 
@@ -196,8 +214,7 @@ def batched_block(ctx, steps, warmup):
     ctx.flush()  # every chunk of every scene: one batched extraction + BLAS build
     t_blas = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for sc in scenes:
-        sc.commit()
+    vrg.commit_scenes(scenes)  # all top-level trees in one SAH build, all lamp trees in another
     t_tl = time.perf_counter() - t0
     br = vrg.BatchRenderer(ctx, res, 2)
     seeds = vrg.Pcg32(C2_SEED)
@@ -244,13 +261,15 @@ def run_reference(args, d):
     world = vrg.terrain_blocks(SEED, NX, NZ, EMISSIVE)
     rows = args.ref_rows
     threads = cpu_threads()
+    smp = OracleSampler(world, mats, n, rows)
     for w in range(args.warmup):
-        oracle_sample(world, mats, n, rows, 1, w)
+        smp.frame(w)
     times, rays_all = [], 0
     for s in range(args.steps):
-        mr, dt, rays = oracle_sample(world, mats, n, rows, 1, args.warmup + s)
+        dt, rays = smp.frame(args.warmup + s)
         times.append(dt)
         rays_all += rays
+    smp.close()
     total = sum(times)
     value = rays_all / total / 1e6
     line = {
@@ -378,7 +397,9 @@ def run_ours(args, d):
     if not args.no_batched:
         r.close()  # the batch needs the memory of the 1080p renderer
         batched = batched_block(ctx, steps=16, warmup=3)
-    cpu_mr, cpu_dt, cpu_rays = oracle_sample(world, mats, n, args.ref_rows, 1, 0) if not args.no_cpu else (None, 0, 0)
+    cpu_frames = args.cpu_frames
+    cpu_mr, cpu_dt, cpu_rays = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0) if not args.no_cpu
+                                else (None, 0, 0))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total_s_max / args.steps, 4),
@@ -416,7 +437,8 @@ def run_ours(args, d):
         "clocks": clocks,
         "cpu_baseline": None if cpu_mr is None else {
             "value": round(cpu_mr, 4), "unit": "Mrays/s", "cores": cpu_threads(), "kind": "port",
-            "sample": f"{args.ref_rows} of {H} rows of frame 0 ({cpu_dt:.1f} s, {cpu_rays} rays)"},
+            "sample": f"{min(args.ref_rows, H)} of {H} rows of orbit frames 0-{cpu_frames - 1} "
+                      f"({cpu_dt:.1f} s, {cpu_rays} rays)"},
     }
     print(json.dumps(line), flush=True)
     d.close()
@@ -428,7 +450,8 @@ def main():
     ap.add_argument("--steps", type=int, default=64)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--ref-rows", type=int, default=96, help="image rows the CPU baseline traces per frame")
+    ap.add_argument("--ref-rows", type=int, default=1080, help="image rows the CPU baseline traces per frame")
+    ap.add_argument("--cpu-frames", type=int, default=16, help="frames of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")

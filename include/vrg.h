@@ -215,6 +215,10 @@ VRG_API vrg_status vrg_scene_remove(vrg_scene *scene, uint64_t key);
 /* = get_tlas: rebuilds the top levels (light TL BVH, geometry TL BVH) and
  * the traversal layouts when something changed; frees retired objects. */
 VRG_API vrg_status vrg_scene_commit(vrg_scene *scene);
+/* Commits several scenes of one context at once (no reference counterpart):
+ * the same result per scene as vrg_scene_commit, with all their top-level
+ * trees built by one SAH build and all their lamp-block trees by another. */
+VRG_API vrg_status vrg_scene_commit_many(vrg_scene *const *scenes, uint32_t n);
 /* Copies the top-level BVHs (which: 0 light TL, 1 geometry TL). */
 VRG_API vrg_status vrg_scene_read_tl(vrg_scene *scene, uint32_t which, vrg_bvh_node *nodes,
                                      uint32_t cap, uint32_t *n_nodes);

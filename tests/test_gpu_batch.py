@@ -133,3 +133,50 @@ def test_batched_rejects_mismatched_views(gpu_ctx, world):
     assert lib.vrg_render(br.h, scenes[0].h, C.byref(cam), C.byref(_params()), None, None) == vrg.ERR_STATE
     r.close()
     br.close()
+
+
+def test_commit_many_matches_single_commits(gpu_ctx):
+    """Scenes committed together (one top-level and one lamp SAH build for all)
+    equal the same scenes committed one by one: top-level node arrays and
+    rendered frames, bit for bit.  Includes a scene without lights and an
+    empty scene."""
+    mats, n = vrg.terrain_materials(MAT_SEED)
+    gpu_ctx.set_materials(mats, n)
+    specs = [(21, 2, 2, 0.01), (22, 1, 1, 0.0), (23, 3, 1, 0.02), None]
+
+    def make():
+        out = []
+        for spec in specs:
+            if spec is None:
+                out.append((vrg.Scene(gpu_ctx), []))
+            else:
+                seed, nx, nz, em = spec
+                out.append(vrg.build_world(gpu_ctx, vrg.terrain_blocks(seed, nx, nz, em)))
+        return out
+
+    one = make()
+    for sc, _ in one:
+        sc.commit()
+    many = make()
+    vrg.commit_scenes([sc for sc, _ in many])
+    for (a, _), (b, _), spec in zip(one, many, specs):
+        ta, tb = a.get_tlas(), b.get_tlas()  # already committed: reads the top levels
+        for x, y in zip(ta, tb):
+            assert x.tobytes() == y.tobytes()
+        nx, nz = (1, 1) if spec is None else spec[1:3]
+        cam = vrg.orbit_camera(nx, nz, 3, 64, 48, 32)
+        imgs = []
+        for sc in (a, b):  # a fresh renderer each: same frame index, empty history
+            r = vrg.Renderer(gpu_ctx, 48, 32, 2)
+            p = _params()
+            p.temporal_seed, p.spatial_seed = 5, 6
+            _, rad = r.render_params(sc, cam, p, want_image=False, want_radiance=True)
+            imgs.append(rad.copy())
+            assert r.last_stats.error_flags == 0
+            r.close()
+        assert _same_bits(imgs[0], imgs[1])
+    for group in (one, many):
+        for sc, objs in group:
+            sc.close()
+            for o in objs:
+                o.release()

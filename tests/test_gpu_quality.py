@@ -47,3 +47,5 @@ def test_cache_beats_plain_at_equal_time(gpu_ctx):
     assert res["cache"]["relmse_1spp"] < res["plain"]["relmse_1spp"], res
     assert res["cache"]["relmse_mean_of_frames"] < res["plain"]["relmse_mean_of_frames"], res
     assert res["cache"]["nonfinite"] == 0.0 and np.isfinite(res["restir"]["relmse_1spp"])
+    # and under ReSTIR: resampling cache-terminated paths beats resampling plain ones
+    assert res["restir_cache"]["relmse_1spp"] < res["restir"]["relmse_1spp"], res

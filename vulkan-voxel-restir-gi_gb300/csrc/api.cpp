@@ -332,6 +332,16 @@ VRG_API vrg_status vrg_scene_commit(vrg_scene *scene) {
     return scene_commit(scene);
 }
 
+VRG_API vrg_status vrg_scene_commit_many(vrg_scene *const *scenes, uint32_t n) {
+    if (!scenes && n) return VRG_ERR_INVALID_ARGUMENT;
+    std::vector<Scene *> scs(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (!scenes[i]) return VRG_ERR_INVALID_ARGUMENT;
+        scs[i] = scenes[i];
+    }
+    return scene_commit_many(scs.data(), n);
+}
+
 VRG_API vrg_status vrg_scene_read_tl(vrg_scene *scene, uint32_t which, vrg_bvh_node *nodes, uint32_t cap,
                                      uint32_t *n_nodes) {
     if (!scene || which > 1) return VRG_ERR_INVALID_ARGUMENT;
@@ -891,7 +901,11 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
         }
     }
     cudaStream_t s = r->ctx->stream;
-    for (uint32_t v = 0; v < n_views; v++) VRG_TRY(scene_commit(views[v].scene));
+    {
+        std::vector<Scene *> scs(n_views);
+        for (uint32_t v = 0; v < n_views; v++) scs[v] = views[v].scene;
+        VRG_TRY(scene_commit_many(scs.data(), n_views));
+    }
     bool want_rad = false;
     if (outs)
         for (uint32_t v = 0; v < n_views; v++) want_rad |= outs[v].radiance != nullptr;

@@ -6,12 +6,16 @@
 //     (light_bvh_tl_idx, scene.rs:282-287);
 //   * the geometry top-level BVH over objects (same builder), replacing the
 //     driver TLAS (scene.rs:728-971);
-//   * the traversal layouts: one world-space BVH2 per structure in which
-//     each 64-byte node holds both children's boxes (translated to world
-//     space and widened by BOX_MARGIN, so culling is conservative) and child
-//     references (>= 0 node, < 0 ~record), with top-level leaves linked
-//     straight to the object's BLAS root; and 16-byte world-space records per
-//     surface block / light triangle.
+//   * the closest-hit traversal layout: a world-space 4-wide BVH over the
+//     combined [top level | every object's BLAS] tree, in which each
+//     128-byte node holds its (up to) four grandchild-level children's boxes
+//     as SoA (translated to world space and widened by BOX_MARGIN, so culling
+//     is conservative) and child references (>= 0 node, < 0 ~record), with
+//     top-level leaves linked straight to the object's BLAS root; and
+//     16-byte world-space records per surface block / light triangle;
+//   * the light any-hit layout: a 2-wide world-space BVH over lamp blocks.
+// Several scenes commit together with one SAH build for all their top-level
+// trees and one for all their lamp trees.
 #include <algorithm>
 
 #include "vrg_internal.h"
@@ -33,57 +37,6 @@ struct InstBuild {
 
 __device__ __forceinline__ int bl_root_ref(const InstBuild &I) {
     return I.bl[0].left_node_idx != INVALID ? (int)I.wbase : ~(int)(I.rbase + I.leaf[0]);
-}
-
-// one thread per node of the combined index space [TL nodes | BLAS nodes...]
-__global__ void k_wide(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *inst, uint32_t n_inst,
-                       uint32_t n_total, float4 *wide) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n_total) return;
-    const vrg_bvh_node *node;
-    int k = -1;
-    uint32_t j;
-    if (g < n_tl) {
-        node = &tl[g];
-        j = g;
-    } else {
-        int lo = 0, hi = (int)n_inst - 1;
-        while (lo < hi) {  // last instance with wbase <= g
-            int mid = (lo + hi + 1) >> 1;
-            if (inst[mid].wbase <= g) lo = mid; else hi = mid - 1;
-        }
-        k = lo;
-        j = g - inst[k].wbase;
-        node = &inst[k].bl[j];
-    }
-    if (node->left_node_idx == INVALID) return;
-    uint32_t ch[2] = {node->left_node_idx, node->right_node_idx_or_prim_idx};
-    float box[2][6];
-    int ref[2];
-    for (int s = 0; s < 2; s++) {
-        const vrg_bvh_node *c;
-        float off[3] = {0.0f, 0.0f, 0.0f};
-        if (k < 0) {
-            c = &tl[ch[s]];
-            if (c->left_node_idx != INVALID) ref[s] = (int)ch[s];
-            else ref[s] = bl_root_ref(inst[c->right_node_idx_or_prim_idx]);
-        } else {
-            const InstBuild &I = inst[k];
-            c = &I.bl[ch[s]];
-            off[0] = I.off[0]; off[1] = I.off[1]; off[2] = I.off[2];
-            if (c->left_node_idx != INVALID) ref[s] = (int)(I.wbase + ch[s]);
-            else ref[s] = ~(int)(I.rbase + I.leaf[ch[s]]);
-        }
-        for (int a = 0; a < 3; a++) {
-            box[s][a] = (c->min[a] + off[a]) - BOX_MARGIN;
-            box[s][3 + a] = (c->max[a] + off[a]) + BOX_MARGIN;
-        }
-    }
-    float4 *w = wide + 4 * (size_t)g;
-    w[0] = make_float4(box[0][0], box[0][3], box[0][1], box[0][4]);
-    w[1] = make_float4(box[0][2], box[0][5], box[1][0], box[1][3]);
-    w[2] = make_float4(box[1][1], box[1][4], box[1][2], box[1][5]);
-    w[3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), 0.0f, 0.0f);
 }
 
 // 4-wide traversal node for every inner node g of the combined index space:
@@ -352,72 +305,6 @@ __global__ void k_wide_single(const vrg_bvh_node *nodes, const uint32_t *leaf, u
 
 }  // namespace
 
-// The light any-hit walk (nee_pdf's candidate enumeration) runs over a
-// world-space SAH BVH of the lamp blocks: a leaf tests the block's emissive
-// faces and maps the hit (face, half) to its light-BLAS leaf, so the set of
-// light triangles found is the same as walking the triangle light BVH.
-static vrg_status build_lamp_layout(Scene *sc, const int4 *light_rec, uint32_t n_light, uint32_t *depth) {
-    cudaStream_t s = sc->ctx->stream;
-    DevScene &D = sc->dev;
-    D.lamp_root = EMPTY_ROOT;
-    *depth = 0;
-    if (n_light == 0) return VRG_OK;
-    auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
-    const uint64_t n = n_light;
-    uint64_t o = 0;
-    uint64_t o_flag = o; o += al(n * 4);
-    uint64_t o_tot = o; o += 256;
-    uint64_t o_lo = o; o += al(n * 16);
-    uint64_t o_hi = o; o += al(n * 16);
-    uint64_t o_cen = o; o += al(n * 16);
-    uint64_t o_id = o; o += al(n * 4);
-    uint64_t o_perm = o; o += al(n * 4);
-    uint64_t o_nodes = o; o += al(2 * n * sizeof(vrg_bvh_node));
-    uint64_t o_leaf = o; o += al(2 * n * 4);
-    uint64_t o_rec = o; o += al(n * 16);
-    uint64_t o_tab = o; o += al(n * 12 * 4);
-    uint64_t o_wide = o; o += al(2 * n * 64);
-    DevBufPtr buf;
-    VRG_TRY(dev_alloc(s, o, buf));
-    uint8_t *B = (uint8_t *)buf->ptr;
-    uint32_t *flag = (uint32_t *)(B + o_flag), *tot = (uint32_t *)(B + o_tot);
-    int4 *lamp = (int4 *)(B + o_rec);
-    uint32_t *table = (uint32_t *)(B + o_tab);
-    VRG_CUDA_TRY(cudaMemsetAsync(lamp, 0, n * 16, s));
-    VRG_CUDA_TRY(cudaMemsetAsync(table, 0xFF, n * 48, s));
-    k_lamp_flags<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, n_light, flag);
-    k_scan_inclusive<<<1, 1024, 0, s>>>(flag, n_light, tot);
-    k_lamp_fill<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, flag, n_light, lamp, table,
-                                                           (float4 *)(B + o_lo), (float4 *)(B + o_hi),
-                                                           (float4 *)(B + o_cen), (uint32_t *)(B + o_id));
-    VRG_CUDA_TRY(cudaGetLastError());
-    uint32_t n_lamps = 0;
-    VRG_CUDA_TRY(cudaMemcpyAsync(&n_lamps, tot, 4, cudaMemcpyDeviceToHost, s));
-    VRG_CUDA_TRY(cudaStreamSynchronize(s));
-    std::vector<SahTree> trees{SahTree{n_lamps, 0, 0, 0}};
-    SahInputs in{(const float4 *)(B + o_lo), (const float4 *)(B + o_hi), (const float4 *)(B + o_cen),
-                 (const uint32_t *)(B + o_id)};
-    vrg_bvh_node *nodes = (vrg_bvh_node *)(B + o_nodes);
-    uint32_t *leaf = (uint32_t *)(B + o_leaf);
-    SahOutputs out{nodes, (uint32_t *)(B + o_perm), leaf};
-    uint32_t levels = 0;
-    VRG_TRY(sah_build(s, trees, n_lamps, 2 * n_lamps - 1, in, out, &levels));
-    float4 *wide = (float4 *)(B + o_wide);
-    if (n_lamps > 1) {
-        k_wide_single<<<(2 * n_lamps - 1 + 255) / 256, 256, 0, s>>>(nodes, leaf, 2 * n_lamps - 1, wide);
-        VRG_CUDA_TRY(cudaGetLastError());
-        D.lamp_root = 0;
-    } else {
-        D.lamp_root = ~0;
-    }
-    D.lamp_wide = wide;
-    D.lamp_rec = lamp;
-    D.lamp_table = table;
-    sc->lamp_buf = buf;
-    *depth = levels + 2;
-    return VRG_OK;
-}
-
 vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t *n, const uint32_t *prim_offset,
                           const uint32_t *node_offset, const float *prims, const float *translations,
                           const float *power, const uint32_t *ids, vrg_bvh_node *nodes_out, uint32_t *order_out) {
@@ -483,22 +370,42 @@ vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t
     return VRG_OK;
 }
 
-vrg_status scene_commit(Scene *sc) {
-    Context *ctx = sc->ctx;
-    cudaStream_t s = ctx->stream;
-    {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        std::vector<Object *> pend;
-        pend.swap(ctx->pending);
-        vrg_status st = extract_and_build(ctx, pend);
-        if (st != VRG_OK) {
-            ctx->pending.insert(ctx->pending.end(), pend.begin(), pend.end());
-            return st;
-        }
-        for (Object *o : pend)  // drop the pending list's reference
-            if (--o->refs == 0) delete o;
-    }
-    if (!sc->dirty) return VRG_OK;
+// ---- scene commit ----------------------------------------------------------
+//
+// Several scenes commit together: their top-level trees (light and geometry)
+// are built by ONE level-synchronous SAH build, and so are their lamp-block
+// trees, so the per-level host round trips of the builder are paid once per
+// commit, not once per scene.  Each scene's result is the same as a commit of
+// that scene alone (the builder's trees are independent).
+//
+// The light any-hit walk (nee_pdf's candidate enumeration) runs over a
+// world-space SAH BVH of the lamp blocks: a leaf tests the block's emissive
+// faces and maps the hit (face, half) to its light-BLAS leaf, so the set of
+// light triangles found is the same as walking the triangle light BVH.
+
+namespace {
+
+struct CommitPrep {
+    Scene *sc = nullptr;
+    uint32_t ni = 0, n_light_inst = 0, n_geo_inst = 0, n_light_tl = 1, n_geo_tl = 0;
+    std::vector<float> tl_in;        // [prims][10]: lo3 hi3 off3 power
+    std::vector<uint32_t> tl_ids;
+    std::vector<InstBuild> gb, lb;
+    uint64_t geo_recs = 0, light_recs = 0, n_geo_wide = 0;
+    uint32_t max_levels = 0;
+    DevBufPtr buf;
+    uint8_t *B = nullptr;
+    uint64_t o_gw = 0, o_gr = 0, o_lr = 0, o_tln = 0, o_inst = 0, o_gb = 0, o_lb = 0;
+    uint32_t tl_prim_off = 0, tl_node_off = 0;  // in the shared top-level build
+    uint64_t lamp_off = 0;                      // in the shared lamp build
+    uint32_t n_lamps = 0;
+    DevBufPtr lamp_buf;
+    uint32_t lamp_depth = 0;
+    DevScene dev{};                             // installed only when the whole commit succeeds
+};
+
+vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
+    cp.sc = sc;
     // instances: non-empty objects in key order (scene.rs:245-260)
     sc->inst_objs.clear();
     sc->inst_off.clear();
@@ -517,19 +424,17 @@ vrg_status scene_commit(Scene *sc) {
         set_error("more than 65535 instances");
         return VRG_ERR_UNSUPPORTED;
     }
-    // top-level inputs
-    std::vector<float> tl_in;
-    std::vector<uint32_t> tl_ids;
-    uint32_t n_light_inst = 0, n_geo_inst = 0;
+    cp.ni = ni;
+    // top-level inputs: light roots, then geometry roots
     for (uint32_t i = 0; i < ni; i++) {
         const ChunkSummary &cs = sc->inst_objs[i]->sum;
         if (cs.n_light == 0) continue;
         const float *o = sc->inst_off[i].data();
         float r[10] = {cs.light_lo[0], cs.light_lo[1], cs.light_lo[2], cs.light_hi[0], cs.light_hi[1],
                        cs.light_hi[2], o[0], o[1], o[2], cs.light_power};
-        tl_in.insert(tl_in.end(), r, r + 10);
-        tl_ids.push_back(i);
-        n_light_inst++;
+        cp.tl_in.insert(cp.tl_in.end(), r, r + 10);
+        cp.tl_ids.push_back(i);
+        cp.n_light_inst++;
     }
     for (uint32_t i = 0; i < ni; i++) {
         const ChunkSummary &cs = sc->inst_objs[i]->sum;
@@ -537,106 +442,153 @@ vrg_status scene_commit(Scene *sc) {
         const float *o = sc->inst_off[i].data();
         float r[10] = {cs.geo_lo[0], cs.geo_lo[1], cs.geo_lo[2], cs.geo_hi[0], cs.geo_hi[1], cs.geo_hi[2],
                        o[0], o[1], o[2], 0.0f};
-        tl_in.insert(tl_in.end(), r, r + 10);
-        tl_ids.push_back(i);
-        n_geo_inst++;
+        cp.tl_in.insert(cp.tl_in.end(), r, r + 10);
+        cp.tl_ids.push_back(i);
+        cp.n_geo_inst++;
     }
-    const uint32_t n_tl_prims = n_light_inst + n_geo_inst;
-    const uint32_t n_light_tl = n_light_inst ? 2 * n_light_inst - 1 : 1;
-    const uint32_t n_geo_tl = n_geo_inst ? 2 * n_geo_inst - 1 : 0;
+    cp.n_light_tl = cp.n_light_inst ? 2 * cp.n_light_inst - 1 : 1;
+    cp.n_geo_tl = cp.n_geo_inst ? 2 * cp.n_geo_inst - 1 : 0;
     // per-instance layout
-    uint64_t geo_nodes = 0, geo_recs = 0, light_nodes = 0, light_recs = 0;
-    std::vector<InstBuild> gb(ni), lb(ni);
-    uint32_t max_levels = 0;
+    uint64_t geo_nodes = 0, light_nodes = 0;
+    cp.gb.resize(ni);
+    cp.lb.resize(ni);
     for (uint32_t i = 0; i < ni; i++) {
         Object *o = sc->inst_objs[i];
         const ChunkSummary &cs = o->sum;
+        InstBuild &g = cp.gb[i], &l = cp.lb[i];
         for (int a = 0; a < 3; a++) {
             float t = sc->inst_off[i][a];
             if (t != floorf(t) || fabsf(t) > 16384.0f) {
                 set_error("instance translation must be integral and within +-16384");
                 return VRG_ERR_UNSUPPORTED;
             }
-            gb[i].off[a] = lb[i].off[a] = t;
-            gb[i].ioff[a] = lb[i].ioff[a] = (int)t;
+            g.off[a] = l.off[a] = t;
+            g.ioff[a] = l.ioff[a] = (int)t;
         }
-        gb[i].bl = o->geo_nodes;
-        gb[i].leaf = o->geo_leaf;
-        gb[i].geo_local = o->geo_local;
-        gb[i].light_tri = nullptr;
-        gb[i].n_prims = cs.n_geo;
-        gb[i].wbase = n_geo_tl + (uint32_t)geo_nodes;
-        gb[i].rbase = (uint32_t)geo_recs;
+        g.bl = o->geo_nodes;
+        g.leaf = o->geo_leaf;
+        g.geo_local = o->geo_local;
+        g.light_tri = nullptr;
+        g.n_prims = cs.n_geo;
+        g.wbase = cp.n_geo_tl + (uint32_t)geo_nodes;
+        g.rbase = (uint32_t)cp.geo_recs;
         geo_nodes += cs.n_geo ? 2 * (uint64_t)cs.n_geo - 1 : 0;
-        geo_recs += cs.n_geo;
-        lb[i].bl = o->light_nodes;
-        lb[i].leaf = o->light_leaf;
-        lb[i].geo_local = nullptr;
-        lb[i].light_tri = o->light_tri;
-        lb[i].n_prims = cs.n_light;
-        lb[i].wbase = n_light_tl + (uint32_t)light_nodes;
-        lb[i].rbase = (uint32_t)light_recs;
+        cp.geo_recs += cs.n_geo;
+        l.bl = o->light_nodes;
+        l.leaf = o->light_leaf;
+        l.geo_local = nullptr;
+        l.light_tri = o->light_tri;
+        l.n_prims = cs.n_light;
+        l.wbase = cp.n_light_tl + (uint32_t)light_nodes;
+        l.rbase = (uint32_t)cp.light_recs;
         light_nodes += cs.n_light ? 2 * (uint64_t)cs.n_light - 1 : 0;
-        light_recs += cs.n_light;
-        max_levels = std::max(max_levels, o->levels);
+        cp.light_recs += cs.n_light;
+        cp.max_levels = std::max(cp.max_levels, o->levels);
     }
-    // instances without geometry/lights must not appear in the binary search
-    // of k_wide (wbase stays monotone: they own zero nodes), fine as is.
+    if (cp.n_geo_tl + geo_nodes >= 0x7FFFFFFFull || cp.geo_recs >= 0x7FFFFFFFull) {
+        set_error("scene too large for 31-bit node references");
+        return VRG_ERR_UNSUPPORTED;
+    }
     auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
     uint64_t o = 0;
-    const uint64_t n_geo_wide = n_geo_tl + geo_nodes;
-    uint64_t o_gw = o; o += al(n_geo_wide * 128);
-    uint64_t o_gr = o; o += al(geo_recs * 16);
-    uint64_t o_lr = o; o += al(light_recs * 16);
-    uint64_t o_tln = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * sizeof(vrg_bvh_node));
-    uint64_t o_inst = o; o += al((uint64_t)ni * sizeof(InstDev));
-    uint64_t o_gb = o; o += al((uint64_t)ni * sizeof(InstBuild));
-    uint64_t o_lb = o; o += al((uint64_t)ni * sizeof(InstBuild));
-    // TL build scratch
-    uint64_t o_tin = o; o += al((uint64_t)n_tl_prims * 40);
-    uint64_t o_tid = o; o += al((uint64_t)n_tl_prims * 4);
-    uint64_t o_tlo = o; o += al((uint64_t)n_tl_prims * 16);
-    uint64_t o_thi = o; o += al((uint64_t)n_tl_prims * 16);
-    uint64_t o_tcen = o; o += al((uint64_t)n_tl_prims * 16);
-    uint64_t o_tidd = o; o += al((uint64_t)n_tl_prims * 4);
-    uint64_t o_tperm = o; o += al((uint64_t)n_tl_prims * 4);
-    uint64_t o_tleaf = o; o += al((uint64_t)(n_light_tl + n_geo_tl) * 4);
-    DevBufPtr buf;
-    VRG_TRY(dev_alloc(s, std::max<uint64_t>(o, 256), buf));
-    uint8_t *B = (uint8_t *)buf->ptr;
-    vrg_bvh_node *d_tl = (vrg_bvh_node *)(B + o_tln);  // [light TL | geometry TL]
-    uint32_t tl_levels = 0;
-    if (n_tl_prims) {
-        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_tin, tl_in.data(), tl_in.size() * 4, cudaMemcpyHostToDevice, s));
-        VRG_CUDA_TRY(cudaMemcpyAsync(B + o_tid, tl_ids.data(), tl_ids.size() * 4, cudaMemcpyHostToDevice, s));
-        k_tl_inputs<<<(n_tl_prims + 127) / 128, 128, 0, s>>>((const float *)(B + o_tin), (const uint32_t *)(B + o_tid),
-                                                              n_tl_prims, (float4 *)(B + o_tlo), (float4 *)(B + o_thi),
-                                                              (float4 *)(B + o_tcen), (uint32_t *)(B + o_tidd));
-        VRG_CUDA_TRY(cudaGetLastError());
+    cp.n_geo_wide = cp.n_geo_tl + geo_nodes;
+    cp.o_gw = o; o += al(cp.n_geo_wide * 128);
+    cp.o_gr = o; o += al(cp.geo_recs * 16);
+    cp.o_lr = o; o += al(cp.light_recs * 16);
+    cp.o_tln = o; o += al((uint64_t)(cp.n_light_tl + cp.n_geo_tl) * sizeof(vrg_bvh_node));
+    cp.o_inst = o; o += al((uint64_t)ni * sizeof(InstDev));
+    cp.o_gb = o; o += al((uint64_t)ni * sizeof(InstBuild));
+    cp.o_lb = o; o += al((uint64_t)ni * sizeof(InstBuild));
+    VRG_TRY(dev_alloc(sc->ctx->stream, std::max<uint64_t>(o, 256), cp.buf));
+    cp.B = (uint8_t *)cp.buf->ptr;
+    return VRG_OK;
+}
+
+// all scenes' top-level trees in one SAH build; fills h_light_tl / h_geo_tl
+// and each scene's device copy of its nodes ([light TL | geometry TL])
+vrg_status commit_top_levels(cudaStream_t s, std::vector<CommitPrep> &cps, uint32_t *tl_levels) {
+    uint32_t n_prims = 0, n_nodes = 0;
+    for (auto &cp : cps) {
+        cp.tl_prim_off = n_prims;
+        cp.tl_node_off = n_nodes;
+        n_prims += cp.n_light_inst + cp.n_geo_inst;
+        n_nodes += cp.n_light_tl + cp.n_geo_tl;
+    }
+    *tl_levels = 0;
+    std::vector<vrg_bvh_node> h_nodes(n_nodes);
+    if (n_prims) {
+        auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
+        uint64_t o = 0;
+        uint64_t o_tin = o; o += al((uint64_t)n_prims * 40);
+        uint64_t o_tid = o; o += al((uint64_t)n_prims * 4);
+        uint64_t o_lo = o; o += al((uint64_t)n_prims * 16);
+        uint64_t o_hi = o; o += al((uint64_t)n_prims * 16);
+        uint64_t o_cen = o; o += al((uint64_t)n_prims * 16);
+        uint64_t o_id = o; o += al((uint64_t)n_prims * 4);
+        uint64_t o_perm = o; o += al((uint64_t)n_prims * 4);
+        uint64_t o_nodes = o; o += al((uint64_t)n_nodes * sizeof(vrg_bvh_node));
+        uint64_t o_leaf = o; o += al((uint64_t)n_nodes * 4);
+        DevBufPtr sb;
+        VRG_TRY(dev_alloc(s, o, sb));
+        uint8_t *S = (uint8_t *)sb->ptr;
+        std::vector<float> tin;
+        std::vector<uint32_t> tid;
+        tin.reserve((size_t)n_prims * 10);
+        tid.reserve(n_prims);
         std::vector<SahTree> trees;
-        if (n_light_inst) trees.push_back(SahTree{n_light_inst, 0, 0, 0});
-        if (n_geo_inst) trees.push_back(SahTree{n_geo_inst, n_light_inst, n_light_tl, 0});
-        SahInputs in{(const float4 *)(B + o_tlo), (const float4 *)(B + o_thi), (const float4 *)(B + o_tcen),
-                     (const uint32_t *)(B + o_tidd)};
-        SahOutputs out{d_tl, (uint32_t *)(B + o_tperm), (uint32_t *)(B + o_tleaf)};
-        VRG_TRY(sah_build(s, trees, n_tl_prims, n_light_tl + n_geo_tl, in, out, &tl_levels));
-    }
-    if (!n_light_inst) {  // dummy node (BvhNode::default, bvh/mod.rs:27-38; scene.rs:276-277)
-        vrg_bvh_node d;
-        d.left_node_idx = d.right_node_idx_or_prim_idx = d.parent_idx = INVALID;
-        for (int a = 0; a < 3; a++) d.min[a] = d.max[a] = 0.0f;
-        d.power = 0.0f;
-        VRG_CUDA_TRY(cudaMemcpyAsync(d_tl, &d, sizeof(d), cudaMemcpyHostToDevice, s));
-    }
-    sc->h_light_tl.resize(n_light_tl);
-    sc->h_geo_tl.resize(n_geo_tl);
-    VRG_CUDA_TRY(cudaMemcpyAsync(sc->h_light_tl.data(), d_tl, n_light_tl * sizeof(vrg_bvh_node),
-                                 cudaMemcpyDeviceToHost, s));
-    if (n_geo_tl)
-        VRG_CUDA_TRY(cudaMemcpyAsync(sc->h_geo_tl.data(), d_tl + n_light_tl, n_geo_tl * sizeof(vrg_bvh_node),
+        for (auto &cp : cps) {
+            tin.insert(tin.end(), cp.tl_in.begin(), cp.tl_in.end());
+            tid.insert(tid.end(), cp.tl_ids.begin(), cp.tl_ids.end());
+            if (cp.n_light_inst) trees.push_back(SahTree{cp.n_light_inst, cp.tl_prim_off, cp.tl_node_off, 0});
+            if (cp.n_geo_inst)
+                trees.push_back(SahTree{cp.n_geo_inst, cp.tl_prim_off + cp.n_light_inst,
+                                        cp.tl_node_off + cp.n_light_tl, 0});
+        }
+        VRG_CUDA_TRY(cudaMemcpyAsync(S + o_tin, tin.data(), tin.size() * 4, cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(S + o_tid, tid.data(), tid.size() * 4, cudaMemcpyHostToDevice, s));
+        k_tl_inputs<<<(n_prims + 127) / 128, 128, 0, s>>>((const float *)(S + o_tin), (const uint32_t *)(S + o_tid),
+                                                           n_prims, (float4 *)(S + o_lo), (float4 *)(S + o_hi),
+                                                           (float4 *)(S + o_cen), (uint32_t *)(S + o_id));
+        VRG_CUDA_TRY(cudaGetLastError());
+        SahInputs in{(const float4 *)(S + o_lo), (const float4 *)(S + o_hi), (const float4 *)(S + o_cen),
+                     (const uint32_t *)(S + o_id)};
+        vrg_bvh_node *nodes = (vrg_bvh_node *)(S + o_nodes);
+        SahOutputs out{nodes, (uint32_t *)(S + o_perm), (uint32_t *)(S + o_leaf)};
+        VRG_TRY(sah_build(s, trees, n_prims, n_nodes, in, out, tl_levels));
+        for (auto &cp : cps) {
+            vrg_bvh_node *d_tl = (vrg_bvh_node *)(cp.B + cp.o_tln);
+            VRG_CUDA_TRY(cudaMemcpyAsync(d_tl, nodes + cp.tl_node_off,
+                                         (size_t)(cp.n_light_tl + cp.n_geo_tl) * sizeof(vrg_bvh_node),
+                                         cudaMemcpyDeviceToDevice, s));
+        }
+        VRG_CUDA_TRY(cudaMemcpyAsync(h_nodes.data(), nodes, (size_t)n_nodes * sizeof(vrg_bvh_node),
                                      cudaMemcpyDeviceToHost, s));
+    }
+    // a scene without lights gets the dummy node (BvhNode::default, bvh/mod.rs:27-38; scene.rs:276-277)
+    vrg_bvh_node dummy;
+    dummy.left_node_idx = dummy.right_node_idx_or_prim_idx = dummy.parent_idx = INVALID;
+    for (int a = 0; a < 3; a++) dummy.min[a] = dummy.max[a] = 0.0f;
+    dummy.power = 0.0f;
+    for (auto &cp : cps) {
+        if (cp.n_light_inst) continue;
+        VRG_CUDA_TRY(cudaMemcpyAsync(cp.B + cp.o_tln, &dummy, sizeof(dummy), cudaMemcpyHostToDevice, s));
+    }
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
-    // instance table (prim2node)
+    for (auto &cp : cps) {
+        const vrg_bvh_node *h = h_nodes.data() + cp.tl_node_off;
+        cp.sc->h_light_tl.assign(h, h + cp.n_light_tl);
+        if (!cp.n_light_inst) cp.sc->h_light_tl[0] = dummy;
+        cp.sc->h_geo_tl.assign(h + cp.n_light_tl, h + cp.n_light_tl + cp.n_geo_tl);
+    }
+    return VRG_OK;
+}
+
+// instance table, traversal layouts and records of one scene
+vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_tl) {
+    Scene *sc = cp.sc;
+    const uint32_t ni = cp.ni;
+    uint8_t *B = cp.B;
+    // instance table (prim2node, scene.rs:282-287)
     std::vector<InstDev> idev(ni);
     for (uint32_t i = 0; i < ni; i++) {
         for (int a = 0; a < 3; a++) idev[i].off[a] = sc->inst_off[i][a];
@@ -644,70 +596,209 @@ vrg_status scene_commit(Scene *sc) {
         idev[i].light_bl = sc->inst_objs[i]->light_nodes;
         idev[i].light_leaf_tri = sc->inst_objs[i]->light_leaf_tri;
     }
-    if (n_light_inst)
-        for (uint32_t j = 0; j < n_light_tl; j++)
-            if (sc->h_light_tl[j].left_node_idx == INVALID) idev[sc->h_light_tl[j].right_node_idx_or_prim_idx].light_bvh_tl_idx = j;
-    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_inst, idev.data(), ni * sizeof(InstDev), cudaMemcpyHostToDevice, s));
-    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_gb, gb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
-    VRG_CUDA_TRY(cudaMemcpyAsync(B + o_lb, lb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
-    const InstBuild *d_gb = (const InstBuild *)(B + o_gb), *d_lb = (const InstBuild *)(B + o_lb);
-    // wide layouts + records
-    if (n_geo_wide) {
-        k_wide4<<<(uint32_t)((n_geo_wide + 255) / 256), 256, 0, s>>>(d_tl + n_light_tl, n_geo_tl, d_gb, ni,
-                                                                    (uint32_t)n_geo_wide, (float4 *)(B + o_gw));
+    if (cp.n_light_inst)
+        for (uint32_t j = 0; j < cp.n_light_tl; j++)
+            if (sc->h_light_tl[j].left_node_idx == INVALID)
+                idev[sc->h_light_tl[j].right_node_idx_or_prim_idx].light_bvh_tl_idx = j;
+    if (ni) {
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + cp.o_inst, idev.data(), ni * sizeof(InstDev), cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + cp.o_gb, cp.gb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(B + cp.o_lb, cp.lb.data(), ni * sizeof(InstBuild), cudaMemcpyHostToDevice, s));
+    }
+    const InstBuild *d_gb = (const InstBuild *)(B + cp.o_gb), *d_lb = (const InstBuild *)(B + cp.o_lb);
+    if (cp.n_geo_wide) {
+        k_wide4<<<(uint32_t)((cp.n_geo_wide + 255) / 256), 256, 0, s>>>(d_tl + cp.n_light_tl, cp.n_geo_tl, d_gb, ni,
+                                                                       (uint32_t)cp.n_geo_wide,
+                                                                       (float4 *)(B + cp.o_gw));
         VRG_CUDA_TRY(cudaGetLastError());
     }
     for (uint32_t i = 0; i < ni; i++) {
-        if (gb[i].n_prims) {
-            k_geo_records<<<std::min(64u, (gb[i].n_prims + 255) / 256), 256, 0, s>>>(d_gb, i, (int4 *)(B + o_gr));
-        }
-        if (lb[i].n_prims) {
-            k_light_records<<<std::min(64u, (2 * lb[i].n_prims + 254) / 256), 256, 0, s>>>(d_lb, i, (int4 *)(B + o_lr));
-        }
+        if (cp.gb[i].n_prims)
+            k_geo_records<<<std::min(64u, (cp.gb[i].n_prims + 255) / 256), 256, 0, s>>>(d_gb, i,
+                                                                                       (int4 *)(B + cp.o_gr));
+        if (cp.lb[i].n_prims)
+            k_light_records<<<std::min(64u, (2 * cp.lb[i].n_prims + 254) / 256), 256, 0, s>>>(
+                d_lb, i, (int4 *)(B + cp.o_lr));
     }
     VRG_CUDA_TRY(cudaGetLastError());
-    // roots
-    DevScene &D = sc->dev;
-    D.geo_wide = (const float4 *)(B + o_gw);
-    D.geo_rec = (const int4 *)(B + o_gr);
-
+    DevScene &D = cp.dev;
+    D.geo_wide = (const float4 *)(B + cp.o_gw);
+    D.geo_rec = (const int4 *)(B + cp.o_gr);
     D.light_tl = d_tl;
-    D.inst = (const InstDev *)(B + o_inst);
-    D.mats = (const vrg_material *)ctx->d_mats->ptr;
+    D.inst = (const InstDev *)(B + cp.o_inst);
+    D.mats = (const vrg_material *)sc->ctx->d_mats->ptr;
     D.n_inst = ni;
-    auto root_of = [&](const std::vector<vrg_bvh_node> &tl, uint32_t n_tl, const std::vector<InstBuild> &ib,
-                       bool light) -> vrg_status {
-        (void)light;
-        int *dst = &D.geo_root;
-        if (n_tl == 0) { *dst = EMPTY_ROOT; return VRG_OK; }
-        if (tl[0].left_node_idx != INVALID) { *dst = 0; return VRG_OK; }
-        // single object: the TL root is a leaf -> its BLAS root
-        uint32_t k = tl[0].right_node_idx_or_prim_idx;
+    // geometry root: the TL root, or with one object its BLAS root / single record
+    if (cp.n_geo_tl == 0) {
+        D.geo_root = EMPTY_ROOT;
+    } else if (sc->h_geo_tl[0].left_node_idx != INVALID) {
+        D.geo_root = 0;
+    } else {
+        const uint32_t k = sc->h_geo_tl[0].right_node_idx_or_prim_idx;
         vrg_bvh_node r;
-        VRG_CUDA_TRY(cudaMemcpy(&r, ib[k].bl, sizeof(r), cudaMemcpyDeviceToHost));
-        if (r.left_node_idx != INVALID) { *dst = (int)ib[k].wbase; return VRG_OK; }
-        uint32_t p0;
-        VRG_CUDA_TRY(cudaMemcpy(&p0, ib[k].leaf, 4, cudaMemcpyDeviceToHost));
-        *dst = ~(int)(ib[k].rbase + p0);
-        return VRG_OK;
-    };
-    VRG_TRY(root_of(sc->h_geo_tl, n_geo_tl, gb, false));
-    uint32_t lamp_depth = 0;
-    VRG_TRY(build_lamp_layout(sc, (const int4 *)(B + o_lr), (uint32_t)light_recs, &lamp_depth));
-    // the 4-wide walk pushes up to 3 refs per 4-wide level (half the binary depth)
-    sc->depth_bound = std::max(3 * ((tl_levels + max_levels + 4 + 1) / 2) + 1, lamp_depth);
-    if (sc->depth_bound >= (uint32_t)TRAV_STACK) {
-        set_error("BVH depth bound %u exceeds the traversal stack (%d)", sc->depth_bound, TRAV_STACK);
-        return VRG_ERR_UNSUPPORTED;
+        VRG_CUDA_TRY(cudaMemcpy(&r, cp.gb[k].bl, sizeof(r), cudaMemcpyDeviceToHost));
+        if (r.left_node_idx != INVALID) {
+            D.geo_root = (int)cp.gb[k].wbase;
+        } else {
+            uint32_t p0;
+            VRG_CUDA_TRY(cudaMemcpy(&p0, cp.gb[k].leaf, 4, cudaMemcpyDeviceToHost));
+            D.geo_root = ~(int)(cp.gb[k].rbase + p0);
+        }
     }
-    VRG_CUDA_TRY(cudaStreamSynchronize(s));
-    sc->d_buf = buf;
-    sc->dirty = false;
-    for (Object *r : sc->retired) {
-        if (--r->refs == 0) delete r;
-    }
-    sc->retired.clear();
     return VRG_OK;
 }
+
+// all scenes' lamp-block trees in one SAH build
+vrg_status commit_lamps(cudaStream_t s, std::vector<CommitPrep> &cps) {
+    uint64_t L = 0;
+    for (auto &cp : cps) {
+        cp.lamp_off = L;
+        L += cp.light_recs;
+        cp.dev.lamp_root = EMPTY_ROOT;
+    }
+    if (L == 0) return VRG_OK;
+    if (2 * L >= 0x7FFFFFFFull) {
+        set_error("too many light triangles in one commit");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    const uint32_t nc = (uint32_t)cps.size();
+    auto al = [](uint64_t x) { return (x + 255) & ~255ull; };
+    uint64_t o = 0;
+    uint64_t o_flag = o; o += al(L * 4);
+    uint64_t o_tot = o; o += al((uint64_t)nc * 4);
+    uint64_t o_lo = o; o += al(L * 16);
+    uint64_t o_hi = o; o += al(L * 16);
+    uint64_t o_cen = o; o += al(L * 16);
+    uint64_t o_id = o; o += al(L * 4);
+    uint64_t o_perm = o; o += al(L * 4);
+    uint64_t o_nodes = o; o += al(2 * L * sizeof(vrg_bvh_node));
+    uint64_t o_leaf = o; o += al(2 * L * 4);
+    DevBufPtr sb;
+    VRG_TRY(dev_alloc(s, o, sb));
+    uint8_t *S = (uint8_t *)sb->ptr;
+    uint32_t *tot = (uint32_t *)(S + o_tot);
+    VRG_CUDA_TRY(cudaMemsetAsync(tot, 0, (size_t)nc * 4, s));
+    for (uint32_t c = 0; c < nc; c++) {
+        CommitPrep &cp = cps[c];
+        const uint64_t n = cp.light_recs;
+        if (n == 0) continue;
+        uint64_t q = 0;
+        const uint64_t q_rec = q; q += al(n * 16);
+        const uint64_t q_tab = q; q += al(n * 12 * 4);
+        const uint64_t q_wide = q; q += al(2 * n * 64);
+        VRG_TRY(dev_alloc(s, q, cp.lamp_buf));
+        uint8_t *Q = (uint8_t *)cp.lamp_buf->ptr;
+        int4 *lamp = (int4 *)(Q + q_rec);
+        uint32_t *table = (uint32_t *)(Q + q_tab);
+        VRG_CUDA_TRY(cudaMemsetAsync(lamp, 0, n * 16, s));
+        VRG_CUDA_TRY(cudaMemsetAsync(table, 0xFF, n * 48, s));
+        const int4 *light_rec = (const int4 *)(cp.B + cp.o_lr);
+        uint32_t *flag = (uint32_t *)(S + o_flag) + cp.lamp_off;
+        k_lamp_flags<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, (uint32_t)n, flag);
+        k_scan_inclusive<<<1, 1024, 0, s>>>(flag, (uint32_t)n, tot + c);
+        k_lamp_fill<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(
+            light_rec, flag, (uint32_t)n, lamp, table, (float4 *)(S + o_lo) + cp.lamp_off,
+            (float4 *)(S + o_hi) + cp.lamp_off, (float4 *)(S + o_cen) + cp.lamp_off,
+            (uint32_t *)(S + o_id) + cp.lamp_off);
+        VRG_CUDA_TRY(cudaGetLastError());
+        DevScene &D = cp.dev;
+        D.lamp_wide = (const float4 *)(Q + q_wide);
+        D.lamp_rec = lamp;
+        D.lamp_table = table;
+    }
+    std::vector<uint32_t> n_lamps(nc);
+    VRG_CUDA_TRY(cudaMemcpyAsync(n_lamps.data(), tot, (size_t)nc * 4, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<SahTree> trees;
+    for (uint32_t c = 0; c < nc; c++) {
+        cps[c].n_lamps = n_lamps[c];
+        if (n_lamps[c]) trees.push_back(SahTree{n_lamps[c], (uint32_t)cps[c].lamp_off, 2 * (uint32_t)cps[c].lamp_off, 0});
+    }
+    SahInputs in{(const float4 *)(S + o_lo), (const float4 *)(S + o_hi), (const float4 *)(S + o_cen),
+                 (const uint32_t *)(S + o_id)};
+    vrg_bvh_node *nodes = (vrg_bvh_node *)(S + o_nodes);
+    uint32_t *leaf = (uint32_t *)(S + o_leaf);
+    SahOutputs out{nodes, (uint32_t *)(S + o_perm), leaf};
+    uint32_t levels = 0;
+    VRG_TRY(sah_build(s, trees, (uint32_t)L, (uint32_t)(2 * L), in, out, &levels));
+    for (auto &cp : cps) {
+        if (!cp.n_lamps) continue;
+        DevScene &D = cp.dev;
+        if (cp.n_lamps > 1) {
+            const uint32_t nn = 2 * cp.n_lamps - 1;
+            k_wide_single<<<(nn + 255) / 256, 256, 0, s>>>(nodes + 2 * cp.lamp_off, leaf + 2 * cp.lamp_off, nn,
+                                                           (float4 *)D.lamp_wide);
+            VRG_CUDA_TRY(cudaGetLastError());
+            D.lamp_root = 0;
+        } else {
+            D.lamp_root = ~0;
+        }
+        cp.lamp_depth = levels + 2;
+    }
+    return VRG_OK;
+}
+
+}  // namespace
+
+vrg_status scene_commit_many(Scene *const *scs, uint32_t n) {
+    if (n == 0) return VRG_OK;
+    Context *ctx = scs[0]->ctx;
+    for (uint32_t i = 1; i < n; i++)
+        if (scs[i]->ctx != ctx) {
+            set_error("scenes of one commit share a context");
+            return VRG_ERR_INVALID_ARGUMENT;
+        }
+    cudaStream_t s = ctx->stream;
+    {  // chunks uploaded since the last commit: one batched extraction + BLAS build
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        std::vector<Object *> pend;
+        pend.swap(ctx->pending);
+        vrg_status st = extract_and_build(ctx, pend);
+        if (st != VRG_OK) {
+            ctx->pending.insert(ctx->pending.end(), pend.begin(), pend.end());
+            return st;
+        }
+        for (Object *o : pend)  // drop the pending list's reference
+            if (--o->refs == 0) delete o;
+    }
+    std::vector<CommitPrep> cps;
+    for (uint32_t i = 0; i < n; i++) {
+        Scene *sc = scs[i];
+        if (!sc->dirty) continue;
+        bool seen = false;
+        for (auto &cp : cps) seen |= cp.sc == sc;
+        if (seen) continue;
+        cps.emplace_back();
+        VRG_TRY(commit_prepare(sc, cps.back()));
+    }
+    if (cps.empty()) return VRG_OK;
+    uint32_t tl_levels = 0;
+    VRG_TRY(commit_top_levels(s, cps, &tl_levels));
+    for (auto &cp : cps) VRG_TRY(commit_layouts(s, cp, (const vrg_bvh_node *)(cp.B + cp.o_tln)));
+    VRG_TRY(commit_lamps(s, cps));
+    for (auto &cp : cps) {
+        // the 4-wide walk pushes up to 3 refs per 4-wide level (half the binary depth)
+        const uint32_t bound = std::max(3 * ((tl_levels + cp.max_levels + 4 + 1) / 2) + 1, cp.lamp_depth);
+        if (bound >= (uint32_t)TRAV_STACK) {
+            set_error("BVH depth bound %u exceeds the traversal stack (%d)", bound, TRAV_STACK);
+            return VRG_ERR_UNSUPPORTED;
+        }
+        cp.sc->depth_bound = bound;
+    }
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    for (auto &cp : cps) {
+        Scene *sc = cp.sc;
+        sc->dev = cp.dev;
+        sc->d_buf = cp.buf;
+        sc->lamp_buf = cp.lamp_buf;
+        sc->dirty = false;
+        for (Object *r : sc->retired)
+            if (--r->refs == 0) delete r;
+        sc->retired.clear();
+    }
+    return VRG_OK;
+}
+
+vrg_status scene_commit(Scene *sc) { return scene_commit_many(&sc, 1); }
 
 }  // namespace vrg

@@ -140,6 +140,9 @@ struct Scene {
     std::vector<Object *> retired;        // released when the next commit completes
 };
 vrg_status scene_commit(Scene *sc);
+// Commits every dirty scene of scs (one context); their top-level and lamp
+// trees are built by one SAH build each.
+vrg_status scene_commit_many(Scene *const *scs, uint32_t n);
 // Standalone batched builds of the C ABI: tri == false -> build_tl_bvh over
 // (aabb[6], translation[3]) prims, tri == true -> build_bl_bvh over triangles.
 vrg_status standalone_sah(Context *ctx, bool tri, uint32_t count, const uint32_t *n, const uint32_t *prim_offset,

@@ -1,12 +1,16 @@
 """Image-quality measurement of the renderer: an FP64-accumulated ground truth
 of the plain path tracer and the relative MSE of other estimators against it,
-with the cache-terminated tracer compared to the plain one at equal frame
+with the cache-terminated tracers compared to the plain one at equal frame
 time (none of this has a reference counterpart: the reference renders 1 spp
 per frame with no error metric).
 
 relMSE(x, gt) = mean over pixels and channels of (x - gt)^2 / (gt^2 + 0.01).
+
+Equal time: a method whose frame takes t_m ms is compared with the plain
+tracer accumulated over ceil(t_m / t_plain) frames, so that the plain tracer
+always gets at least the method's device time.
 """
-import time
+import math
 
 import numpy as np
 
@@ -49,8 +53,9 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
     """Renders `frames` 1-spp frames of `method` at a fixed camera; returns
     (mean image, list of single-frame radiance images, mean device ms/frame).
     method: 'plain' (3 bounces), 'restir' (3 bounces + ReSTIR view), 'cache'
-    (2 bounces ending into the radiance cache, 4 more for 1/16 training paths)."""
-    if method == "cache":
+    (2 bounces ending into the radiance cache, 4 more for 1/16 training paths),
+    'restir_cache' (the cache-terminated paths resampled by ReSTIR)."""
+    if method in ("cache", "restir_cache"):
         renderer.set_cache(cache)
     singles, ms = [], []
     for f in range(warmup + frames):
@@ -62,6 +67,9 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
             p.spatial_iterations = 3
         else:
             p = _params(2, vrg.RENDER_CACHE, seed0 + f, accumulate=0)
+            if method == "restir_cache":
+                p.debug_view = 1
+                p.spatial_iterations = 3
         _, rad = renderer.render_params(scene, cam, p, want_image=False, want_radiance=True)
         if f >= warmup:
             singles.append(rad.astype(np.float32))
@@ -70,13 +78,17 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
     return np.mean(clean, axis=0), singles, float(np.mean(ms))
 
 
+METHODS = ("plain", "restir", "cache", "restir_cache")
+
+
 def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames=16, cache_warmup=64, seed=7):
     """Single-frame and equal-time relMSE of plain, ReSTIR and cache-terminated
-    tracing against `gt`.  The cache is trained online for `cache_warmup`
-    frames at this camera before the measured frames (it keeps training)."""
+    tracing (alone and resampled by ReSTIR) against `gt`.  The cache is
+    trained online for `cache_warmup` frames at this camera before the
+    measured frames (it keeps training)."""
     cache = vrg.RadianceCache(ctx, scene_min, scene_max, seed=seed)
     out = {}
-    for method in ("plain", "restir", "cache"):
+    for method in METHODS:
         warm = cache_warmup if method == "cache" else 2
         mean_img, singles, ms = run_method(renderer, scene, cam, method, frames, seed0=1000, warmup=warm,
                                            cache=cache)
@@ -85,15 +97,20 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
                        "nonfinite": round(float(np.mean([nonfinite_fraction(s) for s in singles])), 8),
                        "relmse_mean_of_frames": round(relmse(mean_img, gt), 6), "frames": frames}
     renderer.set_cache(None)
-    # equal time: how many 1-spp plain frames fit in one cache frame's budget
-    t_plain, t_cache = out["plain"]["ms_per_frame"], out["cache"]["ms_per_frame"]
-    out["plain_frames_per_cache_frame"] = round(t_cache / t_plain, 3) if t_plain > 0 else None
-    # plain accumulated over the same device time as one cache frame
-    k = max(1, int(round(t_cache / t_plain))) if t_plain > 0 else 1
-    acc_img, _, _ = run_method(renderer, scene, cam, "plain", k, seed0=5000)
-    out["equal_time"] = {"plain_frames": k, "relmse_plain": round(relmse(acc_img, gt), 6),
-                         "relmse_cache_1spp": out["cache"]["relmse_1spp"]}
-    out["equal_time"]["cache_gain"] = round(out["equal_time"]["relmse_plain"] /
-                                            max(out["equal_time"]["relmse_cache_1spp"], 1e-12), 3)
+    # equal time: each method's 1-spp frame against the plain tracer
+    # accumulated over at least the same device time
+    t_plain = out["plain"]["ms_per_frame"]
+    eq = {}
+    plain_acc = {}
+    for method in METHODS[1:]:
+        t_m = out[method]["ms_per_frame"]
+        k = max(1, int(math.ceil(t_m / t_plain - 1e-9))) if t_plain > 0 else 1
+        if k not in plain_acc:
+            acc_img, _, _ = run_method(renderer, scene, cam, "plain", k, seed0=5000)
+            plain_acc[k] = relmse(acc_img, gt)
+        eq[method] = {"plain_frames": k, "plain_time_ratio": round(k * t_plain / t_m, 3),
+                      "relmse_plain": round(plain_acc[k], 6), "relmse_method_1spp": out[method]["relmse_1spp"],
+                      "gain": round(plain_acc[k] / max(out[method]["relmse_1spp"], 1e-12), 3)}
+    out["equal_time"] = eq
     cache.close()
     return out

@@ -119,6 +119,7 @@ SIGNATURES = [
     ("vrg_scene_update", C.c_int32, [_P, C.c_uint64, C.POINTER(C.c_float)]),
     ("vrg_scene_remove", C.c_int32, [_P, C.c_uint64]),
     ("vrg_scene_commit", C.c_int32, [_P]),
+    ("vrg_scene_commit_many", C.c_int32, [_P, C.c_uint32]),
     ("vrg_scene_read_tl", C.c_int32, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     ("vrg_renderer_create", C.c_int32, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_P)]),
     ("vrg_renderer_destroy", C.c_int32, [_P]),
@@ -384,6 +385,15 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+
+def commit_scenes(scenes):
+    """Commits several scenes together (one top-level and one lamp SAH build for all)."""
+    if not scenes:
+        return
+    ctx = scenes[0].ctx
+    arr = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
+    check(ctx.lib.vrg_scene_commit_many(arr, len(scenes)), "vrg_scene_commit_many")
 
 
 class Renderer:
