@@ -451,7 +451,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-rows", type=int, default=1080, help="image rows the CPU baseline traces per frame")
-    ap.add_argument("--cpu-frames", type=int, default=16, help="frames of the CPU baseline sample")
+    ap.add_argument("--cpu-frames", type=int, default=48, help="frames of the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")
