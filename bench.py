@@ -184,6 +184,12 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
     return rays / dt / 1e6, dt, rays
 
 
+# k_trace DRAM bytes (read + write) per pixel per frame, all bounces, from one
+# ncu --set full capture of the workload at 960x540 (3.66 + 20.14 + 16.77 MB over
+# 518,400 pixels; profiles/k_trace_restir540p.md); the 1080p launches are too
+# large to capture with --set full, and the traffic scales with the pixel count
+TRACE_DRAM_BYTES_PER_PX = 40.58e6 / (960 * 540)
+
 C2_SEED = 20240602
 C2_SCENES = 64
 C2_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
@@ -419,7 +425,10 @@ def run_ours(args, d):
         "rays_per_frame": rays // max(args.steps, 1),
         "scene_build_ms": round(build_s * 1000, 2),
         "roofline": {"bound": "hbm", "kernel": "k_trace", "achieved": round(achieved, 2), "peak": hbm_peak,
-                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                     "traffic": round(TRACE_DRAM_BYTES_PER_PX * W * H / NB),
+                     "traffic_source": "ncu dram__bytes_read+write of k_trace at 960x540, scaled by pixels, per launch",
+                     "algorithmic_bytes_per_launch": round(trace_bytes / max(args.steps, 1) / NB),
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
                      "algorithmic_bytes": "16 B hit per ray + 36 B ray/queue per secondary ray",
                      "note": "k_trace is issue/latency bound: its BVH walk is served from L1/L2 (see traversal)"},
