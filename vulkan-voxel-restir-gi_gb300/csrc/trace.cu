@@ -253,19 +253,39 @@ __device__ __forceinline__ void cswap(float &ta, int &ra, float &tb, int &rb) {
     }
 }
 
+// three-input min / max (sm_100+); NaN inputs are ignored as by fminf/fmaxf
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // slab test of the 4 children of a 4-wide node; returns the entry distances
-// sorted ascending (+inf for a miss) with their refs
-__device__ __forceinline__ void slab4(float4 LX, float4 HX, float4 LY, float4 HY, float4 LZ, float4 HZ, float4 RF,
+// sorted ascending (+inf for a miss) with their refs.  NX..FZ are the near and
+// far planes per axis, picked per ray by the sign of its direction (so the
+// per-axis min/max of the classic slab test is not needed).  For such a pick
+// the near distance of a non-empty box is <= its far distance, exactly, since
+// rounding is monotonic; a NaN distance (a ray parallel to an axis starting
+// on a box plane) is ignored by min/max, which only keeps more boxes: the test
+// stays conservative and the closest hit does not depend on it.
+__device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY, float4 NZ, float4 FZ, float4 RF,
                                       f3 inv, f3 oi, float tmin, float tmax, float tk[4], int rk[4]) {
-    const float lx[4] = {LX.x, LX.y, LX.z, LX.w}, hx[4] = {HX.x, HX.y, HX.z, HX.w};
-    const float ly[4] = {LY.x, LY.y, LY.z, LY.w}, hy[4] = {HY.x, HY.y, HY.z, HY.w};
-    const float lz[4] = {LZ.x, LZ.y, LZ.z, LZ.w}, hz[4] = {HZ.x, HZ.y, HZ.z, HZ.w};
+    const float nx[4] = {NX.x, NX.y, NX.z, NX.w}, fx[4] = {FX.x, FX.y, FX.z, FX.w};
+    const float ny[4] = {NY.x, NY.y, NY.z, NY.w}, fy[4] = {FY.x, FY.y, FY.z, FY.w};
+    const float nz[4] = {NZ.x, NZ.y, NZ.z, NZ.w}, fz[4] = {FZ.x, FZ.y, FZ.z, FZ.w};
     const int rf[4] = {__float_as_int(RF.x), __float_as_int(RF.y), __float_as_int(RF.z), __float_as_int(RF.w)};
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        float tn;
-        const bool h = slab_fma(lx[i], hx[i], ly[i], hy[i], lz[i], hz[i], inv, oi, tmin, tmax, tn);
-        tk[i] = (h && rf[i] != EMPTY_ROOT) ? tn : INFINITY;  // unused slots never enter the walk
+        const float tn = fmax3(__fmaf_rn(nx[i], inv.x, oi.x), __fmaf_rn(ny[i], inv.y, oi.y),
+                               fmaxf(__fmaf_rn(nz[i], inv.z, oi.z), tmin));
+        const float tf = fmin3(__fmaf_rn(fx[i], inv.x, oi.x), __fmaf_rn(fy[i], inv.y, oi.y),
+                               fminf(__fmaf_rn(fz[i], inv.z, oi.z), tmax));
+        tk[i] = (tn <= tf && rf[i] != EMPTY_ROOT) ? tn : INFINITY;  // unused slots never enter the walk
         rk[i] = rf[i];
     }
     // sorting network for 4
@@ -302,6 +322,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     uint64_t best_key = 0;
     int node = 0, sp = 0, hrec = -1;
     uint32_t hfh = 0;
+    int px = 0, py = 2, pz = 4;  // float4 index of the near plane per axis (the far one is next to it)
     int stack[TRAV_STACK];
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
@@ -326,6 +347,9 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                     else { o = ld3(a.ray_o[p]); d = ld3(a.ray_d[p]); }
                     inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+                    px = signbit(inv.x) ? 1 : 0;
+                    py = signbit(inv.y) ? 3 : 2;
+                    pz = signbit(inv.z) ? 5 : 4;
                     best_t = 1000.0f;
                     best_key = ~0ull;
                     node = root;
@@ -341,12 +365,13 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
             // descend through 4-wide inner nodes to the next leaf
             while (!done && node >= 0) {
                 const float4 *w = wide + 8 * (size_t)node;
-                const float4 LX = __ldg(w), HX = __ldg(w + 1), LY = __ldg(w + 2), HY = __ldg(w + 3);
-                const float4 LZ = __ldg(w + 4), HZ = __ldg(w + 5), RF = __ldg(w + 6);
+                const float4 NX = __ldg(w + px), FX = __ldg(w + (px ^ 1)), NY = __ldg(w + py);
+                const float4 FY = __ldg(w + (py ^ 1)), NZ = __ldg(w + pz), FZ = __ldg(w + (pz ^ 1));
+                const float4 RF = __ldg(w + 6);
                 n_nodes++;
                 float tk[4];
                 int rk[4];
-                slab4(LX, HX, LY, HY, LZ, HZ, RF, inv, oi, EPS_TRACE, best_t, tk, rk);
+                slab4(NX, FX, NY, FY, NZ, FZ, RF, inv, oi, EPS_TRACE, best_t, tk, rk);
                 // tk sorted ascending (misses at +inf)
                 if (tk[0] == INFINITY) {
                     if (sp == 0) done = true;
@@ -835,14 +860,18 @@ static int occupancy_grid(const void *fn, int threads) {
 
 // One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
 // A batched frame (a.views set) runs the variants that look up each pixel's view.
-static int g_trace = 0, g_shade = 0, g_any = 0;
+// grids of the persistent bounce kernels, [single view, batched] (set once,
+// before any stream capture)
+static int g_trace[2] = {0, 0}, g_shade[2] = {0, 0}, g_any[2] = {0, 0};
 
-// grids of the persistent bounce kernels (set once, before any stream capture)
 static void init_grids() {
-    if (g_trace) return;
-    g_shade = occupancy_grid((const void *)k_shade<false, false>, 128);
-    g_any = occupancy_grid((const void *)k_anyhit<false, false>, 128);
-    g_trace = occupancy_grid((const void *)k_trace<false>, 128);
+    if (g_trace[0]) return;
+    g_shade[0] = occupancy_grid((const void *)k_shade<false, false>, 128);
+    g_shade[1] = occupancy_grid((const void *)k_shade<false, true>, 128);
+    g_any[0] = occupancy_grid((const void *)k_anyhit<false, false>, 128);
+    g_any[1] = occupancy_grid((const void *)k_anyhit<false, true>, 128);
+    g_trace[1] = occupancy_grid((const void *)k_trace<true>, 128);
+    g_trace[0] = occupancy_grid((const void *)k_trace<false>, 128);
 }
 
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade) {
@@ -852,21 +881,22 @@ vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEve
         set_error("capture is not available for batched frames");
         return VRG_ERR_UNSUPPORTED;
     }
-    if (batch) k_trace<true><<<g_trace, 128, 0, s>>>(a, b);
-    else k_trace<false><<<g_trace, 128, 0, s>>>(a, b);
+    const int v = batch ? 1 : 0;
+    if (batch) k_trace<true><<<g_trace[v], 128, 0, s>>>(a, b);
+    else k_trace<false><<<g_trace[v], 128, 0, s>>>(a, b);
     if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
-    if (batch) k_shade<false, true><<<g_shade, 128, 0, s>>>(a, b);
-    else if (a.capture) k_shade<true, false><<<g_shade, 128, 0, s>>>(a, b);
-    else k_shade<false, false><<<g_shade, 128, 0, s>>>(a, b);
+    if (batch) k_shade<false, true><<<g_shade[v], 128, 0, s>>>(a, b);
+    else if (a.capture) k_shade<true, false><<<g_shade[v], 128, 0, s>>>(a, b);
+    else k_shade<false, false><<<g_shade[v], 128, 0, s>>>(a, b);
     if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
     if (b + 1 < a.nb) {
-        if (batch) k_anyhit<false, true><<<g_any, 128, 0, s>>>(a, b);
-        else if (a.capture) k_anyhit<true, false><<<g_any, 128, 0, s>>>(a, b);
-        else k_anyhit<false, false><<<g_any, 128, 0, s>>>(a, b);
-        if (batch) k_hit_eval<true><<<g_shade, 128, 0, s>>>(a);
-        else k_hit_eval<false><<<g_shade, 128, 0, s>>>(a);
-        if (a.capture) k_hit_sum<true><<<g_shade, 128, 0, s>>>(a, b);
-        else k_hit_sum<false><<<g_shade, 128, 0, s>>>(a, b);
+        if (batch) k_anyhit<false, true><<<g_any[v], 128, 0, s>>>(a, b);
+        else if (a.capture) k_anyhit<true, false><<<g_any[v], 128, 0, s>>>(a, b);
+        else k_anyhit<false, false><<<g_any[v], 128, 0, s>>>(a, b);
+        if (batch) k_hit_eval<true><<<g_shade[v], 128, 0, s>>>(a);
+        else k_hit_eval<false><<<g_shade[v], 128, 0, s>>>(a);
+        if (a.capture) k_hit_sum<true><<<g_shade[v], 128, 0, s>>>(a, b);
+        else k_hit_sum<false><<<g_shade[v], 128, 0, s>>>(a, b);
         VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
     }
     VRG_CUDA_TRY(cudaGetLastError());
