@@ -58,6 +58,7 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
     if method in ("cache", "restir_cache"):
         renderer.set_cache(cache)
     singles, ms = [], []
+    stages = None
     for f in range(warmup + frames):
         if method == "plain":
             p = _params(3, vrg.RENDER_PLAIN_ONLY, seed0 + f, accumulate=0)
@@ -74,7 +75,12 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
         if f >= warmup:
             singles.append(rad.astype(np.float32))
             ms.append(frame_ms(renderer))
+            st = renderer.last_stats
+            stages = {"bounces": [round(st.ms_bounce[b], 4) for b in range(p.num_bounces + (
+                p.cache_train_bounces if p.flags & vrg.RENDER_CACHE else 0))],
+                "resolve_and_cache": round(st.ms_resolve, 4), "spatial": round(st.ms_spatial, 4)}
     clean = [np.nan_to_num(s, nan=0.0, posinf=0.0, neginf=0.0) for s in singles]
+    run_method.last_stages = stages
     return np.mean(clean, axis=0), singles, float(np.mean(ms))
 
 
@@ -95,7 +101,8 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
         out[method] = {"ms_per_frame": round(ms, 4),
                        "relmse_1spp": round(float(np.mean([relmse(s, gt) for s in singles])), 6),
                        "nonfinite": round(float(np.mean([nonfinite_fraction(s) for s in singles])), 8),
-                       "relmse_mean_of_frames": round(relmse(mean_img, gt), 6), "frames": frames}
+                       "relmse_mean_of_frames": round(relmse(mean_img, gt), 6), "frames": frames,
+                       "stages_ms_last_frame": run_method.last_stages}
     renderer.set_cache(None)
     # equal time: each method's 1-spp frame against the plain tracer
     # accumulated over at least the same device time

@@ -517,6 +517,13 @@ class BatchRenderer:
                                               C.byref(self.last_stats)), "vrg_render_batched")
         return imgs, rads
 
+    def set_cache(self, cache):
+        check(self.ctx.lib.vrg_renderer_set_cache(self.h, None if cache is None else cache.h),
+              "vrg_renderer_set_cache")
+
+    def reset_accumulation(self):
+        check(self.ctx.lib.vrg_renderer_reset_accumulation(self.h), "vrg_renderer_reset_accumulation")
+
     def read_accumulation(self):
         n = C.c_uint32()
         a = np.zeros(self.pixels * 3, dtype=np.float32)
