@@ -460,6 +460,21 @@ def run_ours(args, d):
 
     for f in range(args.warmup):
         render(f, out_dev, stats)
+    tuning = None
+    if not args.no_autotune:
+        # launch configuration chosen by the autotuner on this workload's
+        # frames (scheduling only; the frames it renders are not counted and
+        # the renderer's frame counter and history are restored)
+        default_ms = []
+        for f in range(5):
+            render(args.warmup + f, out_dev, stats)
+            default_ms.append(stats.ms_total)
+        cam0 = vrg.orbit_camera(NX, NZ, 0, ORBIT, W, H)
+        t0 = time.perf_counter()
+        best, best_ms = r.autotune(scene, cam0, frame_params(0), frames=3)
+        tuning = {"config": best.as_dict(), "tuned_ms": round(best_ms, 4),
+                  "default_ms": round(float(np.median(default_ms)), 4),
+                  "tuner_seconds": round(time.perf_counter() - t0, 2)}
     # device-timed frames
     d.barrier()
     clk = ClockSampler(d.local)
@@ -585,6 +600,7 @@ def run_ours(args, d):
                 "d2h_bytes_per_step": W * H * 4},
         "gpu_launches": (3 * NB - 1 + 2) * args.steps,
         "quality": quality_block,
+        "autotune": tuning,
         "batched": batched,
         "clocks": clocks,
         "cpu_baseline": None if cpu_mr is None else {
@@ -611,6 +627,7 @@ def main():
     ap.add_argument("--gt-spp", type=int, default=None,
                     help="ground-truth samples per pixel (4096; 512 for the large workload)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched workload")
+    ap.add_argument("--no-autotune", action="store_true", help="time the default launch configuration")
     ap.add_argument("--workload", default="restir", choices=["restir", "large"],
                     help="restir: the 1080p ReSTIR headline line; large: the 32x32-chunk four-view 4K workload")
     args = ap.parse_args()

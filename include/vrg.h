@@ -258,6 +258,35 @@ enum {
 };
 VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes);
 
+/* ---- launch configuration and autotuner (no reference counterpart) -----
+ * Every field changes only how the frame's work is scheduled, never a result
+ * (the tests render the same bits under any configuration).  0 = default. */
+typedef struct vrg_tuning {
+    uint32_t trace_blocks_per_sm;   /* persistent closest-hit grid: CTAs of 128 threads per SM
+                                       (default and maximum: full occupancy) */
+    uint32_t trace_refill;          /* idle lanes of a warp that trigger its ray refill, 1..32 (8) */
+    uint32_t shade_blocks_per_sm;   /* shading / light-pdf evaluation grids */
+    uint32_t anyhit_blocks_per_sm;  /* light-hit collection grid */
+    uint32_t anyhit_refill;         /* as trace_refill, for the light-hit collection (8) */
+    uint32_t stream_block;          /* threads per CTA of the per-pixel kernels: 64, 128 or 256 (256) */
+    uint32_t reserved[2];
+} vrg_tuning;
+
+VRG_API vrg_status vrg_renderer_set_tuning(vrg_renderer *r, const vrg_tuning *t);
+/* The configuration in effect, defaults resolved to their values. */
+VRG_API vrg_status vrg_renderer_get_tuning(vrg_renderer *r, vrg_tuning *t);
+/* Autotuner: renders frames of (scene, cam, params) under candidate launch
+ * configurations, one field at a time over its candidate values (coordinate
+ * descent, two passes), each candidate timed as the median device time of
+ * `frames` frames after one untimed frame; installs the fastest and returns
+ * it with its time.  The tuning frames do not count: the frame counter,
+ * reservoir history and accumulation are restored afterwards.  Single-view
+ * renderers; params must not carry VRG_RENDER_CACHE / CAPTURE / GRAPH (the
+ * result applies to those frames as well). */
+VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
+                                         const vrg_render_params *params, uint32_t frames, vrg_tuning *best,
+                                         float *best_ms);
+
 /* ---- batched views (no reference counterpart: the reference renders one
  * swapchain view per Renderer::render) ------------------------------------
  * A batched renderer owns n_views views of independent extents; one

@@ -49,3 +49,33 @@ def test_cache_beats_plain_at_equal_time(gpu_ctx):
     assert res["cache"]["nonfinite"] == 0.0 and np.isfinite(res["restir"]["relmse_1spp"])
     # and under ReSTIR: resampling cache-terminated paths beats resampling plain ones
     assert res["restir_cache"]["relmse_1spp"] < res["restir"]["relmse_1spp"], res
+
+
+def test_cache_frame_fork_matches_single_stream(gpu_ctx):
+    """A cache frame runs its training branch on a second stream; with capture
+    on it runs on one stream.  The first frame (before any training step has
+    changed the weights) must match bit for bit, and the trained weights after
+    it must agree up to the order of the gradient atomics."""
+    scene, objs, lo, hi = _scene(gpu_ctx, seed=9)
+    W, H = 96, 64
+    cam = vrg.orbit_camera(2, 2, 7, 64, W, H)
+    outs, weights = [], []
+    for flags in (0, vrg.RENDER_CAPTURE):
+        r = vrg.Renderer(gpu_ctx, W, H, 8)
+        cache = vrg.RadianceCache(gpu_ctx, lo, hi, seed=3)
+        r.set_cache(cache)
+        p = quality._params(2, vrg.RENDER_CACHE | flags, 11, accumulate=0)
+        p.debug_view = 1
+        p.spatial_iterations = 3
+        _, rad = r.render_params(scene, cam, p, want_image=False, want_radiance=True)
+        assert r.last_stats.error_flags == 0
+        outs.append(rad.copy())
+        weights.append(cache.read(vrg.NRC_WEIGHTS).copy())
+        r.set_cache(None)
+        cache.close()
+        r.close()
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+    # Adam's first step moves each weight by about +-lr along its gradient's
+    # sign, so a gradient at rounding level may flip: allow a handful
+    close = np.isclose(weights[0], weights[1], rtol=1e-3, atol=1e-6)
+    assert close.mean() > 0.999, close.mean()

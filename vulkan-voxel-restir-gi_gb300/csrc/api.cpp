@@ -14,11 +14,13 @@
 namespace vrg {
 
 vrg_status upload_frames(cudaStream_t s);
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade);
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
+                         uint32_t max_rays);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a);
 int bounce_blocks_per_sm();
+void bounce_occupancy(bool batch, int occ[3], int *sms);
 
 static thread_local char g_err[512] = "";
 
@@ -432,6 +434,13 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
 }
 
 static vrg_status renderer_events(vrg_renderer *r) {
+    // the training branch of a cache frame is the frame's critical path: it
+    // runs on a higher-priority stream, so its few blocks are placed first
+    int lo_prio = 0, hi_prio = 0;
+    VRG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux, cudaStreamNonBlocking, hi_prio));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
@@ -547,6 +556,12 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
             if (e) cudaEventDestroy(e);
     for (auto &e : r->ev_stage)
         if (e) cudaEventDestroy(e);
+    if (r->ev_fork) cudaEventDestroy(r->ev_fork);
+    if (r->ev_join) cudaEventDestroy(r->ev_join);
+    if (r->aux) {
+        cudaStreamSynchronize(r->aux);
+        cudaStreamDestroy(r->aux);
+    }
     if (r->h_pinned) cudaFreeHost(r->h_pinned);
     if (r->h_views) cudaFreeHost(r->h_views);
     r->res_buf.reset();
@@ -617,6 +632,47 @@ static vrg_status ensure_capture(vrg_renderer *r) {
     return VRG_OK;
 }
 
+static vrg_status ensure_ring(vrg_renderer *r, uint32_t slots) {
+    if (slots == r->ring_slots) return VRG_OK;
+    const size_t P = (size_t)r->P;
+    cudaStream_t s = r->ctx->stream;
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(s, (size_t)slots * 5 * P * 16, b));
+    VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, (size_t)slots * 5 * P * 16, s));
+    drop_graphs(r);
+    r->res_buf = b;
+    r->res = (float4 *)b->ptr;
+    r->ring_slots = slots;
+    return VRG_OK;
+}
+
+// the renderer's launch configuration with defaults resolved
+static vrg_tuning effective_tuning(const vrg_renderer *r) {
+    int occ[3], sms = 1;
+    bounce_occupancy(r->n_views != 0, occ, &sms);
+    const vrg_tuning &t = r->tune;
+    vrg_tuning e{};
+    e.trace_blocks_per_sm = t.trace_blocks_per_sm ? std::min<uint32_t>(t.trace_blocks_per_sm, occ[0]) : occ[0];
+    e.shade_blocks_per_sm = t.shade_blocks_per_sm ? std::min<uint32_t>(t.shade_blocks_per_sm, occ[1]) : occ[1];
+    e.anyhit_blocks_per_sm = t.anyhit_blocks_per_sm ? std::min<uint32_t>(t.anyhit_blocks_per_sm, occ[2]) : occ[2];
+    e.trace_refill = t.trace_refill ? t.trace_refill : 8;
+    e.anyhit_refill = t.anyhit_refill ? t.anyhit_refill : 8;
+    e.stream_block = t.stream_block ? t.stream_block : 256;
+    return e;
+}
+
+static void apply_tuning(const vrg_renderer *r, FrameArgs &a) {
+    int occ[3], sms = 1;
+    bounce_occupancy(r->n_views != 0, occ, &sms);
+    const vrg_tuning e = effective_tuning(r);
+    a.refill_trace = e.trace_refill;
+    a.refill_any = e.anyhit_refill;
+    a.grid_trace = (uint32_t)sms * e.trace_blocks_per_sm;
+    a.grid_shade = (uint32_t)sms * e.shade_blocks_per_sm;
+    a.grid_any = (uint32_t)sms * e.anyhit_blocks_per_sm;
+    a.stream_block = e.stream_block;
+}
+
 // Frame set-up shared by vrg_render and vrg_render_batched: parameter checks,
 // the reservoir ring, capture and cache buffers, and every FrameArgs field but
 // the view ones.
@@ -629,15 +685,7 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     const size_t P = (size_t)r->P;
     const uint32_t slots = pr->history_slots ? pr->history_slots : 3;
     if (slots > 8) return VRG_ERR_INVALID_ARGUMENT;
-    if (slots != r->ring_slots) {
-        DevBufPtr b;
-        VRG_TRY(dev_alloc(s, (size_t)slots * 5 * P * 16, b));
-        VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, (size_t)slots * 5 * P * 16, s));
-        drop_graphs(r);
-        r->res_buf = b;
-        r->res = (float4 *)b->ptr;
-        r->ring_slots = slots;
-    }
+    VRG_TRY(ensure_ring(r, slots));
     const bool capture = (pr->flags & VRG_RENDER_CAPTURE) != 0;
     if (capture) VRG_TRY(ensure_capture(r));
     const bool cache = (pr->flags & VRG_RENDER_CACHE) != 0;
@@ -737,6 +785,7 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.c_L = r->c_L;
     a.c_q = r->c_q;
     a.c_hit = r->c_hit;
+    apply_tuning(r, a);
     r->last_ring = ring;
     return VRG_OK;
 }
@@ -745,27 +794,51 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // around every stage (r->ev: frame start, after each bounce, after resolve,
 // after spatial; r->ev_k: after k_trace / k_shade of each bounce); a graph
 // recording passes false.
+//
+// A cache frame forks after the query vertex: the training paths' extra
+// bounces and the cache's training step run on the renderer's second stream
+// while the main stream infers the cache for the rendered paths and runs
+// resolve and spatial (nothing of one branch reads what the other writes;
+// the training step's weights serve the next frame, after the join).  With
+// capture the frame stays on one stream.
 static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) {
     cudaStream_t s = r->ctx->stream;
-    int ei = 0;
+    const bool fork = a.cache && !a.capture;
+    const uint32_t nb_main = fork ? a.nb_render : a.nb;
     VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
-    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
-    for (uint32_t b = 0; b < a.nb; b++) {
-        VRG_TRY(launch_bounce(s, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr));
-        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
+    for (uint32_t b = 0; b < nb_main; b++) {
+        VRG_TRY(launch_bounce(s, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr, 0));
+        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
+    }
+    cudaStream_t st = s;  // stream of the training branch
+    if (fork) {
+        st = r->aux;
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_fork, s));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_fork, 0));
+        for (uint32_t b = nb_main; b < a.nb; b++) {
+            VRG_TRY(launch_bounce(st, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr,
+                                  a.train_cap));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], st));
+        }
+        VRG_TRY(launch_train_targets(st, a));
+        VRG_TRY(nrc_train(r->cache, st, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
+                          nullptr, r->target, true));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
     }
     if (a.cache)  // radiance-cache queries of every path that ends into the cache
         VRG_TRY(nrc_infer(r->cache, s, a.P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
                           r->pred));
     VRG_TRY(launch_resolve(s, a));
-    if (a.cache) {  // one training step on this frame's long paths
+    if (a.cache && !fork) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));
         VRG_TRY(nrc_train(r->cache, s, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
                           nullptr, r->target, true));
     }
-    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
-    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[ei++], s));
+    if (fork) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_join, 0));
+    if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 2], s));
     return VRG_OK;
 }
 
@@ -788,7 +861,8 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
             cudaEventElapsedTime(&ms, r->ev_k[1][b], r->ev[b + 1]);
             stats->ms_anyhit[b] = ms;
         }
-        cudaEventElapsedTime(&ms, r->ev[a.nb], r->ev[a.nb + 1]);
+        // a forked cache frame's resolve stage starts at the fork (it runs beside the training branch)
+        cudaEventElapsedTime(&ms, r->ev[(a.cache && !a.capture) ? a.nb_render : a.nb], r->ev[a.nb + 1]);
         stats->ms_resolve = ms;
         cudaEventElapsedTime(&ms, r->ev[a.nb + 1], r->ev[a.nb + 2]);
         stats->ms_spatial = ms;
@@ -994,6 +1068,125 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
     frame_done(r, a, pr);
     if (stats) return frame_stats(r, a, !graph, stats);
     if (host_out) VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_set_tuning(vrg_renderer *r, const vrg_tuning *t) {
+    if (!r || !t) return VRG_ERR_INVALID_ARGUMENT;
+    if (t->trace_refill > 32 || t->anyhit_refill > 32 || t->trace_blocks_per_sm > 64 ||
+        t->shade_blocks_per_sm > 64 || t->anyhit_blocks_per_sm > 64 ||
+        (t->stream_block != 0 && t->stream_block != 64 && t->stream_block != 128 && t->stream_block != 256)) {
+        set_error("tuning out of range (refills 0..32, CTAs per SM 0..64, stream_block 0/64/128/256)");
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    r->tune = *t;
+    memset(r->tune.reserved, 0, sizeof(r->tune.reserved));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_get_tuning(vrg_renderer *r, vrg_tuning *t) {
+    if (!r || !t) return VRG_ERR_INVALID_ARGUMENT;
+    *t = effective_tuning(r);
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
+                                         const vrg_render_params *params, uint32_t frames, vrg_tuning *best,
+                                         float *best_ms) {
+    if (!r || !scene || !cam || !params) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views) {
+        set_error("the autotuner renders single-view frames (tune one view, then vrg_renderer_set_tuning)");
+        return VRG_ERR_STATE;
+    }
+    if (params->flags & (VRG_RENDER_CACHE | VRG_RENDER_CAPTURE | VRG_RENDER_GRAPH)) {
+        set_error("the autotuner takes no cache, capture or graph frames");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    frames = std::max(1u, std::min(frames, 64u));
+    cudaStream_t s = r->ctx->stream;
+    const uint32_t slots = params->history_slots ? params->history_slots : 3;
+    if (slots > 8) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_TRY(scene_commit(scene));
+    VRG_TRY(ensure_ring(r, slots));
+    // state the tuning frames change: frame counter and reservoir history
+    const size_t ring_bytes = (size_t)slots * 5 * (size_t)r->P * 16;
+    DevBufPtr saved;
+    VRG_TRY(dev_alloc(s, ring_bytes, saved));
+    VRG_CUDA_TRY(cudaMemcpyAsync(saved->ptr, r->res, ring_bytes, cudaMemcpyDeviceToDevice, s));
+    const uint32_t frame0 = r->frame, accum0 = r->accum_n, last_nb0 = r->last_nb, last_ring0 = r->last_ring;
+    const bool captured0 = r->captured;
+    const vrg_tuning user = r->tune;
+    vrg_render_params p = *params;
+    p.accumulate = 0;
+    auto measure = [&](const vrg_tuning &t, float *ms_out) -> vrg_status {
+        r->tune = t;
+        std::vector<float> ms;
+        vrg_frame_stats st;
+        for (uint32_t f = 0; f <= frames; f++) {
+            VRG_TRY(vrg_render(r, scene, cam, &p, nullptr, &st));
+            if (f) ms.push_back(st.ms_total);
+        }
+        std::sort(ms.begin(), ms.end());
+        *ms_out = ms[ms.size() / 2];
+        return VRG_OK;
+    };
+    int occ[3], sms = 1;
+    bounce_occupancy(false, occ, &sms);
+    auto bpsm_candidates = [](int o) {
+        std::vector<uint32_t> c;
+        for (int k : {1, 2, 3, 4, 6, 8, 12, 16})
+            if (k < o) c.push_back((uint32_t)k);
+        c.push_back((uint32_t)o);
+        return c;
+    };
+    const std::vector<uint32_t> refills = {1, 2, 4, 8, 12, 16, 24, 32};
+    struct Field {
+        uint32_t vrg_tuning::*m;
+        std::vector<uint32_t> cand;
+    };
+    const std::vector<Field> fields = {
+        {&vrg_tuning::trace_refill, refills},
+        {&vrg_tuning::trace_blocks_per_sm, bpsm_candidates(occ[0])},
+        {&vrg_tuning::shade_blocks_per_sm, bpsm_candidates(occ[1])},
+        {&vrg_tuning::anyhit_refill, refills},
+        {&vrg_tuning::anyhit_blocks_per_sm, bpsm_candidates(occ[2])},
+        {&vrg_tuning::stream_block, {64, 128, 256}},
+    };
+    vrg_tuning cur = effective_tuning(r);
+    float cur_ms = 0.0f;
+    vrg_status st = measure(cur, &cur_ms);
+    for (int pass = 0; pass < 2 && st == VRG_OK; pass++) {
+        for (const Field &fd : fields) {
+            for (uint32_t v : fd.cand) {
+                if (cur.*(fd.m) == v) continue;
+                vrg_tuning t = cur;
+                t.*(fd.m) = v;
+                float ms = 0.0f;
+                st = measure(t, &ms);
+                if (st != VRG_OK) break;
+                if (ms < cur_ms) {
+                    cur = t;
+                    cur_ms = ms;
+                }
+            }
+            if (st != VRG_OK) break;
+        }
+    }
+    // restore the state the tuning frames changed
+    VRG_CUDA_TRY(cudaMemcpyAsync(r->res, saved->ptr, ring_bytes, cudaMemcpyDeviceToDevice, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    r->frame = frame0;
+    r->accum_n = accum0;
+    r->last_nb = last_nb0;
+    r->last_ring = last_ring0;
+    r->captured = captured0;
+    if (st != VRG_OK) {
+        r->tune = user;
+        return st;
+    }
+    r->tune = cur;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
     return VRG_OK;
 }
 

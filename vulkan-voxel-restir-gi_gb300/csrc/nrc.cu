@@ -126,13 +126,15 @@ __device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 
                            __nv_bfloat16 *row) {
     const f3 p = normalize_pos(P, pos);
     const size_t T = (size_t)1 << P.log2_t;
+    // unrolled so that the gathers of several levels are in flight together
+#pragma unroll 4
     for (int l = 0; l < P.levels; l++) {
         Corner c;
         level_corners(P, l, p, c);
         float f0 = 0.0f, f1 = 0.0f;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const float2 v = __half22float2(table[(size_t)l * T + c.idx[k]]);
+            const float2 v = __half22float2(__ldg(table + (size_t)l * T + c.idx[k]));
             f0 += c.w[k] * v.x;
             f1 += c.w[k] * v.y;
         }
@@ -214,7 +216,8 @@ __device__ __forceinline__ void store_a(__nv_bfloat16 *dst, const uint32_t a[4][
     }
 }
 
-constexpr int NRC_WARPS = 4;
+constexpr int NRC_WARPS = 4;   // training kernel
+constexpr int NRC_IWARPS = 12; // inference kernel: 12 warps share one copy of the weights (2 CTAs per SM)
 
 struct InferArgs {
     NrcParams P;
@@ -239,7 +242,7 @@ __device__ __forceinline__ f3 face_normal(int f) {
 }
 
 // inference: per warp 32 queries per iteration (2 tiles of 16)
-__global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_infer(InferArgs a) {
+__global__ void __launch_bounds__(NRC_IWARPS * 32) k_nrc_infer(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
     __nv_bfloat16 *tiles = W + WFWD_ELEMS;
@@ -251,9 +254,9 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_infer(InferArgs a) {
     }
     __syncthreads();
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
-    const uint32_t warps = gridDim.x * NRC_WARPS;
+    const uint32_t warps = gridDim.x * NRC_IWARPS;
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
-    for (uint32_t base = (blockIdx.x * NRC_WARPS + w) * 32; base < n; base += warps * 32) {
+    for (uint32_t base = (blockIdx.x * NRC_IWARPS + w) * 32; base < n; base += warps * 32) {
         const uint32_t i = base + lane;
         uint32_t id = 0;
         if (i < n) {
@@ -633,7 +636,7 @@ struct Nrc {
     int grid_infer = 0, grid_train = 0;
 };
 
-static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2; }
+static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_IWARPS * 32 * NRC_STRIDE * 2; }
 static size_t train_smem() {
     return WPACK_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2 + (size_t)NRC_WARPS * 32 * NRC_OUT * 4;
 }
@@ -729,7 +732,7 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
     VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
     int bi = 0, bt = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bi, k_nrc_infer, NRC_WARPS * 32, infer_smem());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bi, k_nrc_infer, NRC_IWARPS * 32, infer_smem());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_nrc_train, NRC_WARPS * 32, train_smem());
     N->grid_infer = std::max(1, ctx->num_sms * std::max(1, bi));
     N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
@@ -742,8 +745,8 @@ vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
                      const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out) {
     if (n == 0) return VRG_OK;
     InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out};
-    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
-    k_nrc_infer<<<blocks, NRC_WARPS * 32, infer_smem(), s>>>(a);
+    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_IWARPS * 32 - 1) / (NRC_IWARPS * 32));
+    k_nrc_infer<<<blocks, NRC_IWARPS * 32, infer_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

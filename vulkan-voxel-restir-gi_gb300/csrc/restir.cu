@@ -57,7 +57,10 @@ __global__ void __launch_bounds__(256) k_resolve(const __grid_constant__ FrameAr
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     const uint32_t nb = a.nb;
-    const uint32_t nl = a.nlive[p];
+    // a path that reached the cache's query vertex with a hit needs no more of
+    // its length here (its training continuation may still be running on
+    // another stream and writing nlive); every other path ended by then
+    const uint32_t nl = (!CAPTURE && a.cache && a.qflag[p]) ? a.nb_render : a.nlive[p];
     const float inv2pi = 1.0f / (2.0f * PI_F);
     f3 L = f3{0.0f, 0.0f, 0.0f}, L1 = f3{0.0f, 0.0f, 0.0f};
     float q0 = inv2pi;
@@ -267,20 +270,25 @@ vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a) {
     return VRG_OK;
 }
 
+// per-pixel kernels: CTAs of a.stream_block threads (64, 128 or 256)
+static uint32_t stream_block(const FrameArgs &a) { return a.stream_block ? a.stream_block : 256u; }
+
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a) {
-    dim3 g((a.P + 255) / 256);
-    if (a.views) k_resolve<false, true><<<g, 256, 0, s>>>(a);
-    else if (a.capture) k_resolve<true, false><<<g, 256, 0, s>>>(a);
-    else k_resolve<false, false><<<g, 256, 0, s>>>(a);
+    const uint32_t t = stream_block(a);
+    dim3 g((a.P + t - 1) / t);
+    if (a.views) k_resolve<false, true><<<g, t, 0, s>>>(a);
+    else if (a.capture) k_resolve<true, false><<<g, t, 0, s>>>(a);
+    else k_resolve<false, false><<<g, t, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }
 
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a) {
-    dim3 g((a.P + 255) / 256);
-    if (a.views) k_spatial<false, true><<<g, 256, 0, s>>>(a);
-    else if (a.capture) k_spatial<true, false><<<g, 256, 0, s>>>(a);
-    else k_spatial<false, false><<<g, 256, 0, s>>>(a);
+    const uint32_t t = stream_block(a);
+    dim3 g((a.P + t - 1) / t);
+    if (a.views) k_spatial<false, true><<<g, t, 0, s>>>(a);
+    else if (a.capture) k_spatial<true, false><<<g, t, 0, s>>>(a);
+    else k_spatial<false, false><<<g, t, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

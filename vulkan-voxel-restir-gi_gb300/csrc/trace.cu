@@ -208,7 +208,6 @@ __device__ float nee_pdf_of(const DevScene &sc, f3 point, f3 normal, f3 dir, uin
 }
 
 constexpr int LIGHT_LIST = 32;
-constexpr int REFILL_MIN = 8;  // refill a warp once this many lanes are idle
 constexpr uint32_t FULL = 0xffffffffu;
 
 __device__ __forceinline__ void st3(float *a, size_t i, f3 v) {
@@ -300,7 +299,7 @@ __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY
 // k_trace: closest hit over the voxel faces (replaces getIntersectionInfo,
 // raytrace.rs:354-388).  Persistent warps; each lane owns one ray and, when
 // its traversal ends, takes a new ray from the bounce queue (warp-aggregated
-// fetch once REFILL_MIN lanes are idle), so a warp does not wait for its
+// fetch once a.refill_trace lanes are idle), so a warp does not wait for its
 // longest ray.  The result is independent of traversal order: ties on t go
 // to the smaller (instance, triangle) key and boxes are culled only when
 // strictly beyond the current best t.  In a batched frame each lane reads the
@@ -309,6 +308,7 @@ __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
+    const int REFILL = (int)a.refill_trace;
     const uint32_t n_in = (b == 0) ? a.P : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *err = a.counters + CNT_ERROR;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     int stack[TRAV_STACK];
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
-        if (!exhausted && need && (__popc(need) >= REFILL_MIN || need == FULL)) {
+        if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(&a.counters[CNT_FETCH + b], (uint32_t)__popc(need));
             base = __shfl_sync(FULL, base, 0);
@@ -548,6 +548,9 @@ __global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs
                 anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
             }
             // radiance cache: the vertex where rendered paths end into the cache
+            // (every pixel's flag is cleared at bounce 0, so a path that ends
+            // before the query vertex never reads a stale one)
+            if (a.cache && b == 0 && !at_query) a.qflag[p] = 0;
             if (at_query) {
                 qhit = hv.x >= 0;
                 a.qflag[p] = qhit ? 1 : 0;
@@ -682,6 +685,7 @@ __device__ __forceinline__ void finish_job(const FrameArgs &a, uint32_t b, uint3
 template <bool CAPTURE, bool BATCH>
 __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
+    const int REFILL = (int)a.refill_any;
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
     uint32_t *err = a.counters + CNT_ERROR;
     const float4 *wide = a.v0.sc.lamp_wide;
@@ -701,7 +705,7 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
         atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANY), (unsigned long long)n_in);
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
-        if (!exhausted && need && (__popc(need) >= REFILL_MIN || need == FULL)) {
+        if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(&a.counters[CNT_AFETCH + b], (uint32_t)__popc(need));
             base = __shfl_sync(FULL, base, 0);
@@ -858,14 +862,17 @@ static int occupancy_grid(const void *fn, int threads) {
     return std::max(1, sms) * std::max(1, n);
 }
 
-// One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
-// A batched frame (a.views set) runs the variants that look up each pixel's view.
-// grids of the persistent bounce kernels, [single view, batched] (set once,
-// before any stream capture)
+// full-occupancy grids of the persistent bounce kernels, [single view,
+// batched] (set once, before any stream capture)
 static int g_trace[2] = {0, 0}, g_shade[2] = {0, 0}, g_any[2] = {0, 0};
+static int g_sms = 1;
 
 static void init_grids() {
     if (g_trace[0]) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    g_sms = std::max(1, g_sms);
     g_shade[0] = occupancy_grid((const void *)k_shade<false, false>, 128);
     g_shade[1] = occupancy_grid((const void *)k_shade<false, true>, 128);
     g_any[0] = occupancy_grid((const void *)k_anyhit<false, false>, 128);
@@ -874,7 +881,24 @@ static void init_grids() {
     g_trace[0] = occupancy_grid((const void *)k_trace<false>, 128);
 }
 
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade) {
+// resident CTAs per SM at full occupancy of (closest hit, shading, light
+// hits), the bound of a tuned persistent grid; and the SM count
+void bounce_occupancy(bool batch, int occ[3], int *sms) {
+    init_grids();
+    const int v = batch ? 1 : 0;
+    occ[0] = std::max(1, g_trace[v] / g_sms);
+    occ[1] = std::max(1, g_shade[v] / g_sms);
+    occ[2] = std::max(1, g_any[v] / g_sms);
+    *sms = g_sms;
+}
+
+// One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
+// A batched frame (a.views set) runs the variants that look up each pixel's view.
+// max_rays > 0 bounds the rays of this bounce (a cache frame's training paths):
+// the persistent grids then shrink to one lane per ray, leaving the other SMs
+// to the work that runs beside them.
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
+                         uint32_t max_rays) {
     init_grids();
     const bool batch = a.views != nullptr;
     if (batch && a.capture) {
@@ -882,21 +906,30 @@ vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEve
         return VRG_ERR_UNSUPPORTED;
     }
     const int v = batch ? 1 : 0;
-    if (batch) k_trace<true><<<g_trace[v], 128, 0, s>>>(a, b);
-    else k_trace<false><<<g_trace[v], 128, 0, s>>>(a, b);
+    int gt = a.grid_trace ? std::min((int)a.grid_trace, g_trace[v]) : g_trace[v];
+    int gs = a.grid_shade ? std::min((int)a.grid_shade, g_shade[v]) : g_shade[v];
+    int ga = a.grid_any ? std::min((int)a.grid_any, g_any[v]) : g_any[v];
+    if (max_rays) {
+        const int cap = (int)std::max<uint32_t>(1u, (max_rays + 127) / 128);
+        gt = std::min(gt, cap);
+        gs = std::min(gs, cap);
+        ga = std::min(ga, cap);
+    }
+    if (batch) k_trace<true><<<gt, 128, 0, s>>>(a, b);
+    else k_trace<false><<<gt, 128, 0, s>>>(a, b);
     if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
-    if (batch) k_shade<false, true><<<g_shade[v], 128, 0, s>>>(a, b);
-    else if (a.capture) k_shade<true, false><<<g_shade[v], 128, 0, s>>>(a, b);
-    else k_shade<false, false><<<g_shade[v], 128, 0, s>>>(a, b);
+    if (batch) k_shade<false, true><<<gs, 128, 0, s>>>(a, b);
+    else if (a.capture) k_shade<true, false><<<gs, 128, 0, s>>>(a, b);
+    else k_shade<false, false><<<gs, 128, 0, s>>>(a, b);
     if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
     if (b + 1 < a.nb) {
-        if (batch) k_anyhit<false, true><<<g_any[v], 128, 0, s>>>(a, b);
-        else if (a.capture) k_anyhit<true, false><<<g_any[v], 128, 0, s>>>(a, b);
-        else k_anyhit<false, false><<<g_any[v], 128, 0, s>>>(a, b);
-        if (batch) k_hit_eval<true><<<g_shade[v], 128, 0, s>>>(a);
-        else k_hit_eval<false><<<g_shade[v], 128, 0, s>>>(a);
-        if (a.capture) k_hit_sum<true><<<g_shade[v], 128, 0, s>>>(a, b);
-        else k_hit_sum<false><<<g_shade[v], 128, 0, s>>>(a, b);
+        if (batch) k_anyhit<false, true><<<ga, 128, 0, s>>>(a, b);
+        else if (a.capture) k_anyhit<true, false><<<ga, 128, 0, s>>>(a, b);
+        else k_anyhit<false, false><<<ga, 128, 0, s>>>(a, b);
+        if (batch) k_hit_eval<true><<<gs, 128, 0, s>>>(a);
+        else k_hit_eval<false><<<gs, 128, 0, s>>>(a);
+        if (a.capture) k_hit_sum<true><<<gs, 128, 0, s>>>(a, b);
+        else k_hit_sum<false><<<gs, 128, 0, s>>>(a, b);
         VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
     }
     VRG_CUDA_TRY(cudaGetLastError());

@@ -47,6 +47,10 @@ struct FrameArgs {
     uint32_t mode, spatial_iters;
     float spatial_radius;
     uint32_t m_cap, debug_view, accumulate, pack;
+    // launch configuration (scheduling only, never a result): idle lanes that
+    // trigger a warp's refill, persistent grids (CTAs), per-pixel CTA size
+    uint32_t refill_trace, refill_any;
+    uint32_t grid_trace, grid_shade, grid_any, stream_block;
     // wavefront state
     float4 *ray_o, *ray_d;
     uint32_t *queue[2];

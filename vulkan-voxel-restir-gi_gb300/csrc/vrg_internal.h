@@ -221,6 +221,8 @@ struct Renderer {
     // host staging
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
+    cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev[16] = {};
     cudaEvent_t ev_k[2][8] = {};          // after k_trace / after k_shade, per bounce
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
@@ -229,6 +231,7 @@ struct Renderer {
     uint32_t *infer_list = nullptr, *train_list = nullptr;
     uint8_t *qflag = nullptr;
     int grid_bounce = 0;
+    vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
 };
 
 }  // namespace vrg

@@ -79,6 +79,16 @@ class NrcDesc(C.Structure):
                 ("scene_max", C.c_float * 3)]
 
 
+class Tuning(C.Structure):
+    """Launch configuration (scheduling only); 0 fields mean the default."""
+    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill", C.c_uint32),
+                ("shade_blocks_per_sm", C.c_uint32), ("anyhit_blocks_per_sm", C.c_uint32),
+                ("anyhit_refill", C.c_uint32), ("stream_block", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class View(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("temporal_seed", C.c_uint32),
                 ("spatial_seed", C.c_uint32)]
@@ -144,6 +154,10 @@ SIGNATURES = [
     ("vrg_nrc_write", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
     ("vrg_nrc_layout", C.c_int32, [_P, C.POINTER(C.c_uint32), _P, _P, _P]),
     ("vrg_renderer_set_cache", C.c_int32, [_P, _P]),
+    ("vrg_renderer_set_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
+    ("vrg_renderer_get_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
+    ("vrg_renderer_autotune", C.c_int32, [_P, _P, C.POINTER(Camera), C.POINTER(RenderParams), C.c_uint32,
+                                          C.POINTER(Tuning), C.POINTER(C.c_float)]),
     ("vrg_renderer_create_batched", C.c_int32, [_P, C.c_uint32, _P, _P, C.c_uint32, C.POINTER(_P)]),
     ("vrg_renderer_view_offset", C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_uint64)]),
     ("vrg_render_batched", C.c_int32, [_P, C.POINTER(View), C.c_uint32, C.POINTER(RenderParams), _P,
@@ -421,6 +435,22 @@ class Renderer:
     def set_cache(self, cache):
         check(self.ctx.lib.vrg_renderer_set_cache(self.h, None if cache is None else cache.h),
               "vrg_renderer_set_cache")
+
+    def set_tuning(self, tuning: "Tuning"):
+        check(self.ctx.lib.vrg_renderer_set_tuning(self.h, C.byref(tuning)), "vrg_renderer_set_tuning")
+
+    def get_tuning(self) -> "Tuning":
+        t = Tuning()
+        check(self.ctx.lib.vrg_renderer_get_tuning(self.h, C.byref(t)), "vrg_renderer_get_tuning")
+        return t
+
+    def autotune(self, scene: "Scene", cam: "Camera", params: "RenderParams", frames: int = 3):
+        """Times candidate launch configurations on these frames and installs
+        the fastest; returns (Tuning, ms per frame)."""
+        t, ms = Tuning(), C.c_float()
+        check(self.ctx.lib.vrg_renderer_autotune(self.h, scene.h, C.byref(cam), C.byref(params), frames,
+                                                 C.byref(t), C.byref(ms)), "vrg_renderer_autotune")
+        return t, ms.value
 
     def render_params(self, scene: Scene, cam: Camera, params: RenderParams, want_image=True,
                       want_radiance=False):
