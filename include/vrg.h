@@ -229,6 +229,21 @@ VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_
 VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r);
 /* Renderer::rebuild: new extent, all per-pixel state reset. */
 VRG_API vrg_status vrg_renderer_resize(vrg_renderer *r, uint32_t width, uint32_t height);
+/* Renderer.scale (interactive_rendering.rs:329,1010; postprocess.rs:39-88):
+ * frames are traced at scale x the output extent, and each output pixel (BGRA8
+ * and radiance) is the mean of its scale x scale traced pixels.  Cameras keep
+ * the output extent; accumulation and debug readback are at the traced
+ * resolution.  1..8 (1 = the reference's default); reallocates like
+ * vrg_renderer_resize.  Single-view renderers. */
+VRG_API vrg_status vrg_renderer_set_scale(vrg_renderer *r, uint32_t scale);
+
+/* Image files of a frame (replacing the swapchain copy,
+ * interactive_rendering.rs:1625-1629): BGRA8 as binary PPM (P6) or PNG
+ * (8-bit RGB, stored deflate blocks), float RGB as PFM (little-endian,
+ * bottom row first as the format requires).  Host buffers, row 0 = top. */
+VRG_API vrg_status vrg_image_write_ppm(const char *path, const uint8_t *bgra8, uint32_t width, uint32_t height);
+VRG_API vrg_status vrg_image_write_png(const char *path, const uint8_t *bgra8, uint32_t width, uint32_t height);
+VRG_API vrg_status vrg_image_write_pfm(const char *path, const float *rgb, uint32_t width, uint32_t height);
 /* Renderer::render.  frame_index = the renderer's frame counter, advanced by
  * one per call (interactive_rendering.rs:1668); the raytrace invocation seed
  * is frame_index*num_bounces + bounce (:1189). */

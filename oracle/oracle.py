@@ -49,6 +49,7 @@ def lib():
                                      C.c_int64]),
             ("orc_readback", C.c_int, [_P, C.c_uint32, _P, C.c_uint64]),
             ("orc_read_image", C.c_int, [_P, _P, _P]),
+            ("orc_postprocess_scaled", C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
             ("orc_read_accum", C.c_uint32, [_P, _P]),
             ("orc_ray_counts", None, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         ]
@@ -140,6 +141,17 @@ class World:
         if self.h:
             lib().orc_world_destroy(self.h)
             self.h = None
+
+
+def postprocess_scaled(view, scale):
+    """postprocess.rs:39-88 with srcscale = scale: (H, W, 3) float view colours of
+    the traced frame -> ((H/s, W/s, 4) BGRA8, (H/s, W/s, 3) float mean)."""
+    view = np.ascontiguousarray(view, np.float32)
+    H, W = view.shape[:2]
+    img = np.zeros((H // scale, W // scale, 4), np.uint8)
+    out = np.zeros((H // scale, W // scale, 3), np.float32)
+    assert lib().orc_postprocess_scaled(_p(view), W, H, scale, _p(img), _p(out)) == 0
+    return img, out
 
 
 def build_world(mats, n, world):

@@ -1484,6 +1484,44 @@ ORC_API int orc_read_image(orc_renderer *r, uint8_t *bgra, float *view) {
     if (view) memcpy(view, r->R.view.data(), P * 12);
     return 0;
 }
+// postprocess with srcscale = scale, dstscale = 1 (postprocess.rs:39-88): the
+// per-pixel view colours of a W x H traced frame (row-major float RGB) to
+// (W/scale) x (H/scale) output pixels, each the sum of its scale x scale
+// samples (rows outer, columns inner, from vec3(0.0)) divided by
+// float(scale*scale), packed as u8(bgr*255) with alpha 255.
+ORC_API int orc_postprocess_scaled(const float *view, uint32_t W, uint32_t H, uint32_t scale, uint8_t *bgra,
+                                   float *out) {
+    if (scale == 0 || W % scale || H % scale) return 1;
+    const uint32_t ow = W / scale, oh = H / scale;
+    for (uint32_t oy = 0; oy < oh; oy++)
+        for (uint32_t ox = 0; ox < ow; ox++) {
+            V3 c = v3(0.0f, 0.0f, 0.0f);
+            for (uint32_t sy = 0; sy < scale; sy++) {
+                const uint32_t y = oy * scale + sy;
+                for (uint32_t sx = 0; sx < scale; sx++) {
+                    const uint32_t x = ox * scale + sx;
+                    const size_t id = (size_t)y * W + x;
+                    c = v3(c.x + view[3 * id], c.y + view[3 * id + 1], c.z + view[3 * id + 2]);
+                }
+            }
+            const float n = (float)(scale * scale);
+            c = v3(c.x / n, c.y / n, c.z / n);
+            const size_t o = (size_t)oy * ow + ox;
+            if (bgra) {
+                bgra[4 * o] = to_u8(c.z);
+                bgra[4 * o + 1] = to_u8(c.y);
+                bgra[4 * o + 2] = to_u8(c.x);
+                bgra[4 * o + 3] = 255;
+            }
+            if (out) {
+                out[3 * o] = c.x;
+                out[3 * o + 1] = c.y;
+                out[3 * o + 2] = c.z;
+            }
+        }
+    return 0;
+}
+
 ORC_API void orc_ray_counts(orc_renderer *r, uint64_t *closest, uint64_t *any) {
     *closest = r->R.rays_closest;
     *any = r->R.rays_any;

@@ -116,3 +116,34 @@ def test_golden_tiny_frame_gpu(gpu_ctx):
         assert np.array_equal(r.readback(vrg.DBG_HIT, 3), g[f"f{f}_hit"])
         for what, key in ((vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_FINAL, "final")):
             assert r.readback(what, 3).tobytes() == g[f"f{f}_{key}"].tobytes(), (f, key)
+
+
+@pytest.mark.parametrize("scale", [2, 3])
+def test_supersampled_frame_bit_exact(gpu_ctx, orc, scale):
+    """Renderer.scale: traced at scale x the output extent, each output pixel
+    the mean of its scale x scale samples (postprocess.rs:39-88) — against the
+    oracle frame at the traced extent, postprocessed by the oracle."""
+    OWd, OHd = 40, 24
+    mats, n, world = terrain_world(4, 1, 2, 0.01)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    OW = orc.build_world(mats, n, world)
+    try:
+        gr = vrg.Renderer(gpu_ctx, OWd, OHd, 3, scale=scale)
+        orr = orc.Renderer(OWd * scale, OHd * scale, 3)
+        for f in range(2):
+            cam = vrg.orbit_camera(1, 2, f, 64, OWd, OHd)
+            ocam = vrg.orbit_camera(1, 2, f, 64, OWd * scale, OHd * scale)
+            p = params(nee=1, view=1, spatial=3, nb=3, seeds=(f, 10 + f, 20 + f))
+            img, rad = gr.render_params(scene, cam, p, want_image=True, want_radiance=True)
+            orr.render(OW, ocam, p)
+            _, oview = orr.image()
+            oimg, orad = orc.postprocess_scaled(oview, scale)
+            assert img.shape == (OHd, OWd, 4) and rad.shape == (OHd, OWd, 3)
+            assert np.array_equal(img, oimg), f
+            assert np.array_equal(rad.view(np.uint32), orad.view(np.uint32)), f
+            assert gr.last_stats.error_flags == 0
+        gr.close()
+        orr.close()
+    finally:
+        OW.close()

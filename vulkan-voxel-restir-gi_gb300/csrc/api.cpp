@@ -420,6 +420,14 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->radiance = (float *)(B + o_rad);
     r->accum = (double *)(B + o_acc);
     VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, r->ctx->stream));
+    r->out_buf.reset();
+    r->radiance_out = nullptr;
+    if (r->scale > 1) {
+        DevBufPtr ob;
+        VRG_TRY(dev_alloc(r->ctx->stream, (size_t)r->out_w * r->out_h * 12, ob));
+        r->out_buf = ob;
+        r->radiance_out = (float *)ob->ptr;
+    }
     drop_graphs(r);
     r->buf = b;
     r->res = nullptr;
@@ -455,8 +463,8 @@ VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_
     if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
     vrg_renderer *r = new vrg_renderer();
     r->ctx = ctx;
-    r->W = width;
-    r->H = height;
+    r->W = r->out_w = width;
+    r->H = r->out_h = height;
     r->P = (uint64_t)width * height;
     r->nb_max = max_bounces;
     vrg_status st = renderer_alloc(r);
@@ -488,8 +496,8 @@ VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_view
     }
     vrg_renderer *r = new vrg_renderer();
     r->ctx = ctx;
-    r->W = widths[0];
-    r->H = heights[0];
+    r->W = r->out_w = widths[0];
+    r->H = r->out_h = heights[0];
     r->P = P;
     r->nb_max = max_bounces;
     r->n_views = n_views;
@@ -575,11 +583,29 @@ VRG_API vrg_status vrg_renderer_resize(vrg_renderer *r, uint32_t width, uint32_t
         set_error("a batched renderer has fixed view extents");
         return VRG_ERR_STATE;
     }
-    if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
+    if ((uint64_t)width * height * r->scale * r->scale >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
     cudaStreamSynchronize(r->ctx->stream);
-    r->W = width;
-    r->H = height;
-    r->P = (uint64_t)width * height;
+    r->out_w = width;
+    r->out_h = height;
+    r->W = width * r->scale;
+    r->H = height * r->scale;
+    r->P = (uint64_t)r->W * r->H;
+    return renderer_alloc(r);
+}
+
+VRG_API vrg_status vrg_renderer_set_scale(vrg_renderer *r, uint32_t scale) {
+    if (!r || scale == 0 || scale > 8) return VRG_ERR_INVALID_ARGUMENT;
+    if (r->n_views) {
+        set_error("a batched renderer renders at scale 1");
+        return VRG_ERR_STATE;
+    }
+    if (scale == r->scale) return VRG_OK;
+    if ((uint64_t)r->out_w * r->out_h * scale * scale >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
+    cudaStreamSynchronize(r->ctx->stream);
+    r->scale = scale;
+    r->W = r->out_w * scale;
+    r->H = r->out_h * scale;
+    r->P = (uint64_t)r->W * r->H;
     return renderer_alloc(r);
 }
 
@@ -771,7 +797,12 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.spatial = r->spatial;
     a.final_t = r->final_t;
     a.bgra = r->bgra;
-    a.radiance = want_radiance ? r->radiance : nullptr;
+    a.radiance = (want_radiance || r->scale > 1) ? r->radiance : nullptr;
+    a.scale = r->scale;
+    a.out_w = r->out_w;
+    a.out_h = r->out_h;
+    a.out_bgra = r->bgra;
+    a.out_radiance = (want_radiance && r->scale > 1) ? r->radiance_out : nullptr;
     a.accum = r->accum;
     a.capture = capture ? 1u : 0u;
     a.c_origin = r->c_origin;
@@ -903,9 +934,9 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         set_error("a batched renderer renders with vrg_render_batched");
         return VRG_ERR_STATE;
     }
-    if (cam->width != r->W || cam->height != r->H) {
+    if (cam->width != r->out_w || cam->height != r->out_h) {
         set_error("camera extent %ux%u differs from the renderer's %ux%u (call vrg_renderer_resize)", cam->width,
-                  cam->height, r->W, r->H);
+                  cam->height, r->out_w, r->out_h);
         return VRG_ERR_INVALID_ARGUMENT;
     }
     if (pr->flags & VRG_RENDER_GRAPH) {
@@ -933,14 +964,24 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     a.v0.frame = r->frame;
     a.v0.temporal_seed = pr->temporal_seed;
     a.v0.spatial_seed = pr->spatial_seed;
-    if (out && !out->host && out->radiance) a.radiance = out->radiance;
-    if (out && !out->host && out->bgra8) a.bgra = out->bgra8;
+    if (out && !out->host) {  // device outputs are written in place
+        if (r->scale > 1) {
+            if (out->radiance) a.out_radiance = out->radiance;
+            if (out->bgra8) a.out_bgra = out->bgra8;
+        } else {
+            if (out->radiance) a.radiance = out->radiance;
+            if (out->bgra8) a.bgra = out->bgra8;
+        }
+    }
     VRG_TRY(frame_launch(r, a, true));
     if (out && out->host) {
+        const size_t Po = (size_t)r->out_w * r->out_h;
         if (out->bgra8 && a.pack)
-            VRG_CUDA_TRY(cudaMemcpyAsync(out->bgra8, a.bgra, P * 4, cudaMemcpyDeviceToHost, s));
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->bgra8, r->scale > 1 ? a.out_bgra : a.bgra, Po * 4,
+                                         cudaMemcpyDeviceToHost, s));
         if (out->radiance)
-            VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, a.radiance, P * 12, cudaMemcpyDeviceToHost, s));
+            VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, r->scale > 1 ? a.out_radiance : a.radiance, Po * 12,
+                                         cudaMemcpyDeviceToHost, s));
     }
     frame_done(r, a, pr);
     if (stats) return frame_stats(r, a, true, stats);

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameAr
     if (a.debug_view == 0) c = ld3(a.plain[p]);
     else if (a.debug_view == 1) c = fin;
     else { const float dv = ucw_view / 10.0f; c = f3{dv, dv, dv}; }
-    if (a.pack) {
+    if (a.pack && a.scale <= 1) {
         uchar4 px = make_uchar4(to_u8(c.z), to_u8(c.y), to_u8(c.x), 255);
         reinterpret_cast<uchar4 *>(a.bgra)[p] = px;
     }
@@ -243,6 +243,28 @@ __global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameAr
         a.accum[3 * (size_t)p + 1] += (double)c.y;
         a.accum[3 * (size_t)p + 2] += (double)c.z;
     }
+}
+
+// postprocess with scale > 1 (postprocess.rs:39-88, srcscale = scale,
+// dstscale = 1): each output pixel is the mean of its scale x scale traced
+// pixels, summed row by row from zero as the shader does, then packed
+__global__ void __launch_bounds__(256) k_downsample(const __grid_constant__ FrameArgs a) {
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= a.out_w * a.out_h) return;
+    const uint32_t ox = o % a.out_w, oy = o / a.out_w, s = a.scale, src_w = a.out_w * s;
+    f3 c = f3{0.0f, 0.0f, 0.0f};
+    for (uint32_t sy = 0; sy < s; sy++) {
+        const uint32_t y = oy * s + sy;
+        for (uint32_t sx = 0; sx < s; sx++) {
+            const uint32_t x = ox * s + sx;
+            const size_t id = (size_t)y * src_w + x;
+            c = f3{c.x + a.radiance[3 * id], c.y + a.radiance[3 * id + 1], c.z + a.radiance[3 * id + 2]};
+        }
+    }
+    const float n = (float)(s * s);
+    c = f3{c.x / n, c.y / n, c.z / n};
+    if (a.pack) reinterpret_cast<uchar4 *>(a.out_bgra)[o] = make_uchar4(to_u8(c.z), to_u8(c.y), to_u8(c.x), 255);
+    if (a.out_radiance) st3(a.out_radiance, o, c);
 }
 
 // training targets of the radiance cache: the outgoing radiance at vertex
@@ -290,6 +312,11 @@ vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a) {
     else if (a.capture) k_spatial<true, false><<<g, t, 0, s>>>(a);
     else k_spatial<false, false><<<g, t, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
+    if (a.scale > 1 && (a.pack || a.out_radiance)) {
+        const uint32_t n = a.out_w * a.out_h;
+        k_downsample<<<(n + 255) / 256, 256, 0, s>>>(a);
+        VRG_CUDA_TRY(cudaGetLastError());
+    }
     return VRG_OK;
 }
 

@@ -50,6 +50,11 @@ struct FrameArgs {
     // launch configuration (scheduling only, never a result): idle lanes that
     // trigger a warp's refill, persistent grids (CTAs), per-pixel CTA size
     uint32_t refill_trace, refill_any;
+    // supersampling (Renderer.scale): the frame is traced at scale x the
+    // output extent; k_downsample packs out_w x out_h pixels
+    uint32_t scale, out_w, out_h;
+    uint8_t *out_bgra;
+    float *out_radiance;
     uint32_t grid_trace, grid_shade, grid_any, stream_block;
     // wavefront state
     float4 *ray_o, *ray_d;

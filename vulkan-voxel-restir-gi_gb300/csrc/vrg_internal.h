@@ -171,6 +171,10 @@ struct Renderer {
     Context *ctx = nullptr;
     uint32_t W = 0, H = 0, nb_max = 0;
     uint64_t P = 0;                       // pixels of a frame (all views of a batched renderer)
+    uint32_t scale = 1;                   // supersampling: W x H = out_w*scale x out_h*scale traced pixels
+    uint32_t out_w = 0, out_h = 0;        // output extent (the camera's)
+    DevBufPtr out_buf;                    // output-resolution radiance when scale > 1
+    float *radiance_out = nullptr;
     // batched views (n_views == 0: single-view renderer)
     uint32_t n_views = 0;
     std::vector<uint32_t> vw, vh;         // view extents

@@ -154,6 +154,10 @@ SIGNATURES = [
     ("vrg_nrc_write", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
     ("vrg_nrc_layout", C.c_int32, [_P, C.POINTER(C.c_uint32), _P, _P, _P]),
     ("vrg_renderer_set_cache", C.c_int32, [_P, _P]),
+    ("vrg_renderer_set_scale", C.c_int32, [_P, C.c_uint32]),
+    ("vrg_image_write_ppm", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
+    ("vrg_image_write_png", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
+    ("vrg_image_write_pfm", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
     ("vrg_renderer_set_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
     ("vrg_renderer_get_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
     ("vrg_renderer_autotune", C.c_int32, [_P, _P, C.POINTER(Camera), C.POINTER(RenderParams), C.c_uint32,
@@ -410,16 +414,37 @@ def commit_scenes(scenes):
     check(ctx.lib.vrg_scene_commit_many(arr, len(scenes)), "vrg_scene_commit_many")
 
 
-class Renderer:
-    """Renderer (interactive_rendering.rs:328-1669), headless."""
+def write_image(path: str, img: np.ndarray):
+    """Writes a frame: BGRA8 (h, w, 4) as .ppm or .png, float RGB (h, w, 3) as .pfm."""
+    lib = load_library()
+    img = np.ascontiguousarray(img)
+    h, w = img.shape[:2]
+    ext = os.path.splitext(path)[1].lower()
+    if ext == ".pfm":
+        fn, want = lib.vrg_image_write_pfm, np.float32
+    elif ext == ".png":
+        fn, want = lib.vrg_image_write_png, np.uint8
+    else:
+        fn, want = lib.vrg_image_write_ppm, np.uint8
+    img = np.ascontiguousarray(img, dtype=want)
+    check(fn(path.encode(), _ptr(img), w, h), "vrg_image_write")
 
-    def __init__(self, ctx: Context, width: int, height: int, num_bounces: int = 3):
+
+class Renderer:
+    """Renderer (interactive_rendering.rs:328-1669), headless.  scale > 1
+    traces scale x the extent and averages scale x scale samples per output
+    pixel (Renderer.scale)."""
+
+    def __init__(self, ctx: Context, width: int, height: int, num_bounces: int = 3, scale: int = 1):
         self.ctx = ctx
         self.width, self.height, self.num_bounces = width, height, num_bounces
+        self.scale = scale
         self.h = C.c_void_p()
         check(ctx.lib.vrg_renderer_create(ctx.h, width, height, num_bounces, C.byref(self.h)),
               "vrg_renderer_create")
         ctx.adopt(self)
+        if scale != 1:
+            check(ctx.lib.vrg_renderer_set_scale(self.h, scale), "vrg_renderer_set_scale")
         self.seeds = Pcg32(0x5eed)
         self.last_stats = FrameStats()
 
@@ -471,7 +496,7 @@ class Renderer:
         return img
 
     def readback(self, what: int, nb: int):
-        P = self.width * self.height
+        P = self.width * self.height * self.scale * self.scale
         shapes = {DBG_ORIGIN: (nb + 1, P, 3), DBG_DIRECTION: (nb + 1, P, 3), DBG_NORMAL: (nb, P, 3),
                   DBG_EMISSIVITY: (nb, P, 3), DBG_REFLECTIVITY: (nb, P, 3), DBG_MIS: (nb, P),
                   DBG_BSDF_PDF: (nb, P), DBG_NEE_PDF: (nb, P), DBG_RADIANCE: (nb, P, 3), DBG_Q: (nb, P),
@@ -483,10 +508,11 @@ class Renderer:
 
     def read_accumulation(self):
         n = C.c_uint32()
-        a = np.zeros(self.width * self.height * 3, dtype=np.float32)
+        w, h = self.width * self.scale, self.height * self.scale
+        a = np.zeros(w * h * 3, dtype=np.float32)
         check(self.ctx.lib.vrg_renderer_read_accumulation(self.h, _ptr(a), C.byref(n)),
               "vrg_renderer_read_accumulation")
-        return a.reshape(self.height, self.width, 3), n.value
+        return a.reshape(h, w, 3), n.value
 
     def reset_accumulation(self):
         check(self.ctx.lib.vrg_renderer_reset_accumulation(self.h), "vrg_renderer_reset_accumulation")
