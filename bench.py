@@ -287,6 +287,23 @@ def view_cameras(nx, nz, frame, w, h, n_views=4):
     return cams
 
 
+def update_commit_ms(scene, nx, nz, reps=5):
+    """Commit time after moving one chunk (a transform update: the chunk BLASes
+    are kept, the top levels and world-space layouts are rebuilt); the chunk
+    goes back to its place at the end."""
+    key = (nx // 2) * nz + nz // 2
+    home = (32 * (nx // 2), 0, 32 * (nz // 2))
+    ms = []
+    for i in range(reps):
+        scene.update_object(key, (home[0], 40 + 8 * i, home[2]))
+        t0 = time.perf_counter()
+        scene.commit()
+        ms.append(1000 * (time.perf_counter() - t0))
+    scene.update_object(key, home)
+    scene.commit()
+    return round(float(np.median(ms)), 3)
+
+
 def run_large(args, d):
     """Large workload: 32x32 chunks (1024x32x1024 blocks, 0.2% emissive), four
     3840x2160 views of one orbit eye rendered as one batch, 1 spp ReSTIR over
@@ -378,7 +395,8 @@ def run_large(args, d):
                    "method": "2 bounces ending into the radiance cache + ReSTIR (3 spatial, 30 px, M-cap 20), "
                              "1/16 paths trace 4 more bounces and train the cache",
                    "parallelism": "single GPU, one batched launch sequence"},
-        "scene_build": {"blas_ms": round(1000 * t_blas, 1), "commit_ms": round(1000 * t_commit, 1)},
+        "scene_build": {"blas_ms": round(1000 * t_blas, 1), "commit_ms": round(1000 * t_commit, 1),
+                        "update_commit_ms": update_commit_ms(scene, C4_N, C4_N)},
         "methods": out,
         "ground_truth": {"spp": n_gt, "bounces": 8, "accumulation": "fp64 on the GPU", "seconds": round(gt_s, 1)},
         "equal_time": {"plain_frames": k, "relmse_plain": round(rel_plain_k, 5),
@@ -561,6 +579,7 @@ def run_ours(args, d):
     if not args.no_batched:
         r.close()  # the batch needs the memory of the 1080p renderer
         batched = batched_block(ctx, steps=16, warmup=3)
+    upd_ms = update_commit_ms(scene, NX, NZ)
     cpu_frames = args.cpu_frames
     cpu_mr, cpu_dt, cpu_rays = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0) if not args.no_cpu
                                 else (None, 0, 0))
@@ -582,6 +601,7 @@ def run_ours(args, d):
                          "spatial_finalize_pack": round(ms_sp / args.steps, 4)},
         "rays_per_frame": rays // max(args.steps, 1),
         "scene_build_ms": round(build_s * 1000, 2),
+        "update_commit_ms": upd_ms,
         "roofline": {"bound": "hbm", "kernel": "k_trace", "achieved": round(achieved, 2), "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                      "traffic": round(TRACE_DRAM_BYTES_PER_PX * W * H / NB),

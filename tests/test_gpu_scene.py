@@ -67,3 +67,45 @@ def test_update_missing_key_is_error(gpu_ctx):
     with pytest.raises(vrg.VrgError) as e:
         sc.update_object(12345, (0, 0, 0))
     assert e.value.status == vrg.ERR_NOT_FOUND
+
+
+def test_transform_update_matches_oracle(gpu_ctx, orc):
+    """Scene::update_object (scene.rs:205): moving a chunk keeps its BLAS and
+    rebuilds the top levels and world-space layouts; the committed top levels
+    and a rendered frame equal the oracle's world built with the chunk at its
+    new place."""
+    from helpers import compare_frame, params
+    mats, n, world = terrain_world(12, 3, 2, 0.02)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    scene.commit()
+    moved = {1: (0, 24, 32), 4: (64, -8, 32)}  # key = cx * nz + cz
+    for key, t in moved.items():
+        scene.update_object(key, t)
+    lt, gt = scene.get_tlas()
+    floor = np.zeros(vrg.CHUNK_BLOCKS, dtype=np.uint8)
+    OW = orc.World(mats, n)
+    try:
+        for cx in range(3):
+            for cz in range(2):
+                key = cx * 2 + cz
+                t = moved.get(key, (32 * cx, 0, 32 * cz))
+                OW.add_chunk(key, world[cx, cz], vrg.chunk_neighbours(world, cx, cz, floor), t)
+        OW.commit()
+        assert nodes_equal(lt, OW.read_tl(0)), first_node_diff(lt, OW.read_tl(0))
+        assert nodes_equal(gt, OW.read_tl(1)), first_node_diff(gt, OW.read_tl(1))
+        W, H = 64, 48
+        gr = vrg.Renderer(gpu_ctx, W, H, 3)
+        orr = orc.Renderer(W, H, 3)
+        cam = vrg.orbit_camera(3, 2, 5, 64, W, H)
+        p = params(nee=1, view=1, spatial=3, nb=3, seeds=(1, 2, 3))
+        img, rad = gr.render_params(scene, cam, p, want_image=True, want_radiance=True)
+        orr.render(OW, cam, p)
+        oimg, orad = orr.image()
+        diffs = compare_frame(gr, orr, 3)
+        assert all(v == 0 for v in diffs.values()), diffs
+        assert np.array_equal(img.reshape(-1), oimg.reshape(-1))
+        gr.close()
+        orr.close()
+    finally:
+        OW.close()

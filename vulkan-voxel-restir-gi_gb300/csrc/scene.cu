@@ -148,29 +148,55 @@ __global__ void k_wide4(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *
     w[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-__global__ void k_geo_records(const InstBuild *inst, uint32_t k, int4 *rec) {
-    const InstBuild I = inst[k];
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < I.n_prims; p += gridDim.x * blockDim.x) {
-        int2 l = I.geo_local[p];
-        uint32_t blk = (uint32_t)l.x & 0x7FFFu;
-        int wx = (int)(blk >> 10) + I.ioff[0], wy = (int)((blk >> 5) & 31u) + I.ioff[1],
-            wz = (int)(blk & 31u) + I.ioff[2];
-        rec[I.rbase + p] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16), l.x, l.y);
+// last instance k with key(k) <= g (keys non-decreasing, key(0) <= g).  An
+// instance that owns no nodes or records shares its key with the next one,
+// so the last of equal keys is the owner.
+template <typename Key>
+__device__ __forceinline__ uint32_t inst_of(const InstBuild *inst, uint32_t n_inst, uint32_t g, Key key) {
+    uint32_t lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (key(inst[mid]) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// world-space surface-block records of every instance, one thread per record
+// (records of instance k start at its rbase)
+__global__ void k_geo_records(const InstBuild *inst, uint32_t n_inst, uint32_t n_rec, int4 *rec) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_rec; g += gridDim.x * blockDim.x) {
+        const uint32_t k = inst_of(inst, n_inst, g, [](const InstBuild &I) { return I.rbase; });
+        const InstBuild &I = inst[k];
+        const uint32_t p = g - I.rbase;
+        const int2 l = I.geo_local[p];
+        const uint32_t blk = (uint32_t)l.x & 0x7FFFu;
+        const int wx = (int)(blk >> 10) + I.ioff[0], wy = (int)((blk >> 5) & 31u) + I.ioff[1],
+                  wz = (int)(blk & 31u) + I.ioff[2];
+        rec[g] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16), l.x, l.y);
     }
 }
 
-__global__ void k_light_records(const InstBuild *inst, uint32_t k, int4 *rec) {
-    const InstBuild I = inst[k];
-    uint32_t n_nodes = 2 * I.n_prims - 1;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_nodes; j += gridDim.x * blockDim.x) {
-        uint32_t p = I.leaf[j];
+// world-space light-triangle records of every instance, one thread per light
+// BLAS node (node j of instance k is index wbase - base + j); leaves write
+// their prim's record
+__global__ void k_light_records(const InstBuild *inst, uint32_t n_inst, uint32_t base, uint32_t n_nodes_all,
+                                int4 *rec) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes_all; g += gridDim.x * blockDim.x) {
+        const uint32_t k =
+            inst_of(inst, n_inst, g + base, [](const InstBuild &I) { return I.wbase; });
+        const InstBuild &I = inst[k];
+        if (I.n_prims == 0) continue;
+        const uint32_t j = g + base - I.wbase;
+        if (j >= 2 * I.n_prims - 1) continue;
+        const uint32_t p = I.leaf[j];
         if (p == INVALID) continue;
-        uint32_t t = I.light_tri[p];
-        int wx = (int)(t & 31u) + I.ioff[0], wy = (int)((t >> 5) & 31u) + I.ioff[1],
-            wz = (int)((t >> 10) & 31u) + I.ioff[2];
-        uint32_t f = (t >> 15) & 7u, h = (t >> 18) & 1u;
-        rec[I.rbase + p] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16), (int)(f | (h << 3)),
-                                     (int)j);
+        const uint32_t t = I.light_tri[p];
+        const int wx = (int)(t & 31u) + I.ioff[0], wy = (int)((t >> 5) & 31u) + I.ioff[1],
+                  wz = (int)((t >> 10) & 31u) + I.ioff[2];
+        const uint32_t f = (t >> 15) & 7u, h = (t >> 18) & 1u;
+        rec[I.rbase + p] = make_int4((wx & 0xFFFF) | (wz << 16), (wy & 0xFFFF) | (int)(k << 16),
+                                     (int)(f | (h << 3)), (int)j);
     }
 }
 
@@ -391,7 +417,7 @@ struct CommitPrep {
     std::vector<float> tl_in;        // [prims][10]: lo3 hi3 off3 power
     std::vector<uint32_t> tl_ids;
     std::vector<InstBuild> gb, lb;
-    uint64_t geo_recs = 0, light_recs = 0, n_geo_wide = 0;
+    uint64_t geo_recs = 0, light_recs = 0, n_geo_wide = 0, n_light_nodes_all = 0;
     uint32_t max_levels = 0;
     DevBufPtr buf;
     uint8_t *B = nullptr;
@@ -485,6 +511,7 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
         cp.light_recs += cs.n_light;
         cp.max_levels = std::max(cp.max_levels, o->levels);
     }
+    cp.n_light_nodes_all = light_nodes;
     if (cp.n_geo_tl + geo_nodes >= 0x7FFFFFFFull || cp.geo_recs >= 0x7FFFFFFFull) {
         set_error("scene too large for 31-bit node references");
         return VRG_ERR_UNSUPPORTED;
@@ -612,13 +639,14 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
                                                                        (float4 *)(B + cp.o_gw));
         VRG_CUDA_TRY(cudaGetLastError());
     }
-    for (uint32_t i = 0; i < ni; i++) {
-        if (cp.gb[i].n_prims)
-            k_geo_records<<<std::min(64u, (cp.gb[i].n_prims + 255) / 256), 256, 0, s>>>(d_gb, i,
-                                                                                       (int4 *)(B + cp.o_gr));
-        if (cp.lb[i].n_prims)
-            k_light_records<<<std::min(64u, (2 * cp.lb[i].n_prims + 254) / 256), 256, 0, s>>>(
-                d_lb, i, (int4 *)(B + cp.o_lr));
+    if (cp.geo_recs) {
+        const uint32_t n = (uint32_t)cp.geo_recs;
+        k_geo_records<<<std::min(4096u, (n + 255) / 256), 256, 0, s>>>(d_gb, ni, n, (int4 *)(B + cp.o_gr));
+    }
+    if (cp.light_recs) {
+        const uint32_t n = (uint32_t)(cp.n_light_nodes_all);
+        k_light_records<<<std::min(4096u, (n + 255) / 256), 256, 0, s>>>(d_lb, ni, cp.n_light_tl, n,
+                                                                        (int4 *)(B + cp.o_lr));
     }
     VRG_CUDA_TRY(cudaGetLastError());
     DevScene &D = cp.dev;
