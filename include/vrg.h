@@ -180,6 +180,20 @@ VRG_API const char *vrg_last_error(void);
  * Scene::new (interactive_rendering.rs:379-444, scene.rs:112).  n must be a
  * multiple of 6; air is block id n/6 (block.rs:106-107,121-123). */
 VRG_API vrg_status vrg_material_table_set(vrg_context *ctx, const vrg_material *mats, uint32_t n);
+/* The texture atlas itself (interactive_rendering.rs:379-444,736-760;
+ * block.rs:70-119): per material slot t = 6*block + face (the slots of the
+ * material table), three RGBA8 sRGB maps of width x height texels —
+ * reflectivity + alpha, emissivity, metallicity (.r) — laid out
+ * [slot][map][row][column][rgba], row 0 first.  With an atlas, shading samples
+ * the three maps at the hit's interpolated gen_mesh uv (nearest texel, clamped
+ * to the edge, sRGB decoded; raytrace.rs:457-480) in place of the slot's
+ * constant colours, and the emission is 1000 * emissivity.rgb; each slot's
+ * luminance becomes the mean of r8+g8+b8 over its emissivity map
+ * (get_texture_luminances, utils.rs:223-235).  Set it after the material
+ * table (n_slots = its length) and before uploading chunks, as the reference
+ * fixes the luminances at Scene::new.  rgba8 == NULL removes the atlas. */
+VRG_API vrg_status vrg_texture_atlas_set(vrg_context *ctx, const uint8_t *rgba8, uint32_t n_slots, uint32_t width,
+                                         uint32_t height);
 
 /* ---- objects (SceneUploader::upload_object, scene.rs:547) -------------- */
 /* One 32^3 chunk of u8 block ids plus its six neighbours (L,R,D,U,B,F as

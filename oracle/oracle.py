@@ -50,6 +50,7 @@ def lib():
             ("orc_readback", C.c_int, [_P, C.c_uint32, _P, C.c_uint64]),
             ("orc_read_image", C.c_int, [_P, _P, _P]),
             ("orc_postprocess_scaled", C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
+            ("orc_world_set_atlas", C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32]),
             ("orc_read_accum", C.c_uint32, [_P, _P]),
             ("orc_ray_counts", None, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         ]
@@ -100,6 +101,12 @@ class World:
         self.h = lib().orc_world_create(mats, n)
         assert self.h
         self.chunks = {}
+
+    def set_atlas(self, rgba):
+        """rgba: (slots, 3, h, w, 4) uint8 — before adding chunks."""
+        rgba = np.ascontiguousarray(rgba, np.uint8)
+        n, _, h, w, _ = rgba.shape
+        assert lib().orc_world_set_atlas(self.h, _p(rgba), n, w, h) == 0
 
     def add_chunk(self, key, blocks, neighbours, translation):
         blocks = np.ascontiguousarray(blocks, np.uint8).reshape(-1)

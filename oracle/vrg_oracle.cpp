@@ -431,6 +431,15 @@ static const uint8_t FACE_TRI[6][2][3] = {
     {{0b010, 0b100, 0b000}, {0b010, 0b110, 0b100}},  // back
     {{0b001, 0b101, 0b011}, {0b101, 0b111, 0b011}},  // front
 };
+// gen_mesh texture coordinates of each triangle vertex (chunk.rs:225-285)
+static const float FACE_UV[6][2][3][2] = {
+    {{{0, 1}, {1, 0}, {1, 1}}, {{0, 0}, {1, 0}, {0, 1}}},  // left
+    {{{0, 0}, {1, 1}, {0, 1}}, {{0, 0}, {1, 0}, {1, 1}}},  // right
+    {{{0, 0}, {1, 0}, {0, 1}}, {{1, 0}, {1, 1}, {0, 1}}},  // down
+    {{{1, 1}, {0, 0}, {1, 0}}, {{1, 1}, {0, 1}, {0, 0}}},  // up
+    {{{0, 0}, {1, 1}, {0, 1}}, {{0, 0}, {1, 0}, {1, 1}}},  // back
+    {{{1, 1}, {0, 1}, {1, 0}}, {{0, 1}, {0, 0}, {1, 0}}},  // front
+};
 static inline V3 corner_pos(int bx, int by, int bz, uint8_t bits) {
     return v3((float)(bx + ((bits >> 2) & 1)), (float)(by + ((bits >> 1) & 1)), (float)(bz + (bits & 1)));
 }
@@ -466,6 +475,10 @@ struct OChunk {
 struct OMaterials {
     std::vector<vrg_material> mats;
     uint32_t n_types = 0;
+    // texture atlas (interactive_rendering.rs:379-444): [slot][3 maps][h][w] RGBA8 sRGB
+    std::vector<uint8_t> atlas;
+    uint32_t atlas_w = 0, atlas_h = 0;
+    float srgb[256];
     uint32_t air() const { return n_types; }
     bool translucent(uint8_t b) const {
         if (b == n_types) return true;
@@ -1104,7 +1117,8 @@ static void render_frame(ORenderer &R, const OWorld &W, const vrg_camera &cam, c
             V3 bit = cross3(nrm, tan);
             V3 n = normalize3(nrm), tg = normalize3(tan), bt = normalize3(bit);
             uint8_t blk = W.inst[info.inst].ch->blocks[info.block];
-            const vrg_material &m = W.M.mats[6u * blk + (uint32_t)info.face];
+            const uint32_t slot = 6u * blk + (uint32_t)info.face;
+            const vrg_material &m = W.M.mats[slot];
             V3 new_origin = (tri[0] * b0 + tri[1] * info.b1) + tri[2] * info.b2;
             V3 new_dir;
             V3 reflectivity = v3(m.reflectivity[0], m.reflectivity[1], m.reflectivity[2]);
@@ -1112,6 +1126,25 @@ static void render_frame(ORenderer &R, const OWorld &W, const vrg_camera &cam, c
             float ndd = -dot3(direction, n);
             V3 emissivity = v3(m.emission[0] * ndd, m.emission[1] * ndd, m.emission[2] * ndd);
             float metallicity = m.metallic;
+            if (!W.M.atlas.empty()) {
+                // raytrace.rs:457-480: uv = v0.uv*b0 + v1.uv*b1 + v2.uv*b2; texture()
+                // with the default sampler taken as nearest, clamp to edge
+                const float(*uv)[2] = FACE_UV[info.face][info.half];
+                const float u = ((uv[0][0] * b0) + (uv[1][0] * info.b1)) + (uv[2][0] * info.b2);
+                const float vv = ((uv[0][1] * b0) + (uv[1][1] * info.b1)) + (uv[2][1] * info.b2);
+                const int aw = (int)W.M.atlas_w, ah = (int)W.M.atlas_h;
+                const int ix = std::min(std::max((int)std::floor(u * (float)aw), 0), aw - 1);
+                const int iy = std::min(std::max((int)std::floor(vv * (float)ah), 0), ah - 1);
+                auto texel = [&](int map) {
+                    return W.M.atlas.data() + 4 * ((((size_t)slot * 3 + map) * ah + iy) * aw + ix);
+                };
+                const uint8_t *t0 = texel(0), *t1 = texel(1), *t2 = texel(2);
+                const float *lin = W.M.srgb;
+                reflectivity = v3(lin[t0[0]], lin[t0[1]], lin[t0[2]]);
+                alpha = (float)t0[3] / 255.0f;
+                emissivity = v3((1000.0f * lin[t1[0]]) * ndd, (1000.0f * lin[t1[1]]) * ndd, (1000.0f * lin[t1[2]]) * ndd);
+                metallicity = lin[t2[0]];
+            }
             float mis_w = 0.0f, bsdf_pdf;
             float r0 = mm_rand(mm_combine(seed, 0));
             if (r0 < metallicity) {
@@ -1367,6 +1400,28 @@ ORC_API orc_world *orc_world_create(const vrg_material *mats, uint32_t n) {
     return w;
 }
 ORC_API void orc_world_destroy(orc_world *w) { delete w; }
+
+// texture atlas [slot][3 maps][h][w] RGBA8 sRGB; slot luminance = mean of
+// r8+g8+b8 over the emissivity map (utils.rs:223-235).  Before building chunks.
+ORC_API int orc_world_set_atlas(orc_world *w, const uint8_t *rgba8, uint32_t n_slots, uint32_t aw, uint32_t ah) {
+    OMaterials &M = w->W.M;
+    if (n_slots != M.mats.size() || aw == 0 || ah == 0) return 1;
+    const size_t map = (size_t)aw * ah;
+    M.atlas.assign(rgba8, rgba8 + (size_t)n_slots * 3 * map * 4);
+    M.atlas_w = aw;
+    M.atlas_h = ah;
+    for (uint32_t t = 0; t < n_slots; t++) {
+        const uint8_t *e = rgba8 + ((size_t)t * 3 + 1) * map * 4;
+        float L = 0.0f;
+        for (size_t i = 0; i < map; i++) L += ((float)e[4 * i] + (float)e[4 * i + 1]) + (float)e[4 * i + 2];
+        M.mats[t].luminance = L / (float)(aw * ah);
+    }
+    for (int i = 0; i < 256; i++) {  // sRGB EOTF
+        const double c = (double)i / 255.0;
+        M.srgb[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
+    return 0;
+}
 
 // gen_mesh + upload_object for one chunk with explicit neighbours (NULL = air)
 ORC_API orc_chunk *orc_chunk_build(orc_world *w, const uint8_t *blocks, const uint8_t *const nb[6]) {

@@ -147,3 +147,64 @@ def test_supersampled_frame_bit_exact(gpu_ctx, orc, scale):
         orr.close()
     finally:
         OW.close()
+
+
+def _atlas(rng, mats, n_types, size=16):
+    """Random RGBA8 maps per slot; block type 0 is a mirror (metallicity 1),
+    type 1 glass (alpha 0.3, translucent); emissive types keep emissive maps."""
+    n = 6 * n_types
+    a = np.zeros((n, 3, size, size, 4), np.uint8)
+    a[:, 0, :, :, :3] = rng.integers(40, 220, size=(n, size, size, 3))
+    a[:, 0, :, :, 3] = 255
+    for t in range(n):
+        if mats[t].emission[0] > 0:
+            a[t, 1, :, :, :3] = rng.integers(30, 90, size=(size, size, 3))
+    a[:, 1, :, :, 3] = 255
+    a[:, 2, :, :, 3] = 255
+    a[0:6, 2, :, :, 0] = 255          # mirror
+    a[6:12, 0, :, :, 3] = 77          # glass
+    return a
+
+
+def test_texture_atlas_mirror_glass_bit_exact(gpu_ctx, orc):
+    """Texture-atlas materials (three sRGB maps per slot sampled at the hit's
+    gen_mesh uv, raytrace.rs:457-480), with mirror and glass blocks exercising
+    the specular and transmissive branches (raytrace.rs:481-494)."""
+    rng = np.random.default_rng(77)
+    mats, n, world = terrain_world(6, 2, 2, 0.02)
+    world[world == 2] = 0  # more mirror blocks
+    world[(world == 3)] = 1  # and glass
+    mats[6].flags = vrg.MAT_TRANSLUCENT  # block type 1 (slots 6..11) is glass
+    atlas = _atlas(rng, mats, n // 6)
+    gpu_ctx.set_materials(mats, n)
+    gpu_ctx.set_atlas(atlas)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    OW = orc.World(mats, n)
+    OW.set_atlas(atlas)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, dtype=np.uint8)
+    for cx in range(2):
+        for cz in range(2):
+            OW.add_chunk(cx * 2 + cz, world[cx, cz], vrg.chunk_neighbours(world, cx, cz, floor), (32 * cx, 0, 32 * cz))
+    OW.commit()
+    try:
+        W, H = 72, 48
+        gr = vrg.Renderer(gpu_ctx, W, H, 3)
+        orr = orc.Renderer(W, H, 3)
+        for f in range(3):
+            cam = vrg.orbit_camera(2, 2, 3 * f, 64, W, H)
+            p = params(nee=1, view=1, spatial=3, nb=3, seeds=(f, 40 + f, 80 + f))
+            img, rad, oimg, orad = _frame(scene, OW, gr, orr, cam, p)
+            diffs = compare_frame(gr, orr, 3)
+            assert all(v == 0 for v in diffs.values()), (f, diffs)
+            assert np.array_equal(img.reshape(-1), oimg.reshape(-1))
+            # the specular / transmissive branches (bsdf pdf 1 at a hit) were taken
+            pdf = gr.readback(vrg.DBG_BSDF_PDF, 3)
+            hit = gr.readback(vrg.DBG_HIT, 3)
+            assert ((pdf == 1.0) & (hit[..., 0] != 0xFFFFFFFF)).sum() > 0
+        gr.close()
+        orr.close()
+        lt, _ = scene.get_tlas()  # light TL over atlas luminances
+        assert lt.tobytes() == OW.read_tl(0).tobytes()
+    finally:
+        gpu_ctx.set_atlas(None)
+        OW.close()

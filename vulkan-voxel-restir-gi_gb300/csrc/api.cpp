@@ -138,11 +138,66 @@ VRG_API vrg_status vrg_material_table_set(vrg_context *ctx, const vrg_material *
     }
     ctx->mats.assign(mats, mats + n);
     ctx->n_types = n / 6;
+    ctx->d_atlas.reset();  // an atlas belongs to one table: set it again after a new table
+    ctx->atlas_w = ctx->atlas_h = 0;
+    ctx->d_srgb = nullptr;
     DevBufPtr b;
     VRG_TRY(dev_alloc(ctx->stream, n * sizeof(vrg_material), b));
     VRG_CUDA_TRY(cudaMemcpyAsync(b->ptr, mats, n * sizeof(vrg_material), cudaMemcpyHostToDevice, ctx->stream));
     VRG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     ctx->d_mats = b;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_texture_atlas_set(vrg_context *ctx, const uint8_t *rgba8, uint32_t n_slots, uint32_t width,
+                                         uint32_t height) {
+    if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->pending.empty()) {
+        set_error("texture atlas changed with uploads pending");
+        return VRG_ERR_STATE;
+    }
+    if (!rgba8) {
+        ctx->d_atlas.reset();
+        ctx->atlas_w = ctx->atlas_h = 0;
+        ctx->d_srgb = nullptr;
+        return VRG_OK;
+    }
+    if (ctx->mats.empty() || n_slots != ctx->mats.size() || width == 0 || height == 0 || width > 4096 ||
+        height > 4096) {
+        set_error("atlas needs one slot per material-table entry (%zu) and 1..4096 texels a side", ctx->mats.size());
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    const size_t map = (size_t)width * height;
+    // get_texture_luminances (utils.rs:223-235): mean of r8+g8+b8 over the emissivity map
+    std::vector<vrg_material> mats = ctx->mats;
+    for (uint32_t t = 0; t < n_slots; t++) {
+        const uint8_t *e = rgba8 + ((size_t)t * 3 + 1) * map * 4;
+        float L = 0.0f;
+        for (size_t i = 0; i < map; i++) L += ((float)e[4 * i] + (float)e[4 * i + 1]) + (float)e[4 * i + 2];
+        mats[t].luminance = L / (float)(width * height);
+    }
+    // sRGB decode of the R8G8B8A8_SRGB maps (the EOTF, evaluated in double)
+    float lut[256];
+    for (int i = 0; i < 256; i++) {
+        const double c = (double)i / 255.0;
+        lut[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
+    const size_t atlas_bytes = (size_t)n_slots * 3 * map * 4, lut_off = (atlas_bytes + 255) & ~(size_t)255;
+    DevBufPtr ab, mb;
+    VRG_TRY(dev_alloc(ctx->stream, lut_off + sizeof(lut), ab));
+    VRG_TRY(dev_alloc(ctx->stream, mats.size() * sizeof(vrg_material), mb));
+    VRG_CUDA_TRY(cudaMemcpyAsync(ab->ptr, rgba8, atlas_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA_TRY(cudaMemcpyAsync((uint8_t *)ab->ptr + lut_off, lut, sizeof(lut), cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA_TRY(cudaMemcpyAsync(mb->ptr, mats.data(), mats.size() * sizeof(vrg_material), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    VRG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->mats = mats;
+    ctx->d_mats = mb;
+    ctx->d_atlas = ab;
+    ctx->atlas_w = width;
+    ctx->atlas_h = height;
+    ctx->d_srgb = (const float *)((const uint8_t *)ab->ptr + lut_off);
     return VRG_OK;
 }
 
@@ -952,7 +1007,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
     VRG_TRY(frame_setup(r, pr, out && out->radiance, a));
     if (a.cache && !scene->h_geo_tl.empty())
         nrc_set_bounds(r->cache, scene->h_geo_tl[0].min, scene->h_geo_tl[0].max);
-    a.v0.sc = scene->dev;
+    a.v0.sc = frame_scene(scene);
     a.v0.eye = f3{cam->eye[0], cam->eye[1], cam->eye[2]};
     a.v0.front = f3{cam->front[0], cam->front[1], cam->front[2]};
     a.v0.right = f3{cam->right[0], cam->right[1], cam->right[2]};
@@ -1046,7 +1101,7 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
         const vrg_view &w = views[v];
         ViewDev &d = hv[v];
         memset(&d, 0, sizeof(d));
-        d.sc = w.scene->dev;
+        d.sc = frame_scene(w.scene);
         d.eye = f3{w.camera.eye[0], w.camera.eye[1], w.camera.eye[2]};
         d.front = f3{w.camera.front[0], w.camera.front[1], w.camera.front[2]};
         d.right = f3{w.camera.right[0], w.camera.right[1], w.camera.right[2]};

@@ -829,4 +829,15 @@ vrg_status scene_commit_many(Scene *const *scs, uint32_t n) {
 
 vrg_status scene_commit(Scene *sc) { return scene_commit_many(&sc, 1); }
 
+DevScene frame_scene(const Scene *sc) {
+    DevScene D = sc->dev;
+    const Context *ctx = sc->ctx;
+    D.mats = ctx->d_mats ? (const vrg_material *)ctx->d_mats->ptr : nullptr;
+    D.atlas = ctx->d_atlas ? (const uchar4 *)ctx->d_atlas->ptr : nullptr;
+    D.srgb = ctx->d_srgb;
+    D.atlas_w = ctx->atlas_w;
+    D.atlas_h = ctx->atlas_h;
+    return D;
+}
+
 }  // namespace vrg

@@ -502,13 +502,37 @@ __global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs
                 const Frame fr = c_frames[2 * face + half];
                 n = fr.n;
                 const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
-                const vrg_material &m = V.sc.mats[6u * blk_id + (uint32_t)face];
+                const uint32_t slot = 6u * blk_id + (uint32_t)face;
                 const float b0 = (1.0f - b1) - b2;
                 new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
-                R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
-                const float alpha = __ldg(&m.alpha), metal = __ldg(&m.metallic);
                 const float ndd = -dot3(d, n);
-                E = f3{__ldg(&m.emission[0]) * ndd, __ldg(&m.emission[1]) * ndd, __ldg(&m.emission[2]) * ndd};
+                float alpha, metal;
+                if (V.sc.atlas) {
+                    // texture atlas: the three maps at the interpolated uv
+                    // (raytrace.rs:457-480), nearest texel clamped to the edge
+                    const uint32_t q0 = face_uv(face, half, 0), q1 = face_uv(face, half, 1),
+                                   q2 = face_uv(face, half, 2);
+                    const float u = (((float)(q0 & 1u) * b0) + ((float)(q1 & 1u) * b1)) + ((float)(q2 & 1u) * b2);
+                    const float v = (((float)(q0 >> 1) * b0) + ((float)(q1 >> 1) * b1)) + ((float)(q2 >> 1) * b2);
+                    const int aw = (int)V.sc.atlas_w, ah = (int)V.sc.atlas_h;
+                    const int ix = min(max((int)floorf(u * (float)aw), 0), aw - 1);
+                    const int iy = min(max((int)floorf(v * (float)ah), 0), ah - 1);
+                    const size_t texel = (size_t)slot * 3 * aw * ah + (size_t)iy * aw + ix, map = (size_t)aw * ah;
+                    const uchar4 x0 = __ldg(V.sc.atlas + texel), x1 = __ldg(V.sc.atlas + texel + map),
+                                 x2 = __ldg(V.sc.atlas + texel + 2 * map);
+                    const float *lin = V.sc.srgb;
+                    R = f3{__ldg(lin + x0.x), __ldg(lin + x0.y), __ldg(lin + x0.z)};
+                    alpha = (float)x0.w / 255.0f;
+                    E = f3{(1000.0f * __ldg(lin + x1.x)) * ndd, (1000.0f * __ldg(lin + x1.y)) * ndd,
+                           (1000.0f * __ldg(lin + x1.z)) * ndd};
+                    metal = __ldg(lin + x2.x);
+                } else {
+                    const vrg_material &m = V.sc.mats[slot];
+                    R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
+                    alpha = __ldg(&m.alpha);
+                    metal = __ldg(&m.metallic);
+                    E = f3{__ldg(&m.emission[0]) * ndd, __ldg(&m.emission[1]) * ndd, __ldg(&m.emission[2]) * ndd};
+                }
                 const float r0 = mm_rand(mm_combine(seed, 0));
                 if (r0 < metal) {
                     pdf = 1.0f;

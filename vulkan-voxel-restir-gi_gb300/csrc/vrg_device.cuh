@@ -115,6 +115,23 @@ __host__ __device__ __forceinline__ uint32_t face_corner(int f, int h, int j) {
     };
     return (uint32_t)((T[f] >> (9 * h + 3 * j)) & 7u);
 }
+// gen_mesh texture coordinates per (face, triangle, vertex) as u | v << 1
+// (chunk.rs:225-285: each face's four corners carry fixed uvs)
+__host__ __device__ __forceinline__ uint32_t face_uv(int f, int h, int j) {
+    // packed: 2 bits per vertex, 6 bits per triangle, 12 bits per face
+#define VRG_UV3(a, b, c) ((a) | (b) << 2 | (c) << 4)
+    constexpr uint32_t T[6] = {
+        VRG_UV3(2u, 1u, 3u) | VRG_UV3(0u, 1u, 2u) << 6,  // left:  (0,1) (1,0) (1,1) | (0,0) (1,0) (0,1)
+        VRG_UV3(0u, 3u, 2u) | VRG_UV3(0u, 1u, 3u) << 6,  // right: (0,0) (1,1) (0,1) | (0,0) (1,0) (1,1)
+        VRG_UV3(0u, 1u, 2u) | VRG_UV3(1u, 3u, 2u) << 6,  // down:  (0,0) (1,0) (0,1) | (1,0) (1,1) (0,1)
+        VRG_UV3(3u, 0u, 1u) | VRG_UV3(3u, 2u, 0u) << 6,  // up:    (1,1) (0,0) (1,0) | (1,1) (0,1) (0,0)
+        VRG_UV3(0u, 3u, 2u) | VRG_UV3(0u, 1u, 3u) << 6,  // back:  (0,0) (1,1) (0,1) | (0,0) (1,0) (1,1)
+        VRG_UV3(3u, 2u, 1u) | VRG_UV3(2u, 0u, 1u) << 6,  // front: (1,1) (0,1) (1,0) | (0,1) (0,0) (1,0)
+    };
+#undef VRG_UV3
+    return (T[f] >> (6 * h + 2 * j)) & 3u;
+}
+
 __host__ __device__ __forceinline__ f3 corner_pos(int bx, int by, int bz, uint32_t bits) {
     return f3{(float)(bx + (int)((bits >> 2) & 1u)), (float)(by + (int)((bits >> 1) & 1u)),
               (float)(bz + (int)(bits & 1u))};
@@ -221,6 +238,11 @@ struct DevScene {
     const InstDev *inst;
     const vrg_material *mats;
     uint32_t n_inst;
+    // texture atlas (NULL: constant slot colours): [slot][3 maps][h][w] RGBA8,
+    // and the sRGB-to-linear table of the 256 byte values
+    const uchar4 *atlas;
+    const float *srgb;
+    uint32_t atlas_w, atlas_h;
 };
 
 constexpr int EMPTY_ROOT = (int)0x80000000;

@@ -111,6 +111,9 @@ struct Context {
     cudaStream_t stream = nullptr;
     std::vector<vrg_material> mats;
     DevBufPtr d_mats;
+    DevBufPtr d_atlas;                   // texture atlas (RGBA8) + sRGB table, or empty
+    uint32_t atlas_w = 0, atlas_h = 0;
+    const float *d_srgb = nullptr;
     uint32_t n_types = 0;
     std::mutex mu;                       // guards pending + stream use from upload threads
     std::vector<Object *> pending;
@@ -140,6 +143,9 @@ struct Scene {
     std::vector<Object *> retired;        // released when the next commit completes
 };
 vrg_status scene_commit(Scene *sc);
+// the scene's device description with the context's current material table
+// and texture atlas
+DevScene frame_scene(const Scene *sc);
 // Commits every dirty scene of scs (one context); their top-level and lamp
 // trees are built by one SAH build each.
 vrg_status scene_commit_many(Scene *const *scs, uint32_t n);

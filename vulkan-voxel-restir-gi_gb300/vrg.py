@@ -31,6 +31,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_NOT_FOUND, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_UNSUPP
     ERR_OVERFLOW, ERR_STATE, ERR_NO_DEVICE = range(9)
 
 MODE_PARITY, MODE_CONFIG = 0, 1
+MAT_TRANSLUCENT = 1
 RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY, RENDER_GRAPH = 1, 2, 4, 8, 16
 NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS = range(5)
 (DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
@@ -117,6 +118,7 @@ SIGNATURES = [
     ("vrg_status_string", C.c_char_p, [C.c_int32]),
     ("vrg_last_error", C.c_char_p, []),
     ("vrg_material_table_set", C.c_int32, [_P, C.POINTER(Material), C.c_uint32]),
+    ("vrg_texture_atlas_set", C.c_int32, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("vrg_upload_chunk", C.c_int32, [_P, _P, C.POINTER(_P), C.POINTER(_P)]),
     ("vrg_flush_uploads", C.c_int32, [_P]),
     ("vrg_object_release", C.c_int32, [_P]),
@@ -276,6 +278,17 @@ class Context:
     def set_materials(self, mats, n=None):
         n = len(mats) if n is None else n
         check(self.lib.vrg_material_table_set(self.h, mats, n), "vrg_material_table_set")
+
+    def set_atlas(self, rgba):
+        """Texture atlas, (slots, 3, h, w, 4) uint8 sRGB maps per material slot
+        (reflectivity+alpha, emissivity, metallicity); None removes it."""
+        if rgba is None:
+            check(self.lib.vrg_texture_atlas_set(self.h, None, 0, 0, 0), "vrg_texture_atlas_set")
+            return
+        rgba = np.ascontiguousarray(rgba, np.uint8)
+        n, maps, h, w, c = rgba.shape
+        assert maps == 3 and c == 4
+        check(self.lib.vrg_texture_atlas_set(self.h, _ptr(rgba), n, w, h), "vrg_texture_atlas_set")
 
     def flush(self):
         check(self.lib.vrg_flush_uploads(self.h), "vrg_flush_uploads")
