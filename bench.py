@@ -401,7 +401,10 @@ def run_large(args, d):
         "ground_truth": {"spp": n_gt, "bounces": 8, "accumulation": "fp64 on the GPU", "seconds": round(gt_s, 1)},
         "equal_time": {"plain_frames": k, "relmse_plain": round(rel_plain_k, 5),
                        "relmse_restir_cache_1spp": out["restir_cache"]["relmse_1spp"],
-                       "gain": round(rel_plain_k / max(out["restir_cache"]["relmse_1spp"], 1e-12), 3)},
+                       "gain": round(rel_plain_k / max(out["restir_cache"]["relmse_1spp"], 1e-12), 3),
+                       "gain_lower_bound": round(out["plain"]["relmse_1spp"] / max(
+                           1.0, out["restir_cache"]["ms_per_frame"] / out["plain"]["ms_per_frame"]) /
+                           max(out["restir_cache"]["relmse_1spp"], 1e-12), 3)},
         "hbm_peak_gbs": hbm_peak,
     }
     cache.close()

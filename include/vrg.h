@@ -283,7 +283,10 @@ enum {
     VRG_DBG_ORIGIN = 0, VRG_DBG_DIRECTION, VRG_DBG_NORMAL, VRG_DBG_EMISSIVITY,
     VRG_DBG_REFLECTIVITY, VRG_DBG_MIS, VRG_DBG_BSDF_PDF, VRG_DBG_NEE_PDF,
     VRG_DBG_RADIANCE, VRG_DBG_Q, VRG_DBG_HIT, VRG_DBG_TEMPORAL, VRG_DBG_SPATIAL,
-    VRG_DBG_FINAL, VRG_DBG_COUNT
+    VRG_DBG_FINAL,
+    VRG_DBG_CACHE_TARGET,  /* (1, 4): the radiance cache's training target per pixel (rgb, 0) as
+                              left by the last cache frame (no capture needed) */
+    VRG_DBG_COUNT
 };
 VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes);
 

@@ -59,7 +59,7 @@ def test_cache_frame_fork_matches_single_stream(gpu_ctx):
     scene, objs, lo, hi = _scene(gpu_ctx, seed=9)
     W, H = 96, 64
     cam = vrg.orbit_camera(2, 2, 7, 64, W, H)
-    outs, weights = [], []
+    outs, weights, targets = [], [], []
     for flags in (0, vrg.RENDER_CAPTURE):
         r = vrg.Renderer(gpu_ctx, W, H, 8)
         cache = vrg.RadianceCache(gpu_ctx, lo, hi, seed=3)
@@ -70,11 +70,15 @@ def test_cache_frame_fork_matches_single_stream(gpu_ctx):
         _, rad = r.render_params(scene, cam, p, want_image=False, want_radiance=True)
         assert r.last_stats.error_flags == 0
         outs.append(rad.copy())
+        targets.append(r.readback(vrg.DBG_CACHE_TARGET, 0))
         weights.append(cache.read(vrg.NRC_WEIGHTS).copy())
         r.set_cache(None)
         cache.close()
         r.close()
     assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+    # the training paths' targets, forked against single-stream, bit for bit
+    assert np.array_equal(targets[0].view(np.uint32), targets[1].view(np.uint32))
+    assert np.count_nonzero(targets[0][:, :3]) > 0
     # Adam's first step moves each weight by about +-lr along its gradient's
     # sign, so a gradient at rounding level may flip: allow a handful
     close = np.isclose(weights[0], weights[1], rtol=1e-3, atol=1e-6)

@@ -1288,6 +1288,17 @@ VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, cons
 
 VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes) {
     if (!r || !dst || what >= VRG_DBG_COUNT) return VRG_ERR_INVALID_ARGUMENT;
+    if (what == VRG_DBG_CACHE_TARGET) {
+        const size_t n = (size_t)r->P * 16;
+        if (!r->target) {
+            set_error("no cache frame rendered");
+            return VRG_ERR_STATE;
+        }
+        if (bytes < n) return VRG_ERR_INVALID_ARGUMENT;
+        VRG_CUDA_TRY(cudaMemcpyAsync(dst, r->target, n, cudaMemcpyDeviceToHost, r->ctx->stream));
+        VRG_CUDA_TRY(cudaStreamSynchronize(r->ctx->stream));
+        return VRG_OK;
+    }
     if (!r->captured) {
         set_error("last frame was not rendered with VRG_RENDER_CAPTURE");
         return VRG_ERR_STATE;

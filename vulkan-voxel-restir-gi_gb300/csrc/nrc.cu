@@ -216,7 +216,8 @@ __device__ __forceinline__ void store_a(__nv_bfloat16 *dst, const uint32_t a[4][
     }
 }
 
-constexpr int NRC_WARPS = 4;   // training kernel
+constexpr int NRC_WARPS = 4;   // training kernel (more warps per SM only add contention on the
+                               // hash-grid gradient atomics of the coarse levels)
 constexpr int NRC_IWARPS = 12; // inference kernel: 12 warps share one copy of the weights (2 CTAs per SM)
 
 struct InferArgs {
@@ -473,8 +474,23 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
     if (lane == 0 && loss_acc != 0.0f) atomicAdd(a.loss, loss_acc);
 }
 
-// dW_l[n][k] += sum_b dZ_l[b][n] * H_l[b][k]: split-K over the batch, one warp per
-// 16-row block of n, atomics into the fp32 gradient
+// 8x8 b16 matrices from shared memory, transposed (ldmatrix .trans): thread t
+// gives the address of row (t & 7) of matrix t >> 3 and receives
+// {M[2q][g], M[2q+1][g]} of each of the four matrices
+__device__ __forceinline__ void ldsm_x4_t(const __nv_bfloat16 *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
+                                          uint32_t &r3) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
+constexpr int DW_CHUNK = 64;  // samples staged per step
+
+// dW_l[n][k] += sum_b dZ_l[b][n] * H_l[b][k]: split-K over the batch (a CTA per
+// rows_per_cta samples of one layer, staged DW_CHUNK at a time for all its
+// warps), one warp per 16-row block of n, atomics into the fp32 gradient
+
 __global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __nv_bfloat16 *dZ, size_t n_pad,
                                                 uint32_t n_cap, const uint32_t *n_dev, float *dW,
                                                 uint32_t rows_per_cta) {
@@ -482,20 +498,25 @@ __global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __
     const uint32_t n = n_dev ? min(*n_dev, n_cap) : n_cap;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
     const int mdim = out_dim(l);
-    if (w * 16 >= mdim) return;
-    __shared__ __align__(16) __nv_bfloat16 sz[4][16][NRC_STRIDE];
-    __shared__ __align__(16) __nv_bfloat16 sh[4][16][NRC_STRIDE];
+    const bool active = w * 16 < mdim;  // the 16-wide output layer uses warp 0 only
+    // dZ and H of DW_CHUNK samples, staged once per CTA (row stride 72 bf16:
+    // 16-byte aligned rows for ldmatrix)
+    __shared__ __align__(16) __nv_bfloat16 sz[DW_CHUNK][NRC_STRIDE];
+    __shared__ __align__(16) __nv_bfloat16 sh[DW_CHUNK][NRC_STRIDE];
     const __nv_bfloat16 *Hl = H + (size_t)l * n_pad * NRC_W;
     const __nv_bfloat16 *Zl = dZ + (size_t)l * n_pad * NRC_W;
     float acc[8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
     const size_t r0 = (size_t)blockIdx.x * rows_per_cta;
-    if (r0 >= n) return;
+    if (r0 >= n) return;  // uniform over the CTA
     const size_t r1 = min((size_t)n, r0 + rows_per_cta);
-    for (size_t s0 = r0; s0 < r1; s0 += 16) {
-        // stage 16 samples of dZ and H (each warp its own copy: no block barrier)
-        for (int e = lane; e < 16 * 8; e += 32) {
+    const int m0 = w * 16;
+    // per-thread ldmatrix row / column selectors (see ldsm_x4_t)
+    const int a_row = (lane & 7) + ((lane >> 4) << 3), a_col = ((lane >> 3) & 1) * 8;
+    const int b_row = (lane & 7) + (((lane >> 3) & 1) << 3), b_col = (lane >> 4) * 8;
+    for (size_t s0 = r0; s0 < r1; s0 += DW_CHUNK) {
+        for (int e = threadIdx.x; e < DW_CHUNK * 8; e += blockDim.x) {
             const int r = e >> 3, cc = (e & 7) * 8;
             const size_t row = s0 + r;
             uint4 vz = make_uint4(0, 0, 0, 0), vh = make_uint4(0, 0, 0, 0);
@@ -503,28 +524,28 @@ __global__ void __launch_bounds__(128) k_nrc_dw(const __nv_bfloat16 *H, const __
                 vz = *reinterpret_cast<const uint4 *>(Zl + row * NRC_W + cc);
                 vh = *reinterpret_cast<const uint4 *>(Hl + row * NRC_W + cc);
             }
-            *reinterpret_cast<uint4 *>(&sz[w][r][cc]) = vz;
-            *reinterpret_cast<uint4 *>(&sh[w][r][cc]) = vh;
+            *reinterpret_cast<uint4 *>(&sz[r][cc]) = vz;
+            *reinterpret_cast<uint4 *>(&sh[r][cc]) = vh;
         }
-        __syncwarp();
-        // A[m = n-index][k = sample] = dZ[sample][n]; B[k = sample][col = k-index] = H[sample][k]
-        uint32_t af[4];
-        const int m0 = w * 16;
-        auto lo_hi = [](__nv_bfloat16 lo, __nv_bfloat16 hi) {
-            return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-        };
-        af[0] = lo_hi(sz[w][2 * q][m0 + g], sz[w][2 * q + 1][m0 + g]);
-        af[1] = lo_hi(sz[w][2 * q][m0 + g + 8], sz[w][2 * q + 1][m0 + g + 8]);
-        af[2] = lo_hi(sz[w][2 * q + 8][m0 + g], sz[w][2 * q + 9][m0 + g]);
-        af[3] = lo_hi(sz[w][2 * q + 8][m0 + g + 8], sz[w][2 * q + 9][m0 + g + 8]);
+        __syncthreads();
+        if (active) {
+            // A[m = output][k = sample] = dZ[sample][m0 + m]; B[k = sample][n = input] = H[sample][n]
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const uint32_t b0 = lo_hi(sh[w][2 * q][nt * 8 + g], sh[w][2 * q + 1][nt * 8 + g]);
-            const uint32_t b1 = lo_hi(sh[w][2 * q + 8][nt * 8 + g], sh[w][2 * q + 9][nt * 8 + g]);
-            mma16816(acc[nt], af, b0, b1);
+            for (int kk = 0; kk < DW_CHUNK / 16; kk++) {
+                uint32_t af[4];
+                ldsm_x4_t(&sz[kk * 16 + a_row][m0 + a_col], af[0], af[1], af[2], af[3]);
+#pragma unroll
+                for (int ntp = 0; ntp < 4; ntp++) {
+                    uint32_t b00, b01, b10, b11;
+                    ldsm_x4_t(&sh[kk * 16 + b_row][ntp * 16 + b_col], b00, b01, b10, b11);
+                    mma16816(acc[2 * ntp], af, b00, b01);
+                    mma16816(acc[2 * ntp + 1], af, b10, b11);
+                }
+            }
         }
-        __syncwarp();
+        __syncthreads();
     }
+    if (!active) return;
     float *dWl = dW + m_off(l);
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {

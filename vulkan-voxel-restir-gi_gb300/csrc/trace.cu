@@ -434,6 +434,121 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     }
 }
 
+// Shading of one path vertex (raytrace.rs:405-577): the hit's material
+// (constant slot colours or the texture atlas), emission, and the sampled
+// continuation (mirror, transmission, or Lambertian with light-BVH NEE
+// sampling).
+struct ShadeOut {
+    f3 n, E, R, new_o, new_d;
+    float mis, pdf;
+    int face, half;
+    int4 rc;
+};
+
+__device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_type, uint32_t b, uint32_t seed, f3 o,
+                                             f3 d, int4 hv, ShadeOut &out) {
+    f3 n, E, R, new_o, new_d;
+    float mis = 0.0f, pdf = 1.0f;
+    int face = 0, half = 0;
+    int4 rc = make_int4(0, 0, 0, 0);
+    if (hv.x < 0) {
+        new_o = add3(o, scl3(d, 5000.0f));
+        new_d = f3{0.0f, 0.0f, 0.0f};
+        n = f3{0.0f, 0.0f, 0.0f};
+        const float sky = (dot3(d, f3{0.0f, 1.0f, 0.0f}) > 0.9f) ? 50.0f : 0.0f;
+        E = f3{sky, sky, sky};
+        R = f3{0.0f, 0.0f, 0.0f};
+    } else {
+        rc = __ldg(S.geo_rec + hv.x);
+        face = hv.y & 7;
+        half = (hv.y >> 3) & 1;
+        const float b1 = __int_as_float(hv.z), b2 = __int_as_float(hv.w);
+        const int wx = rec_wx(rc), wy = rec_wy(rc), wz = rec_wz(rc);
+        const f3 t0 = corner_pos(wx, wy, wz, face_corner(face, half, 0));
+        const f3 t1 = corner_pos(wx, wy, wz, face_corner(face, half, 1));
+        const f3 t2 = corner_pos(wx, wy, wz, face_corner(face, half, 2));
+        const Frame fr = c_frames[2 * face + half];
+        n = fr.n;
+        const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
+        const uint32_t slot = 6u * blk_id + (uint32_t)face;
+        const float b0 = (1.0f - b1) - b2;
+        new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
+        const float ndd = -dot3(d, n);
+        float alpha, metal;
+        if (S.atlas) {
+            // texture atlas: the three maps at the interpolated uv
+            // (raytrace.rs:457-480), nearest texel clamped to the edge
+            const uint32_t q0 = face_uv(face, half, 0), q1 = face_uv(face, half, 1),
+                           q2 = face_uv(face, half, 2);
+            const float u = (((float)(q0 & 1u) * b0) + ((float)(q1 & 1u) * b1)) + ((float)(q2 & 1u) * b2);
+            const float v = (((float)(q0 >> 1) * b0) + ((float)(q1 >> 1) * b1)) + ((float)(q2 >> 1) * b2);
+            const int aw = (int)S.atlas_w, ah = (int)S.atlas_h;
+            const int ix = min(max((int)floorf(u * (float)aw), 0), aw - 1);
+            const int iy = min(max((int)floorf(v * (float)ah), 0), ah - 1);
+            const size_t texel = (size_t)slot * 3 * aw * ah + (size_t)iy * aw + ix, map = (size_t)aw * ah;
+            const uchar4 x0 = __ldg(S.atlas + texel), x1 = __ldg(S.atlas + texel + map),
+                         x2 = __ldg(S.atlas + texel + 2 * map);
+            const float *lin = S.srgb;
+            R = f3{__ldg(lin + x0.x), __ldg(lin + x0.y), __ldg(lin + x0.z)};
+            alpha = (float)x0.w / 255.0f;
+            E = f3{(1000.0f * __ldg(lin + x1.x)) * ndd, (1000.0f * __ldg(lin + x1.y)) * ndd,
+                   (1000.0f * __ldg(lin + x1.z)) * ndd};
+            metal = __ldg(lin + x2.x);
+        } else {
+            const vrg_material &m = S.mats[slot];
+            R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
+            alpha = __ldg(&m.alpha);
+            metal = __ldg(&m.metallic);
+            E = f3{__ldg(&m.emission[0]) * ndd, __ldg(&m.emission[1]) * ndd, __ldg(&m.emission[2]) * ndd};
+        }
+        const float r0 = mm_rand(mm_combine(seed, 0));
+        if (r0 < metal) {
+            pdf = 1.0f;
+            new_d = sub3(d, lscl3(2.0f * dot3(n, d), n));
+        } else if (r0 < metal + (1.0f - alpha)) {
+            new_d = d;
+            R = f3{1.0f, 1.0f, 1.0f};
+            pdf = 1.0f;
+        } else {
+            new_o = add3(new_o, lscl3(EPS_TRACE * 1.5f, n));
+            R = f3{R.x / PI_F, R.y / PI_F, R.z / PI_F};
+            Descent res;
+            res.success = false;
+            res.importance = 0.0f;
+            if (nee_type == 1 || (nee_type == 2 && b == 1))
+                res = light_descent(S, new_o, n, mm_combine(seed, 2));
+            if (res.success && res.importance > 0.0f) mis = 0.3f;
+            const float mis_rand = mm_rand(mm_combine(seed, 3));
+            float ux = mm_rand(mm_combine(seed, 4)), uy = mm_rand(mm_combine(seed, 5));
+            if (mis_rand < mis) {
+                f3 lt[3];
+                light_tri_world(S, res.inst, res.leaf, lt);
+                if (ux + uy > 1.0f) { ux = 1.0f - ux; uy = 1.0f - uy; }  // triangleSample
+                const float bx = (1.0f - ux) - uy;
+                const f3 sp = add3(add3(lscl3(bx, lt[0]), lscl3(ux, lt[1])), lscl3(uy, lt[2]));
+                new_d = norm3(sub3(sp, new_o));
+            } else {
+                float s, c;
+                sincos_turns(ux, &s, &c);
+                const float vv = sqrtf(fmaxf(0.0f, 1.0f - uy * uy));
+                const f3 hs = f3{vv * c, uy, vv * s};
+                new_d = norm3(add3(add3(lscl3(hs.x, fr.t), lscl3(hs.y, fr.n)), lscl3(hs.z, fr.b)));
+            }
+            pdf = dot3(new_d, n) / PI_F;
+        }
+    }
+    out.n = n;
+    out.E = E;
+    out.R = R;
+    out.new_o = new_o;
+    out.new_d = new_d;
+    out.mis = mis;
+    out.pdf = pdf;
+    out.face = face;
+    out.half = half;
+    out.rc = rc;
+}
+
 // ---------------------------------------------------------------------------
 // k_shade: shading of the hit, light-BVH descent and direction sampling
 // (raytrace.rs:405-577).  Rays whose light pdf is needed are queued for
@@ -479,98 +594,19 @@ __global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs
             }
             const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
             const int4 hv = a.hits[p];
-            f3 n, E, R;
-            float mis = 0.0f;
-            int half = 0;
-            int4 rc = make_int4(0, 0, 0, 0);
-            if (hv.x < 0) {
-                new_o = add3(o, scl3(d, 5000.0f));
-                new_d = f3{0.0f, 0.0f, 0.0f};
-                n = f3{0.0f, 0.0f, 0.0f};
-                const float sky = (dot3(d, f3{0.0f, 1.0f, 0.0f}) > 0.9f) ? 50.0f : 0.0f;
-                E = f3{sky, sky, sky};
-                R = f3{0.0f, 0.0f, 0.0f};
-            } else {
-                rc = __ldg(V.sc.geo_rec + hv.x);
-                face = hv.y & 7;
-                half = (hv.y >> 3) & 1;
-                const float b1 = __int_as_float(hv.z), b2 = __int_as_float(hv.w);
-                const int wx = rec_wx(rc), wy = rec_wy(rc), wz = rec_wz(rc);
-                const f3 t0 = corner_pos(wx, wy, wz, face_corner(face, half, 0));
-                const f3 t1 = corner_pos(wx, wy, wz, face_corner(face, half, 1));
-                const f3 t2 = corner_pos(wx, wy, wz, face_corner(face, half, 2));
-                const Frame fr = c_frames[2 * face + half];
-                n = fr.n;
-                const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
-                const uint32_t slot = 6u * blk_id + (uint32_t)face;
-                const float b0 = (1.0f - b1) - b2;
-                new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
-                const float ndd = -dot3(d, n);
-                float alpha, metal;
-                if (V.sc.atlas) {
-                    // texture atlas: the three maps at the interpolated uv
-                    // (raytrace.rs:457-480), nearest texel clamped to the edge
-                    const uint32_t q0 = face_uv(face, half, 0), q1 = face_uv(face, half, 1),
-                                   q2 = face_uv(face, half, 2);
-                    const float u = (((float)(q0 & 1u) * b0) + ((float)(q1 & 1u) * b1)) + ((float)(q2 & 1u) * b2);
-                    const float v = (((float)(q0 >> 1) * b0) + ((float)(q1 >> 1) * b1)) + ((float)(q2 >> 1) * b2);
-                    const int aw = (int)V.sc.atlas_w, ah = (int)V.sc.atlas_h;
-                    const int ix = min(max((int)floorf(u * (float)aw), 0), aw - 1);
-                    const int iy = min(max((int)floorf(v * (float)ah), 0), ah - 1);
-                    const size_t texel = (size_t)slot * 3 * aw * ah + (size_t)iy * aw + ix, map = (size_t)aw * ah;
-                    const uchar4 x0 = __ldg(V.sc.atlas + texel), x1 = __ldg(V.sc.atlas + texel + map),
-                                 x2 = __ldg(V.sc.atlas + texel + 2 * map);
-                    const float *lin = V.sc.srgb;
-                    R = f3{__ldg(lin + x0.x), __ldg(lin + x0.y), __ldg(lin + x0.z)};
-                    alpha = (float)x0.w / 255.0f;
-                    E = f3{(1000.0f * __ldg(lin + x1.x)) * ndd, (1000.0f * __ldg(lin + x1.y)) * ndd,
-                           (1000.0f * __ldg(lin + x1.z)) * ndd};
-                    metal = __ldg(lin + x2.x);
-                } else {
-                    const vrg_material &m = V.sc.mats[slot];
-                    R = f3{__ldg(&m.reflectivity[0]), __ldg(&m.reflectivity[1]), __ldg(&m.reflectivity[2])};
-                    alpha = __ldg(&m.alpha);
-                    metal = __ldg(&m.metallic);
-                    E = f3{__ldg(&m.emission[0]) * ndd, __ldg(&m.emission[1]) * ndd, __ldg(&m.emission[2]) * ndd};
-                }
-                const float r0 = mm_rand(mm_combine(seed, 0));
-                if (r0 < metal) {
-                    pdf = 1.0f;
-                    new_d = sub3(d, lscl3(2.0f * dot3(n, d), n));
-                } else if (r0 < metal + (1.0f - alpha)) {
-                    new_d = d;
-                    R = f3{1.0f, 1.0f, 1.0f};
-                    pdf = 1.0f;
-                } else {
-                    new_o = add3(new_o, lscl3(EPS_TRACE * 1.5f, n));
-                    R = f3{R.x / PI_F, R.y / PI_F, R.z / PI_F};
-                    Descent res;
-                    res.success = false;
-                    res.importance = 0.0f;
-                    if (a.nee_type == 1 || (a.nee_type == 2 && b == 1))
-                        res = light_descent(V.sc, new_o, n, mm_combine(seed, 2));
-                    if (res.success && res.importance > 0.0f) mis = 0.3f;
-                    const float mis_rand = mm_rand(mm_combine(seed, 3));
-                    float ux = mm_rand(mm_combine(seed, 4)), uy = mm_rand(mm_combine(seed, 5));
-                    if (mis_rand < mis) {
-                        f3 lt[3];
-                        light_tri_world(V.sc, res.inst, res.leaf, lt);
-                        if (ux + uy > 1.0f) { ux = 1.0f - ux; uy = 1.0f - uy; }  // triangleSample
-                        const float bx = (1.0f - ux) - uy;
-                        const f3 sp = add3(add3(lscl3(bx, lt[0]), lscl3(ux, lt[1])), lscl3(uy, lt[2]));
-                        new_d = norm3(sub3(sp, new_o));
-                    } else {
-                        float s, c;
-                        sincos_turns(ux, &s, &c);
-                        const float vv = sqrtf(fmaxf(0.0f, 1.0f - uy * uy));
-                        const f3 hs = f3{vv * c, uy, vv * s};
-                        new_d = norm3(add3(add3(lscl3(hs.x, fr.t), lscl3(hs.y, fr.n)), lscl3(hs.z, fr.b)));
-                    }
-                    pdf = dot3(new_d, n) / PI_F;
-                }
-                // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
-                anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
-            }
+            ShadeOut so;
+            shade_vertex(V.sc, a.nee_type, b, seed, o, d, hv, so);
+            const f3 n = so.n, E = so.E;
+            f3 R = so.R;
+            const float mis = so.mis;
+            const int half = so.half;
+            const int4 rc = so.rc;
+            new_o = so.new_o;
+            new_d = so.new_d;
+            pdf = so.pdf;
+            face = so.face;
+            // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
+            if (hv.x >= 0) anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
             // radiance cache: the vertex where rendered paths end into the cache
             // (every pixel's flag is cleared at bounce 0, so a path that ends
             // before the query vertex never reads a stale one)

@@ -6,9 +6,16 @@ per frame with no error metric).
 
 relMSE(x, gt) = mean over pixels and channels of (x - gt)^2 / (gt^2 + 0.01).
 
-Equal time: a method whose frame takes t_m ms is compared with the plain
-tracer accumulated over ceil(t_m / t_plain) frames, so that the plain tracer
-always gets at least the method's device time.
+Equal time, two ways:
+  * measured: the method's 1-spp frame against the plain tracer accumulated
+    over ceil(t_m / t_plain) frames (the plain tracer gets at least the
+    method's device time, up to one frame more);
+  * lower bound: the mean of N independent plain frames has relMSE
+    b + v/N >= (b + v)/N = relMSE_1spp / N (b: its bias against the ground
+    truth, v: its one-frame variance), so relMSE_1spp / N_eq with
+    N_eq = max(1, t_m / t_plain) bounds the plain tracer's error at exactly
+    the method's time from below, and the gain computed with it bounds the
+    equal-time gain from below.
 """
 import math
 
@@ -115,9 +122,12 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
         if k not in plain_acc:
             acc_img, _, _ = run_method(renderer, scene, cam, "plain", k, seed0=5000)
             plain_acc[k] = relmse(acc_img, gt)
+        n_eq = max(1.0, t_m / t_plain) if t_plain > 0 else 1.0
+        rel_m = max(out[method]["relmse_1spp"], 1e-12)
         eq[method] = {"plain_frames": k, "plain_time_ratio": round(k * t_plain / t_m, 3),
                       "relmse_plain": round(plain_acc[k], 6), "relmse_method_1spp": out[method]["relmse_1spp"],
-                      "gain": round(plain_acc[k] / max(out[method]["relmse_1spp"], 1e-12), 3)}
+                      "gain": round(plain_acc[k] / rel_m, 3),
+                      "gain_lower_bound": round(out["plain"]["relmse_1spp"] / n_eq / rel_m, 3)}
     out["equal_time"] = eq
     cache.close()
     return out

@@ -35,7 +35,7 @@ MAT_TRANSLUCENT = 1
 RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY, RENDER_GRAPH = 1, 2, 4, 8, 16
 NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS = range(5)
 (DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
- DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL) = range(14)
+ DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL, DBG_CACHE_TARGET) = range(15)
 
 
 class BvhNode(C.Structure):
@@ -513,7 +513,8 @@ class Renderer:
         shapes = {DBG_ORIGIN: (nb + 1, P, 3), DBG_DIRECTION: (nb + 1, P, 3), DBG_NORMAL: (nb, P, 3),
                   DBG_EMISSIVITY: (nb, P, 3), DBG_REFLECTIVITY: (nb, P, 3), DBG_MIS: (nb, P),
                   DBG_BSDF_PDF: (nb, P), DBG_NEE_PDF: (nb, P), DBG_RADIANCE: (nb, P, 3), DBG_Q: (nb, P),
-                  DBG_HIT: (nb, P, 4), DBG_TEMPORAL: (P, 20), DBG_SPATIAL: (P, 20), DBG_FINAL: (P, 3)}
+                  DBG_HIT: (nb, P, 4), DBG_TEMPORAL: (P, 20), DBG_SPATIAL: (P, 20), DBG_FINAL: (P, 3),
+                  DBG_CACHE_TARGET: (P, 4)}
         dt = np.uint32 if what == DBG_HIT else np.float32
         a = np.zeros(shapes[what], dtype=dt)
         check(self.ctx.lib.vrg_debug_readback(self.h, what, _ptr(a), a.nbytes), "vrg_debug_readback")
