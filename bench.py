@@ -525,10 +525,16 @@ def run_ours(args, d):
     total_s_max = d.max(total_s)
     rays_all = d.sum(rays)
     value = rays_all / total_s_max / 1e6
-    # end to end through the public API with host buffers
-    img = np.empty(W * H * 4, np.uint8)
-    out_host = vrg.FrameOutput(img.ctypes.data, None, 1, 0)
-    # pin the host image buffer for the device->host copy
+    # end to end through the public API: each frame copied back into a pinned
+    # host buffer (page-locked, so the device->host copy runs at link speed)
+    try:
+        import torch
+        host_img = torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True)
+        img_ptr = host_img.data_ptr()
+    except Exception:  # no pinned allocator: pageable memory
+        host_img = np.empty(W * H * 4, np.uint8)
+        img_ptr = host_img.ctypes.data
+    out_host = vrg.FrameOutput(img_ptr, None, 1, 0)
     d.barrier()
     t0 = time.perf_counter()
     e2e_rays = 0

@@ -126,6 +126,7 @@ __device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 
                            __nv_bfloat16 *row) {
     const f3 p = normalize_pos(P, pos);
     const size_t T = (size_t)1 << P.log2_t;
+    uint32_t *row32 = reinterpret_cast<uint32_t *>(row);
     // unrolled so that the gathers of several levels are in flight together
 #pragma unroll 4
     for (int l = 0; l < P.levels; l++) {
@@ -138,38 +139,59 @@ __device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 
             f0 += c.w[k] * v.x;
             f1 += c.w[k] * v.y;
         }
-        row[2 * l] = __float2bfloat16_rn(f0);
-        row[2 * l + 1] = __float2bfloat16_rn(f1);
+        // one 32-bit store per bf16 pair (rows of 144 bytes: 2-byte stores
+        // of a warp's 32 rows would meet 8-way bank conflicts)
+        row32[l] = pack_bf16(f0, f1);
     }
     float a, b;
     oct_encode(nrm, a, b);
-    row[2 * P.levels] = __float2bfloat16_rn(a);
-    row[2 * P.levels + 1] = __float2bfloat16_rn(b);
+    row32[P.levels] = pack_bf16(a, b);
     oct_encode(dir, a, b);
-    row[2 * P.levels + 2] = __float2bfloat16_rn(a);
-    row[2 * P.levels + 3] = __float2bfloat16_rn(b);
-    for (int k = 2 * P.levels + 4; k < NRC_W; k++) row[k] = __float2bfloat16_rn(0.0f);
+    row32[P.levels + 1] = pack_bf16(a, b);
+    for (int k = P.levels + 2; k < NRC_W / 2; k++) row32[k] = 0u;
 }
 
-// A fragments of a 16-row tile held row-major in shared memory
+// four 8x8 b16 matrices from shared memory (ldmatrix): thread t gives the
+// address of row (t & 7) of matrix t >> 3 and receives {M[g][2q], M[g][2q+1]}
+// of each — the mma.m16n8k16 A / B fragment layout
+__device__ __forceinline__ void ldsm_x4(const __nv_bfloat16 *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
+                                        uint32_t &r3) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
+// A fragments of a 16-row tile held row-major in shared memory (rows of
+// NRC_STRIDE bf16, 16-byte aligned): per 16-column chunk kc the matrices
+// (rows 0-7, kc), (rows 8-15, kc), (rows 0-7, kc + 8), (rows 8-15, kc + 8)
 __device__ __forceinline__ void load_a(const __nv_bfloat16 *tile, int g, int q, uint32_t a[4][4]) {
+    const int lane = (g << 2) | q;
+    const __nv_bfloat16 *row = tile + ((lane & 7) + ((lane >> 3) & 1) * 8) * NRC_STRIDE + (lane >> 4) * 8;
 #pragma unroll
-    for (int kc = 0; kc < 4; kc++) {
-        a[kc][0] = ld32(tile + g * NRC_STRIDE + kc * 16 + 2 * q);
-        a[kc][1] = ld32(tile + (g + 8) * NRC_STRIDE + kc * 16 + 2 * q);
-        a[kc][2] = ld32(tile + g * NRC_STRIDE + kc * 16 + 8 + 2 * q);
-        a[kc][3] = ld32(tile + (g + 8) * NRC_STRIDE + kc * 16 + 8 + 2 * q);
-    }
+    for (int kc = 0; kc < 4; kc++) ldsm_x4(row + kc * 16, a[kc][0], a[kc][1], a[kc][2], a[kc][3]);
+}
+
+// B fragments of n-tile nt of a row-major [out][in] weight block for the
+// chunk pair (kc, kc + 1) = (2 kp, 2 kp + 1): b0, b1 of each
+__device__ __forceinline__ void load_b2(const __nv_bfloat16 *W, int nt, int kp, int lane, uint32_t &b00, uint32_t &b01,
+                                        uint32_t &b10, uint32_t &b11) {
+    ldsm_x4(W + (nt * 8 + (lane & 7)) * NRC_STRIDE + kp * 32 + (lane >> 3) * 8, b00, b01, b10, b11);
 }
 
 // one 64 -> 64 layer: C = A * W^T
 __device__ __forceinline__ void layer64(const __nv_bfloat16 *W, const uint32_t a[4][4], int g, int q, float c[8][4]) {
+    const int lane = (g << 2) | q;
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {
         c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-        const __nv_bfloat16 *wr = W + (nt * 8 + g) * NRC_STRIDE;
 #pragma unroll
-        for (int kc = 0; kc < 4; kc++) mma16816(c[nt], a[kc], ld32(wr + kc * 16 + 2 * q), ld32(wr + kc * 16 + 8 + 2 * q));
+        for (int kp = 0; kp < 2; kp++) {
+            uint32_t b00, b01, b10, b11;
+            load_b2(W, nt, kp, lane, b00, b01, b10, b11);
+            mma16816(c[nt], a[2 * kp], b00, b01);
+            mma16816(c[nt], a[2 * kp + 1], b10, b11);
+        }
     }
 }
 
@@ -196,12 +218,17 @@ __device__ __forceinline__ uint32_t relu_pack(float c[8][4], uint32_t a[4][4]) {
 
 // output layer (16 padded outputs): y[2][4] fragments
 __device__ __forceinline__ void layer_out(const __nv_bfloat16 *W5, const uint32_t a[4][4], int g, int q, float y[2][4]) {
+    const int lane = (g << 2) | q;
 #pragma unroll
     for (int nt = 0; nt < 2; nt++) {
         y[nt][0] = y[nt][1] = y[nt][2] = y[nt][3] = 0.0f;
-        const __nv_bfloat16 *wr = W5 + (nt * 8 + g) * NRC_STRIDE;
 #pragma unroll
-        for (int kc = 0; kc < 4; kc++) mma16816(y[nt], a[kc], ld32(wr + kc * 16 + 2 * q), ld32(wr + kc * 16 + 8 + 2 * q));
+        for (int kp = 0; kp < 2; kp++) {
+            uint32_t b00, b01, b10, b11;
+            load_b2(W5, nt, kp, lane, b00, b01, b10, b11);
+            mma16816(y[nt], a[2 * kp], b00, b01);
+            mma16816(y[nt], a[2 * kp + 1], b10, b11);
+        }
     }
 }
 
@@ -243,7 +270,7 @@ __device__ __forceinline__ f3 face_normal(int f) {
 }
 
 // inference: per warp 32 queries per iteration (2 tiles of 16)
-__global__ void __launch_bounds__(NRC_IWARPS * 32) k_nrc_infer(InferArgs a) {
+__global__ void __launch_bounds__(NRC_IWARPS * 32, 2) k_nrc_infer(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
     __nv_bfloat16 *tiles = W + WFWD_ELEMS;
@@ -266,7 +293,7 @@ __global__ void __launch_bounds__(NRC_IWARPS * 32) k_nrc_infer(InferArgs a) {
             const f3 nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
             encode_row(a.P, a.table, ld3(pp), nrm, f3{-dd.x, -dd.y, -dd.z}, tile + lane * NRC_STRIDE);
         } else {
-            for (int k = 0; k < NRC_W; k++) tile[lane * NRC_STRIDE + k] = __float2bfloat16_rn(0.0f);
+            for (int k = 0; k < NRC_W / 2; k++) reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE)[k] = 0u;
         }
         __syncwarp();
 #pragma unroll 1
@@ -347,7 +374,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
             tg = a.target[id];
             encode_row(a.P, a.table, pos, nrm, vdir, tile + lane * NRC_STRIDE);
         } else {
-            for (int k = 0; k < NRC_W; k++) tile[lane * NRC_STRIDE + k] = __float2bfloat16_rn(0.0f);
+            for (int k = 0; k < NRC_W / 2; k++) reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE)[k] = 0u;
         }
         __syncwarp();
 #pragma unroll 1

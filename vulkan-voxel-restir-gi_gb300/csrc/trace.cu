@@ -44,16 +44,6 @@ __device__ __forceinline__ NodeV ldnode(const vrg_bvh_node *n) {
     return r;
 }
 
-__device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz, f3 o, f3 inv,
-                                     float tmin, float tmax, float &tn) {
-    float t0x = (lox - o.x) * inv.x, t1x = (hix - o.x) * inv.x;
-    float t0y = (loy - o.y) * inv.y, t1y = (hiy - o.y) * inv.y;
-    float t0z = (loz - o.z) * inv.z, t1z = (hiz - o.z) * inv.z;
-    tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
-    return tn <= tf;
-}
-
 // nodeImportance (raytrace.rs:181-208: uint visibility, EPS 1e-3;
 // nee_pdf.rs:125-152: float visibility, EPS 1e-4); translation transforms
 template <bool NEE>
@@ -136,8 +126,7 @@ __device__ Descent light_descent(const DevScene &sc, f3 point, f3 normal, uint32
         float lI = node_importance<false>(point, normal, off, left);
         float rI = node_importance<false>(point, normal, off, right);
         float tot = lI + rI;
-        float ln = lI / tot, rn = rI / tot;
-        (void)rn;
+        const float ln = lI / tot;  // the shader's right ratio is never read
         if (mm_rand(seed) < ln) { node = left; node_idx = li; importance = lI; }
         else { node = right; node_idx = ri; importance = rI; }
         seed = mm_combine(seed, 0);
