@@ -305,6 +305,49 @@ __global__ void k_lamp_fill(const int4 *rec, const uint32_t *grp, uint32_t n, in
     }
 }
 
+// 4-wide traversal layout of a single-level tree whose leaf prim p is record p
+// (the lamp-block tree): for every inner node, its children with each inner
+// child replaced by that child's two children; the layout of k_wide4
+// (lo/hi x, y, z SoA, refs: >= 0 node, < 0 ~record, EMPTY_ROOT unused)
+__global__ void k_wide4_single(const vrg_bvh_node *nodes, const uint32_t *leaf, uint32_t n_nodes, float4 *wide4) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_nodes) return;
+    const vrg_bvh_node &nd = nodes[g];
+    if (nd.left_node_idx == INVALID) return;
+    uint32_t out[4];
+    int n = 0;
+    const uint32_t ch[2] = {nd.left_node_idx, nd.right_node_idx_or_prim_idx};
+    for (int s = 0; s < 2; s++) {
+        const vrg_bvh_node &c = nodes[ch[s]];
+        if (c.left_node_idx != INVALID) {
+            out[n++] = c.left_node_idx;
+            out[n++] = c.right_node_idx_or_prim_idx;
+        } else {
+            out[n++] = ch[s];
+        }
+    }
+    float b[6][4];
+    int refs[4];
+    for (int i = 0; i < 4; i++) {
+        if (i < n) {
+            const vrg_bvh_node &c = nodes[out[i]];
+            for (int a = 0; a < 3; a++) {
+                b[2 * a][i] = c.min[a] - BOX_MARGIN;
+                b[2 * a + 1][i] = c.max[a] + BOX_MARGIN;
+            }
+            refs[i] = c.left_node_idx != INVALID ? (int)out[i] : ~(int)leaf[out[i]];
+        } else {
+            for (int a = 0; a < 3; a++) b[2 * a][i] = b[2 * a + 1][i] = INFINITY;
+            refs[i] = EMPTY_ROOT;
+        }
+    }
+    float4 *w = wide4 + 8 * (size_t)g;
+    for (int r = 0; r < 6; r++) w[r] = make_float4(b[r][0], b[r][1], b[r][2], b[r][3]);
+    w[6] = make_float4(__int_as_float(refs[0]), __int_as_float(refs[1]), __int_as_float(refs[2]),
+                       __int_as_float(refs[3]));
+    w[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 // traversal layout of a single-level tree whose leaf prim p is record p
 __global__ void k_wide_single(const vrg_bvh_node *nodes, const uint32_t *leaf, uint32_t n_nodes, float4 *wide) {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -713,7 +756,7 @@ vrg_status commit_lamps(cudaStream_t s, std::vector<CommitPrep> &cps) {
         uint64_t q = 0;
         const uint64_t q_rec = q; q += al(n * 16);
         const uint64_t q_tab = q; q += al(n * 12 * 4);
-        const uint64_t q_wide = q; q += al(2 * n * 64);
+        const uint64_t q_wide = q; q += al(2 * n * 128);
         VRG_TRY(dev_alloc(s, q, cp.lamp_buf));
         uint8_t *Q = (uint8_t *)cp.lamp_buf->ptr;
         int4 *lamp = (int4 *)(Q + q_rec);
@@ -754,14 +797,14 @@ vrg_status commit_lamps(cudaStream_t s, std::vector<CommitPrep> &cps) {
         DevScene &D = cp.dev;
         if (cp.n_lamps > 1) {
             const uint32_t nn = 2 * cp.n_lamps - 1;
-            k_wide_single<<<(nn + 255) / 256, 256, 0, s>>>(nodes + 2 * cp.lamp_off, leaf + 2 * cp.lamp_off, nn,
-                                                           (float4 *)D.lamp_wide);
+            k_wide4_single<<<(nn + 255) / 256, 256, 0, s>>>(nodes + 2 * cp.lamp_off, leaf + 2 * cp.lamp_off, nn,
+                                                            (float4 *)D.lamp_wide);
             VRG_CUDA_TRY(cudaGetLastError());
             D.lamp_root = 0;
         } else {
             D.lamp_root = ~0;
         }
-        cp.lamp_depth = levels + 2;
+        cp.lamp_depth = 3 * ((levels + 2 + 1) / 2) + 1;  // up to 3 pushes per 4-wide level
     }
     return VRG_OK;
 }

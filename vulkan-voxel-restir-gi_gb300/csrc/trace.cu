@@ -747,6 +747,7 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
     f3 o = f3{0, 0, 0}, d = f3{0, 0, 0}, inv = f3{0, 0, 0}, oi = f3{0, 0, 0};
     float pdf = 0.0f;
     int node = 0, sp = 0, nh = 0;
+    int px = 0, py = 2, pz = 4;  // near-plane float4 per axis, picked by the ray's direction signs
     int stack[TRAV_STACK];
     uint64_t keys[LIGHT_LIST];
     float b1s[LIGHT_LIST], b2s[LIGHT_LIST];
@@ -777,6 +778,9 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
                     pdf = rd.w;
                     inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+                    px = signbit(inv.x) ? 1 : 0;
+                    py = signbit(inv.y) ? 3 : 2;
+                    pz = signbit(inv.z) ? 5 : 4;
                     node = root;
                     sp = 0;
                     nh = 0;
@@ -787,26 +791,39 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
         if (!__any_sync(FULL, has)) break;
         if (has) {
             bool done = (node == EMPTY_ROOT);
+            // 4-wide lamp nodes: every crossed light counts, so children are
+            // visited in slot order (no sorting); the first hit child is taken,
+            // the others pushed
             while (!done && node >= 0) {
-                const float4 *w = wide + 4 * (size_t)node;
-                const float4 A = __ldg(w), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
-                float tn0, tn1;
-                const bool h0 = slab_fma(A.x, A.y, A.z, A.w, B.x, B.y, inv, oi, tmin, tmax, tn0);
-                const bool h1 = slab_fma(B.z, B.w, C.x, C.y, C.z, C.w, inv, oi, tmin, tmax, tn1);
-                const int r0 = __float_as_int(D.x), r1 = __float_as_int(D.y);
-                if (h0 && h1) {
-                    if (sp < TRAV_STACK) stack[sp++] = r1;
-                    else atomicOr(err, ERR_STACK);
-                    node = r0;
-                } else if (h0) {
-                    node = r0;
-                } else if (h1) {
-                    node = r1;
-                } else if (sp == 0) {
-                    done = true;
-                } else {
-                    node = stack[--sp];
+                const float4 *w = wide + 8 * (size_t)node;
+                const float4 NX = __ldg(w + px), FX = __ldg(w + (px ^ 1)), NY = __ldg(w + py);
+                const float4 FY = __ldg(w + (py ^ 1)), NZ = __ldg(w + pz), FZ = __ldg(w + (pz ^ 1));
+                const float4 RF = __ldg(w + 6);
+                const float nx[4] = {NX.x, NX.y, NX.z, NX.w}, fx[4] = {FX.x, FX.y, FX.z, FX.w};
+                const float ny[4] = {NY.x, NY.y, NY.z, NY.w}, fy[4] = {FY.x, FY.y, FY.z, FY.w};
+                const float nz[4] = {NZ.x, NZ.y, NZ.z, NZ.w}, fz[4] = {FZ.x, FZ.y, FZ.z, FZ.w};
+                const int rf[4] = {__float_as_int(RF.x), __float_as_int(RF.y), __float_as_int(RF.z),
+                                   __float_as_int(RF.w)};
+                int next = EMPTY_ROOT;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float tn = fmax3(__fmaf_rn(nx[i], inv.x, oi.x), __fmaf_rn(ny[i], inv.y, oi.y),
+                                           fmaxf(__fmaf_rn(nz[i], inv.z, oi.z), tmin));
+                    const float tf = fmin3(__fmaf_rn(fx[i], inv.x, oi.x), __fmaf_rn(fy[i], inv.y, oi.y),
+                                           fminf(__fmaf_rn(fz[i], inv.z, oi.z), tmax));
+                    if (tn <= tf && rf[i] != EMPTY_ROOT) {
+                        if (next == EMPTY_ROOT) {
+                            next = rf[i];
+                        } else if (sp < TRAV_STACK) {
+                            stack[sp++] = rf[i];
+                        } else {
+                            atomicOr(err, ERR_STACK);
+                        }
+                    }
                 }
+                if (next != EMPTY_ROOT) node = next;
+                else if (sp == 0) done = true;
+                else node = stack[--sp];
                 if (++steps > TRAV_GUARD) {
                     atomicOr(err, ERR_GUARD);
                     done = true;

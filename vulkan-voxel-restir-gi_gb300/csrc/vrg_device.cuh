@@ -230,7 +230,7 @@ struct DevScene {
     const float4 *geo_wide;   // 8 float4 per node: 4-wide child boxes (world, +margin, SoA) and refs
     const int4 *geo_rec;
     int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
-    const float4 *lamp_wide;  // any-hit layout over lamp blocks (world space, +margin)
+    const float4 *lamp_wide;  // any-hit layout over lamp blocks: 8 float4 per node, 4-wide as geo_wide
     const int4 *lamp_rec;     // per lamp block: x/y packed coords + instance, z emissive face mask, w table base
     const uint32_t *lamp_table;  // 12 per lamp block: light-BLAS leaf of (face, half), INVALID if none
     int lamp_root;
