@@ -290,6 +290,18 @@ enum {
 };
 VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst, uint64_t bytes);
 
+/* ---- cross-frame state (no reference counterpart) ------------------------
+ * Everything a renderer carries from one frame to the next — the reservoir
+ * history ring (5 x 16 bytes per pixel and slot), the frame counter (which
+ * seeds the per-pixel streams) and the FP64 accumulation with its frame count
+ * — as one host blob, for checkpoints and deterministic replay: frames
+ * rendered after a load repeat, bit for bit, the frames rendered after the
+ * save.  A blob loads only into a renderer of the same pixel count and ring
+ * length.  The radiance cache is saved apart (vrg_nrc_read / vrg_nrc_write). */
+VRG_API vrg_status vrg_renderer_state_size(vrg_renderer *r, uint64_t *bytes);
+VRG_API vrg_status vrg_renderer_state_save(vrg_renderer *r, void *dst, uint64_t bytes);
+VRG_API vrg_status vrg_renderer_state_load(vrg_renderer *r, const void *src, uint64_t bytes);
+
 /* ---- launch configuration and autotuner (no reference counterpart) -----
  * Every field changes only how the frame's work is scheduled, never a result
  * (the tests render the same bits under any configuration).  0 = default. */

@@ -41,6 +41,7 @@ vrg_status dev_alloc(cudaStream_t s, size_t bytes, DevBufPtr &out) {
     b->bytes = bytes;
     cudaError_t e = cudaMallocAsync(&b->ptr, bytes ? bytes : 16, s);
     if (e != cudaSuccess) {
+        cudaGetLastError();  // a failed allocation is reported here, not by the next launch check
         b->ptr = nullptr;
         set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? VRG_ERR_OUT_OF_MEMORY : VRG_ERR_CUDA;
@@ -1164,6 +1165,65 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
     frame_done(r, a, pr);
     if (stats) return frame_stats(r, a, !graph, stats);
     if (host_out) VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+// ---- cross-frame state -------------------------------------------------------
+
+struct StateHeader {
+    uint32_t magic;     // 'VRGS'
+    uint32_t version;
+    uint64_t pixels;
+    uint32_t ring_slots;
+    uint32_t frame;
+    uint32_t accum_n;
+    uint32_t pad;
+};
+static constexpr uint32_t STATE_MAGIC = 0x53475256u;
+
+static uint64_t state_bytes(const vrg_renderer *r) {
+    return sizeof(StateHeader) + (uint64_t)r->ring_slots * 5 * r->P * 16 + r->P * 24;
+}
+
+VRG_API vrg_status vrg_renderer_state_size(vrg_renderer *r, uint64_t *bytes) {
+    if (!r || !bytes) return VRG_ERR_INVALID_ARGUMENT;
+    *bytes = state_bytes(r);
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_state_save(vrg_renderer *r, void *dst, uint64_t bytes) {
+    if (!r || !dst || bytes < state_bytes(r)) return VRG_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = r->ctx->stream;
+    StateHeader h{STATE_MAGIC, 1u, r->P, r->ring_slots, r->frame, r->accum_n, 0u};
+    uint8_t *d = (uint8_t *)dst;
+    memcpy(d, &h, sizeof(h));
+    d += sizeof(h);
+    const size_t ring = (size_t)r->ring_slots * 5 * r->P * 16;
+    if (ring) VRG_CUDA_TRY(cudaMemcpyAsync(d, r->res, ring, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(d + ring, r->accum, (size_t)r->P * 24, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_state_load(vrg_renderer *r, const void *src, uint64_t bytes) {
+    if (!r || !src || bytes < sizeof(StateHeader)) return VRG_ERR_INVALID_ARGUMENT;
+    StateHeader h;
+    memcpy(&h, src, sizeof(h));
+    if (h.magic != STATE_MAGIC || h.version != 1u || h.pixels != r->P || h.ring_slots > 8) {
+        set_error("state blob does not fit this renderer (%llu pixels, ring %u)", (unsigned long long)h.pixels,
+                  h.ring_slots);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    const size_t ring = (size_t)h.ring_slots * 5 * r->P * 16;
+    if (bytes < sizeof(h) + ring + r->P * 24) return VRG_ERR_INVALID_ARGUMENT;
+    if (h.ring_slots) VRG_TRY(ensure_ring(r, h.ring_slots));
+    cudaStream_t s = r->ctx->stream;
+    const uint8_t *p = (const uint8_t *)src + sizeof(h);
+    if (ring) VRG_CUDA_TRY(cudaMemcpyAsync(r->res, p, ring, cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(r->accum, p + ring, (size_t)r->P * 24, cudaMemcpyHostToDevice, s));
+    VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    r->frame = h.frame;
+    r->accum_n = h.accum_n;
     return VRG_OK;
 }
 

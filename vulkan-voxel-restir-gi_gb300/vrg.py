@@ -160,6 +160,9 @@ SIGNATURES = [
     ("vrg_image_write_ppm", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
     ("vrg_image_write_png", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
     ("vrg_image_write_pfm", C.c_int32, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
+    ("vrg_renderer_state_size", C.c_int32, [_P, C.POINTER(C.c_uint64)]),
+    ("vrg_renderer_state_save", C.c_int32, [_P, _P, C.c_uint64]),
+    ("vrg_renderer_state_load", C.c_int32, [_P, _P, C.c_uint64]),
     ("vrg_renderer_set_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
     ("vrg_renderer_get_tuning", C.c_int32, [_P, C.POINTER(Tuning)]),
     ("vrg_renderer_autotune", C.c_int32, [_P, _P, C.POINTER(Camera), C.POINTER(RenderParams), C.c_uint32,
@@ -473,6 +476,18 @@ class Renderer:
     def set_cache(self, cache):
         check(self.ctx.lib.vrg_renderer_set_cache(self.h, None if cache is None else cache.h),
               "vrg_renderer_set_cache")
+
+    def save_state(self) -> np.ndarray:
+        """Reservoir history, frame counter and accumulation as a byte array."""
+        n = C.c_uint64()
+        check(self.ctx.lib.vrg_renderer_state_size(self.h, C.byref(n)), "vrg_renderer_state_size")
+        blob = np.empty(n.value, np.uint8)
+        check(self.ctx.lib.vrg_renderer_state_save(self.h, _ptr(blob), blob.nbytes), "vrg_renderer_state_save")
+        return blob
+
+    def load_state(self, blob: np.ndarray):
+        blob = np.ascontiguousarray(blob, np.uint8)
+        check(self.ctx.lib.vrg_renderer_state_load(self.h, _ptr(blob), blob.nbytes), "vrg_renderer_state_load")
 
     def set_tuning(self, tuning: "Tuning"):
         check(self.ctx.lib.vrg_renderer_set_tuning(self.h, C.byref(tuning)), "vrg_renderer_set_tuning")
