@@ -627,7 +627,9 @@ def run_ours(args, d):
                             "unit": "GB/s", "frac": round(stream_gbs / hbm_peak, 4), "bytes_per_px": 252},
         "e2e": {"value": None if e2e_value is None else round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),
                 "d2h_bytes_per_step": W * H * 4},
-        "gpu_launches": (3 * NB - 1 + 2) * args.steps,
+        # per frame: k_trace and k_shade per bounce, k_anyhit + k_hit_eval +
+        # k_hit_sum per bounce but the last, k_resolve, k_spatial
+        "gpu_launches": (2 * NB + 3 * (NB - 1) + 2) * args.steps,
         "quality": quality_block,
         "autotune": tuning,
         "batched": batched,
