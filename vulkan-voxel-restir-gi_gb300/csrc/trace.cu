@@ -14,6 +14,8 @@
 // one warp ballot + one atomic per warp.  State per pixel stays in SoA
 // float4 arrays; the per-bounce record (E, w=pdf/q) (R, q) feeds the
 // backward radiance recurrence of the resolve kernel.
+#include <mutex>
+
 #include "vrg_frame.cuh"
 #include "vrg_internal.h"
 
@@ -932,9 +934,9 @@ static int occupancy_grid(const void *fn, int threads) {
 // batched] (set once, before any stream capture)
 static int g_trace[2] = {0, 0}, g_shade[2] = {0, 0}, g_any[2] = {0, 0};
 static int g_sms = 1;
+static std::once_flag g_grids_once;
 
-static void init_grids() {
-    if (g_trace[0]) return;
+static void init_grids_once() {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -946,6 +948,9 @@ static void init_grids() {
     g_trace[1] = occupancy_grid((const void *)k_trace<true>, 128);
     g_trace[0] = occupancy_grid((const void *)k_trace<false>, 128);
 }
+
+// (thread-safe: renderers may be created from several threads)
+static void init_grids() { std::call_once(g_grids_once, init_grids_once); }
 
 // resident CTAs per SM at full occupancy of (closest hit, shading, light
 // hits), the bound of a tuned persistent grid; and the SM count
