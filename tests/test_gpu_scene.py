@@ -109,3 +109,39 @@ def test_transform_update_matches_oracle(gpu_ctx, orc):
         orr.close()
     finally:
         OW.close()
+
+
+def test_concurrent_uploads_match_serial(gpu_ctx):
+    """SceneUploader is Clone and called from the chunk workers' pool
+    (chunk_manager.rs:234-248): chunks uploaded from 8 threads at once give
+    the same committed scene (top levels and every chunk's BLAS) as serial
+    uploads."""
+    from concurrent.futures import ThreadPoolExecutor
+    mats, n, world = terrain_world(17, 4, 4, 0.01)
+    gpu_ctx.set_materials(mats, n)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, dtype=np.uint8)
+    up = vrg.SceneUploader(gpu_ctx)
+    keys = [(cx, cz) for cx in range(4) for cz in range(4)]
+
+    def upload(k):
+        cx, cz = k
+        return up.upload_chunk(world[cx, cz], vrg.chunk_neighbours(world, cx, cz, floor))
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        objs = list(ex.map(upload, keys))
+    par = vrg.Scene(gpu_ctx)
+    for (cx, cz), o in zip(keys, objs):
+        par.add_object(cx * 4 + cz, o, (32 * cx, 0, 32 * cz))
+    ser, ser_objs = vrg.build_world(gpu_ctx, world)
+    tp, ts = par.get_tlas(), ser.get_tlas()
+    for a, b in zip(tp, ts):
+        assert nodes_equal(a, b)
+    for (cx, cz), o, so in zip(keys, objs, ser_objs):
+        for which in (0, 1):
+            na, pa = o.read_bvh(which)
+            nb_, pb = so.read_bvh(which)
+            assert nodes_equal(na, nb_) and np.array_equal(pa, pb), (cx, cz, which)
+    for sc in (par, ser):
+        sc.close()
+    for o in objs + ser_objs:
+        o.release()

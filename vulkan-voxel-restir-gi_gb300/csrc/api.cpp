@@ -910,17 +910,17 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) 
         }
         VRG_TRY(launch_train_targets(st, a));
         VRG_TRY(nrc_train(r->cache, st, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true));
+                          nullptr, r->target, true, r->counters + CNT_ERROR));
         VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
     }
     if (a.cache)  // radiance-cache queries of every path that ends into the cache
         VRG_TRY(nrc_infer(r->cache, s, a.P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
-                          r->pred));
+                          r->pred, r->counters + CNT_ERROR));
     VRG_TRY(launch_resolve(s, a));
     if (a.cache && !fork) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));
         VRG_TRY(nrc_train(r->cache, s, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true));
+                          nullptr, r->target, true, r->counters + CNT_ERROR));
     }
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));

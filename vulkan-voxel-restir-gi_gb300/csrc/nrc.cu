@@ -162,6 +162,47 @@ __device__ __forceinline__ void ldsm_x4(const __nv_bfloat16 *p, uint32_t &r0, ui
                  : "r"(a));
 }
 
+// Stages `bytes` (a multiple of 16, 16-byte aligned at both ends) from global
+// into shared memory with one bulk copy (cp.async.bulk, completing on an
+// mbarrier) issued by thread 0; every thread of the CTA waits for it.  The wait
+// is bounded: past the limit the kernel flags ERR_COPY, waits once more
+// (bounded) for the copy in flight, and the caller returns.
+__device__ __forceinline__ bool stage_bulk(void *dst, const void *src, uint32_t bytes, uint64_t *bar, uint32_t *err) {
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar), d = (uint32_t)__cvta_generic_to_shared(dst);
+    if ((d & 15u) || ((uintptr_t)src & 15u) || (bytes & 15u)) {  // not a bulk-copy shape: plain copy
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+        for (uint32_t i = threadIdx.x; i < bytes / 16; i += blockDim.x) d4[i] = s4[i];
+        __syncthreads();
+        return true;
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(d),
+                     "l"(src), "r"(bytes), "r"(b)
+                     : "memory");
+    }
+    __syncthreads();
+    auto wait = [&](uint32_t limit) {
+        for (uint32_t it = 0; it < limit; it++) {
+            uint32_t done;
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(b)
+                : "memory");
+            if (done) return true;
+        }
+        return false;
+    };
+    if (wait(1u << 22)) return true;
+    if (threadIdx.x == 0 && err) atomicOr(err, ERR_COPY);
+    wait(1u << 22);
+    return false;
+}
+
 // A fragments of a 16-row tile held row-major in shared memory (rows of
 // NRC_STRIDE bf16, 16-byte aligned): per 16-column chunk kc the matrices
 // (rows 0-7, kc), (rows 8-15, kc), (rows 0-7, kc + 8), (rows 8-15, kc + 8)
@@ -258,6 +299,7 @@ struct InferArgs {
     const float4 *dir;
     const float4 *nrm;         // optional explicit normals (NULL: from the face in pos.w)
     float4 *out;               // rgb per pixel / query
+    uint32_t *err;             // error word (ERR_COPY)
 };
 
 __device__ __forceinline__ f3 face_normal(int f) {
@@ -275,12 +317,8 @@ __global__ void __launch_bounds__(NRC_IWARPS * 32, 2) k_nrc_infer(InferArgs a) {
     __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
     __nv_bfloat16 *tiles = W + WFWD_ELEMS;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack);
-        uint4 *dst = reinterpret_cast<uint4 *>(W);
-        for (size_t i = threadIdx.x; i < WFWD_ELEMS * 2 / 16; i += blockDim.x) dst[i] = src[i];
-    }
-    __syncthreads();
+    __shared__ __align__(8) uint64_t bar;
+    if (!stage_bulk(W, a.wpack, (uint32_t)(WFWD_ELEMS * 2), &bar, a.err)) return;  // forward weights
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
     const uint32_t warps = gridDim.x * NRC_IWARPS;
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
@@ -340,6 +378,7 @@ struct TrainArgs {
     __nv_bfloat16 *dZ;          // [6][n_pad][64] pre-activation gradients (layer 5: 16 used)
     float2 *gtable;             // hash-grid gradients (fp32)
     float *loss;                // summed loss
+    uint32_t *err;              // error word (ERR_COPY)
 };
 
 __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
@@ -347,12 +386,8 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
     __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
     __nv_bfloat16 *tiles = W + WPACK_ELEMS;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack);
-        uint4 *dst = reinterpret_cast<uint4 *>(W);
-        for (size_t i = threadIdx.x; i < WPACK_ELEMS * 2 / 16; i += blockDim.x) dst[i] = src[i];
-    }
-    __syncthreads();
+    __shared__ __align__(8) uint64_t bar;
+    if (!stage_bulk(W, a.wpack, (uint32_t)(WPACK_ELEMS * 2), &bar, a.err)) return;  // weights and transposes
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
     float *ybuf = reinterpret_cast<float *>(tiles + (size_t)NRC_WARPS * 32 * NRC_STRIDE) + (size_t)w * 32 * NRC_OUT;
     const size_t n_pad = ((size_t)a.n + 31) & ~(size_t)31;
@@ -677,6 +712,7 @@ struct Nrc {
     float *w_master = nullptr, *w_m = nullptr, *w_v = nullptr, *w_grad = nullptr;
     __nv_bfloat16 *wpack = nullptr;
     float *loss = nullptr;
+    uint32_t *err = nullptr;  // error word of the host-array entry points
     DevBufPtr act;  // training activations
     size_t act_rows = 0;
     __nv_bfloat16 *H = nullptr, *dZ = nullptr;
@@ -758,6 +794,7 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     N->w_grad = (float *)(B + o_wg);
     N->wpack = (__nv_bfloat16 *)(B + o_wp);
     N->loss = (float *)(B + o_ls);
+    N->err = (uint32_t *)(B + o_ls + 4);
     VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, s));
     k_init_table<<<(uint32_t)((te + 255) / 256), 256, 0, s>>>(N->t_master, N->table, te, d->seed ^ 0x7ab1eull);
     // He-uniform hidden layers, Xavier-uniform output layer (rows 0..2)
@@ -790,9 +827,9 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
 }
 
 vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
-                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out) {
+                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out, uint32_t *err) {
     if (n == 0) return VRG_OK;
-    InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out};
+    InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out, err ? err : N->err};
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_IWARPS * 32 - 1) / (NRC_IWARPS * 32));
     k_nrc_infer<<<blocks, NRC_IWARPS * 32, infer_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
@@ -815,11 +852,13 @@ static vrg_status ensure_act(Nrc *N, size_t rows) {
 // gradients of one batch (accumulated into w_grad / t_grad); update == true
 // also runs the Adam step
 vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
-                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update) {
+                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
+                     uint32_t *err) {
     if (n == 0) return VRG_OK;
     VRG_TRY(ensure_act(N, n));
     const size_t n_pad = N->act_rows;
-    TrainArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, target, N->H, N->dZ, N->t_grad, N->loss};
+    TrainArgs a{N->P,   N->table, N->wpack, n,        n_dev,    list,   pos, dir, nrm, target,
+                N->H,   N->dZ,    N->t_grad, N->loss, err ? err : N->err};
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
     k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
@@ -872,10 +911,17 @@ vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, pos, n, 3, dp));
     VRG_TRY(stage4(s, dir, n, 3, dd));
     VRG_TRY(stage4(s, nrm, n, 3, dn));
-    VRG_TRY(nrc_infer(N, s, n, nullptr, nullptr, dp, dd, dn, dout));
+    VRG_CUDA_TRY(cudaMemsetAsync(N->err, 0, 4, s));
+    VRG_TRY(nrc_infer(N, s, n, nullptr, nullptr, dp, dd, dn, dout, nullptr));
     std::vector<float4> h(n);
+    uint32_t err = 0;
     VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), dout, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(&err, N->err, 4, cudaMemcpyDeviceToHost, s));
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (err) {
+        set_error("radiance cache kernel error flags 0x%x", err);
+        return VRG_ERR_OVERFLOW;
+    }
     for (uint32_t i = 0; i < n; i++) { rgb[3 * i] = h[i].x; rgb[3 * i + 1] = h[i].y; rgb[3 * i + 2] = h[i].z; }
     return VRG_OK;
 }
@@ -890,11 +936,17 @@ vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, dir, n, 3, dd));
     VRG_TRY(stage4(s, nrm, n, 3, dn));
     VRG_TRY(stage4(s, target, n, 3, dt));
-    VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 4, s));
-    VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0));
+    VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 8, s));  // loss and error word
+    VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0, nullptr));
     float l = 0.0f;
+    uint32_t err = 0;
     VRG_CUDA_TRY(cudaMemcpyAsync(&l, N->loss, 4, cudaMemcpyDeviceToHost, s));
+    VRG_CUDA_TRY(cudaMemcpyAsync(&err, N->err, 4, cudaMemcpyDeviceToHost, s));
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (err) {
+        set_error("radiance cache kernel error flags 0x%x", err);
+        return VRG_ERR_OVERFLOW;
+    }
     if (loss_out) *loss_out = l;
     return VRG_OK;
 }

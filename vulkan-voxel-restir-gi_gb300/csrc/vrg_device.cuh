@@ -250,6 +250,7 @@ constexpr int TRAV_STACK = 96;
 constexpr uint32_t ERR_STACK = 1u;
 constexpr uint32_t ERR_LIGHT_LIST = 2u;
 constexpr uint32_t ERR_GUARD = 4u;
+constexpr uint32_t ERR_COPY = 8u;           // a bulk copy into shared memory did not complete in time
 constexpr uint32_t TRAV_GUARD = 1u << 22;  // iteration bound of every traversal loop
 
 }  // namespace vrg

@@ -160,10 +160,13 @@ struct Nrc;
 vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out);
 void nrc_destroy(Nrc *N);
 vrg_status nrc_set_bounds(Nrc *N, const float lo[3], const float hi[3]);
+// err: the device error word the kernels flag (NULL: the cache's own word,
+// checked by the host-array entry points)
 vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
-                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out);
+                     const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out, uint32_t *err);
 vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
-                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update);
+                     const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
+                     uint32_t *err);
 uint32_t nrc_batch(const Nrc *N);
 vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb);
 vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
