@@ -16,6 +16,8 @@ namespace vrg {
 vrg_status upload_frames(cudaStream_t s);
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
                          uint32_t max_rays);
+vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, uint32_t max_rays);
+vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a);
@@ -433,7 +435,10 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     size_t o_q0 = o; o += al(P * 4);
     size_t o_q1 = o; o += al(P * 4);
     size_t o_cnt = o; o += al(CNT_WORDS * 4);
-    size_t o_aq = o; o += al(P * 4);
+    size_t o_aq0 = o; o += al(P * 4);
+    size_t o_aq1 = o; o += al(P * 4);
+    size_t o_aj0 = o; o += al(P * 32);
+    size_t o_aj1 = o; o += al(P * 32);
     size_t o_hit = o; o += al(P * 16);
     size_t o_hb = o; o += al(P * 2 * 32);
     size_t o_hv = o; o += al(P * 2 * 4);
@@ -458,7 +463,10 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->queue[0] = (uint32_t *)(B + o_q0);
     r->queue[1] = (uint32_t *)(B + o_q1);
     r->counters = (uint32_t *)(B + o_cnt);
-    r->aqueue = (uint32_t *)(B + o_aq);
+    r->aqueue[0] = (uint32_t *)(B + o_aq0);
+    r->aqueue[1] = (uint32_t *)(B + o_aq1);
+    r->ajob[0] = (float4 *)(B + o_aj0);
+    r->ajob[1] = (float4 *)(B + o_aj1);
     r->hits = (int4 *)(B + o_hit);
     r->hitbuf = (uint4 *)(B + o_hb);
     r->hitval = (float *)(B + o_hv);
@@ -503,6 +511,11 @@ static vrg_status renderer_events(vrg_renderer *r) {
     int lo_prio = 0, hi_prio = 0;
     VRG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux, cudaStreamNonBlocking, hi_prio));
+    VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->lps, cudaStreamNonBlocking));
+    for (auto &e : r->ev_shaded) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : r->ev_lpdone) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &row : r->ev_lp)
+        for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
@@ -620,6 +633,17 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
             if (e) cudaEventDestroy(e);
     for (auto &e : r->ev_stage)
         if (e) cudaEventDestroy(e);
+    for (auto &e : r->ev_shaded)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : r->ev_lpdone)
+        if (e) cudaEventDestroy(e);
+    for (auto &row : r->ev_lp)
+        for (auto &e : row)
+            if (e) cudaEventDestroy(e);
+    if (r->lps) {
+        cudaStreamSynchronize(r->lps);
+        cudaStreamDestroy(r->lps);
+    }
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
     if (r->aux) {
@@ -835,7 +859,10 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.ray_d = r->ray_d;
     a.queue[0] = r->queue[0];
     a.queue[1] = r->queue[1];
-    a.aqueue = r->aqueue;
+    a.aqueue[0] = r->aqueue[0];
+    a.aqueue[1] = r->aqueue[1];
+    a.ajob[0] = r->ajob[0];
+    a.ajob[1] = r->ajob[1];
     a.hits = r->hits;
     a.hitbuf = r->hitbuf;
     a.hitval = r->hitval;
@@ -894,10 +921,29 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) 
     const uint32_t nb_main = fork ? a.nb_render : a.nb;
     VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
+    // Bounce b's light-pdf walk runs on the light-pdf stream beside bounce
+    // b + 1's closest hit and shading.  Ordering: the walk of b waits for the
+    // shading of b; the shading of b + 2 (which refills the job buffers of
+    // parity b & 1) waits for the walk of b; resolve waits for every walk.
+    int last_lp = -1;
     for (uint32_t b = 0; b < nb_main; b++) {
-        VRG_TRY(launch_bounce(s, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr, 0));
-        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
+        if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[b - 2], 0));
+        VRG_TRY(launch_trace_shade(s, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
+        if (timed) {
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
+        }
+        if (b + 1 < a.nb) {
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[b], s));
+            VRG_CUDA_TRY(cudaStreamWaitEvent(r->lps, r->ev_shaded[b], 0));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], r->lps));
+            VRG_TRY(launch_light_pdf(r->lps, a, b, 0));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[1][b], r->lps));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[b], r->lps));
+            last_lp = (int)b;
+        }
     }
+    if (last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[last_lp], 0));
     cudaStream_t st = s;  // stream of the training branch
     if (fork) {
         st = r->aux;
@@ -938,6 +984,9 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
     if (per_kernel) {
         cudaEventElapsedTime(&ms, r->ev[0], r->ev[a.nb + 2]);
         stats->ms_total = ms;
+        // main-stream bounces: closest hit + shading; their light-pdf walks
+        // run beside the next bounce and are timed on their own stream
+        const uint32_t nb_main = (a.cache && !a.capture) ? a.nb_render : a.nb;
         for (uint32_t b = 0; b < a.nb && b < 8; b++) {
             cudaEventElapsedTime(&ms, r->ev[b], r->ev[b + 1]);
             stats->ms_bounce[b] = ms;
@@ -945,8 +994,15 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
             stats->ms_trace[b] = ms;
             cudaEventElapsedTime(&ms, r->ev_k[0][b], r->ev_k[1][b]);
             stats->ms_shade[b] = ms;
-            cudaEventElapsedTime(&ms, r->ev_k[1][b], r->ev[b + 1]);
-            stats->ms_anyhit[b] = ms;
+            if (b < nb_main) {
+                if (b + 1 < a.nb) {
+                    cudaEventElapsedTime(&ms, r->ev_lp[0][b], r->ev_lp[1][b]);
+                    stats->ms_anyhit[b] = ms;
+                }
+            } else {
+                cudaEventElapsedTime(&ms, r->ev_k[1][b], r->ev[b + 1]);
+                stats->ms_anyhit[b] = ms;
+            }
         }
         // a forked cache frame's resolve stage starts at the fork (it runs beside the training branch)
         cudaEventElapsedTime(&ms, r->ev[(a.cache && !a.capture) ? a.nb_render : a.nb], r->ev[a.nb + 1]);

@@ -707,7 +707,12 @@ __global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs
         qb = __shfl_sync(FULL, qb, 0);
         ab = __shfl_sync(FULL, ab, 0);
         if (cont) qout[qb + __popc(cm & lanemask_lt())] = p;
-        if (anyj) a.aqueue[ab + __popc(am & lanemask_lt())] = p;
+        if (anyj) {
+            const uint32_t j = ab + __popc(am & lanemask_lt());
+            a.aqueue[b & 1][j] = p;
+            a.ajob[b & 1][2 * (size_t)j] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+            a.ajob[b & 1][2 * (size_t)j + 1] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
+        }
     }
 }
 
@@ -766,7 +771,7 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
                 idx = base + (uint32_t)__popc(need & lanemask_lt());
                 if (idx < n_in) {
                     has = true;
-                    p = a.aqueue[idx];
+                    p = a.aqueue[b & 1][idx];
                     if constexpr (BATCH) {
                         const ViewDev &V = view_of<BATCH>(a, p);
                         wide = V.sc.lamp_wide;
@@ -774,7 +779,7 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
                         table = V.sc.lamp_table;
                         root = V.sc.lamp_root;
                     }
-                    const float4 ro = a.ray_o[p], rd = a.ray_d[p];
+                    const float4 ro = a.ajob[b & 1][2 * (size_t)idx], rd = a.ajob[b & 1][2 * (size_t)idx + 1];
                     o = ld3(ro);
                     d = ld3(rd);
                     pdf = rd.w;
@@ -876,7 +881,7 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
                     for (int j = 0; j < nh; j++) {
                         a.hitbuf[2 * (size_t)(hb + j)] =
                             make_uint4(p, (uint32_t)(keys[j] >> 32), (uint32_t)keys[j], __float_as_uint(b1s[j]));
-                        a.hitbuf[2 * (size_t)(hb + j) + 1] = make_uint4(__float_as_uint(b2s[j]), 0u, 0u, 0u);
+                        a.hitbuf[2 * (size_t)(hb + j) + 1] = make_uint4(__float_as_uint(b2s[j]), idx, 0u, 0u);
                     }
                 }
                 a.jmeta[idx] = make_uint2(hb, (uint32_t)nh);
@@ -887,12 +892,12 @@ __global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArg
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(128) k_hit_eval(const __grid_constant__ FrameArgs a) {
+__global__ void __launch_bounds__(128) k_hit_eval(const __grid_constant__ FrameArgs a, uint32_t b) {
     const uint32_t n = min(a.counters[CNT_HITS], a.hit_cap);
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
         const uint4 A = a.hitbuf[2 * (size_t)h], B = a.hitbuf[2 * (size_t)h + 1];
         const uint32_t p = A.x;
-        const float4 ro = a.ray_o[p], rd = a.ray_d[p];
+        const float4 ro = a.ajob[b & 1][2 * (size_t)B.y], rd = a.ajob[b & 1][2 * (size_t)B.y + 1];
         const f3 n3 = c_frames[2 * __float_as_int(ro.w)].n;
         a.hitval[h] = nee_pdf_of(view_of<BATCH>(a, p).sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
     }
@@ -904,10 +909,10 @@ __global__ void __launch_bounds__(128) k_hit_sum(const __grid_constant__ FrameAr
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += gridDim.x * blockDim.x) {
         const uint2 m = a.jmeta[i];
         if (m.y == 0) continue;
-        const uint32_t p = a.aqueue[i];
+        const uint32_t p = a.aqueue[b & 1][i];
         float nee = 0.0f;
         for (uint32_t j = 0; j < m.y; j++) nee += a.hitval[m.x + j];
-        finish_job(a, b, p, a.ray_d[p].w, nee);
+        finish_job(a, b, p, a.ajob[b & 1][2 * (size_t)i + 1].w, nee);
         if (CAPTURE) a.c_nee[(size_t)b * a.P + p] = nee;
     }
 }
@@ -963,48 +968,69 @@ void bounce_occupancy(bool batch, int occ[3], int *sms) {
     *sms = g_sms;
 }
 
-// One bounce: closest hit, shading, light-pdf walk (if another bounce follows).
-// A batched frame (a.views set) runs the variants that look up each pixel's view.
-// max_rays > 0 bounds the rays of this bounce (a cache frame's training paths):
-// the persistent grids then shrink to one lane per ray, leaving the other SMs
-// to the work that runs beside them.
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
-                         uint32_t max_rays) {
+// A bounce in two launches groups.  A batched frame (a.views set) runs the
+// variants that look up each pixel's view.  max_rays > 0 bounds the rays of the
+// bounce (a cache frame's training paths): the persistent grids then shrink to
+// one lane per ray, leaving the other SMs to the work that runs beside them.
+static void bounce_grids(const FrameArgs &a, uint32_t max_rays, int &gt, int &gs, int &ga) {
     init_grids();
-    const bool batch = a.views != nullptr;
-    if (batch && a.capture) {
-        set_error("capture is not available for batched frames");
-        return VRG_ERR_UNSUPPORTED;
-    }
-    const int v = batch ? 1 : 0;
-    int gt = a.grid_trace ? std::min((int)a.grid_trace, g_trace[v]) : g_trace[v];
-    int gs = a.grid_shade ? std::min((int)a.grid_shade, g_shade[v]) : g_shade[v];
-    int ga = a.grid_any ? std::min((int)a.grid_any, g_any[v]) : g_any[v];
+    const int v = a.views ? 1 : 0;
+    gt = a.grid_trace ? std::min((int)a.grid_trace, g_trace[v]) : g_trace[v];
+    gs = a.grid_shade ? std::min((int)a.grid_shade, g_shade[v]) : g_shade[v];
+    ga = a.grid_any ? std::min((int)a.grid_any, g_any[v]) : g_any[v];
     if (max_rays) {
         const int cap = (int)std::max<uint32_t>(1u, (max_rays + 127) / 128);
         gt = std::min(gt, cap);
         gs = std::min(gs, cap);
         ga = std::min(ga, cap);
     }
+}
+
+// closest hit and shading of bounce b
+vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace,
+                              uint32_t max_rays) {
+    const bool batch = a.views != nullptr;
+    if (batch && a.capture) {
+        set_error("capture is not available for batched frames");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    int gt, gs, ga;
+    bounce_grids(a, max_rays, gt, gs, ga);
     if (batch) k_trace<true><<<gt, 128, 0, s>>>(a, b);
     else k_trace<false><<<gt, 128, 0, s>>>(a, b);
     if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
     if (batch) k_shade<false, true><<<gs, 128, 0, s>>>(a, b);
     else if (a.capture) k_shade<true, false><<<gs, 128, 0, s>>>(a, b);
     else k_shade<false, false><<<gs, 128, 0, s>>>(a, b);
-    if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
-    if (b + 1 < a.nb) {
-        if (batch) k_anyhit<false, true><<<ga, 128, 0, s>>>(a, b);
-        else if (a.capture) k_anyhit<true, false><<<ga, 128, 0, s>>>(a, b);
-        else k_anyhit<false, false><<<ga, 128, 0, s>>>(a, b);
-        if (batch) k_hit_eval<true><<<gs, 128, 0, s>>>(a);
-        else k_hit_eval<false><<<gs, 128, 0, s>>>(a);
-        if (a.capture) k_hit_sum<true><<<gs, 128, 0, s>>>(a, b);
-        else k_hit_sum<false><<<gs, 128, 0, s>>>(a, b);
-        VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
-    }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
+}
+
+// the light-pdf walk of bounce b's jobs (bounces before the last): it reads only
+// the jobs' own ray copies, so it may run beside bounce b + 1
+vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
+    if (b + 1 >= a.nb) return VRG_OK;
+    const bool batch = a.views != nullptr;
+    int gt, gs, ga;
+    bounce_grids(a, max_rays, gt, gs, ga);
+    if (batch) k_anyhit<false, true><<<ga, 128, 0, s>>>(a, b);
+    else if (a.capture) k_anyhit<true, false><<<ga, 128, 0, s>>>(a, b);
+    else k_anyhit<false, false><<<ga, 128, 0, s>>>(a, b);
+    if (batch) k_hit_eval<true><<<gs, 128, 0, s>>>(a, b);
+    else k_hit_eval<false><<<gs, 128, 0, s>>>(a, b);
+    if (a.capture) k_hit_sum<true><<<gs, 128, 0, s>>>(a, b);
+    else k_hit_sum<false><<<gs, 128, 0, s>>>(a, b);
+    VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
+    VRG_CUDA_TRY(cudaGetLastError());
+    return VRG_OK;
+}
+
+// One bounce on one stream: closest hit, shading, light-pdf walk.
+vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
+                         uint32_t max_rays) {
+    VRG_TRY(launch_trace_shade(s, a, b, ev_trace, max_rays));
+    if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
+    return launch_light_pdf(s, a, b, max_rays);
 }
 
 int bounce_blocks_per_sm() {

@@ -59,7 +59,11 @@ struct FrameArgs {
     // wavefront state
     float4 *ray_o, *ray_d;
     uint32_t *queue[2];
-    uint32_t *aqueue;             // any-hit jobs of the current bounce
+    // light-pdf jobs of bounce b in [b & 1] (double-buffered by bounce parity:
+    // the jobs of bounce b are walked while bounce b + 1 traces and shades):
+    // the pixel, and a copy of its ray (origin | face, direction | bsdf pdf)
+    uint32_t *aqueue[2];
+    float4 *ajob[2];              // 2 float4 per job
     uint4 *hitbuf;                // light hits: (pixel, instance, leaf, b1 bits), then (b2 bits, 0, 0, 0)
     float *hitval;                // light-sampling pdf of each hit
     uint2 *jmeta;                 // per any-hit job: (first hit, hit count)

@@ -209,7 +209,8 @@ struct Renderer {
     float4 *ray_o = nullptr, *ray_d = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};
     uint32_t *counters = nullptr;         // CNT_* words of vrg_frame.cuh
-    uint32_t *aqueue = nullptr;           // any-hit job queue
+    uint32_t *aqueue[2] = {nullptr, nullptr};  // light-pdf jobs by bounce parity
+    float4 *ajob[2] = {nullptr, nullptr};      // their ray copies (2 float4 per job)
     int4 *hits = nullptr;                 // closest hit per pixel
     uint4 *hitbuf = nullptr;              // light hits of the any-hit pass
     float *hitval = nullptr;
@@ -236,6 +237,9 @@ struct Renderer {
     size_t h_pinned_bytes = 0;
     cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t lps = nullptr;           // light-pdf stream: bounce b's walk beside bounce b + 1
+    cudaEvent_t ev_shaded[8] = {}, ev_lpdone[8] = {};  // dependency events per bounce
+    cudaEvent_t ev_lp[2][8] = {};         // timing: light-pdf passes of bounce b begin / end
     cudaEvent_t ev[16] = {};
     cudaEvent_t ev_k[2][8] = {};          // after k_trace / after k_shade, per bounce
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
