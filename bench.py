@@ -98,7 +98,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -107,9 +107,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, window=None):
+        """Summary of the samples taken inside window = (t0, t1) (perf_counter
+        seconds; all samples if none fell inside it)."""
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -120,7 +122,10 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = [ln for t, ln in self.lines if window is None or window[0] <= t <= window[1]]
+        if not lines:
+            lines = [ln for _, ln in self.lines]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -197,7 +202,7 @@ C2_SCENES = 64
 C2_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
 
 
-def batched_block(ctx, steps, warmup):
+def batched_block(ctx, steps, warmup, tuning=None):
     """Batched workload: 64 independent scenes, chunk grids drawn from 1x1..8x8
     and resolutions from {256^2, 640x480, 1280x720, 1920x1080}, each with its
     own terrain seed and orbit camera, 2 bounces + ReSTIR (1 temporal, 3
@@ -225,6 +230,8 @@ def batched_block(ctx, steps, warmup):
     vrg.commit_scenes(scenes)  # all top-level trees in one SAH build, all lamp trees in another
     t_tl = time.perf_counter() - t0
     br = vrg.BatchRenderer(ctx, res, 2)
+    if tuning is not None:  # the launch configuration tuned on the single-view workload
+        br.set_tuning(tuning)
     seeds = vrg.Pcg32(C2_SEED)
 
     def step(f, flags):
@@ -238,6 +245,7 @@ def batched_block(ctx, steps, warmup):
         return st.ms_total, st.rays_closest + st.rays_any
 
     out = {"workload": "batched-64-scenes", "scenes": C2_SCENES, "pixels": br.pixels,
+           "tuning": None if tuning is None else tuning.as_dict(),
            "chunks": int((grids[:, 0] * grids[:, 1]).sum()), "bounces": 2,
            "resolutions": {f"{w}x{h}": sum(1 for r in res if r == (w, h)) for w, h in C2_RES},
            "upload_s": round(t_upload, 3), "blas_build_ms": round(1000 * t_blas, 2),
@@ -481,7 +489,7 @@ def run_ours(args, d):
 
     for f in range(args.warmup):
         render(f, out_dev, stats)
-    tuning = None
+    tuning, best_tuning = None, None
     if not args.no_autotune:
         # launch configuration chosen by the autotuner on this workload's
         # frames (scheduling only; the frames it renders are not counted and
@@ -493,13 +501,38 @@ def run_ours(args, d):
         cam0 = vrg.orbit_camera(NX, NZ, 0, ORBIT, W, H)
         t0 = time.perf_counter()
         best, best_ms = r.autotune(scene, cam0, frame_params(0), frames=3)
+        best_tuning = best
         tuning = {"config": best.as_dict(), "tuned_ms": round(best_ms, 4),
                   "default_ms": round(float(np.median(default_ms)), 4),
                   "tuner_seconds": round(time.perf_counter() - t0, 2)}
-    # device-timed frames
+    # Timed region: the K frames enqueued back to back (no per-frame stats, so
+    # frames are in flight together as in an interactive loop), bracketed by
+    # CUDA events on the library's own stream with a synchronize on both sides.
+    import torch
+    dev_ord = d.local if args.gpus > 1 else 0
+    torch.cuda.set_device(dev_ord)
+    lib_stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", dev_ord))
+    blob = r.save_state()  # the breakdown pass below replays the same frames from here
+    torch.cuda.synchronize()
     d.barrier()
     clk = ClockSampler(d.local)
     clk.start()
+    time.sleep(0.25)  # the sampler's first reading lands before the region
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    ev0.record(lib_stream)
+    for s in range(args.steps):
+        render(args.warmup + s, out_dev, None)
+    ev1.record(lib_stream)
+    ev1.synchronize()
+    w1 = time.perf_counter()
+    time.sleep(0.15)
+    clocks = clk.stop((w0, w1 + 0.1))
+    total_s = ev0.elapsed_time(ev1) / 1000.0
+    # Replay of the same K frames, one at a time with stats: their ray counts
+    # (identical frames: the renderer state is restored) and the per-stage
+    # CUDA-event breakdown
+    r.load_state(blob)
     ms, rays, ms_b, ms_res, ms_sp = [], 0, [0.0] * NB, 0.0, 0.0
     ms_tr, ms_sh, ms_ah = [0.0] * NB, [0.0] * NB, [0.0] * NB
     closest, nodes, leaves = 0, 0, 0
@@ -519,8 +552,6 @@ def run_ours(args, d):
             ms_ah[b] += stats.ms_anyhit[b]
         ms_res += stats.ms_resolve
         ms_sp += stats.ms_spatial
-    clocks = clk.stop()
-    total_s = sum(ms) / 1000.0
     d.barrier()
     total_s_max = d.max(total_s)
     rays_all = d.sum(rays)
@@ -535,14 +566,16 @@ def run_ours(args, d):
         host_img = np.empty(W * H * 4, np.uint8)
         img_ptr = host_img.ctypes.data
     out_host = vrg.FrameOutput(img_ptr, None, 1, 0)
+    # the same K frames again (state restored), each returning its image in
+    # host memory before the call returns; wall clock, same ray counts
+    r.load_state(blob)
+    torch.cuda.synchronize()
     d.barrier()
     t0 = time.perf_counter()
-    e2e_rays = 0
     for s in range(0 if args.no_e2e else args.steps):
-        render(args.warmup + args.steps + s, out_host, stats)
-        e2e_rays += stats.rays_closest + stats.rays_any
+        render(args.warmup + s, out_host, None)
     e2e_s = d.max(time.perf_counter() - t0)
-    e2e_value = d.sum(e2e_rays) / e2e_s / 1e6 if e2e_rays else None
+    e2e_value = rays_all / e2e_s / 1e6 if not args.no_e2e else None
     if d.rank != 0:
         d.close()
         return
@@ -587,7 +620,7 @@ def run_ours(args, d):
     batched = None
     if not args.no_batched:
         r.close()  # the batch needs the memory of the 1080p renderer
-        batched = batched_block(ctx, steps=16, warmup=3)
+        batched = batched_block(ctx, steps=16, warmup=3, tuning=best_tuning)
     upd_ms = update_commit_ms(scene, NX, NZ)
     cpu_frames = args.cpu_frames
     cpu_mr, cpu_dt, cpu_rays = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0) if not args.no_cpu
@@ -601,6 +634,9 @@ def run_ours(args, d):
                    "bounces": NB, "temporal_history": 1, "spatial_neighbours": 3, "radius_px": 30,
                    "m_cap": 20, "emissive_fraction": EMISSIVE, "orbit_frames": ORBIT,
                    "l2": "per-frame state (~1.2 GB of rays, records, reservoirs) exceeds L2; BVH L2-resident",
+                   "timing": "K frames enqueued back to back on the library stream (frames in flight), "
+                             "CUDA events on that stream; ray counts and stage times from a replay of the "
+                             "same frames one at a time",
                    "parallelism": f"replicas{args.gpus}"},
         "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b],
                          "k_trace": [round(x / args.steps, 4) for x in ms_tr],
@@ -608,6 +644,7 @@ def run_ours(args, d):
                          "k_anyhit": [round(x / args.steps, 4) for x in ms_ah],
                          "resolve_temporal": round(ms_res / args.steps, 4),
                          "spatial_finalize_pack": round(ms_sp / args.steps, 4)},
+        "ms_per_frame_alone": round(sum(ms) / max(args.steps, 1), 4),
         "rays_per_frame": rays // max(args.steps, 1),
         "scene_build_ms": round(build_s * 1000, 2),
         "update_commit_ms": upd_ms,

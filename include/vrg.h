@@ -151,7 +151,8 @@ typedef struct vrg_frame_output {
 
 typedef struct vrg_frame_stats {
     float ms_total;            /* device time of the whole frame (CUDA events) */
-    float ms_bounce[8];        /* per bounce: closest hit + shading + light-pdf walk */
+    float ms_bounce[8];        /* per bounce: closest hit + shading (the light-pdf walk of
+                                  bounce b runs on its own stream beside bounce b+1) */
     float ms_resolve;          /* outgoing radiance + temporal (+ cache inference/training) */
     float ms_spatial;          /* spatial + finalize + pack */
     uint64_t rays_closest;     /* closest-hit queries issued */
@@ -160,7 +161,8 @@ typedef struct vrg_frame_stats {
     uint32_t reserved;
     float ms_trace[8];         /* per bounce: k_trace alone */
     float ms_shade[8];         /* per bounce: k_shade alone */
-    float ms_anyhit[8];        /* per bounce: k_anyhit alone */
+    float ms_anyhit[8];        /* per bounce: the light-pdf walk (k_anyhit, k_hit_eval,
+                                  k_hit_sum) on its stream */
     uint64_t nodes_visited;    /* closest-hit traversal: 4-wide inner nodes fetched (128 B each) */
     uint64_t leaves_visited;   /* closest-hit traversal: surface-block records tested (16 B each) */
 } vrg_frame_stats;
@@ -173,6 +175,11 @@ typedef struct vrg_renderer vrg_renderer;
 /* ---- context ---------------------------------------------------------- */
 VRG_API vrg_status vrg_context_create(const vrg_context_desc *desc, vrg_context **out);
 VRG_API vrg_status vrg_context_destroy(vrg_context *ctx);
+/* The cudaStream_t the context submits on (the queue the reference's Scene
+ * and Renderer submit to, scene.rs:112, interactive_rendering.rs:447).  A
+ * caller orders its own work after a frame, or times frames with CUDA events,
+ * on this stream. */
+VRG_API vrg_status vrg_context_stream(vrg_context *ctx, void **stream);
 VRG_API const char *vrg_status_string(vrg_status s);
 VRG_API const char *vrg_last_error(void);
 
@@ -260,7 +267,14 @@ VRG_API vrg_status vrg_image_write_png(const char *path, const uint8_t *bgra8, u
 VRG_API vrg_status vrg_image_write_pfm(const char *path, const float *rgb, uint32_t width, uint32_t height);
 /* Renderer::render.  frame_index = the renderer's frame counter, advanced by
  * one per call (interactive_rendering.rs:1668); the raytrace invocation seed
- * is frame_index*num_bounces + bounce (:1189). */
+ * is frame_index*num_bounces + bounce (:1189).
+ * With stats == NULL and device (or no) outputs the call only enqueues the
+ * frame and returns; the frame is complete when the library's stream has
+ * passed it.  Such frames are in flight together, as the reference's frames
+ * in flight are: a frame's primary closest hit starts beside the previous
+ * frame's resolve and spatial passes (it reads only the committed scene and
+ * the camera).  The images are those of frames rendered one by one.  With
+ * stats the frame runs alone and is timed stage by stage. */
 VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
                               const vrg_render_params *params, const vrg_frame_output *out,
                               vrg_frame_stats *stats);

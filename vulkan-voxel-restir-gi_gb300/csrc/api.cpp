@@ -17,6 +17,8 @@ vrg_status upload_frames(cudaStream_t s);
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
                          uint32_t max_rays);
 vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, uint32_t max_rays);
+vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
+vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
@@ -115,6 +117,12 @@ VRG_API vrg_status vrg_context_create(const vrg_context_desc *desc, vrg_context 
         return st;
     }
     *out = c;
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_context_stream(vrg_context *ctx, void **stream) {
+    if (!ctx || !stream) return VRG_ERR_INVALID_ARGUMENT;
+    *stream = (void *)ctx->stream;
     return VRG_OK;
 }
 
@@ -484,6 +492,8 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->radiance = (float *)(B + o_rad);
     r->accum = (double *)(B + o_acc);
     VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, r->ctx->stream));
+    // the next frame's early closest hit starts after this clear
+    if (r->ev_next_ok) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, r->ctx->stream));
     r->out_buf.reset();
     r->radiance_out = nullptr;
     if (r->scale > 1) {
@@ -521,6 +531,10 @@ static vrg_status renderer_events(vrg_renderer *r) {
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
+    VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->pre, cudaStreamNonBlocking));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_next_ok, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_pre, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, r->ctx->stream));  // after the buffers' clear
     r->grid_bounce = r->ctx->num_sms * bounce_blocks_per_sm();
     return VRG_OK;
 }
@@ -644,6 +658,12 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
         cudaStreamSynchronize(r->lps);
         cudaStreamDestroy(r->lps);
     }
+    if (r->pre) {
+        cudaStreamSynchronize(r->pre);
+        cudaStreamDestroy(r->pre);
+    }
+    if (r->ev_next_ok) cudaEventDestroy(r->ev_next_ok);
+    if (r->ev_pre) cudaEventDestroy(r->ev_pre);
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
     if (r->aux) {
@@ -915,11 +935,29 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // resolve and spatial (nothing of one branch reads what the other writes;
 // the training step's weights serve the next frame, after the join).  With
 // capture the frame stays on one stream.
-static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) {
+// pipelined: frames in flight.  The primary closest hit of this frame reads
+// only the committed scene and the camera and writes only the hit buffer and
+// the counters; the previous frame's resolve and spatial passes read neither.
+// So it runs on its own stream as soon as the previous frame's bounces and
+// light-pdf walks are done (ev_next_ok), beside that frame's resolve and
+// spatial passes; the library stream waits for it before this frame's shading,
+// so the frame is complete on the library stream when its work there is.
+// Scene commits synchronize the library stream before they return, so a
+// scene's device data is final before any frame reads it.
+static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, bool pipelined = false) {
     cudaStream_t s = r->ctx->stream;
     const bool fork = a.cache && !a.capture;
     const uint32_t nb_main = fork ? a.nb_render : a.nb;
-    VRG_CUDA_TRY(cudaMemsetAsync(r->counters, 0, CNT_WORDS * 4, s));
+    const bool early = pipelined && !a.cache && !a.capture && !a.views && !timed;
+    if (early) {
+        VRG_CUDA_TRY(cudaStreamWaitEvent(r->pre, r->ev_next_ok, 0));
+        VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, r->pre));
+        VRG_TRY(launch_trace(r->pre, a, 0, 0));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_pre, r->pre));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_pre, 0));
+    } else {
+        VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, s));
+    }
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
     // Bounce b's light-pdf walk runs on the light-pdf stream beside bounce
     // b + 1's closest hit and shading.  Ordering: the walk of b waits for the
@@ -928,7 +966,8 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) 
     int last_lp = -1;
     for (uint32_t b = 0; b < nb_main; b++) {
         if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[b - 2], 0));
-        VRG_TRY(launch_trace_shade(s, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
+        if (early && b == 0) VRG_TRY(launch_shade(s, a, 0, 0));
+        else VRG_TRY(launch_trace_shade(s, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
         if (timed) {
             VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
             VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
@@ -944,6 +983,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) 
         }
     }
     if (last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[last_lp], 0));
+    // a plain frame's resolve and spatial passes read neither the hit buffer
+    // nor the counters: the next frame's early closest hit may start here
+    if (!a.views && !a.cache && !a.capture) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, s));
     cudaStream_t st = s;  // stream of the training branch
     if (fork) {
         st = r->aux;
@@ -955,22 +997,23 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed) 
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], st));
         }
         VRG_TRY(launch_train_targets(st, a));
-        VRG_TRY(nrc_train(r->cache, st, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true, r->counters + CNT_ERROR));
+        VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
+                          nullptr, r->target, true, a.counters + CNT_ERROR));
         VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
     }
     if (a.cache)  // radiance-cache queries of every path that ends into the cache
-        VRG_TRY(nrc_infer(r->cache, s, a.P, r->counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
-                          r->pred, r->counters + CNT_ERROR));
+        VRG_TRY(nrc_infer(r->cache, s, a.P, a.counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
+                          r->pred, a.counters + CNT_ERROR));
     VRG_TRY(launch_resolve(s, a));
     if (a.cache && !fork) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));
-        VRG_TRY(nrc_train(r->cache, s, a.train_cap, r->counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true, r->counters + CNT_ERROR));
+        VRG_TRY(nrc_train(r->cache, s, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
+                          nullptr, r->target, true, a.counters + CNT_ERROR));
     }
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
     if (fork) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_join, 0));
+    if (!a.views && (a.cache || a.capture)) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, s));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 2], s));
     return VRG_OK;
 }
@@ -1014,7 +1057,7 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
         stats->ms_total = ms;
     }
     uint32_t cnt[CNT_WORDS];
-    VRG_CUDA_TRY(cudaMemcpy(cnt, r->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    VRG_CUDA_TRY(cudaMemcpy(cnt, a.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
     uint64_t rays, any, nn, nlv;
     memcpy(&rays, cnt + CNT_RAYS, 8);
     memcpy(&any, cnt + CNT_ANY, 8);
@@ -1085,7 +1128,8 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
             if (out->bgra8) a.bgra = out->bgra8;
         }
     }
-    VRG_TRY(frame_launch(r, a, true));
+    // without stats the frame is not timed and may start beside the previous one
+    VRG_TRY(frame_launch(r, a, stats != nullptr, stats == nullptr));
     if (out && out->host) {
         const size_t Po = (size_t)r->out_w * r->out_h;
         if (out->bgra8 && a.pack)

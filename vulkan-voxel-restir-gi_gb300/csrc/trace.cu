@@ -986,24 +986,37 @@ static void bounce_grids(const FrameArgs &a, uint32_t max_rays, int &gt, int &gs
     }
 }
 
-// closest hit and shading of bounce b
-vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace,
-                              uint32_t max_rays) {
-    const bool batch = a.views != nullptr;
-    if (batch && a.capture) {
-        set_error("capture is not available for batched frames");
-        return VRG_ERR_UNSUPPORTED;
-    }
+// closest hit of bounce b
+vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
     int gt, gs, ga;
     bounce_grids(a, max_rays, gt, gs, ga);
-    if (batch) k_trace<true><<<gt, 128, 0, s>>>(a, b);
+    if (a.views) k_trace<true><<<gt, 128, 0, s>>>(a, b);
     else k_trace<false><<<gt, 128, 0, s>>>(a, b);
-    if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
-    if (batch) k_shade<false, true><<<gs, 128, 0, s>>>(a, b);
+    VRG_CUDA_TRY(cudaGetLastError());
+    return VRG_OK;
+}
+
+// shading of bounce b
+vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
+    int gt, gs, ga;
+    bounce_grids(a, max_rays, gt, gs, ga);
+    if (a.views) k_shade<false, true><<<gs, 128, 0, s>>>(a, b);
     else if (a.capture) k_shade<true, false><<<gs, 128, 0, s>>>(a, b);
     else k_shade<false, false><<<gs, 128, 0, s>>>(a, b);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
+}
+
+// closest hit and shading of bounce b
+vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace,
+                              uint32_t max_rays) {
+    if (a.views && a.capture) {
+        set_error("capture is not available for batched frames");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    VRG_TRY(launch_trace(s, a, b, max_rays));
+    if (ev_trace) VRG_CUDA_TRY(cudaEventRecord(ev_trace, s));
+    return launch_shade(s, a, b, max_rays);
 }
 
 // the light-pdf walk of bounce b's jobs (bounces before the last): it reads only

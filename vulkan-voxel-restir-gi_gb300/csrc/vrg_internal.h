@@ -238,6 +238,11 @@ struct Renderer {
     cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t lps = nullptr;           // light-pdf stream: bounce b's walk beside bounce b + 1
+    // frames in flight: a frame's primary closest hit runs on `pre` beside the
+    // previous frame's resolve and spatial passes, once `ev_next_ok` (the
+    // previous frame's last reader of the hit buffer and counters) has passed
+    cudaStream_t pre = nullptr;
+    cudaEvent_t ev_next_ok = nullptr, ev_pre = nullptr;
     cudaEvent_t ev_shaded[8] = {}, ev_lpdone[8] = {};  // dependency events per bounce
     cudaEvent_t ev_lp[2][8] = {};         // timing: light-pdf passes of bounce b begin / end
     cudaEvent_t ev[16] = {};

@@ -115,6 +115,7 @@ _P = C.c_void_p
 SIGNATURES = [
     ("vrg_context_create", C.c_int32, [C.POINTER(ContextDesc), C.POINTER(_P)]),
     ("vrg_context_destroy", C.c_int32, [_P]),
+    ("vrg_context_stream", C.c_int32, [_P, C.POINTER(C.c_void_p)]),
     ("vrg_status_string", C.c_char_p, [C.c_int32]),
     ("vrg_last_error", C.c_char_p, []),
     ("vrg_material_table_set", C.c_int32, [_P, C.POINTER(Material), C.c_uint32]),
@@ -277,6 +278,12 @@ class Context:
     def adopt(self, obj):
         self._children.add(obj)
         return obj
+
+    def stream(self) -> int:
+        """The cudaStream_t the library submits on, as an integer handle."""
+        p = C.c_void_p()
+        check(self.lib.vrg_context_stream(self.h, C.byref(p)), "vrg_context_stream")
+        return p.value or 0
 
     def set_materials(self, mats, n=None):
         n = len(mats) if n is None else n
@@ -535,6 +542,12 @@ class Renderer:
         check(self.ctx.lib.vrg_debug_readback(self.h, what, _ptr(a), a.nbytes), "vrg_debug_readback")
         return a
 
+    def resize(self, width: int, height: int):
+        """Renderer::rebuild(extent) (interactive_rendering.rs:818): new frame
+        buffers, frame counter and history reset."""
+        check(self.ctx.lib.vrg_renderer_resize(self.h, width, height), "vrg_renderer_resize")
+        self.width, self.height = width, height
+
     def read_accumulation(self):
         n = C.c_uint32()
         w, h = self.width * self.scale, self.height * self.scale
@@ -605,6 +618,9 @@ class BatchRenderer:
     def set_cache(self, cache):
         check(self.ctx.lib.vrg_renderer_set_cache(self.h, None if cache is None else cache.h),
               "vrg_renderer_set_cache")
+
+    def set_tuning(self, tuning: "Tuning"):
+        check(self.ctx.lib.vrg_renderer_set_tuning(self.h, C.byref(tuning)), "vrg_renderer_set_tuning")
 
     def reset_accumulation(self):
         check(self.ctx.lib.vrg_renderer_reset_accumulation(self.h), "vrg_renderer_reset_accumulation")
