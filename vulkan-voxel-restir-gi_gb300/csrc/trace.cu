@@ -236,6 +236,19 @@ __device__ __forceinline__ bool slab_fma(float lox, float hix, float loy, float 
     return tn <= tf;
 }
 
+// Pops the next pending child whose box starts at or before best_t (boxes
+// are culled only when strictly beyond it); false when none is left.
+__device__ __forceinline__ bool pop_near(const int *stack, const float *tstk, int &sp, float best_t, int &node) {
+    while (sp > 0) {
+        --sp;
+        if (tstk[sp] <= best_t) {
+            node = stack[sp];
+            return true;
+        }
+    }
+    return false;
+}
+
 __device__ __forceinline__ void cswap(float &ta, int &ra, float &tb, int &rb) {
     if (tb < ta) {
         const float t = ta; ta = tb; tb = t;
@@ -314,7 +327,11 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     int node = 0, sp = 0, hrec = -1;
     uint32_t hfh = 0;
     int px = 0, py = 2, pz = 4;  // float4 index of the near plane per axis (the far one is next to it)
+    // pending children with their entry distances: a popped entry whose box
+    // starts beyond the current best t is dropped unvisited (every box below
+    // it starts no nearer, so each would be culled by its own test)
     int stack[TRAV_STACK];
+    float tstk[TRAV_STACK];
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
         if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
@@ -365,14 +382,13 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                 slab4(NX, FX, NY, FY, NZ, FZ, RF, inv, oi, EPS_TRACE, best_t, tk, rk);
                 // tk sorted ascending (misses at +inf)
                 if (tk[0] == INFINITY) {
-                    if (sp == 0) done = true;
-                    else node = stack[--sp];
+                    done = !pop_near(stack, tstk, sp, best_t, node);
                 } else {
                     node = rk[0];
                     if (sp + 3 <= TRAV_STACK) {
-                        if (tk[3] != INFINITY) stack[sp++] = rk[3];
-                        if (tk[2] != INFINITY) stack[sp++] = rk[2];
-                        if (tk[1] != INFINITY) stack[sp++] = rk[1];
+                        if (tk[3] != INFINITY) { stack[sp] = rk[3]; tstk[sp++] = tk[3]; }
+                        if (tk[2] != INFINITY) { stack[sp] = rk[2]; tstk[sp++] = tk[2]; }
+                        if (tk[1] != INFINITY) { stack[sp] = rk[1]; tstk[sp++] = tk[1]; }
                     } else {
                         atomicOr(err, ERR_STACK);
                     }
@@ -404,8 +420,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                         }
                     }
                 }
-                if (sp == 0) done = true;
-                else node = stack[--sp];
+                done = !pop_near(stack, tstk, sp, best_t, node);
             }
             if (done) {
                 a.hits[p] = make_int4(hrec, (int)hfh, __float_as_int(hb1), __float_as_int(hb2));
