@@ -138,14 +138,21 @@ typedef struct vrg_render_params {
 #define VRG_RENDER_GRAPH 16u       /* batched frames: record the frame's launch sequence once
                                       in a CUDA graph and replay it (see vrg_render_batched) */
 
-/* Where the frame goes.  Pointers may be NULL (not written).  host != 0 means
- * the pointers are host memory and the library copies the frame back before
- * vrg_render returns (the e2e path); host == 0 means device pointers written
- * on the library's stream. */
+/* Where the frame goes.  Pointers may be NULL (not written).
+ *   host == VRG_OUTPUT_DEVICE: device pointers, written on the library's stream;
+ *   host == VRG_OUTPUT_HOST: host memory, copied back before the call returns;
+ *   host == VRG_OUTPUT_HOST_ASYNC: host memory (page-locked for the copy to
+ *     overlap), copied on the library's stream after the frame; the call returns
+ *     at once and the buffer holds the frame once vrg_renderer_wait_frame says
+ *     that frame is done.  This is the readback of the reference's frames in
+ *     flight, each fenced (interactive_rendering.rs:1633-1660). */
+#define VRG_OUTPUT_DEVICE 0u
+#define VRG_OUTPUT_HOST 1u
+#define VRG_OUTPUT_HOST_ASYNC 2u
 typedef struct vrg_frame_output {
     uint8_t *bgra8;        /* W*H*4 bytes, B,G,R,255 (postprocess.rs:78) */
     float *radiance;       /* W*H*3 floats: the view selected by debug_view */
-    uint32_t host;
+    uint32_t host;         /* VRG_OUTPUT_* */
     uint32_t reserved;
 } vrg_frame_output;
 
@@ -180,6 +187,8 @@ VRG_API vrg_status vrg_context_destroy(vrg_context *ctx);
  * caller orders its own work after a frame, or times frames with CUDA events,
  * on this stream. */
 VRG_API vrg_status vrg_context_stream(vrg_context *ctx, void **stream);
+/* Waits until everything submitted on the context's stream is done. */
+VRG_API vrg_status vrg_context_synchronize(vrg_context *ctx);
 VRG_API const char *vrg_status_string(vrg_status s);
 VRG_API const char *vrg_last_error(void);
 
@@ -279,6 +288,11 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
                               const vrg_render_params *params, const vrg_frame_output *out,
                               vrg_frame_stats *stats);
 VRG_API vrg_status vrg_renderer_frame_index(vrg_renderer *r, uint32_t *frame_index);
+/* Blocks until frame frame_index of this renderer (and its copies out) is
+ * done: the fence of a frame in flight (the reference signals a fence per
+ * frame slot, interactive_rendering.rs:1652, and waits on it before reusing
+ * the slot, :1634-1642).  A frame index not yet rendered is an error. */
+VRG_API vrg_status vrg_renderer_wait_frame(vrg_renderer *r, uint32_t frame_index);
 VRG_API vrg_status vrg_renderer_reset_accumulation(vrg_renderer *r);
 /* Accumulated mean radiance (W*H*3 floats, host) after n frames with accumulate=1. */
 VRG_API vrg_status vrg_renderer_read_accumulation(vrg_renderer *r, float *rgb, uint32_t *n_frames);
@@ -335,9 +349,11 @@ VRG_API vrg_status vrg_renderer_set_tuning(vrg_renderer *r, const vrg_tuning *t)
 VRG_API vrg_status vrg_renderer_get_tuning(vrg_renderer *r, vrg_tuning *t);
 /* Autotuner: renders frames of (scene, cam, params) under candidate launch
  * configurations, one field at a time over its candidate values (coordinate
- * descent, two passes), each candidate timed as the median device time of
- * `frames` frames after one untimed frame; installs the fastest and returns
- * it with its time.  The tuning frames do not count: the frame counter,
+ * descent, two passes).  Each candidate is timed as frames are rendered in
+ * use: `frames` frames enqueued back to back (frames in flight), bracketed by
+ * CUDA events on the library stream, after one untimed frame; the median of
+ * three such runs, per frame.  Installs the fastest and returns it with its
+ * time per frame.  The tuning frames do not count: the frame counter,
  * reservoir history and accumulation are restored afterwards.  Single-view
  * renderers; params must not carry VRG_RENDER_CACHE / CAPTURE / GRAPH (the
  * result applies to those frames as well). */

@@ -112,3 +112,50 @@ def test_frames_in_flight_after_resize(gpu_ctx):
     sc.close()
     for o in objs:
         o.release()
+
+
+def test_async_host_readback_with_frame_fences(gpu_ctx):
+    """VRG_OUTPUT_HOST_ASYNC: each frame's image and radiance are copied into
+    page-locked host buffers behind the frame, the call returns at once, and
+    vrg_renderer_wait_frame fences each frame before its buffers are read.
+    Two buffer sets alternate, as in an interactive loop; every frame equals
+    the frame rendered one by one."""
+    lib = gpu_ctx.lib
+    sc_a, objs_a = _world(gpu_ctx)
+    sc_b, objs_b = _world(gpu_ctx)
+    ra = vrg.Renderer(gpu_ctx, W, H, NB)
+    want = []
+    for f in range(FRAMES):
+        img, rad = ra.render_params(sc_a, _cam(f), _p(f), want_image=True, want_radiance=True)
+        want.append((img.copy(), rad.copy()))
+    rb = vrg.Renderer(gpu_ctx, W, H, NB)
+    pinned = [(torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True),
+               torch.empty(W * H * 3, dtype=torch.float32, pin_memory=True)) for _ in range(2)]
+    got = []
+    for f in range(FRAMES):
+        img_t, rad_t = pinned[f % 2]
+        out = vrg.FrameOutput(img_t.data_ptr(), rad_t.data_ptr(), vrg.OUTPUT_HOST_ASYNC, 0)
+        cam, p = _cam(f), _p(f)
+        vrg.check(lib.vrg_render(rb.h, sc_b.h, C.byref(cam), C.byref(p), C.byref(out), None), "vrg_render")
+        if f >= 1:  # the previous frame's buffers, once its fence has passed
+            rb.wait_frame(f - 1)
+            pi, pr = pinned[(f - 1) % 2]
+            got.append((pi.numpy().copy(), pr.numpy().copy()))
+    rb.wait_frame(FRAMES - 1)
+    pi, pr = pinned[(FRAMES - 1) % 2]
+    got.append((pi.numpy().copy(), pr.numpy().copy()))
+    for f in range(FRAMES):
+        assert np.array_equal(got[f][0].reshape(H, W, 4), want[f][0]), f
+        assert np.array_equal(got[f][1].reshape(H, W, 3).view(np.uint32), want[f][1].view(np.uint32)), f
+    # a frame not rendered yet has no fence; an unknown output kind is refused
+    assert lib.vrg_renderer_wait_frame(rb.h, FRAMES) == vrg.ERR_INVALID_ARGUMENT
+    bad = vrg.FrameOutput(None, None, 3, 0)
+    cam, p = _cam(0), _p(0)
+    assert lib.vrg_render(rb.h, sc_b.h, C.byref(cam), C.byref(p), C.byref(bad), None) == vrg.ERR_INVALID_ARGUMENT
+    gpu_ctx.synchronize()
+    for r in (ra, rb):
+        r.close()
+    for sc, objs in ((sc_a, objs_a), (sc_b, objs_b)):
+        sc.close()
+        for o in objs:
+            o.release()

@@ -126,6 +126,12 @@ VRG_API vrg_status vrg_context_stream(vrg_context *ctx, void **stream) {
     return VRG_OK;
 }
 
+VRG_API vrg_status vrg_context_synchronize(vrg_context *ctx) {
+    if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
+    VRG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return VRG_OK;
+}
+
 VRG_API vrg_status vrg_context_destroy(vrg_context *ctx) {
     if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
     for (Object *o : ctx->pending) release_object(o);
@@ -535,6 +541,7 @@ static vrg_status renderer_events(vrg_renderer *r) {
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_next_ok, cudaEventDisableTiming));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_pre, cudaEventDisableTiming));
     VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, r->ctx->stream));  // after the buffers' clear
+    for (auto &e : r->ev_fence) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     r->grid_bounce = r->ctx->num_sms * bounce_blocks_per_sm();
     return VRG_OK;
 }
@@ -663,6 +670,8 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
         cudaStreamDestroy(r->pre);
     }
     if (r->ev_next_ok) cudaEventDestroy(r->ev_next_ok);
+    for (auto &e : r->ev_fence)
+        if (e) cudaEventDestroy(e);
     if (r->ev_pre) cudaEventDestroy(r->ev_pre);
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
@@ -1075,11 +1084,14 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
     return VRG_OK;
 }
 
-static void frame_done(vrg_renderer *r, const FrameArgs &a, const vrg_render_params *pr) {
+// after the frame's launches and copies out: its fence, then the counters
+static vrg_status frame_done(vrg_renderer *r, const FrameArgs &a, const vrg_render_params *pr) {
+    VRG_CUDA_TRY(cudaEventRecord(r->ev_fence[r->frame % Renderer::FENCES], r->ctx->stream));
     r->last_nb = a.nb;
     r->captured = a.capture != 0;
     if (pr->accumulate) r->accum_n++;
     r->frame++;
+    return VRG_OK;
 }
 
 VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
@@ -1099,6 +1111,7 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
         return VRG_ERR_UNSUPPORTED;
     }
     if (scene->ctx != r->ctx) return VRG_ERR_INVALID_ARGUMENT;
+    if (out && out->host > VRG_OUTPUT_HOST_ASYNC) return VRG_ERR_INVALID_ARGUMENT;
     cudaStream_t s = r->ctx->stream;
     // Renderer::render starts with scene.get_tlas() (interactive_rendering.rs:961)
     VRG_TRY(scene_commit(scene));
@@ -1139,9 +1152,21 @@ VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camer
             VRG_CUDA_TRY(cudaMemcpyAsync(out->radiance, r->scale > 1 ? a.out_radiance : a.radiance, Po * 12,
                                          cudaMemcpyDeviceToHost, s));
     }
-    frame_done(r, a, pr);
+    VRG_TRY(frame_done(r, a, pr));
     if (stats) return frame_stats(r, a, true, stats);
-    if (out && out->host) VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (out && out->host == VRG_OUTPUT_HOST) VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return VRG_OK;
+}
+
+VRG_API vrg_status vrg_renderer_wait_frame(vrg_renderer *r, uint32_t frame_index) {
+    if (!r) return VRG_ERR_INVALID_ARGUMENT;
+    if (frame_index >= r->frame) {
+        set_error("frame %u has not been rendered (next frame index %u)", frame_index, r->frame);
+        return VRG_ERR_INVALID_ARGUMENT;
+    }
+    // the slot holds this frame's fence or a later frame's (stream order: that
+    // one completes after this one)
+    VRG_CUDA_TRY(cudaEventSynchronize(r->ev_fence[frame_index % Renderer::FENCES]));
     return VRG_OK;
 }
 
@@ -1170,6 +1195,7 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
                       w.camera.height, r->vw[v], r->vh[v]);
             return VRG_ERR_INVALID_ARGUMENT;
         }
+        if (outs && outs[v].host > VRG_OUTPUT_HOST_ASYNC) return VRG_ERR_INVALID_ARGUMENT;
     }
     cudaStream_t s = r->ctx->stream;
     {
@@ -1259,10 +1285,10 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
             const cudaMemcpyKind k = o.host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
             if (o.bgra8 && a.pack) VRG_CUDA_TRY(cudaMemcpyAsync(o.bgra8, r->bgra + 4 * off, n * 4, k, s));
             if (o.radiance) VRG_CUDA_TRY(cudaMemcpyAsync(o.radiance, r->radiance + 3 * off, n * 12, k, s));
-            host_out |= o.host && (o.bgra8 || o.radiance);
+            host_out |= o.host == VRG_OUTPUT_HOST && (o.bgra8 || o.radiance);
         }
     }
-    frame_done(r, a, pr);
+    VRG_TRY(frame_done(r, a, pr));
     if (stats) return frame_stats(r, a, !graph, stats);
     if (host_out) VRG_CUDA_TRY(cudaStreamSynchronize(s));
     return VRG_OK;
@@ -1374,16 +1400,21 @@ VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, cons
     const vrg_tuning user = r->tune;
     vrg_render_params p = *params;
     p.accumulate = 0;
+    // per frame, as frames run in use: back to back, in flight
     auto measure = [&](const vrg_tuning &t, float *ms_out) -> vrg_status {
         r->tune = t;
-        std::vector<float> ms;
-        vrg_frame_stats st;
-        for (uint32_t f = 0; f <= frames; f++) {
-            VRG_TRY(vrg_render(r, scene, cam, &p, nullptr, &st));
-            if (f) ms.push_back(st.ms_total);
+        VRG_TRY(vrg_render(r, scene, cam, &p, nullptr, nullptr));
+        float reps[3];
+        for (float &rep : reps) {
+            VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
+            for (uint32_t f = 0; f < frames; f++) VRG_TRY(vrg_render(r, scene, cam, &p, nullptr, nullptr));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev[1], s));
+            VRG_CUDA_TRY(cudaEventSynchronize(r->ev[1]));
+            VRG_CUDA_TRY(cudaEventElapsedTime(&rep, r->ev[0], r->ev[1]));
+            rep /= (float)frames;
         }
-        std::sort(ms.begin(), ms.end());
-        *ms_out = ms[ms.size() / 2];
+        std::sort(reps, reps + 3);
+        *ms_out = reps[1];
         return VRG_OK;
     };
     int occ[3], sms = 1;

@@ -243,6 +243,10 @@ struct Renderer {
     // previous frame's last reader of the hit buffer and counters) has passed
     cudaStream_t pre = nullptr;
     cudaEvent_t ev_next_ok = nullptr, ev_pre = nullptr;
+    // per-frame fences (frame index % FENCES): recorded after the frame and its
+    // copies out; vrg_renderer_wait_frame waits on them
+    static constexpr uint32_t FENCES = 8;
+    cudaEvent_t ev_fence[FENCES] = {};
     cudaEvent_t ev_shaded[8] = {}, ev_lpdone[8] = {};  // dependency events per bounce
     cudaEvent_t ev_lp[2][8] = {};         // timing: light-pdf passes of bounce b begin / end
     cudaEvent_t ev[16] = {};

@@ -95,6 +95,9 @@ class View(C.Structure):
                 ("spatial_seed", C.c_uint32)]
 
 
+OUTPUT_DEVICE, OUTPUT_HOST, OUTPUT_HOST_ASYNC = 0, 1, 2
+
+
 class FrameOutput(C.Structure):
     _fields_ = [("bgra8", C.c_void_p), ("radiance", C.c_void_p), ("host", C.c_uint32),
                 ("reserved", C.c_uint32)]
@@ -116,6 +119,8 @@ SIGNATURES = [
     ("vrg_context_create", C.c_int32, [C.POINTER(ContextDesc), C.POINTER(_P)]),
     ("vrg_context_destroy", C.c_int32, [_P]),
     ("vrg_context_stream", C.c_int32, [_P, C.POINTER(C.c_void_p)]),
+    ("vrg_context_synchronize", C.c_int32, [_P]),
+    ("vrg_renderer_wait_frame", C.c_int32, [_P, C.c_uint32]),
     ("vrg_status_string", C.c_char_p, [C.c_int32]),
     ("vrg_last_error", C.c_char_p, []),
     ("vrg_material_table_set", C.c_int32, [_P, C.POINTER(Material), C.c_uint32]),
@@ -278,6 +283,9 @@ class Context:
     def adopt(self, obj):
         self._children.add(obj)
         return obj
+
+    def synchronize(self):
+        check(self.lib.vrg_context_synchronize(self.h), "vrg_context_synchronize")
 
     def stream(self) -> int:
         """The cudaStream_t the library submits on, as an integer handle."""
@@ -541,6 +549,16 @@ class Renderer:
         a = np.zeros(shapes[what], dtype=dt)
         check(self.ctx.lib.vrg_debug_readback(self.h, what, _ptr(a), a.nbytes), "vrg_debug_readback")
         return a
+
+    def frame_index(self) -> int:
+        """The index the next frame will have."""
+        n = C.c_uint32()
+        check(self.ctx.lib.vrg_renderer_frame_index(self.h, C.byref(n)), "vrg_renderer_frame_index")
+        return n.value
+
+    def wait_frame(self, frame_index: int):
+        """Blocks until that frame (and its copies out) is done."""
+        check(self.ctx.lib.vrg_renderer_wait_frame(self.h, frame_index), "vrg_renderer_wait_frame")
 
     def resize(self, width: int, height: int):
         """Renderer::rebuild(extent) (interactive_rendering.rs:818): new frame
