@@ -277,13 +277,15 @@ VRG_API vrg_status vrg_image_write_pfm(const char *path, const float *rgb, uint3
 /* Renderer::render.  frame_index = the renderer's frame counter, advanced by
  * one per call (interactive_rendering.rs:1668); the raytrace invocation seed
  * is frame_index*num_bounces + bounce (:1189).
- * With stats == NULL and device (or no) outputs the call only enqueues the
- * frame and returns; the frame is complete when the library's stream has
- * passed it.  Such frames are in flight together, as the reference's frames
- * in flight are: a frame's primary closest hit starts beside the previous
- * frame's resolve and spatial passes (it reads only the committed scene and
- * the camera).  The images are those of frames rendered one by one.  With
- * stats the frame runs alone and is timed stage by stage. */
+ * With stats == NULL and device, asynchronous host or no outputs the call
+ * only enqueues the frame and returns; the frame is complete when the
+ * library's stream has passed it (or vrg_renderer_wait_frame returns).  Such
+ * frames are in flight together, as the reference's frames in flight are: a
+ * frame's first bounce starts beside the previous frame's resolve and spatial
+ * passes (it reads only the committed scene, the camera and the materials, and
+ * fills its own set of path records).  The images are those of frames
+ * rendered one by one.  With stats the frame runs alone and is timed stage by
+ * stage. */
 VRG_API vrg_status vrg_render(vrg_renderer *r, vrg_scene *scene, const vrg_camera *cam,
                               const vrg_render_params *params, const vrg_frame_output *out,
                               vrg_frame_stats *stats);

@@ -17,8 +17,6 @@ vrg_status upload_frames(cudaStream_t s);
 vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
                          uint32_t max_rays);
 vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, uint32_t max_rays);
-vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
-vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
@@ -457,12 +455,16 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     size_t o_hb = o; o += al(P * 2 * 32);
     size_t o_hv = o; o += al(P * 2 * 4);
     size_t o_jm = o; o += al(P * 8);
-    size_t o_nl = o; o += al(P);
-    size_t o_rec = o; o += al(P * 32 * nb);
-    size_t o_xv = o; o += al(P * 16);
-    size_t o_nv = o; o += al(P * 16);
-    size_t o_xs = o; o += al(P * 16);
-    size_t o_ns = o; o += al(P * 16);
+    const int sets = r->n_views ? 1 : 2;
+    size_t o_nl[2], o_rec[2], o_xv[2], o_nv[2], o_xs[2], o_ns[2];
+    for (int k = 0; k < sets; k++) {
+        o_nl[k] = o; o += al(P);
+        o_rec[k] = o; o += al(P * 32 * nb);
+        o_xv[k] = o; o += al(P * 16);
+        o_nv[k] = o; o += al(P * 16);
+        o_xs[k] = o; o += al(P * 16);
+        o_ns[k] = o; o += al(P * 16);
+    }
     size_t o_pl = o; o += al(P * 16);
     size_t o_sp = o; o += al(P * 80);
     size_t o_ft = o; o += al(P * 16);
@@ -485,12 +487,15 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->hitbuf = (uint4 *)(B + o_hb);
     r->hitval = (float *)(B + o_hv);
     r->jmeta = (uint2 *)(B + o_jm);
-    r->nlive = B + o_nl;
-    r->rec = (float4 *)(B + o_rec);
-    r->xv = (float4 *)(B + o_xv);
-    r->nv = (float4 *)(B + o_nv);
-    r->xs = (float4 *)(B + o_xs);
-    r->ns = (float4 *)(B + o_ns);
+    for (int k = 0; k < 2; k++) {
+        const int j = k < sets ? k : 0;
+        r->nlive[k] = B + o_nl[j];
+        r->rec[k] = (float4 *)(B + o_rec[j]);
+        r->xv[k] = (float4 *)(B + o_xv[j]);
+        r->nv[k] = (float4 *)(B + o_nv[j]);
+        r->xs[k] = (float4 *)(B + o_xs[j]);
+        r->ns[k] = (float4 *)(B + o_ns[j]);
+    }
     r->plain = (float4 *)(B + o_pl);
     r->spatial = (float4 *)(B + o_sp);
     r->final_t = (float4 *)(B + o_ft);
@@ -898,12 +903,13 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.jmeta = r->jmeta;
     a.hit_cap = (uint32_t)std::min<size_t>(2 * P, 0xFFFFFFF0u);
     a.counters = r->counters;
-    a.nlive = r->nlive;
-    a.rec = r->rec;
-    a.xv = r->xv;
-    a.nv = r->nv;
-    a.xs = r->xs;
-    a.ns = r->ns;
+    const uint32_t set = r->frame & 1u;
+    a.nlive = r->nlive[set];
+    a.rec = r->rec[set];
+    a.xv = r->xv[set];
+    a.nv = r->nv[set];
+    a.xs = r->xs[set];
+    a.ns = r->ns[set];
     a.plain = r->plain;
     a.res = r->res + (size_t)ring * 5 * P;
     a.spatial = r->spatial;
@@ -944,15 +950,19 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // resolve and spatial (nothing of one branch reads what the other writes;
 // the training step's weights serve the next frame, after the join).  With
 // capture the frame stays on one stream.
-// pipelined: frames in flight.  The primary closest hit of this frame reads
-// only the committed scene and the camera and writes only the hit buffer and
-// the counters; the previous frame's resolve and spatial passes read neither.
-// So it runs on its own stream as soon as the previous frame's bounces and
-// light-pdf walks are done (ev_next_ok), beside that frame's resolve and
-// spatial passes; the library stream waits for it before this frame's shading,
-// so the frame is complete on the library stream when its work there is.
-// Scene commits synchronize the library stream before they return, so a
-// scene's device data is final before any frame reads it.
+// pipelined: frames in flight.  The first bounce of this frame (closest hit
+// and shading) reads the committed scene, the camera and the material table,
+// and writes the hit buffer, the counters, the next bounce's rays and jobs and
+// this frame's set of path records (sets alternate by frame parity); the
+// previous frame's resolve and spatial passes read none of these but that
+// frame's own record set.  So the first bounce runs on its own stream as soon
+// as the previous frame's bounces and light-pdf walks are done (ev_next_ok),
+// beside that frame's resolve and spatial passes, and its light-pdf walk
+// follows on the walk stream; the library stream waits for the first bounce
+// before the second, so the frame is complete on the library stream when its
+// work there is.  Scene commits and material / atlas changes synchronize or
+// order the library stream before they return, so a scene's device data is
+// final before any frame reads it.
 static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, bool pipelined = false) {
     cudaStream_t s = r->ctx->stream;
     const bool fork = a.cache && !a.capture;
@@ -961,9 +971,6 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     if (early) {
         VRG_CUDA_TRY(cudaStreamWaitEvent(r->pre, r->ev_next_ok, 0));
         VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, r->pre));
-        VRG_TRY(launch_trace(r->pre, a, 0, 0));
-        VRG_CUDA_TRY(cudaEventRecord(r->ev_pre, r->pre));
-        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_pre, 0));
     } else {
         VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, s));
     }
@@ -975,14 +982,18 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     int last_lp = -1;
     for (uint32_t b = 0; b < nb_main; b++) {
         if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[b - 2], 0));
-        if (early && b == 0) VRG_TRY(launch_shade(s, a, 0, 0));
-        else VRG_TRY(launch_trace_shade(s, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
+        cudaStream_t sb = (early && b == 0) ? r->pre : s;  // stream of this bounce
+        VRG_TRY(launch_trace_shade(sb, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
         if (timed) {
             VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
             VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
         }
+        if (sb != s) {  // the library stream takes over after the first bounce
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_pre, sb));
+            VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_pre, 0));
+        }
         if (b + 1 < a.nb) {
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[b], s));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[b], sb));
             VRG_CUDA_TRY(cudaStreamWaitEvent(r->lps, r->ev_shaded[b], 0));
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], r->lps));
             VRG_TRY(launch_light_pdf(r->lps, a, b, 0));

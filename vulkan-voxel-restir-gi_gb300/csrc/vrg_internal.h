@@ -215,9 +215,12 @@ struct Renderer {
     uint4 *hitbuf = nullptr;              // light hits of the any-hit pass
     float *hitval = nullptr;
     uint2 *jmeta = nullptr;
-    uint8_t *nlive = nullptr;
-    float4 *rec = nullptr;                // [nb][2][P]
-    float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
+    // per-frame path records, two sets by frame parity (one for batched
+    // renderers): a frame's first bounce fills its set while the previous
+    // frame's resolve still reads the other
+    uint8_t *nlive[2] = {};
+    float4 *rec[2] = {};                  // [nb][2][P]
+    float4 *xv[2] = {}, *nv[2] = {}, *xs[2] = {}, *ns[2] = {};
     float4 *plain = nullptr;              // L[0] per pixel
     float4 *res = nullptr;                // [ring][5][P] temporal reservoirs
     DevBufPtr res_buf;
