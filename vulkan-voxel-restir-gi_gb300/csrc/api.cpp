@@ -442,28 +442,32 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     const uint32_t nb = r->nb_max;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     size_t o = 0;
-    size_t o_ro = o; o += al(P * 16);
-    size_t o_rd = o; o += al(P * 16);
-    size_t o_q0 = o; o += al(P * 4);
-    size_t o_q1 = o; o += al(P * 4);
-    size_t o_cnt = o; o += al(CNT_WORDS * 4);
-    size_t o_aq0 = o; o += al(P * 4);
-    size_t o_aq1 = o; o += al(P * 4);
-    size_t o_aj0 = o; o += al(P * 32);
-    size_t o_aj1 = o; o += al(P * 32);
-    size_t o_hit = o; o += al(P * 16);
-    size_t o_hb = o; o += al(P * 2 * 32);
-    size_t o_hv = o; o += al(P * 2 * 4);
-    size_t o_jm = o; o += al(P * 8);
+    // the arrays of a frame's bounces, one set per frame in flight
+    struct SetOff {
+        size_t ro, rd, q0, q1, cnt, aq0, aq1, aj0, aj1, hit, hb, hv, jm, nl, rec, xv, nv, xs, ns;
+    } so[2];
     const int sets = r->n_views ? 1 : 2;
-    size_t o_nl[2], o_rec[2], o_xv[2], o_nv[2], o_xs[2], o_ns[2];
     for (int k = 0; k < sets; k++) {
-        o_nl[k] = o; o += al(P);
-        o_rec[k] = o; o += al(P * 32 * nb);
-        o_xv[k] = o; o += al(P * 16);
-        o_nv[k] = o; o += al(P * 16);
-        o_xs[k] = o; o += al(P * 16);
-        o_ns[k] = o; o += al(P * 16);
+        SetOff &q = so[k];
+        q.ro = o; o += al(P * 16);
+        q.rd = o; o += al(P * 16);
+        q.q0 = o; o += al(P * 4);
+        q.q1 = o; o += al(P * 4);
+        q.cnt = o; o += al(CNT_WORDS * 4);
+        q.aq0 = o; o += al(P * 4);
+        q.aq1 = o; o += al(P * 4);
+        q.aj0 = o; o += al(P * 32);
+        q.aj1 = o; o += al(P * 32);
+        q.hit = o; o += al(P * 16);
+        q.hb = o; o += al(P * 2 * 32);
+        q.hv = o; o += al(P * 2 * 4);
+        q.jm = o; o += al(P * 8);
+        q.nl = o; o += al(P);
+        q.rec = o; o += al(P * 32 * nb);
+        q.xv = o; o += al(P * 16);
+        q.nv = o; o += al(P * 16);
+        q.xs = o; o += al(P * 16);
+        q.ns = o; o += al(P * 16);
     }
     size_t o_pl = o; o += al(P * 16);
     size_t o_sp = o; o += al(P * 80);
@@ -474,27 +478,28 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     DevBufPtr b;
     VRG_TRY(dev_alloc(r->ctx->stream, o, b));
     uint8_t *B = (uint8_t *)b->ptr;
-    r->ray_o = (float4 *)(B + o_ro);
-    r->ray_d = (float4 *)(B + o_rd);
-    r->queue[0] = (uint32_t *)(B + o_q0);
-    r->queue[1] = (uint32_t *)(B + o_q1);
-    r->counters = (uint32_t *)(B + o_cnt);
-    r->aqueue[0] = (uint32_t *)(B + o_aq0);
-    r->aqueue[1] = (uint32_t *)(B + o_aq1);
-    r->ajob[0] = (float4 *)(B + o_aj0);
-    r->ajob[1] = (float4 *)(B + o_aj1);
-    r->hits = (int4 *)(B + o_hit);
-    r->hitbuf = (uint4 *)(B + o_hb);
-    r->hitval = (float *)(B + o_hv);
-    r->jmeta = (uint2 *)(B + o_jm);
     for (int k = 0; k < 2; k++) {
-        const int j = k < sets ? k : 0;
-        r->nlive[k] = B + o_nl[j];
-        r->rec[k] = (float4 *)(B + o_rec[j]);
-        r->xv[k] = (float4 *)(B + o_xv[j]);
-        r->nv[k] = (float4 *)(B + o_nv[j]);
-        r->xs[k] = (float4 *)(B + o_xs[j]);
-        r->ns[k] = (float4 *)(B + o_ns[j]);
+        const SetOff &q = so[k < sets ? k : 0];
+        Renderer::FrameSet &F = r->fs[k];
+        F.ray_o = (float4 *)(B + q.ro);
+        F.ray_d = (float4 *)(B + q.rd);
+        F.queue[0] = (uint32_t *)(B + q.q0);
+        F.queue[1] = (uint32_t *)(B + q.q1);
+        F.counters = (uint32_t *)(B + q.cnt);
+        F.aqueue[0] = (uint32_t *)(B + q.aq0);
+        F.aqueue[1] = (uint32_t *)(B + q.aq1);
+        F.ajob[0] = (float4 *)(B + q.aj0);
+        F.ajob[1] = (float4 *)(B + q.aj1);
+        F.hits = (int4 *)(B + q.hit);
+        F.hitbuf = (uint4 *)(B + q.hb);
+        F.hitval = (float *)(B + q.hv);
+        F.jmeta = (uint2 *)(B + q.jm);
+        F.nlive = B + q.nl;
+        F.rec = (float4 *)(B + q.rec);
+        F.xv = (float4 *)(B + q.xv);
+        F.nv = (float4 *)(B + q.nv);
+        F.xs = (float4 *)(B + q.xs);
+        F.ns = (float4 *)(B + q.ns);
     }
     r->plain = (float4 *)(B + o_pl);
     r->spatial = (float4 *)(B + o_sp);
@@ -503,8 +508,9 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->radiance = (float *)(B + o_rad);
     r->accum = (double *)(B + o_acc);
     VRG_CUDA_TRY(cudaMemsetAsync(B, 0, o, r->ctx->stream));
-    // the next frame's early closest hit starts after this clear
-    if (r->ev_next_ok) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, r->ctx->stream));
+    // frames in flight start their bounces after this clear
+    for (cudaEvent_t e : r->ev_done)
+        if (e) VRG_CUDA_TRY(cudaEventRecord(e, r->ctx->stream));
     r->out_buf.reset();
     r->radiance_out = nullptr;
     if (r->scale > 1) {
@@ -532,9 +538,15 @@ static vrg_status renderer_events(vrg_renderer *r) {
     int lo_prio = 0, hi_prio = 0;
     VRG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux, cudaStreamNonBlocking, hi_prio));
-    VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->lps, cudaStreamNonBlocking));
-    for (auto &e : r->ev_shaded) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    for (auto &e : r->ev_lpdone) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (int k = 0; k < 2; k++) {
+        VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->bs[k], cudaStreamNonBlocking));
+        VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->lps[k], cudaStreamNonBlocking));
+        for (auto &e : r->ev_shaded[k]) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (auto &e : r->ev_lpdone[k]) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_bounced[k], cudaEventDisableTiming));
+        VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_done[k], cudaEventDisableTiming));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_done[k], r->ctx->stream));  // after the buffers' clear
+    }
     for (auto &row : r->ev_lp)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
@@ -542,10 +554,6 @@ static vrg_status renderer_events(vrg_renderer *r) {
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
-    VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->pre, cudaStreamNonBlocking));
-    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_next_ok, cudaEventDisableTiming));
-    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_pre, cudaEventDisableTiming));
-    VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, r->ctx->stream));  // after the buffers' clear
     for (auto &e : r->ev_fence) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     r->grid_bounce = r->ctx->num_sms * bounce_blocks_per_sm();
     return VRG_OK;
@@ -659,25 +667,24 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
             if (e) cudaEventDestroy(e);
     for (auto &e : r->ev_stage)
         if (e) cudaEventDestroy(e);
-    for (auto &e : r->ev_shaded)
-        if (e) cudaEventDestroy(e);
-    for (auto &e : r->ev_lpdone)
-        if (e) cudaEventDestroy(e);
+    for (int k = 0; k < 2; k++) {
+        for (cudaStream_t q : {r->bs[k], r->lps[k]})
+            if (q) {
+                cudaStreamSynchronize(q);
+                cudaStreamDestroy(q);
+            }
+        for (auto &e : r->ev_shaded[k])
+            if (e) cudaEventDestroy(e);
+        for (auto &e : r->ev_lpdone[k])
+            if (e) cudaEventDestroy(e);
+        if (r->ev_bounced[k]) cudaEventDestroy(r->ev_bounced[k]);
+        if (r->ev_done[k]) cudaEventDestroy(r->ev_done[k]);
+    }
     for (auto &row : r->ev_lp)
         for (auto &e : row)
             if (e) cudaEventDestroy(e);
-    if (r->lps) {
-        cudaStreamSynchronize(r->lps);
-        cudaStreamDestroy(r->lps);
-    }
-    if (r->pre) {
-        cudaStreamSynchronize(r->pre);
-        cudaStreamDestroy(r->pre);
-    }
-    if (r->ev_next_ok) cudaEventDestroy(r->ev_next_ok);
     for (auto &e : r->ev_fence)
         if (e) cudaEventDestroy(e);
-    if (r->ev_pre) cudaEventDestroy(r->ev_pre);
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
     if (r->aux) {
@@ -816,6 +823,10 @@ static void apply_tuning(const vrg_renderer *r, FrameArgs &a) {
 // Frame set-up shared by vrg_render and vrg_render_batched: parameter checks,
 // the reservoir ring, capture and cache buffers, and every FrameArgs field but
 // the view ones.
+// the array set of the frame about to be rendered (by frame parity; batched
+// renderers have one)
+static uint32_t frame_set(const vrg_renderer *r) { return r->n_views ? 0u : (r->frame & 1u); }
+
 static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool want_radiance, FrameArgs &a) {
     if (pr->num_bounces == 0 || pr->spatial_iterations > 64 || pr->nee_type > 2 || pr->mode > 1) {
         set_error("invalid render parameters");
@@ -889,27 +900,27 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.debug_view = pr->debug_view;
     a.accumulate = pr->accumulate;
     a.pack = (pr->flags & VRG_RENDER_NO_PACK) ? 0u : 1u;
-    a.ray_o = r->ray_o;
-    a.ray_d = r->ray_d;
-    a.queue[0] = r->queue[0];
-    a.queue[1] = r->queue[1];
-    a.aqueue[0] = r->aqueue[0];
-    a.aqueue[1] = r->aqueue[1];
-    a.ajob[0] = r->ajob[0];
-    a.ajob[1] = r->ajob[1];
-    a.hits = r->hits;
-    a.hitbuf = r->hitbuf;
-    a.hitval = r->hitval;
-    a.jmeta = r->jmeta;
+    const Renderer::FrameSet &F = r->fs[frame_set(r)];
+    a.ray_o = F.ray_o;
+    a.ray_d = F.ray_d;
+    a.queue[0] = F.queue[0];
+    a.queue[1] = F.queue[1];
+    a.aqueue[0] = F.aqueue[0];
+    a.aqueue[1] = F.aqueue[1];
+    a.ajob[0] = F.ajob[0];
+    a.ajob[1] = F.ajob[1];
+    a.hits = F.hits;
+    a.hitbuf = F.hitbuf;
+    a.hitval = F.hitval;
+    a.jmeta = F.jmeta;
     a.hit_cap = (uint32_t)std::min<size_t>(2 * P, 0xFFFFFFF0u);
-    a.counters = r->counters;
-    const uint32_t set = r->frame & 1u;
-    a.nlive = r->nlive[set];
-    a.rec = r->rec[set];
-    a.xv = r->xv[set];
-    a.nv = r->nv[set];
-    a.xs = r->xs[set];
-    a.ns = r->ns[set];
+    a.counters = F.counters;
+    a.nlive = F.nlive;
+    a.rec = F.rec;
+    a.xv = F.xv;
+    a.nv = F.nv;
+    a.xs = F.xs;
+    a.ns = F.ns;
     a.plain = r->plain;
     a.res = r->res + (size_t)ring * 5 * P;
     a.spatial = r->spatial;
@@ -950,30 +961,29 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // resolve and spatial (nothing of one branch reads what the other writes;
 // the training step's weights serve the next frame, after the join).  With
 // capture the frame stays on one stream.
-// pipelined: frames in flight.  The first bounce of this frame (closest hit
-// and shading) reads the committed scene, the camera and the material table,
-// and writes the hit buffer, the counters, the next bounce's rays and jobs and
-// this frame's set of path records (sets alternate by frame parity); the
-// previous frame's resolve and spatial passes read none of these but that
-// frame's own record set.  So the first bounce runs on its own stream as soon
-// as the previous frame's bounces and light-pdf walks are done (ev_next_ok),
-// beside that frame's resolve and spatial passes, and its light-pdf walk
-// follows on the walk stream; the library stream waits for the first bounce
-// before the second, so the frame is complete on the library stream when its
-// work there is.  Scene commits and material / atlas changes synchronize or
-// order the library stream before they return, so a scene's device data is
-// final before any frame reads it.
+// Frames in flight (pipelined, plain frames: no stats, cache or capture).
+// A frame's bounces (closest hit, shading, light-pdf walks) read the committed
+// scene, the camera and the material table, and write only the arrays of the
+// frame's set (sets alternate by frame parity).  So they run on the set's own
+// bounce stream as soon as the set's previous frame, two frames back, has
+// finished (ev_done), beside the previous frame's bounces and its resolve and
+// spatial passes.  The library stream waits for the bounces (ev_bounced) and
+// then runs the frame's resolve and spatial passes, in frame order, so the
+// frame is complete when the library stream has passed it.  Scene commits and
+// material / atlas changes synchronize the library stream before they return,
+// so a scene's device data is final before any frame reads it; a resize
+// clears the arrays on the library stream and re-records ev_done.
+// Other frames run their bounces on the library stream itself.
 static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, bool pipelined = false) {
     cudaStream_t s = r->ctx->stream;
+    const uint32_t k = frame_set(r);
     const bool fork = a.cache && !a.capture;
     const uint32_t nb_main = fork ? a.nb_render : a.nb;
-    const bool early = pipelined && !a.cache && !a.capture && !a.views && !timed;
-    if (early) {
-        VRG_CUDA_TRY(cudaStreamWaitEvent(r->pre, r->ev_next_ok, 0));
-        VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, r->pre));
-    } else {
-        VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, s));
-    }
+    const bool own = pipelined && !a.cache && !a.capture && !a.views && !timed;
+    cudaStream_t bs = own ? r->bs[k] : s;  // stream of the bounces
+    cudaStream_t lp = r->lps[k];
+    if (own) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_done[k], 0));
+    VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, bs));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
     // Bounce b's light-pdf walk runs on the light-pdf stream beside bounce
     // b + 1's closest hit and shading.  Ordering: the walk of b waits for the
@@ -981,31 +991,27 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     // parity b & 1) waits for the walk of b; resolve waits for every walk.
     int last_lp = -1;
     for (uint32_t b = 0; b < nb_main; b++) {
-        if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[b - 2], 0));
-        cudaStream_t sb = (early && b == 0) ? r->pre : s;  // stream of this bounce
-        VRG_TRY(launch_trace_shade(sb, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
-        if (timed) {
+        if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][b - 2], 0));
+        VRG_TRY(launch_trace_shade(bs, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
+        if (timed) {  // (timed frames run their bounces on the library stream)
             VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
             VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
         }
-        if (sb != s) {  // the library stream takes over after the first bounce
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_pre, sb));
-            VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_pre, 0));
-        }
         if (b + 1 < a.nb) {
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[b], sb));
-            VRG_CUDA_TRY(cudaStreamWaitEvent(r->lps, r->ev_shaded[b], 0));
-            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], r->lps));
-            VRG_TRY(launch_light_pdf(r->lps, a, b, 0));
-            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[1][b], r->lps));
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[b], r->lps));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[k][b], bs));
+            VRG_CUDA_TRY(cudaStreamWaitEvent(lp, r->ev_shaded[k][b], 0));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], lp));
+            VRG_TRY(launch_light_pdf(lp, a, b, 0));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[1][b], lp));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[k][b], lp));
             last_lp = (int)b;
         }
     }
-    if (last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[last_lp], 0));
-    // a plain frame's resolve and spatial passes read neither the hit buffer
-    // nor the counters: the next frame's early closest hit may start here
-    if (!a.views && !a.cache && !a.capture) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, s));
+    if (last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][last_lp], 0));
+    if (own) {
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_bounced[k], bs));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_bounced[k], 0));
+    }
     cudaStream_t st = s;  // stream of the training branch
     if (fork) {
         st = r->aux;
@@ -1033,7 +1039,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
     if (fork) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_join, 0));
-    if (!a.views && (a.cache || a.capture)) VRG_CUDA_TRY(cudaEventRecord(r->ev_next_ok, s));
+    // the set is free for the frame two ahead (not recorded inside a batched
+    // frame's graph capture: batched frames never run their bounces apart)
+    if (!a.views) VRG_CUDA_TRY(cudaEventRecord(r->ev_done[k], s));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 2], s));
     return VRG_OK;
 }

@@ -205,22 +205,26 @@ struct Renderer {
     uint32_t last_ring = 0;
     bool captured = false;
     DevBufPtr buf;
-    // device arrays (P = W*H)
-    float4 *ray_o = nullptr, *ray_d = nullptr;
-    uint32_t *queue[2] = {nullptr, nullptr};
-    uint32_t *counters = nullptr;         // CNT_* words of vrg_frame.cuh
-    uint32_t *aqueue[2] = {nullptr, nullptr};  // light-pdf jobs by bounce parity
-    float4 *ajob[2] = {nullptr, nullptr};      // their ray copies (2 float4 per job)
-    int4 *hits = nullptr;                 // closest hit per pixel
-    uint4 *hitbuf = nullptr;              // light hits of the any-hit pass
-    float *hitval = nullptr;
-    uint2 *jmeta = nullptr;
-    // per-frame path records, two sets by frame parity (one for batched
-    // renderers): a frame's first bounce fills its set while the previous
-    // frame's resolve still reads the other
-    uint8_t *nlive[2] = {};
-    float4 *rec[2] = {};                  // [nb][2][P]
-    float4 *xv[2] = {}, *nv[2] = {}, *xs[2] = {}, *ns[2] = {};
+    // Device arrays (P = W*H).  The arrays of a frame's bounces come in two
+    // sets (one for batched renderers), by frame parity: two frames' bounces
+    // may be in flight at once, each in its own set; the arrays after the set
+    // are read and written only by the frames' resolve and spatial passes,
+    // which run one frame after the other on the library stream.
+    struct FrameSet {
+        float4 *ray_o = nullptr, *ray_d = nullptr;
+        uint32_t *queue[2] = {nullptr, nullptr};
+        uint32_t *counters = nullptr;          // CNT_* words of vrg_frame.cuh
+        uint32_t *aqueue[2] = {nullptr, nullptr};  // light-pdf jobs by bounce parity
+        float4 *ajob[2] = {nullptr, nullptr};      // their ray copies (2 float4 per job)
+        int4 *hits = nullptr;                  // closest hit per pixel
+        uint4 *hitbuf = nullptr;               // light hits of the any-hit pass
+        float *hitval = nullptr;
+        uint2 *jmeta = nullptr;
+        uint8_t *nlive = nullptr;
+        float4 *rec = nullptr;                 // [nb][2][P]
+        float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
+    };
+    FrameSet fs[2];
     float4 *plain = nullptr;              // L[0] per pixel
     float4 *res = nullptr;                // [ring][5][P] temporal reservoirs
     DevBufPtr res_buf;
@@ -240,17 +244,17 @@ struct Renderer {
     size_t h_pinned_bytes = 0;
     cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    cudaStream_t lps = nullptr;           // light-pdf stream: bounce b's walk beside bounce b + 1
-    // frames in flight: a frame's primary closest hit runs on `pre` beside the
-    // previous frame's resolve and spatial passes, once `ev_next_ok` (the
-    // previous frame's last reader of the hit buffer and counters) has passed
-    cudaStream_t pre = nullptr;
-    cudaEvent_t ev_next_ok = nullptr, ev_pre = nullptr;
+    // Per set: the bounce stream of frames in flight and the light-pdf stream
+    // (bounce b's walk beside bounce b + 1), the dependency events per bounce,
+    // the end of the set's bounces and the end of its frame (after the
+    // resolve and spatial passes on the library stream).
+    cudaStream_t bs[2] = {}, lps[2] = {};
+    cudaEvent_t ev_shaded[2][8] = {}, ev_lpdone[2][8] = {};
+    cudaEvent_t ev_bounced[2] = {}, ev_done[2] = {};
     // per-frame fences (frame index % FENCES): recorded after the frame and its
     // copies out; vrg_renderer_wait_frame waits on them
     static constexpr uint32_t FENCES = 8;
     cudaEvent_t ev_fence[FENCES] = {};
-    cudaEvent_t ev_shaded[8] = {}, ev_lpdone[8] = {};  // dependency events per bounce
     cudaEvent_t ev_lp[2][8] = {};         // timing: light-pdf passes of bounce b begin / end
     cudaEvent_t ev[16] = {};
     cudaEvent_t ev_k[2][8] = {};          // after k_trace / after k_shade, per bounce
