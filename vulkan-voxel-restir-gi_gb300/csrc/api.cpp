@@ -445,8 +445,8 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     // the arrays of a frame's bounces, one set per frame in flight
     struct SetOff {
         size_t ro, rd, q0, q1, cnt, aq0, aq1, aj0, aj1, hit, hb, hv, jm, nl, rec, xv, nv, xs, ns;
-    } so[2];
-    const int sets = r->n_views ? 1 : 2;
+    } so[Renderer::SETS];
+    const int sets = r->n_views ? 1 : Renderer::SETS;
     for (int k = 0; k < sets; k++) {
         SetOff &q = so[k];
         q.ro = o; o += al(P * 16);
@@ -478,7 +478,7 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     DevBufPtr b;
     VRG_TRY(dev_alloc(r->ctx->stream, o, b));
     uint8_t *B = (uint8_t *)b->ptr;
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < Renderer::SETS; k++) {
         const SetOff &q = so[k < sets ? k : 0];
         Renderer::FrameSet &F = r->fs[k];
         F.ray_o = (float4 *)(B + q.ro);
@@ -538,7 +538,7 @@ static vrg_status renderer_events(vrg_renderer *r) {
     int lo_prio = 0, hi_prio = 0;
     VRG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux, cudaStreamNonBlocking, hi_prio));
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < Renderer::SETS; k++) {
         VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->bs[k], cudaStreamNonBlocking));
         VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->lps[k], cudaStreamNonBlocking));
         for (auto &e : r->ev_shaded[k]) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -667,7 +667,7 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
             if (e) cudaEventDestroy(e);
     for (auto &e : r->ev_stage)
         if (e) cudaEventDestroy(e);
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < Renderer::SETS; k++) {
         for (cudaStream_t q : {r->bs[k], r->lps[k]})
             if (q) {
                 cudaStreamSynchronize(q);
@@ -823,9 +823,9 @@ static void apply_tuning(const vrg_renderer *r, FrameArgs &a) {
 // Frame set-up shared by vrg_render and vrg_render_batched: parameter checks,
 // the reservoir ring, capture and cache buffers, and every FrameArgs field but
 // the view ones.
-// the array set of the frame about to be rendered (by frame parity; batched
+// the array set of the frame about to be rendered (frame index mod SETS; batched
 // renderers have one)
-static uint32_t frame_set(const vrg_renderer *r) { return r->n_views ? 0u : (r->frame & 1u); }
+static uint32_t frame_set(const vrg_renderer *r) { return r->n_views ? 0u : r->frame % (uint32_t)Renderer::SETS; }
 
 static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool want_radiance, FrameArgs &a) {
     if (pr->num_bounces == 0 || pr->spatial_iterations > 64 || pr->nee_type > 2 || pr->mode > 1) {
@@ -964,10 +964,10 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // Frames in flight (pipelined, plain frames: no stats, cache or capture).
 // A frame's bounces (closest hit, shading, light-pdf walks) read the committed
 // scene, the camera and the material table, and write only the arrays of the
-// frame's set (sets alternate by frame parity).  So they run on the set's own
-// bounce stream as soon as the set's previous frame, two frames back, has
-// finished (ev_done), beside the previous frame's bounces and its resolve and
-// spatial passes.  The library stream waits for the bounces (ev_bounced) and
+// frame's set (sets are taken in turn by frame index).  So they run on the
+// set's own bounce stream as soon as the set's previous frame, SETS frames
+// back, has finished (ev_done), beside the previous frames' bounces and their
+// resolve and spatial passes.  The library stream waits for the bounces (ev_bounced) and
 // then runs the frame's resolve and spatial passes, in frame order, so the
 // frame is complete when the library stream has passed it.  Scene commits and
 // material / atlas changes synchronize the library stream before they return,
@@ -1039,7 +1039,7 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
     if (fork) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_join, 0));
-    // the set is free for the frame two ahead (not recorded inside a batched
+    // the set is free for the frame SETS ahead (not recorded inside a batched
     // frame's graph capture: batched frames never run their bounces apart)
     if (!a.views) VRG_CUDA_TRY(cudaEventRecord(r->ev_done[k], s));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 2], s));
