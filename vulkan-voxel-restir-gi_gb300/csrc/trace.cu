@@ -238,11 +238,11 @@ __device__ __forceinline__ bool slab_fma(float lox, float hix, float loy, float 
 
 // Pops the next pending child whose box starts at or before best_t (boxes
 // are culled only when strictly beyond it); false when none is left.
-__device__ __forceinline__ bool pop_near(const int *stack, const float *tstk, int &sp, float best_t, int &node) {
+__device__ __forceinline__ bool pop_near(const int2 *stack, int &sp, float best_t, int &node) {
     while (sp > 0) {
-        --sp;
-        if (tstk[sp] <= best_t) {
-            node = stack[sp];
+        const int2 e = stack[--sp];  // (ref, entry distance bits)
+        if (__int_as_float(e.y) <= best_t) {
+            node = e.x;
             return true;
         }
     }
@@ -330,8 +330,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     // pending children with their entry distances: a popped entry whose box
     // starts beyond the current best t is dropped unvisited (every box below
     // it starts no nearer, so each would be culled by its own test)
-    int stack[TRAV_STACK];
-    float tstk[TRAV_STACK];
+    int2 stack[TRAV_STACK];
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
         if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
@@ -382,13 +381,13 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                 slab4(NX, FX, NY, FY, NZ, FZ, RF, inv, oi, EPS_TRACE, best_t, tk, rk);
                 // tk sorted ascending (misses at +inf)
                 if (tk[0] == INFINITY) {
-                    done = !pop_near(stack, tstk, sp, best_t, node);
+                    done = !pop_near(stack, sp, best_t, node);
                 } else {
                     node = rk[0];
                     if (sp + 3 <= TRAV_STACK) {
-                        if (tk[3] != INFINITY) { stack[sp] = rk[3]; tstk[sp++] = tk[3]; }
-                        if (tk[2] != INFINITY) { stack[sp] = rk[2]; tstk[sp++] = tk[2]; }
-                        if (tk[1] != INFINITY) { stack[sp] = rk[1]; tstk[sp++] = tk[1]; }
+                        if (tk[3] != INFINITY) stack[sp++] = make_int2(rk[3], __float_as_int(tk[3]));
+                        if (tk[2] != INFINITY) stack[sp++] = make_int2(rk[2], __float_as_int(tk[2]));
+                        if (tk[1] != INFINITY) stack[sp++] = make_int2(rk[1], __float_as_int(tk[1]));
                     } else {
                         atomicOr(err, ERR_STACK);
                     }
@@ -420,7 +419,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                         }
                     }
                 }
-                done = !pop_near(stack, tstk, sp, best_t, node);
+                done = !pop_near(stack, sp, best_t, node);
             }
             if (done) {
                 a.hits[p] = make_int4(hrec, (int)hfh, __float_as_int(hb1), __float_as_int(hb2));
