@@ -156,7 +156,9 @@ class OracleSampler:
     def __init__(self, world, mats, n, rows):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
-        self.ow = oracle.build_world(mats, n, world)
+        t0 = time.perf_counter()
+        self.ow = oracle.build_world(mats, n, world)  # meshing, light extraction, SAH builds, commit
+        self.build_s = time.perf_counter() - t0
         self.orr = oracle.Renderer(W, H, NB)
         self.rows = min(rows, H)
 
@@ -178,7 +180,7 @@ class OracleSampler:
 
 
 def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
-    """Returns (Mrays/s, seconds, rays) of `frames` oracle frames."""
+    """Returns (Mrays/s, seconds, rays, scene build seconds) of `frames` oracle frames."""
     smp = OracleSampler(world, mats, n, rows)
     dt, rays = 0.0, 0
     for f in range(frames):
@@ -186,7 +188,7 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
         dt += t
         rays += r_
     smp.close()
-    return rays / dt / 1e6, dt, rays
+    return rays / dt / 1e6, dt, rays, smp.build_s
 
 
 # k_trace DRAM bytes (read + write) per pixel per frame, all bounces, from one
@@ -639,8 +641,8 @@ def run_ours(args, d):
         batched = batched_block(ctx, steps=16, warmup=3, tuning=best_tuning)
     upd_ms = update_commit_ms(scene, NX, NZ)
     cpu_frames = args.cpu_frames
-    cpu_mr, cpu_dt, cpu_rays = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0) if not args.no_cpu
-                                else (None, 0, 0))
+    cpu_mr, cpu_dt, cpu_rays, cpu_build_s = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0)
+                                             if not args.no_cpu else (None, 0, 0, None))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total_s_max / args.steps, 4),
@@ -663,6 +665,9 @@ def run_ours(args, d):
         "ms_per_frame_alone": round(sum(ms) / max(args.steps, 1), 4),
         "rays_per_frame": rays // max(args.steps, 1),
         "scene_build_ms": round(build_s * 1000, 2),
+        # the oracle's build of the same 16 chunks on one host core: meshing,
+        # light extraction, both SAH BLAS builds per chunk and the commit
+        "scene_build_cpu_ms": None if cpu_build_s is None else round(cpu_build_s * 1000, 2),
         "update_commit_ms": upd_ms,
         "roofline": {"bound": "hbm", "kernel": "k_trace", "achieved": round(achieved, 2), "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),

@@ -560,7 +560,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_typ
 // k_anyhit; the others get their (E, w) (R, q) record here.
 // ---------------------------------------------------------------------------
 template <bool CAPTURE, bool BATCH>
-__global__ void __launch_bounds__(128) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
+__global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
     const uint32_t n_in = (b == 0) ? P : a.counters[CNT_QUEUE + b];
@@ -753,7 +753,7 @@ __device__ __forceinline__ void finish_job(const FrameArgs &a, uint32_t b, uint3
 }
 
 template <bool CAPTURE, bool BATCH>
-__global__ void __launch_bounds__(128) k_anyhit(const __grid_constant__ FrameArgs a, uint32_t b) {
+__global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const int REFILL = (int)a.refill_any;
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
