@@ -98,7 +98,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -192,12 +192,14 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
 
 
 # k_trace DRAM bytes (read + write) per pixel per frame, all bounces, from one
-# ncu --set full capture of the workload at 960x540 (3.66 + 20.14 + 16.77 MB over
+# ncu --set full capture of the workload at 960x540 (5.65 + 25.34 + 20.96 MB over
 # 518,400 pixels; profiles/k_trace_restir540p.md); the 1080p launches are too
 # large to capture with --set full, and the traffic scales with the pixel count
-TRACE_DRAM_BYTES_PER_PX = 40.58e6 / (960 * 540)
+TRACE_DRAM_BYTES_PER_PX = 51.95e6 / (960 * 540)
 
 C3_N = 8  # chunks per side of the learned-cache workload
+E2E_SLOTS = 3  # host image buffers of the end-to-end loop (frames in flight)
+REF_MAX_FRAMES = 48  # full 1080p frames the reference arm times on the host cores
 
 C2_SEED = 20240602
 C2_SCENES = 64
@@ -430,13 +432,17 @@ def run_reference(args, d):
         return
     mats, n = vrg.terrain_materials(SEED)
     world = vrg.terrain_blocks(SEED, NX, NZ, EMISSIVE)
-    rows = args.ref_rows
+    # Full frames (the CPU path's stream passes run over the whole image in any
+    # case, so a band of rows would understate its throughput), bounded to the
+    # first REF_MAX_FRAMES of the K timed frames: about 12 s on 16 cores.
+    rows = min(args.ref_rows, H)
+    frames = min(args.steps, REF_MAX_FRAMES)
     threads = cpu_threads()
     smp = OracleSampler(world, mats, n, rows)
-    for w in range(args.warmup):
+    for w in range(min(args.warmup, 2)):
         smp.frame(w)
     times, rays_all = [], 0
-    for s in range(args.steps):
+    for s in range(frames):
         dt, rays = smp.frame(args.warmup + s)
         times.append(dt)
         rays_all += rays
@@ -445,14 +451,15 @@ def run_reference(args, d):
     value = rays_all / total / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "n_gpus": args.gpus, "steps": frames, "requested_steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / frames, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value-noise voxel terrain)",
         "config": {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
                    "bounces": NB, "spatial_neighbours": 3, "radius_px": 30, "m_cap": 20,
                    "sample_rows_per_frame": rows},
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} of {H} rows per frame, {args.steps} frames of the orbit"},
+                         "sample": f"{rows} of {H} rows per frame, orbit frames {args.warmup}-"
+                                   f"{args.warmup + frames - 1} (the first {frames} of the {args.steps} timed)"},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -572,26 +579,28 @@ def run_ours(args, d):
     value = rays_all / total_s_max / 1e6
     # End to end through the public API: the same K frames again (state
     # restored), each frame's image read back into page-locked host memory
-    # (so the device->host copy runs at link speed).  Two buffers alternate,
-    # every frame's copy is queued behind it (VRG_OUTPUT_HOST_ASYNC), and the
-    # host waits on the previous frame's fence and reads that image while the
-    # next one renders.  Wall clock, same ray counts.
-    host_imgs = [torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    # (so the device->host copy runs at link speed).  E2E_SLOTS buffers are
+    # taken in turn, as the reference's swapchain slots are; every frame's copy
+    # is queued behind it (VRG_OUTPUT_HOST_ASYNC), and the host waits on the
+    # fence of the oldest frame in flight and reads its image while the newer
+    # ones render.  Wall clock, same ray counts.
+    host_imgs = [torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True) for _ in range(E2E_SLOTS)]
     outs = [vrg.FrameOutput(t.data_ptr(), None, vrg.OUTPUT_HOST_ASYNC, 0) for t in host_imgs]
     r.load_state(blob)
     f0 = r.frame_index()
     checksum = 0
+    lag = E2E_SLOTS - 1  # frames in flight behind the one just enqueued
     torch.cuda.synchronize()
     d.barrier()
     t0 = time.perf_counter()
     for s in range(0 if args.no_e2e else args.steps):
-        render(args.warmup + s, outs[s % 2], None)
-        if s:
-            r.wait_frame(f0 + s - 1)
-            checksum ^= int(host_imgs[(s - 1) % 2][(s * 4099) % (W * H * 4)])
-    if not args.no_e2e:
-        r.wait_frame(f0 + args.steps - 1)
-        checksum ^= int(host_imgs[(args.steps - 1) % 2][0])
+        render(args.warmup + s, outs[s % E2E_SLOTS], None)
+        if s >= lag:  # the oldest frame in flight: fence, then read its image
+            r.wait_frame(f0 + s - lag)
+            checksum ^= int(host_imgs[(s - lag) % E2E_SLOTS][(s * 4099) % (W * H * 4)])
+    for s in range(max(0, args.steps - lag), 0 if args.no_e2e else args.steps):
+        r.wait_frame(f0 + s)
+        checksum ^= int(host_imgs[s % E2E_SLOTS][0])
     e2e_s = d.max(time.perf_counter() - t0)
     e2e_value = rays_all / e2e_s / 1e6 if not args.no_e2e else None
     if d.rank != 0:
@@ -704,7 +713,7 @@ def run_ours(args, d):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=512)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-rows", type=int, default=1080, help="image rows the CPU baseline traces per frame")
