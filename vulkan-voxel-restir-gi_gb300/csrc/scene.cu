@@ -43,7 +43,8 @@ __device__ __forceinline__ int bl_root_ref(const InstBuild &I) {
 // g's children, with each inner child replaced by its own two children
 // (so inner children of a 4-wide node are nodes two levels down).  Layout
 // (8 float4): lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], refs[4], pad.
-// Unused slots hold ref EMPTY_ROOT (skipped by the walk) and a box at +inf.
+// Unused slots hold ref EMPTY_ROOT and the inverted box lo = +inf, hi = -inf,
+// which the slab test never enters (see slab4 in trace.cu).
 struct ChildRef {
     const vrg_bvh_node *node;
     float off[3];
@@ -134,9 +135,9 @@ __global__ void k_wide4(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *
             }
             refs[i] = out[i].ref;
         } else {
-            for (int a = 0; a < 3; a++) {
+            for (int a = 0; a < 3; a++) {  // an inverted box: no ray enters it
                 b[2 * a][i] = INFINITY;
-                b[2 * a + 1][i] = INFINITY;
+                b[2 * a + 1][i] = -INFINITY;
             }
             refs[i] = EMPTY_ROOT;
         }
@@ -337,7 +338,10 @@ __global__ void k_wide4_single(const vrg_bvh_node *nodes, const uint32_t *leaf, 
             }
             refs[i] = c.left_node_idx != INVALID ? (int)out[i] : ~(int)leaf[out[i]];
         } else {
-            for (int a = 0; a < 3; a++) b[2 * a][i] = b[2 * a + 1][i] = INFINITY;
+            for (int a = 0; a < 3; a++) {  // an inverted box: no ray enters it
+                b[2 * a][i] = INFINITY;
+                b[2 * a + 1][i] = -INFINITY;
+            }
             refs[i] = EMPTY_ROOT;
         }
     }

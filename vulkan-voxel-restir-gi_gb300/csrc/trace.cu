@@ -275,7 +275,12 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
 // the near distance of a non-empty box is <= its far distance, exactly, since
 // rounding is monotonic; a NaN distance (a ray parallel to an axis starting
 // on a box plane) is ignored by min/max, which only keeps more boxes: the test
-// stays conservative and the closest hit does not depend on it.
+// stays conservative and the closest hit does not depend on it.  An unused
+// slot holds the inverted box lo = +inf, hi = -inf: on an axis with a finite
+// inverse direction its near distance is +inf; on an axis the ray is parallel
+// to, the near distance is +inf, or the far distance -inf, or both are NaN
+// (origin on 0) and the axis is ignored; and a unit direction has at least one
+// finite axis.  So the slot is never entered and needs no test of its ref.
 __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY, float4 NZ, float4 FZ, float4 RF,
                                       f3 inv, f3 oi, float tmin, float tmax, float tk[4], int rk[4]) {
     const float nx[4] = {NX.x, NX.y, NX.z, NX.w}, fx[4] = {FX.x, FX.y, FX.z, FX.w};
@@ -288,7 +293,7 @@ __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY
                                fmaxf(__fmaf_rn(nz[i], inv.z, oi.z), tmin));
         const float tf = fmin3(__fmaf_rn(fx[i], inv.x, oi.x), __fmaf_rn(fy[i], inv.y, oi.y),
                                fminf(__fmaf_rn(fz[i], inv.z, oi.z), tmax));
-        tk[i] = (tn <= tf && rf[i] != EMPTY_ROOT) ? tn : INFINITY;  // unused slots never enter the walk
+        tk[i] = (tn <= tf) ? tn : INFINITY;
         rk[i] = rf[i];
     }
     // sorting network for 4
@@ -832,7 +837,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                                            fmaxf(__fmaf_rn(nz[i], inv.z, oi.z), tmin));
                     const float tf = fmin3(__fmaf_rn(fx[i], inv.x, oi.x), __fmaf_rn(fy[i], inv.y, oi.y),
                                            fminf(__fmaf_rn(fz[i], inv.z, oi.z), tmax));
-                    if (tn <= tf && rf[i] != EMPTY_ROOT) {
+                    if (tn <= tf) {  // (an unused slot's inverted box is never entered)
                         if (next == EMPTY_ROOT) {
                             next = rf[i];
                         } else if (sp < TRAV_STACK) {
