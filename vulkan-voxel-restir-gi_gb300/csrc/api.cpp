@@ -14,8 +14,6 @@
 namespace vrg {
 
 vrg_status upload_frames(cudaStream_t s);
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
-                         uint32_t max_rays);
 vrg_status launch_trace_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, uint32_t max_rays);
 vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays);
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
@@ -551,6 +549,7 @@ static vrg_status renderer_events(vrg_renderer *r) {
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_inferred, cudaEventDisableTiming));
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
@@ -687,6 +686,7 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
         if (e) cudaEventDestroy(e);
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
+    if (r->ev_inferred) cudaEventDestroy(r->ev_inferred);
     if (r->aux) {
         cudaStreamSynchronize(r->aux);
         cudaStreamDestroy(r->aux);
@@ -955,11 +955,14 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // after spatial; r->ev_k: after k_trace / k_shade of each bounce); a graph
 // recording passes false.
 //
-// A cache frame forks after the query vertex: the training paths' extra
-// bounces and the cache's training step run on the renderer's second stream
-// while the main stream infers the cache for the rendered paths and runs
-// resolve and spatial (nothing of one branch reads what the other writes;
-// the training step's weights serve the next frame, after the join).  With
+// A cache frame forks after the shading of the query vertex, while that
+// bounce's light-pdf walk still runs: the training paths' extra bounces and
+// the cache's training step run on the renderer's second stream while the
+// main stream infers the cache for the rendered paths and runs resolve (after
+// the walk) and spatial.  Neither branch reads what the other writes, except
+// the cache itself: the training branch computes its gradients beside the
+// queries, and its Adam step, which rewrites the weights and the table the
+// queries read, waits for them; the new cache serves the next frame.  With
 // capture the frame stays on one stream.
 // Frames in flight (pipelined, plain frames: no stats, cache or capture).
 // A frame's bounces (closest hit, shading, light-pdf walks) read the committed
@@ -1007,7 +1010,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
             last_lp = (int)b;
         }
     }
-    if (last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][last_lp], 0));
+    // a cache frame's training branch and cache queries start before the last
+    // main walk ends: only resolve reads what that walk writes
+    if (last_lp >= 0 && !fork) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][last_lp], 0));
     if (own) {
         VRG_CUDA_TRY(cudaEventRecord(r->ev_bounced[k], bs));
         VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_bounced[k], 0));
@@ -1017,19 +1022,33 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         st = r->aux;
         VRG_CUDA_TRY(cudaEventRecord(r->ev_fork, s));
         VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_fork, 0));
+        // training bounce b refills the job buffers of parity b & 1, last
+        // used by walk b - 2; its own walk shares the hit buffer and the hit
+        // counter with the last main walk, so it starts after that walk
+        if (nb_main >= 2) VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][nb_main - 2], 0));
         for (uint32_t b = nb_main; b < a.nb; b++) {
-            VRG_TRY(launch_bounce(st, a, b, timed ? r->ev_k[0][b] : nullptr, timed ? r->ev_k[1][b] : nullptr,
-                                  a.train_cap));
+            VRG_TRY(launch_trace_shade(st, a, b, timed ? r->ev_k[0][b] : nullptr, a.train_cap));
+            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], st));
+            if (b == nb_main && last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_lp], 0));
+            VRG_TRY(launch_light_pdf(st, a, b, a.train_cap));
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], st));
         }
         VRG_TRY(launch_train_targets(st, a));
         VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true, a.counters + CNT_ERROR));
-        VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
+                          nullptr, r->target, false, a.counters + CNT_ERROR));
     }
     if (a.cache)  // radiance-cache queries of every path that ends into the cache
         VRG_TRY(nrc_infer(r->cache, s, a.P, a.counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
                           r->pred, a.counters + CNT_ERROR));
+    if (fork) {
+        // the training step rewrites the weights and table the queries read:
+        // it waits for them; the next frame's queries see the new cache
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_inferred, s));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_inferred, 0));
+        VRG_TRY(nrc_update(r->cache, st));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[k][last_lp], 0));
+    }
     VRG_TRY(launch_resolve(s, a));
     if (a.cache && !fork) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));

@@ -866,21 +866,25 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     dim3 g((n + rows_per_cta - 1) / rows_per_cta, NRC_LAYERS);
     k_nrc_dw<<<g, 128, 0, s>>>(N->H, N->dZ, n_pad, n, n_dev, N->w_grad, rows_per_cta);
     VRG_CUDA_TRY(cudaGetLastError());
-    if (update) {
-        N->step++;
-        AdamArgs A;
-        A.lr = N->desc.learning_rate;
-        A.b1 = 0.9f;
-        A.b2 = 0.99f;
-        A.eps = 1e-8f;
-        A.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)N->step)));
-        A.c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)N->step)));
-        k_adam_weights<<<(uint32_t)((MASTER_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->w_m, N->w_v, N->w_grad, A);
-        k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
-        k_adam_table<<<(uint32_t)((N->table_entries + 255) / 256), 256, 0, s>>>(N->t_master, N->t_m, N->t_v, N->t_grad,
-                                                                               N->table, N->table_entries, A);
-        VRG_CUDA_TRY(cudaGetLastError());
-    }
+    return update ? nrc_update(N, s) : VRG_OK;
+}
+
+// the Adam step of the accumulated gradients: rewrites the weights and the
+// table that inference reads
+vrg_status nrc_update(Nrc *N, cudaStream_t s) {
+    N->step++;
+    AdamArgs A;
+    A.lr = N->desc.learning_rate;
+    A.b1 = 0.9f;
+    A.b2 = 0.99f;
+    A.eps = 1e-8f;
+    A.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)N->step)));
+    A.c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)N->step)));
+    k_adam_weights<<<(uint32_t)((MASTER_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->w_m, N->w_v, N->w_grad, A);
+    k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
+    k_adam_table<<<(uint32_t)((N->table_entries + 255) / 256), 256, 0, s>>>(N->t_master, N->t_m, N->t_v, N->t_grad,
+                                                                           N->table, N->table_entries, A);
+    VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }
 

@@ -1057,14 +1057,6 @@ vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint
     return VRG_OK;
 }
 
-// One bounce on one stream: closest hit, shading, light-pdf walk.
-vrg_status launch_bounce(cudaStream_t s, const FrameArgs &a, uint32_t b, cudaEvent_t ev_trace, cudaEvent_t ev_shade,
-                         uint32_t max_rays) {
-    VRG_TRY(launch_trace_shade(s, a, b, ev_trace, max_rays));
-    if (ev_shade) VRG_CUDA_TRY(cudaEventRecord(ev_shade, s));
-    return launch_light_pdf(s, a, b, max_rays);
-}
-
 int bounce_blocks_per_sm() {
     init_grids();
     return 1;

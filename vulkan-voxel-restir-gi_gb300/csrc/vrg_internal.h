@@ -167,6 +167,7 @@ vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
 vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
                      uint32_t *err);
+vrg_status nrc_update(Nrc *N, cudaStream_t s);
 uint32_t nrc_batch(const Nrc *N);
 vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb);
 vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
@@ -246,7 +247,7 @@ struct Renderer {
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
     cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_inferred = nullptr;
     // Per set: the bounce stream of frames in flight and the light-pdf stream
     // (bounce b's walk beside bounce b + 1), the dependency events per bounce,
     // the end of the set's bounces and the end of its frame (after the
