@@ -51,13 +51,15 @@ def test_cache_beats_plain_at_equal_time(gpu_ctx):
     assert res["restir_cache"]["relmse_1spp"] < res["restir"]["relmse_1spp"], res
 
 
-def test_cache_frame_fork_matches_single_stream(gpu_ctx):
-    """A cache frame runs its training branch on a second stream; with capture
-    on it runs on one stream.  The first frame (before any training step has
+@pytest.mark.parametrize("W,H", [(96, 64), (480, 272)], ids=["small", "wide"])
+def test_cache_frame_fork_matches_single_stream(gpu_ctx, W, H):
+    """A cache frame runs its training branch on a second stream, beside the
+    query bounce's light-pdf walk and the cache queries; with capture on it
+    runs on one stream.  The first frame (before any training step has
     changed the weights) must match bit for bit, and the trained weights after
-    it must agree up to the order of the gradient atomics."""
+    it must agree up to the order of the gradient atomics.  The wide frame
+    gives the branches enough work to run side by side."""
     scene, objs, lo, hi = _scene(gpu_ctx, seed=9)
-    W, H = 96, 64
     cam = vrg.orbit_camera(2, 2, 7, 64, W, H)
     outs, weights, targets = [], [], []
     for flags in (0, vrg.RENDER_CAPTURE):

@@ -850,8 +850,8 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
             set_error("cache mode needs num_bounces >= 2 and num_bounces + cache_train_bounces <= %u", r->nb_max);
             return VRG_ERR_INVALID_ARGUMENT;
         }
-        if (!r->cache_buf) {
-            const uint32_t cap = nrc_batch(r->cache);
+        const uint32_t cap = nrc_batch(r->cache);
+        if (!r->cache_buf || r->cache_cap < cap) {  // (a later cache may train larger batches)
             auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
             size_t o = 0;
             size_t o_qp = o; o += al(P * 16);
@@ -861,6 +861,13 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
             size_t o_il = o; o += al(P * 4);
             size_t o_tl = o; o += al((size_t)cap * 4);
             size_t o_qf = o; o += al(P);
+            size_t o_taq0 = o; o += al((size_t)cap * 4);
+            size_t o_taq1 = o; o += al((size_t)cap * 4);
+            size_t o_taj0 = o; o += al((size_t)cap * 32);
+            size_t o_taj1 = o; o += al((size_t)cap * 32);
+            size_t o_thb = o; o += al((size_t)cap * 2 * 32);
+            size_t o_thv = o; o += al((size_t)cap * 2 * 4);
+            size_t o_tjm = o; o += al((size_t)cap * 8);
             DevBufPtr b;
             VRG_TRY(dev_alloc(s, o, b));
             VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, o, s));
@@ -872,7 +879,15 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
             r->infer_list = (uint32_t *)(B + o_il);
             r->train_list = (uint32_t *)(B + o_tl);
             r->qflag = B + o_qf;
+            r->t_aqueue[0] = (uint32_t *)(B + o_taq0);
+            r->t_aqueue[1] = (uint32_t *)(B + o_taq1);
+            r->t_ajob[0] = (float4 *)(B + o_taj0);
+            r->t_ajob[1] = (float4 *)(B + o_taj1);
+            r->t_hitbuf = (uint4 *)(B + o_thb);
+            r->t_hitval = (float *)(B + o_thv);
+            r->t_jmeta = (uint2 *)(B + o_tjm);
             r->cache_buf = b;
+            r->cache_cap = cap;
         }
     } else if (nb_total > r->nb_max) {
         return VRG_ERR_INVALID_ARGUMENT;
@@ -915,6 +930,7 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.jmeta = F.jmeta;
     a.hit_cap = (uint32_t)std::min<size_t>(2 * P, 0xFFFFFFF0u);
     a.counters = F.counters;
+    a.hit_count = a.counters + CNT_HITS;
     a.nlive = F.nlive;
     a.rec = F.rec;
     a.xv = F.xv;
@@ -956,14 +972,15 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // recording passes false.
 //
 // A cache frame forks after the shading of the query vertex, while that
-// bounce's light-pdf walk still runs: the training paths' extra bounces and
-// the cache's training step run on the renderer's second stream while the
-// main stream infers the cache for the rendered paths and runs resolve (after
-// the walk) and spatial.  Neither branch reads what the other writes, except
-// the cache itself: the training branch computes its gradients beside the
-// queries, and its Adam step, which rewrites the weights and the table the
-// queries read, waits for them; the new cache serves the next frame.  With
-// capture the frame stays on one stream.
+// bounce's light-pdf walk still runs: the training paths' extra bounces (with
+// light-pdf job and hit buffers of their own) and the cache's training step
+// run on the renderer's second stream while the main stream infers the cache
+// for the rendered paths and runs resolve (after the walk) and spatial.
+// Neither branch reads what the other writes, except the cache itself: the
+// training branch computes its gradients beside the queries, and its Adam
+// step, which rewrites the weights and the table the queries read, waits for
+// them; the new cache serves the next frame.  With capture the frame stays on
+// one stream.
 // Frames in flight (pipelined, plain frames: no stats, cache or capture).
 // A frame's bounces (closest hit, shading, light-pdf walks) read the committed
 // scene, the camera and the material table, and write only the arrays of the
@@ -1022,18 +1039,29 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         st = r->aux;
         VRG_CUDA_TRY(cudaEventRecord(r->ev_fork, s));
         VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_fork, 0));
-        // training bounce b refills the job buffers of parity b & 1, last
-        // used by walk b - 2; its own walk shares the hit buffer and the hit
-        // counter with the last main walk, so it starts after that walk
-        if (nb_main >= 2) VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][nb_main - 2], 0));
+        // The training bounces' light-pdf jobs and hits go to buffers of their
+        // own, so they need not wait for the main walks still running (which
+        // read the main job buffers and write their own bounces' records).
+        FrameArgs at = a;
+        for (int q = 0; q < 2; q++) {
+            at.aqueue[q] = r->t_aqueue[q];
+            at.ajob[q] = r->t_ajob[q];
+        }
+        at.hitbuf = r->t_hitbuf;
+        at.hitval = r->t_hitval;
+        at.jmeta = r->t_jmeta;
+        at.hit_cap = 2 * a.train_cap;
+        at.hit_count = a.counters + CNT_HITS_TRAIN;
         for (uint32_t b = nb_main; b < a.nb; b++) {
-            VRG_TRY(launch_trace_shade(st, a, b, timed ? r->ev_k[0][b] : nullptr, a.train_cap));
+            VRG_TRY(launch_trace_shade(st, at, b, timed ? r->ev_k[0][b] : nullptr, a.train_cap));
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], st));
-            if (b == nb_main && last_lp >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_lp], 0));
-            VRG_TRY(launch_light_pdf(st, a, b, a.train_cap));
+            VRG_TRY(launch_light_pdf(st, at, b, a.train_cap));
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], st));
         }
-        VRG_TRY(launch_train_targets(st, a));
+        // the targets' recurrence starts at the query vertex, whose record the
+        // main walk of that bounce completes
+        VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_lp], 0));
+        VRG_TRY(launch_train_targets(st, at));
         VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
                           nullptr, r->target, false, a.counters + CNT_ERROR));
     }

@@ -887,7 +887,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
             if (done) {
                 uint32_t hb = 0;
                 if (nh > 0) {
-                    hb = atomicAdd(&a.counters[CNT_HITS], (uint32_t)nh);
+                    hb = atomicAdd(a.hit_count, (uint32_t)nh);
                     if (hb + (uint32_t)nh > a.hit_cap) {
                         atomicOr(err, ERR_LIGHT_LIST);
                         nh = 0;
@@ -912,7 +912,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
 
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_hit_eval(const __grid_constant__ FrameArgs a, uint32_t b) {
-    const uint32_t n = min(a.counters[CNT_HITS], a.hit_cap);
+    const uint32_t n = min(*a.hit_count, a.hit_cap);
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
         const uint4 A = a.hitbuf[2 * (size_t)h], B = a.hitbuf[2 * (size_t)h + 1];
         const uint32_t p = A.x;
@@ -1052,7 +1052,7 @@ vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint
     else k_hit_eval<false><<<gs, 128, 0, s>>>(a, b);
     if (a.capture) k_hit_sum<true><<<gs, 128, 0, s>>>(a, b);
     else k_hit_sum<false><<<gs, 128, 0, s>>>(a, b);
-    VRG_CUDA_TRY(cudaMemsetAsync(a.counters + CNT_HITS, 0, 4, s));
+    VRG_CUDA_TRY(cudaMemsetAsync(a.hit_count, 0, 4, s));
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

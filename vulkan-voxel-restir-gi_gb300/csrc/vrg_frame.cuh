@@ -17,6 +17,7 @@ constexpr int CNT_SFETCH = 40;   // [40..47] shading work-fetch cursor of bounce
 constexpr int CNT_NODES = 50;    // u64 at words 50-51: inner nodes fetched by k_trace
 constexpr int CNT_LEAVES = 52;   // u64 at words 52-53: leaf records tested by k_trace
 constexpr int CNT_HITS = 54;     // light hits collected by k_anyhit for the current bounce
+constexpr int CNT_HITS_TRAIN = 55;  // the same for a cache frame's training branch (its own job and hit buffers)
 constexpr int CNT_INFER = 48;    // radiance-cache queries of the frame
 constexpr int CNT_TRAIN = 49;    // radiance-cache training paths of the frame
 constexpr int CNT_WORDS = 64;
@@ -68,6 +69,7 @@ struct FrameArgs {
     float *hitval;                // light-sampling pdf of each hit
     uint2 *jmeta;                 // per any-hit job: (first hit, hit count)
     uint32_t hit_cap;
+    uint32_t *hit_count;          // the hits collected for the current bounce (a counter word)
     int4 *hits;                   // closest hit per pixel: (~record or -1, face|half<<3, b1, b2)
     uint32_t *counters;
     uint8_t *nlive;

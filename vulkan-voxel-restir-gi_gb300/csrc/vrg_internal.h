@@ -264,8 +264,16 @@ struct Renderer {
     cudaEvent_t ev_k[2][8] = {};          // after k_trace / after k_shade, per bounce
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
     DevBufPtr cache_buf;                  // per-pixel cache queries / predictions / targets
+    uint32_t cache_cap = 0;               // training paths cache_buf was sized for
     float4 *q_pos = nullptr, *q_dir = nullptr, *pred = nullptr, *target = nullptr;
     uint32_t *infer_list = nullptr, *train_list = nullptr;
+    // the training branch's light-pdf jobs and hits (its walks run beside the
+    // main walk of the query bounce), sized for the training paths
+    uint32_t *t_aqueue[2] = {};
+    float4 *t_ajob[2] = {};
+    uint4 *t_hitbuf = nullptr;
+    float *t_hitval = nullptr;
+    uint2 *t_jmeta = nullptr;
     uint8_t *qflag = nullptr;
     int grid_bounce = 0;
     vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
