@@ -1,19 +1,21 @@
-// Wavefront bounce kernel: ray generation (bounce 0), closest hit over the
-// world-space voxel BVH, shading, light-BVH next-event estimation and the
-// light-sampling pdf of the chosen direction, fused into one kernel per
-// bounce.
+// Wavefront bounce kernels: per bounce, the closest hit over the world-space
+// voxel BVH (k_trace, with ray generation at bounce 0), the shading with its
+// light-BVH next-event estimation (k_shade), and the light-sampling pdf of the
+// chosen direction in three passes (k_anyhit, k_hit_eval, k_hit_sum), which
+// run on their own stream beside the next bounce.
 //
-// Reference stages fused here (one dispatch each in the reference):
+// Reference stages covered here (one dispatch each in the reference):
 //   raygen        raygen.rs:84-111
 //   raytrace      raytrace.rs:390-578 (closest hit replaces the driver ray
 //                 query; traverseBvh 218-281 is the light descent)
 //   nee_pdf       nee_pdf.rs:281-337 (any-hit over light triangles along the
 //                 chosen direction; reverseTraverseBvh 154-228)
-// Work distribution: persistent warps fetch 32 rays at a time from the
-// bounce's queue; rays that continue are compacted into the next queue with
-// one warp ballot + one atomic per warp.  State per pixel stays in SoA
-// float4 arrays; the per-bounce record (E, w=pdf/q) (R, q) feeds the
-// backward radiance recurrence of the resolve kernel.
+// Work distribution: the closest hit and the any-hit walk are persistent
+// warps in which each lane takes a new ray from the bounce's queue when its
+// walk ends; rays that continue, and light-pdf jobs, are compacted into the
+// next queues with one warp ballot + one atomic per warp.  State per pixel
+// stays in SoA float4 arrays; the per-bounce record (E, w=pdf/q) (R, q) feeds
+// the backward radiance recurrence of the resolve kernel.
 #include <mutex>
 
 #include "vrg_frame.cuh"
