@@ -1,6 +1,7 @@
-"""Frames in flight: vrg_render without stats only enqueues the frame, and a
-frame's primary closest hit runs beside the previous frame's resolve and
-spatial passes.  A sequence rendered that way into device buffers, back to
+"""Frames in flight: vrg_render without stats only enqueues the frame, and up
+to three frames' bounces (each frame in its own array set) run beside each
+other and beside the resolve and spatial passes of the frames before them.
+A sequence rendered that way into device buffers, back to
 back, must give the bit-identical frames of the same sequence rendered one
 frame at a time (stats requested, so each frame runs alone), including across
 a scene update committed in mid-sequence, a frame with stats in between, and a
