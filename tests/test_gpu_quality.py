@@ -85,3 +85,28 @@ def test_cache_frame_fork_matches_single_stream(gpu_ctx, W, H):
     # sign, so a gradient at rounding level may flip: allow a handful
     close = np.isclose(weights[0], weights[1], rtol=1e-3, atol=1e-6)
     assert close.mean() > 0.999, close.mean()
+
+
+def test_cache_swap_to_a_larger_training_batch(gpu_ctx):
+    """A renderer that rendered cache frames with a small training batch takes
+    a cache with a larger one: its training buffers grow with it, and the
+    cache frame with the larger batch runs without device error flags and
+    trains more paths."""
+    scene, objs, lo, hi = _scene(gpu_ctx, seed=9)
+    W, H = 160, 96
+    cam = vrg.orbit_camera(2, 2, 7, 64, W, H)
+    r = vrg.Renderer(gpu_ctx, W, H, 8)
+    p = quality._params(2, vrg.RENDER_CACHE, 11, accumulate=0)
+    trained = []
+    for batch in (64, 4096):
+        cache = vrg.RadianceCache(gpu_ctx, lo, hi, batch=batch, seed=3)
+        r.set_cache(cache)
+        _, rad = r.render_params(scene, cam, p, want_image=False, want_radiance=True)
+        assert r.last_stats.error_flags == 0
+        assert np.isfinite(rad).mean() > 0.99
+        targets = r.readback(vrg.DBG_CACHE_TARGET, 0)
+        trained.append(int(np.count_nonzero(np.any(targets[:, :3] != 0, axis=1))))
+        r.set_cache(None)
+        cache.close()
+    assert trained[0] <= 64 and trained[1] > trained[0]
+    r.close()
