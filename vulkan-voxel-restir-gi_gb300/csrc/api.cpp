@@ -895,6 +895,8 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     const uint32_t ring = r->frame % slots;
     memset(&a, 0, sizeof(a));
     a.P = (uint32_t)P;
+    a.tiles_x = (r->W + 7) / 8;
+    a.n0 = r->n_views ? (uint32_t)P : a.tiles_x * ((r->H + 3) / 4) * 32u;
     a.nb = nb_total;
     a.nb_render = pr->num_bounces;
     a.cache = cache ? 1u : 0u;

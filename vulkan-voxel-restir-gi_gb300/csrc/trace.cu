@@ -320,7 +320,7 @@ template <bool BATCH>
 __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const int REFILL = (int)a.refill_trace;
-    const uint32_t n_in = (b == 0) ? a.P : a.counters[CNT_QUEUE + b];
+    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *err = a.counters + CNT_ERROR;
     const float4 *wide = a.v0.sc.geo_wide;
@@ -347,10 +347,9 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
             if (base + (uint32_t)__popc(need) >= n_in) exhausted = true;
             if (!has) {
                 const uint32_t idx = base + (uint32_t)__popc(need & lanemask_lt());
-                if (idx < n_in) {
+                if (idx < n_in && (b == 0 ? bounce0_pixel<BATCH>(a, idx, p) : (p = qin[idx], true))) {
                     has = true;
                     traced++;
-                    p = (b == 0) ? idx : qin[idx];
                     const ViewDev &V = view_of<BATCH>(a, p);
                     if constexpr (BATCH) {
                         wide = V.sc.geo_wide;
@@ -570,7 +569,7 @@ template <bool CAPTURE, bool BATCH>
 __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
-    const uint32_t n_in = (b == 0) ? P : a.counters[CNT_QUEUE + b];
+    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[CNT_QUEUE + b];
     const uint32_t *qin = a.queue[(b + 1) & 1];
     uint32_t *qout = a.queue[b & 1];
     const float inv2pi = 1.0f / (2.0f * PI_F);
@@ -578,19 +577,18 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     for (uint32_t base = wid * 32; base < n_in; base += warps * 32) {
         const uint32_t i = base + lane;
-        const bool active = i < n_in;
+        uint32_t p = 0;
+        const bool active = i < n_in && (b == 0 ? bounce0_pixel<BATCH>(a, i, p) : (p = qin[i], true));
         bool cont = false, anyj = false, qhit = false, want_train = false;
         const bool at_query = a.cache && b + 1 == a.nb_render;
         f3 stash_E = f3{0, 0, 0}, stash_R = f3{0, 0, 0}, stash_n = f3{0, 0, 0};
         float stash_mis = 0.0f;
         int4 stash_hit = make_int4(-1, 0, 0, 0), stash_rc = make_int4(0, 0, 0, 0);
         int stash_half = 0;
-        uint32_t p = 0;
         f3 new_o = f3{0, 0, 0}, new_d = f3{0, 0, 0};
         float pdf = 1.0f;
         int face = 0;
         if (active) {
-            p = (b == 0) ? i : qin[i];
             const ViewDev &V = view_of<BATCH>(a, p);
             const uint32_t lp = p - V.pix_off;
             f3 o, d;

@@ -44,6 +44,7 @@ struct FrameArgs {
     const uint16_t *vtab;         // batched frame: view of pixel group p >> VIEW_SHIFT
     uint32_t n_views;
     uint32_t P;                   // pixels of the frame (all views)
+    uint32_t n0, tiles_x;         // bounce-0 slots and 8x4 tiles per row (bounce0_pixel)
     uint32_t nb, nee_type;
     uint32_t mode, spatial_iters;
     float spatial_radius;
@@ -104,6 +105,23 @@ __device__ __forceinline__ const ViewDev &view_of(const FrameArgs &a, uint32_t p
     } else {
         (void)p;
         return a.v0;
+    }
+}
+
+// Bounce 0 of a single view takes its pixels in 8x4 tiles, so that a warp's
+// primary rays, and through the queue order the secondary rays they spawn,
+// start close together.  Slot i (< n0) is pixel p, or no pixel in the part of
+// an edge tile outside the view.  A batched frame keeps the pixel order.
+template <bool BATCH>
+__device__ __forceinline__ bool bounce0_pixel(const FrameArgs &a, uint32_t i, uint32_t &p) {
+    if constexpr (BATCH) {
+        p = i;
+        return i < a.P;
+    } else {
+        const uint32_t t = i >> 5, k = i & 31u;
+        const uint32_t x = (t % a.tiles_x) * 8u + (k & 7u), y = (t / a.tiles_x) * 4u + (k >> 3);
+        p = y * a.v0.W + x;
+        return x < a.v0.W && y < a.v0.H;
     }
 }
 
