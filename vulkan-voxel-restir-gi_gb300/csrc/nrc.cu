@@ -122,11 +122,14 @@ __device__ __forceinline__ f3 normalize_pos(const NrcParams &P, f3 x) {
 
 // encodes one query into a bf16 row of 64: 2*levels hash features, oct
 // normal, oct view direction, zeros
-__device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 nrm, f3 dir,
-                           __nv_bfloat16 *row) {
+// The input row as packed bf16 pairs, word k at row32[k * stride]: the levels'
+// feature pairs, then the octahedral normal and direction; with FILL the row
+// is zero-filled to NRC_W columns.
+template <bool FILL = true>
+__device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 nrm, f3 dir, uint32_t *row32,
+                           size_t stride = 1) {
     const f3 p = normalize_pos(P, pos);
     const size_t T = (size_t)1 << P.log2_t;
-    uint32_t *row32 = reinterpret_cast<uint32_t *>(row);
     // unrolled so that the gathers of several levels are in flight together
 #pragma unroll 4
     for (int l = 0; l < P.levels; l++) {
@@ -141,14 +144,15 @@ __device__ void encode_row(const NrcParams &P, const __half2 *table, f3 pos, f3 
         }
         // one 32-bit store per bf16 pair (rows of 144 bytes: 2-byte stores
         // of a warp's 32 rows would meet 8-way bank conflicts)
-        row32[l] = pack_bf16(f0, f1);
+        row32[l * stride] = pack_bf16(f0, f1);
     }
     float a, b;
     oct_encode(nrm, a, b);
-    row32[P.levels] = pack_bf16(a, b);
+    row32[P.levels * stride] = pack_bf16(a, b);
     oct_encode(dir, a, b);
-    row32[P.levels + 1] = pack_bf16(a, b);
-    for (int k = P.levels + 2; k < NRC_W / 2; k++) row32[k] = 0u;
+    row32[(P.levels + 1) * stride] = pack_bf16(a, b);
+    if (FILL)
+        for (int k = P.levels + 2; k < NRC_W / 2; k++) row32[k * stride] = 0u;
 }
 
 // four 8x8 b16 matrices from shared memory (ldmatrix): thread t gives the
@@ -300,6 +304,8 @@ struct InferArgs {
     const float4 *nrm;         // optional explicit normals (NULL: from the face in pos.w)
     float4 *out;               // rgb per pixel / query
     uint32_t *err;             // error word (ERR_COPY)
+    uint32_t *enc;             // encoded rows between the two passes: [levels + 2][enc_cap] words
+    uint32_t enc_cap;
 };
 
 __device__ __forceinline__ f3 face_normal(int f) {
@@ -311,7 +317,21 @@ __device__ __forceinline__ f3 face_normal(int f) {
     return n;
 }
 
-// inference: per warp 32 queries per iteration (2 tiles of 16)
+// Inference, encoding pass: one thread per query, many warps per SM so that
+// many queries' hash-grid gathers are in flight.  The packed bf16 input row
+// (encode_row, without the zero columns) goes to enc[k * a.enc_cap + i].
+__global__ void __launch_bounds__(256) k_nrc_encode(InferArgs a) {
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t id = a.list ? a.list[i] : i;
+        const float4 pp = a.pos[id], dd = a.dir[id];
+        const f3 nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
+        encode_row<false>(a.P, a.table, ld3(pp), nrm, f3{-dd.x, -dd.y, -dd.z}, a.enc + i, a.enc_cap);
+    }
+}
+
+// Inference, MLP pass: per warp 32 queries per iteration (2 tiles of 16),
+// their encoded rows read coalesced into the warp's tile
 __global__ void __launch_bounds__(NRC_IWARPS * 32, 2) k_nrc_infer(InferArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
@@ -322,16 +342,16 @@ __global__ void __launch_bounds__(NRC_IWARPS * 32, 2) k_nrc_infer(InferArgs a) {
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
     const uint32_t warps = gridDim.x * NRC_IWARPS;
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const int words = a.P.levels + 2;
     for (uint32_t base = (blockIdx.x * NRC_IWARPS + w) * 32; base < n; base += warps * 32) {
         const uint32_t i = base + lane;
         uint32_t id = 0;
+        uint32_t *row32 = reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE);
         if (i < n) {
             id = a.list ? a.list[i] : i;
-            const float4 pp = a.pos[id], dd = a.dir[id];
-            const f3 nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
-            encode_row(a.P, a.table, ld3(pp), nrm, f3{-dd.x, -dd.y, -dd.z}, tile + lane * NRC_STRIDE);
+            for (int k = 0; k < NRC_W / 2; k++) row32[k] = k < words ? a.enc[(size_t)k * a.enc_cap + i] : 0u;
         } else {
-            for (int k = 0; k < NRC_W / 2; k++) reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE)[k] = 0u;
+            for (int k = 0; k < NRC_W / 2; k++) row32[k] = 0u;
         }
         __syncwarp();
 #pragma unroll 1
@@ -407,7 +427,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
             nrm = a.nrm ? ld3(a.nrm[id]) : face_normal(__float_as_int(pp.w));
             vdir = f3{-dd.x, -dd.y, -dd.z};
             tg = a.target[id];
-            encode_row(a.P, a.table, pos, nrm, vdir, tile + lane * NRC_STRIDE);
+            encode_row(a.P, a.table, pos, nrm, vdir, reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE));
         } else {
             for (int k = 0; k < NRC_W / 2; k++) reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE)[k] = 0u;
         }
@@ -717,7 +737,9 @@ struct Nrc {
     size_t act_rows = 0;
     __nv_bfloat16 *H = nullptr, *dZ = nullptr;
     uint32_t step = 0;
-    int grid_infer = 0, grid_train = 0;
+    int grid_infer = 0, grid_train = 0, grid_encode = 0;
+    DevBufPtr enc_buf;  // encoded query rows of inference
+    size_t enc_cap = 0;
 };
 
 static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_IWARPS * 32 * NRC_STRIDE * 2; }
@@ -821,6 +843,9 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_nrc_train, NRC_WARPS * 32, train_smem());
     N->grid_infer = std::max(1, ctx->num_sms * std::max(1, bi));
     N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
+    int be = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, k_nrc_encode, 256, 0);
+    N->grid_encode = std::max(1, ctx->num_sms * std::max(1, be));
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
     *out = N;
     return VRG_OK;
@@ -829,7 +854,16 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
 vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out, uint32_t *err) {
     if (n == 0) return VRG_OK;
-    InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out, err ? err : N->err};
+    if (N->enc_cap < n) {  // grows on the stream it is used on (stream-ordered allocation)
+        DevBufPtr b;
+        VRG_TRY(dev_alloc(s, (size_t)(N->P.levels + 2) * n * 4, b));
+        N->enc_buf = b;
+        N->enc_cap = n;
+    }
+    InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out, err ? err : N->err,
+                (uint32_t *)N->enc_buf->ptr, (uint32_t)N->enc_cap};
+    const uint32_t eb = std::min<uint32_t>((uint32_t)N->grid_encode, (n + 255) / 256);
+    k_nrc_encode<<<eb, 256, 0, s>>>(a);
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_IWARPS * 32 - 1) / (NRC_IWARPS * 32));
     k_nrc_infer<<<blocks, NRC_IWARPS * 32, infer_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
