@@ -318,7 +318,7 @@ __device__ __forceinline__ f3 face_normal(int f) {
 }
 
 // Inference, encoding pass: one thread per query, many warps per SM so that
-// many queries' hash-grid gathers are in flight.  The packed bf16 input row
+// many queries' hash-grid gathers are in flight (the loop covers any grid).  The packed bf16 input row
 // (encode_row, without the zero columns) goes to enc[k * a.enc_cap + i].
 __global__ void __launch_bounds__(256) k_nrc_encode(InferArgs a) {
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
@@ -737,7 +737,7 @@ struct Nrc {
     size_t act_rows = 0;
     __nv_bfloat16 *H = nullptr, *dZ = nullptr;
     uint32_t step = 0;
-    int grid_infer = 0, grid_train = 0, grid_encode = 0;
+    int grid_infer = 0, grid_train = 0;
     DevBufPtr enc_buf;  // encoded query rows of inference
     size_t enc_cap = 0;
 };
@@ -843,9 +843,7 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_nrc_train, NRC_WARPS * 32, train_smem());
     N->grid_infer = std::max(1, ctx->num_sms * std::max(1, bi));
     N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
-    int be = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, k_nrc_encode, 256, 0);
-    N->grid_encode = std::max(1, ctx->num_sms * std::max(1, be));
+
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
     *out = N;
     return VRG_OK;
@@ -862,8 +860,9 @@ vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     }
     InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out, err ? err : N->err,
                 (uint32_t *)N->enc_buf->ptr, (uint32_t)N->enc_cap};
-    const uint32_t eb = std::min<uint32_t>((uint32_t)N->grid_encode, (n + 255) / 256);
-    k_nrc_encode<<<eb, 256, 0, s>>>(a);
+    // one query per thread: short-lived CTAs, so that a higher-priority
+    // stream's kernels (a cache frame's training branch) get SMs in between
+    k_nrc_encode<<<(n + 255) / 256, 256, 0, s>>>(a);
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_IWARPS * 32 - 1) / (NRC_IWARPS * 32));
     k_nrc_infer<<<blocks, NRC_IWARPS * 32, infer_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
