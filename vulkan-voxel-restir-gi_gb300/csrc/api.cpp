@@ -536,6 +536,7 @@ static vrg_status renderer_events(vrg_renderer *r) {
     int lo_prio = 0, hi_prio = 0;
     VRG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux, cudaStreamNonBlocking, hi_prio));
+    VRG_CUDA_TRY(cudaStreamCreateWithPriority(&r->aux_lp, cudaStreamNonBlocking, hi_prio));
     for (int k = 0; k < Renderer::SETS; k++) {
         VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->bs[k], cudaStreamNonBlocking));
         VRG_CUDA_TRY(cudaStreamCreateWithFlags(&r->lps[k], cudaStreamNonBlocking));
@@ -549,7 +550,8 @@ static vrg_status renderer_events(vrg_renderer *r) {
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
     VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
-    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_inferred, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_start, cudaEventDisableTiming));
+    VRG_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_updated, cudaEventDisableTiming));
     for (auto &e : r->ev) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
@@ -686,11 +688,13 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
         if (e) cudaEventDestroy(e);
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
-    if (r->ev_inferred) cudaEventDestroy(r->ev_inferred);
-    if (r->aux) {
-        cudaStreamSynchronize(r->aux);
-        cudaStreamDestroy(r->aux);
-    }
+    if (r->ev_start) cudaEventDestroy(r->ev_start);
+    if (r->ev_updated) cudaEventDestroy(r->ev_updated);
+    for (cudaStream_t q : {r->aux, r->aux_lp})
+        if (q) {
+            cudaStreamSynchronize(q);
+            cudaStreamDestroy(q);
+        }
     if (r->h_pinned) cudaFreeHost(r->h_pinned);
     if (r->h_views) cudaFreeHost(r->h_views);
     r->res_buf.reset();
@@ -979,10 +983,12 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // run on the renderer's second stream while the main stream infers the cache
 // for the rendered paths and runs resolve (after the walk) and spatial.
 // Neither branch reads what the other writes, except the cache itself: the
-// training branch computes its gradients beside the queries, and its Adam
-// step, which rewrites the weights and the table the queries read, waits for
-// them; the new cache serves the next frame.  With capture the frame stays on
-// one stream.
+// training branch computes its gradients beside the queries, and their Adam
+// step, which rewrites the weights and the table the queries read, is left to
+// the next user of the cache; the next cache frame runs it on its training
+// stream beside its own bounces, before its queries and its own training
+// (the frames see the same cache as with the step at the end of each frame).
+// With capture the frame stays on one stream.
 // Frames in flight (pipelined, plain frames: no stats, cache or capture).
 // A frame's bounces (closest hit, shading, light-pdf walks) read the committed
 // scene, the camera and the material table, and write only the arrays of the
@@ -1005,6 +1011,17 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     cudaStream_t bs = own ? r->bs[k] : s;  // stream of the bounces
     cudaStream_t lp = r->lps[k];
     if (own) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_done[k], 0));
+    // a cache frame runs the previous cache frame's Adam step on the training
+    // stream beside its own bounces (after all earlier work on the library
+    // stream); its cache queries wait for it
+    bool updated = false;
+    if (fork && nrc_pending(r->cache)) {
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_start, s));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(r->aux, r->ev_start, 0));
+        VRG_TRY(nrc_flush(r->cache, r->aux));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_updated, r->aux));
+        updated = true;
+    }
     VRG_CUDA_TRY(cudaMemsetAsync(a.counters, 0, CNT_WORDS * 4, bs));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
     // Bounce b's light-pdf walk runs on the light-pdf stream beside bounce
@@ -1054,12 +1071,25 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         at.jmeta = r->t_jmeta;
         at.hit_cap = 2 * a.train_cap;
         at.hit_count = a.counters + CNT_HITS_TRAIN;
+        // As on the main path, training bounce b's light-pdf walk runs on a
+        // stream of its own beside bounce b + 1; bounce b + 2, which refills
+        // the job buffers of parity b & 1, waits for it.
+        int last_tw = -1;
         for (uint32_t b = nb_main; b < a.nb; b++) {
+            if (b >= nb_main + 2 && (int)b - 2 <= last_tw)
+                VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][b - 2], 0));
             VRG_TRY(launch_trace_shade(st, at, b, timed ? r->ev_k[0][b] : nullptr, a.train_cap));
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], st));
-            VRG_TRY(launch_light_pdf(st, at, b, a.train_cap));
+            if (b + 1 < a.nb) {
+                VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[k][b], st));
+                VRG_CUDA_TRY(cudaStreamWaitEvent(r->aux_lp, r->ev_shaded[k][b], 0));
+                VRG_TRY(launch_light_pdf(r->aux_lp, at, b, a.train_cap));
+                VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[k][b], r->aux_lp));
+                last_tw = (int)b;
+            }
             if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], st));
         }
+        if (last_tw >= 0) VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_tw], 0));
         // the targets' recurrence starts at the query vertex, whose record the
         // main walk of that bounce completes
         VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_lp], 0));
@@ -1067,15 +1097,17 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
                           nullptr, r->target, false, a.counters + CNT_ERROR));
     }
-    if (a.cache)  // radiance-cache queries of every path that ends into the cache
+    if (a.cache) {  // radiance-cache queries of every path that ends into the cache
+        if (updated) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_updated, 0));
+        if (!fork) VRG_TRY(nrc_flush(r->cache, s));
         VRG_TRY(nrc_infer(r->cache, s, a.P, a.counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
                           r->pred, a.counters + CNT_ERROR));
+    }
     if (fork) {
-        // the training step rewrites the weights and table the queries read:
-        // it waits for them; the next frame's queries see the new cache
-        VRG_CUDA_TRY(cudaEventRecord(r->ev_inferred, s));
-        VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_inferred, 0));
-        VRG_TRY(nrc_update(r->cache, st));
+        // This frame's Adam step would rewrite the weights and table that its
+        // queries read: it waits for the next user of the cache (the next
+        // cache frame runs it beside its bounces; any other use runs it first).
+        nrc_defer_update(r->cache);
         VRG_CUDA_TRY(cudaEventRecord(r->ev_join, st));
         VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_lpdone[k][last_lp], 0));
     }

@@ -740,6 +740,9 @@ struct Nrc {
     int grid_infer = 0, grid_train = 0;
     DevBufPtr enc_buf;  // encoded query rows of inference
     size_t enc_cap = 0;
+    // a cache frame's gradients wait for their Adam step, which the next user
+    // of the cache runs first (a cache frame: beside its own bounces)
+    bool pending = false;
 };
 
 static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_IWARPS * 32 * NRC_STRIDE * 2; }
@@ -888,6 +891,7 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
                      const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
                      uint32_t *err) {
     if (n == 0) return VRG_OK;
+    VRG_TRY(nrc_flush(N, s));  // new gradients start from the updated cache
     VRG_TRY(ensure_act(N, n));
     const size_t n_pad = N->act_rows;
     TrainArgs a{N->P,   N->table, N->wpack, n,        n_dev,    list,   pos, dir, nrm, target,
@@ -901,6 +905,16 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     VRG_CUDA_TRY(cudaGetLastError());
     return update ? nrc_update(N, s) : VRG_OK;
 }
+
+// the Adam step of a previous cache frame's gradients, if one waits
+vrg_status nrc_flush(Nrc *N, cudaStream_t s) {
+    if (!N->pending) return VRG_OK;
+    N->pending = false;
+    return nrc_update(N, s);
+}
+
+bool nrc_pending(const Nrc *N) { return N->pending; }
+void nrc_defer_update(Nrc *N) { N->pending = true; }
 
 // the Adam step of the accumulated gradients: rewrites the weights and the
 // table that inference reads
@@ -942,6 +956,7 @@ static vrg_status stage4(cudaStream_t s, const float *src, uint32_t n, int comps
 
 vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb) {
     cudaStream_t s = N->ctx->stream;
+    VRG_TRY(nrc_flush(N, s));
     DevBufPtr b;
     VRG_TRY(dev_alloc(s, (size_t)n * 16 * 4 + 64, b));
     float4 *dp = (float4 *)b->ptr, *dd = dp + n, *dn = dd + n, *dout = dn + n;
@@ -990,6 +1005,7 @@ vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
 
 vrg_status nrc_read(Nrc *N, uint32_t what, void *dst, uint64_t bytes) {
     cudaStream_t s = N->ctx->stream;
+    VRG_TRY(nrc_flush(N, s));
     const void *src = nullptr;
     size_t nb = 0;
     switch (what) {
@@ -1007,6 +1023,7 @@ vrg_status nrc_read(Nrc *N, uint32_t what, void *dst, uint64_t bytes) {
 
 vrg_status nrc_write(Nrc *N, uint32_t what, const void *src, uint64_t bytes) {
     cudaStream_t s = N->ctx->stream;
+    VRG_TRY(nrc_flush(N, s));
     if (what == VRG_NRC_WEIGHTS) {
         if (bytes < MASTER_ELEMS * 4) return VRG_ERR_INVALID_ARGUMENT;
         VRG_CUDA_TRY(cudaMemcpyAsync(N->w_master, src, MASTER_ELEMS * 4, cudaMemcpyHostToDevice, s));

@@ -168,6 +168,9 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
                      const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
                      uint32_t *err);
 vrg_status nrc_update(Nrc *N, cudaStream_t s);
+vrg_status nrc_flush(Nrc *N, cudaStream_t s);
+bool nrc_pending(const Nrc *N);
+void nrc_defer_update(Nrc *N);
 uint32_t nrc_batch(const Nrc *N);
 vrg_status nrc_query_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, float *rgb);
 vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm, const float *dir, const float *target,
@@ -247,7 +250,8 @@ struct Renderer {
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
     cudaStream_t aux = nullptr;           // second stream: a cache frame's training paths and step
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_inferred = nullptr;
+    cudaStream_t aux_lp = nullptr;        // the training bounces' light-pdf walks, beside the next bounce
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_start = nullptr, ev_updated = nullptr;
     // Per set: the bounce stream of frames in flight and the light-pdf stream
     // (bounce b's walk beside bounce b + 1), the dependency events per bounce,
     // the end of the set's bounces and the end of its frame (after the
