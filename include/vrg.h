@@ -473,7 +473,11 @@ VRG_API vrg_status vrg_nrc_train(vrg_nrc *nrc, uint32_t n, const float *pos, con
 VRG_API vrg_status vrg_nrc_read(vrg_nrc *nrc, uint32_t what, void *dst, uint64_t bytes);
 VRG_API vrg_status vrg_nrc_write(vrg_nrc *nrc, uint32_t what, const void *src, uint64_t bytes);
 VRG_API vrg_status vrg_nrc_layout(vrg_nrc *nrc, uint32_t *levels, float *scales, uint32_t *dense, uint32_t *res1);
-/* Attaches a cache to a renderer for VRG_RENDER_CACHE frames (NULL detaches). */
+/* Attaches a cache to a renderer for VRG_RENDER_CACHE frames (NULL detaches).
+ * A cache frame computes its training step's gradients; their Adam step runs
+ * when the cache is next used (the next cache frame, beside its bounces, or
+ * first thing in any vrg_nrc_* call), so every use sees the cache as if the
+ * step had ended the frame. */
 VRG_API vrg_status vrg_renderer_set_cache(vrg_renderer *r, vrg_nrc *nrc);
 
 /* ---- synthetic scenes (no reference counterpart; the reference uses
