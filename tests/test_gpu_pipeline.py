@@ -160,3 +160,39 @@ def test_async_host_readback_with_frame_fences(gpu_ctx):
         sc.close()
         for o in objs:
             o.release()
+
+
+def test_frames_in_flight_alternating_scenes(gpu_ctx):
+    """Frames in flight that alternate between two committed scenes (the
+    temporal reuse carries across the switch, as for frames one by one)."""
+    lib = gpu_ctx.lib
+    mats, n, blocks_x = terrain_world(43, 2, 1, 0.01)
+    _, _, blocks_y = terrain_world(44, 1, 2, 0.02)
+    gpu_ctx.set_materials(mats, n)
+    sx, ox = vrg.build_world(gpu_ctx, blocks_x)
+    sy, oy = vrg.build_world(gpu_ctx, blocks_y)
+    vrg.commit_scenes([sx, sy])
+    scenes = [sx, sy]
+    ra = vrg.Renderer(gpu_ctx, W, H, NB)
+    want = []
+    for f in range(FRAMES):
+        _, rad = ra.render_params(scenes[f % 2], _cam(f), _p(f), want_image=False, want_radiance=True)
+        assert ra.last_stats.error_flags == 0
+        want.append(rad.copy())
+    rb = vrg.Renderer(gpu_ctx, W, H, NB)
+    dev = [torch.empty(W * H * 3, dtype=torch.float32, device="cuda") for _ in range(FRAMES)]
+    torch.cuda.synchronize()
+    for f in range(FRAMES):
+        out = vrg.FrameOutput(None, dev[f].data_ptr(), 0, 0)
+        cam, p = _cam(f), _p(f)
+        vrg.check(lib.vrg_render(rb.h, scenes[f % 2].h, C.byref(cam), C.byref(p), C.byref(out), None), "vrg_render")
+    gpu_ctx.synchronize()
+    for f in range(FRAMES):
+        got = dev[f].cpu().numpy().reshape(H, W, 3)
+        assert np.array_equal(got.view(np.uint32), want[f].view(np.uint32)), f
+    for r in (ra, rb):
+        r.close()
+    for sc, objs in ((sx, ox), (sy, oy)):
+        sc.close()
+        for o in objs:
+            o.release()
