@@ -238,11 +238,15 @@ def batched_block(ctx, steps, warmup, tuning=None):
         br.set_tuning(tuning)
     seeds = vrg.Pcg32(C2_SEED)
 
-    def step(f, flags):
-        cams = [vrg.orbit_camera(int(grids[i, 0]), int(grids[i, 1]), f % ORBIT, ORBIT, w, h)
+    def cams_of(f):
+        return [vrg.orbit_camera(int(grids[i, 0]), int(grids[i, 1]), f % ORBIT, ORBIT, w, h)
                 for i, (w, h) in enumerate(res)]
-        p = vrg.RenderParams(1, 1, 3, 2, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, 0, flags | vrg.RENDER_NO_PACK, 4)
-        br.render(scenes, cams, p, [(seeds.next(), seeds.next()) for _ in res])
+
+    def params_of(flags):
+        return vrg.RenderParams(1, 1, 3, 2, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, 0, flags | vrg.RENDER_NO_PACK, 4)
+
+    def step(f, flags, sd=None):
+        br.render(scenes, cams_of(f), params_of(flags), sd or [(seeds.next(), seeds.next()) for _ in res])
         st = br.last_stats
         if st.error_flags:
             raise RuntimeError(f"device error flags {st.error_flags:#x}")
@@ -266,6 +270,31 @@ def batched_block(ctx, steps, warmup, tuning=None):
         wall = time.perf_counter() - t0
         out[name] = {"mrays_s": round(rays / (ms / 1000.0) / 1e6, 3), "ms_per_step": round(ms / steps, 4),
                      "wall_ms_per_step": round(1000 * wall / steps, 3), "rays_per_step": rays // steps}
+    # frames in flight: the steps enqueued back to back without stats (two
+    # frames' bounces overlap), CUDA events on the library stream; the ray
+    # counts come from a replay of the same frames one at a time
+    import torch
+    lib_stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", torch.cuda.current_device()))
+    f0 = warmup + steps
+    sds = [[(seeds.next(), seeds.next()) for _ in res] for _ in range(steps)]
+    blob = br.save_state()
+    n = len(res)
+    p = params_of(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(lib_stream)
+    for s_ in range(steps):
+        views = (vrg.View * n)()
+        for v, cam in enumerate(cams_of(f0 + s_)):
+            views[v] = vrg.View(scenes[v].h, cam, sds[s_][v][0], sds[s_][v][1])
+        vrg.check(ctx.lib.vrg_render_batched(br.h, views, n, C.byref(p), None, None), "vrg_render_batched")
+    e1.record(lib_stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    br.load_state(blob)
+    rays = sum(step(f0 + s_, 0, sds[s_])[1] for s_ in range(steps))
+    out["in_flight"] = {"mrays_s": round(rays / (ms / 1000.0) / 1e6, 3), "ms_per_step": round(ms / steps, 4),
+                        "rays_per_step": rays // steps}
     br.close()
     for sc in scenes:
         sc.close()

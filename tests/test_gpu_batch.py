@@ -180,3 +180,47 @@ def test_commit_many_matches_single_commits(gpu_ctx):
             sc.close()
             for o in objs:
                 o.release()
+
+
+def test_batched_frames_in_flight_match(gpu_ctx, world):
+    """Batched frames rendered without stats into device buffers are in flight
+    together (two array sets, a view table per set): they must equal, bit for
+    bit, the batched frames rendered one at a time with stats."""
+    torch = pytest.importorskip("torch")
+    scenes, cams, _ = world
+    lib = gpu_ctx.lib
+    n = len(SCENES)
+    frames = 5
+
+    def views_of(f):
+        views = (vrg.View * n)()
+        for v in range(n):
+            ts, ss = _seeds(v, f)
+            views[v] = vrg.View(scenes[v].h, cams[v][f % FRAMES], ts, ss)
+        return views
+
+    ref = vrg.BatchRenderer(gpu_ctx, [(w, h) for *_, w, h in SCENES], 2)
+    want = []
+    for f in range(frames):
+        _, rads = ref.render(scenes, [cams[v][f % FRAMES] for v in range(n)], _params(),
+                             [_seeds(v, f) for v in range(n)], want_image=False, want_radiance=True)
+        assert ref.last_stats.error_flags == 0
+        want.append([r_.copy() for r_ in rads])
+    ref.close()
+    br = vrg.BatchRenderer(gpu_ctx, [(w, h) for *_, w, h in SCENES], 2)
+    dev = [[torch.empty(w * h * 3, dtype=torch.float32, device="cuda") for *_, w, h in SCENES]
+           for _ in range(frames)]
+    torch.cuda.synchronize()
+    for f in range(frames):
+        outs = (vrg.FrameOutput * n)()
+        for v in range(n):
+            outs[v] = vrg.FrameOutput(None, dev[f][v].data_ptr(), 0, 0)
+        p = _params()
+        vrg.check(lib.vrg_render_batched(br.h, views_of(f), n, C.byref(p), C.cast(outs, C.c_void_p), None),
+                  "vrg_render_batched")
+    gpu_ctx.synchronize()
+    for f in range(frames):
+        for v, (_, _, _, w, h) in enumerate(SCENES):
+            got = dev[f][v].cpu().numpy().reshape(h, w, 3)
+            assert _same_bits(got, want[f][v]), (f, v)
+    br.close()

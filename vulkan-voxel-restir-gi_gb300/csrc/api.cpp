@@ -444,7 +444,7 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     struct SetOff {
         size_t ro, rd, q0, q1, cnt, aq0, aq1, aj0, aj1, hit, hb, hv, jm, nl, rec, xv, nv, xs, ns;
     } so[Renderer::SETS];
-    const int sets = r->n_views ? 1 : Renderer::SETS;
+    const int sets = (int)r->n_sets;
     for (int k = 0; k < sets; k++) {
         SetOff &q = so[k];
         q.ro = o; o += al(P * 16);
@@ -608,6 +608,7 @@ VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_view
     r->vw.assign(widths, widths + n_views);
     r->vh.assign(heights, heights + n_views);
     r->voff = off;
+    r->n_sets = 2;  // two frames' bounces in flight (a set is large: all views' pixels)
     auto fail = [&](vrg_status st) {
         vrg_renderer_destroy(r);
         return st;
@@ -617,12 +618,13 @@ VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_view
     if (st != VRG_OK) return fail(st);
     // view table + pixel-group lookup (the view of each group's first pixel)
     const size_t n_groups = (size_t)((P + (1u << VIEW_SHIFT) - 1) >> VIEW_SHIFT);
-    const size_t tab_off = ((size_t)n_views * sizeof(ViewDev) + 255) & ~(size_t)255;
+    const size_t view_tab = ((size_t)n_views * sizeof(ViewDev) + 255) & ~(size_t)255;
+    const size_t tab_off = view_tab * r->n_sets;
     DevBufPtr vb;
     st = dev_alloc(ctx->stream, tab_off + n_groups * 2, vb);
     if (st != VRG_OK) return fail(st);
     r->view_buf = vb;
-    r->d_views = (ViewDev *)vb->ptr;
+    for (uint32_t k = 0; k < r->n_sets; k++) r->d_views[k] = (ViewDev *)((uint8_t *)vb->ptr + k * view_tab);
     r->d_vtab = (uint16_t *)((uint8_t *)vb->ptr + tab_off);
     std::vector<uint16_t> vtab(n_groups);
     uint32_t v = 0;
@@ -829,7 +831,7 @@ static void apply_tuning(const vrg_renderer *r, FrameArgs &a) {
 // the view ones.
 // the array set of the frame about to be rendered (frame index mod SETS; batched
 // renderers have one)
-static uint32_t frame_set(const vrg_renderer *r) { return r->n_views ? 0u : r->frame % (uint32_t)Renderer::SETS; }
+static uint32_t frame_set(const vrg_renderer *r) { return r->frame % r->n_sets; }
 
 static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool want_radiance, FrameArgs &a) {
     if (pr->num_bounces == 0 || pr->spatial_iterations > 64 || pr->nee_type > 2 || pr->mode > 1) {
@@ -1002,12 +1004,13 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // so a scene's device data is final before any frame reads it; a resize
 // clears the arrays on the library stream and re-records ev_done.
 // Other frames run their bounces on the library stream itself.
-static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, bool pipelined = false) {
+static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, bool pipelined = false,
+                               bool in_graph = false) {
     cudaStream_t s = r->ctx->stream;
     const uint32_t k = frame_set(r);
     const bool fork = a.cache && !a.capture;
     const uint32_t nb_main = fork ? a.nb_render : a.nb;
-    const bool own = pipelined && !a.cache && !a.capture && !a.views && !timed;
+    const bool own = pipelined && !a.cache && !a.capture && !timed && !in_graph;
     cudaStream_t bs = own ? r->bs[k] : s;  // stream of the bounces
     cudaStream_t lp = r->lps[k];
     if (own) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_done[k], 0));
@@ -1120,9 +1123,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
     if (fork) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_join, 0));
-    // the set is free for the frame SETS ahead (not recorded inside a batched
-    // frame's graph capture: batched frames never run their bounces apart)
-    if (!a.views) VRG_CUDA_TRY(cudaEventRecord(r->ev_done[k], s));
+    // the set is free for the frame n_sets ahead (recorded after the graph
+    // launch when the frame is recorded in a graph)
+    if (!in_graph) VRG_CUDA_TRY(cudaEventRecord(r->ev_done[k], s));
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 2], s));
     return VRG_OK;
 }
@@ -1341,10 +1344,18 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
         d.temporal_seed = w.temporal_seed;
         d.spatial_seed = w.spatial_seed;
     }
-    VRG_CUDA_TRY(cudaMemcpyAsync(r->d_views, hv, (size_t)n_views * sizeof(ViewDev), cudaMemcpyHostToDevice, s));
-    VRG_CUDA_TRY(cudaEventRecord(r->ev_stage[r->stage], s));
+    // The set's view table: a frame in flight fills it on its set's bounce
+    // stream once the set's previous frame is done; any other frame on the
+    // library stream.
+    const uint32_t set = frame_set(r);
+    const bool in_flight = !graph && !stats && !a.cache;
+    cudaStream_t cs = in_flight ? r->bs[set] : s;
+    if (in_flight) VRG_CUDA_TRY(cudaStreamWaitEvent(cs, r->ev_done[set], 0));
+    VRG_CUDA_TRY(
+        cudaMemcpyAsync(r->d_views[set], hv, (size_t)n_views * sizeof(ViewDev), cudaMemcpyHostToDevice, cs));
+    VRG_CUDA_TRY(cudaEventRecord(r->ev_stage[r->stage], cs));
     r->stage ^= 1u;
-    a.views = r->d_views;
+    a.views = r->d_views[set];
     a.vtab = r->d_vtab;
     a.n_views = n_views;
     if (graph) {
@@ -1357,7 +1368,7 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
             if (r->graphs.size() >= 8) drop_graphs(r);
             cudaGraph_t g = nullptr;
             VRG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            vrg_status st = frame_launch(r, a, false);
+            vrg_status st = frame_launch(r, a, false, false, true);
             cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (st != VRG_OK) {
                 if (g) cudaGraphDestroy(g);
@@ -1374,8 +1385,10 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
         VRG_CUDA_TRY(cudaEventRecord(r->ev[0], s));
         VRG_CUDA_TRY(cudaGraphLaunch(ge->exec, s));
         VRG_CUDA_TRY(cudaEventRecord(r->ev[1], s));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_done[set], s));
     } else {
-        VRG_TRY(frame_launch(r, a, true));
+        // without stats the frame is not timed and may run beside the previous one
+        VRG_TRY(frame_launch(r, a, stats != nullptr, stats == nullptr));
     }
     bool host_out = false;
     if (outs) {

@@ -192,8 +192,8 @@ struct Renderer {
     uint32_t n_views = 0;
     std::vector<uint32_t> vw, vh;         // view extents
     std::vector<uint64_t> voff;           // first pixel of each view
-    DevBufPtr view_buf;                   // ViewDev[n_views] + vtab
-    ViewDev *d_views = nullptr;
+    DevBufPtr view_buf;                   // a ViewDev[n_views] table per array set + vtab
+    ViewDev *d_views[3] = {};
     uint16_t *d_vtab = nullptr;
     ViewDev *h_views = nullptr;           // pinned staging, 2 x n_views
     cudaEvent_t ev_stage[2] = {};         // after the copy out of each staging half
@@ -229,7 +229,8 @@ struct Renderer {
         float4 *rec = nullptr;                 // [nb][2][P]
         float4 *xv = nullptr, *nv = nullptr, *xs = nullptr, *ns = nullptr;
     };
-    static constexpr int SETS = 3;        // frames whose bounces may be in flight at once
+    static constexpr int SETS = 3;        // frames whose bounces may be in flight at once (at most)
+    uint32_t n_sets = SETS;               // this renderer's sets (a batched renderer: 2)
                                           // (2 -> 3: 1.264 -> 1.247 ms per 1080p frame)
     FrameSet fs[SETS];
     float4 *plain = nullptr;              // L[0] per pixel

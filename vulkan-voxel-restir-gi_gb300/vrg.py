@@ -640,6 +640,9 @@ class BatchRenderer:
     def set_tuning(self, tuning: "Tuning"):
         check(self.ctx.lib.vrg_renderer_set_tuning(self.h, C.byref(tuning)), "vrg_renderer_set_tuning")
 
+    save_state = Renderer.save_state
+    load_state = Renderer.load_state
+
     def reset_accumulation(self):
         check(self.ctx.lib.vrg_renderer_reset_accumulation(self.h), "vrg_renderer_reset_accumulation")
 
