@@ -379,7 +379,9 @@ VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, cons
  * flags or the other parameters records a new one) and replayed.
  * VRG_RENDER_GRAPH cannot be combined with VRG_RENDER_CACHE or
  * VRG_RENDER_CAPTURE (VRG_ERR_UNSUPPORTED); the stats of a graph frame carry
- * ms_total and the counters, not the per-kernel times. */
+ * ms_total and the counters, not the per-kernel times.  Without stats, graph
+ * or cache, two batched frames are in flight together, as vrg_render's frames
+ * are (each in its own array set, with its own view table). */
 typedef struct vrg_view {
     vrg_scene *scene;          /* committed by the call if dirty (all views' scenes
                                   are committed before any view renders) */
