@@ -49,6 +49,25 @@ def test_c0_frame_bit_exact(gpu_ctx, orc, nee):
         OW.close()
 
 
+@pytest.mark.parametrize("W,H", [(83, 45), (7, 3)], ids=["83x45", "7x3"])
+def test_odd_extent_bit_exact(gpu_ctx, orc, W, H):
+    """Extents that are not whole 8x4 tiles (bounce 0 takes a single view's
+    pixels tile by tile, the edge tiles partly outside the view): every pixel
+    traced once, bit for bit as the oracle."""
+    scene, objs, OW, gr, orr = _setup(gpu_ctx, orc, 4, 1, 1, 0.01, W, H, 3)
+    try:
+        for f in range(2):
+            cam = vrg.orbit_camera(1, 1, f, 16, W, H)
+            p = params(nee=1, view=1, spatial=3, nb=3, seeds=(f, 300 + f, 600 + f))
+            img, rad, oimg, orad = _frame(scene, OW, gr, orr, cam, p)
+            diffs = compare_frame(gr, orr, 3)
+            assert all(v == 0 for v in diffs.values()), (f, diffs)
+            assert np.array_equal(img.reshape(-1), oimg.reshape(-1))
+            assert gr.last_stats.error_flags == 0
+    finally:
+        OW.close()
+
+
 def test_restir_multi_frame_bit_exact(gpu_ctx, orc):
     """ReSTIR over a 3-slot ring, spatial neighbours, 3 bounces, moving camera."""
     scene, objs, OW, gr, orr = _setup(gpu_ctx, orc, 2, 2, 2, 0.005, 96, 64, 3)
