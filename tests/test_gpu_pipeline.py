@@ -196,3 +196,50 @@ def test_frames_in_flight_alternating_scenes(gpu_ctx):
         sc.close()
         for o in objs:
             o.release()
+
+
+def test_cache_frames_in_flight_match(gpu_ctx):
+    """Cache frames (ReSTIR over cache-terminated paths, training branch
+    forked) in flight equal the same frames rendered one by one.  The cache
+    learns at rate 0, so every frame sees the same cache whatever the order
+    of the training atomics."""
+    lib = gpu_ctx.lib
+    sc, objs = _world(gpu_ctx)
+    lt, gtl = sc.get_tlas()
+    lo, hi = gtl[0]["min"], gtl[0]["max"]
+
+    def cp(f):
+        p = params(nee=1, view=1, spatial=3, nb=2, seeds=(f, 7 * f + 1, 11 * f + 2), accumulate=0,
+                   flags=vrg.RENDER_CACHE)
+        p.cache_train_bounces = 3
+        return p
+
+    want = []
+    ra = vrg.Renderer(gpu_ctx, W, H, 8)
+    ca = vrg.RadianceCache(gpu_ctx, lo, hi, learning_rate=0.0, seed=5)
+    ra.set_cache(ca)
+    for f in range(FRAMES):
+        _, rad = ra.render_params(sc, _cam(f), cp(f), want_image=False, want_radiance=True)
+        assert ra.last_stats.error_flags == 0
+        want.append(rad.copy())
+    rb = vrg.Renderer(gpu_ctx, W, H, 8)
+    cb = vrg.RadianceCache(gpu_ctx, lo, hi, learning_rate=0.0, seed=5)
+    rb.set_cache(cb)
+    dev = [torch.empty(W * H * 3, dtype=torch.float32, device="cuda") for _ in range(FRAMES)]
+    torch.cuda.synchronize()
+    for f in range(FRAMES):
+        out = vrg.FrameOutput(None, dev[f].data_ptr(), 0, 0)
+        cam, p = _cam(f), cp(f)
+        vrg.check(lib.vrg_render(rb.h, sc.h, C.byref(cam), C.byref(p), C.byref(out), None), "vrg_render")
+    gpu_ctx.synchronize()
+    for f in range(FRAMES):
+        got = dev[f].cpu().numpy().reshape(H, W, 3)
+        assert np.array_equal(got.view(np.uint32), want[f].view(np.uint32)), f
+    for r in (ra, rb):
+        r.set_cache(None)
+        r.close()
+    for c in (ca, cb):
+        c.close()
+    sc.close()
+    for o in objs:
+        o.release()

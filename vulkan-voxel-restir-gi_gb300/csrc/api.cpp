@@ -526,6 +526,9 @@ static vrg_status renderer_alloc(vrg_renderer *r) {
     r->accum_n = 0;
     r->cap.reset();
     r->cache_buf.reset();
+    r->cache_cap = 0;
+    for (auto &q : r->cs) q = Renderer::CacheSet{};
+    r->last_cache_set = -1;
     r->captured = false;
     return VRG_OK;
 }
@@ -859,39 +862,49 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
         const uint32_t cap = nrc_batch(r->cache);
         if (!r->cache_buf || r->cache_cap < cap) {  // (a later cache may train larger batches)
             auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+            struct Off {
+                size_t qp, qd, pr, tg, il, tl, qf, taq0, taq1, taj0, taj1, thb, thv, tjm;
+            } off[3];
             size_t o = 0;
-            size_t o_qp = o; o += al(P * 16);
-            size_t o_qd = o; o += al(P * 16);
-            size_t o_pr = o; o += al(P * 16);
-            size_t o_tg = o; o += al(P * 16);
-            size_t o_il = o; o += al(P * 4);
-            size_t o_tl = o; o += al((size_t)cap * 4);
-            size_t o_qf = o; o += al(P);
-            size_t o_taq0 = o; o += al((size_t)cap * 4);
-            size_t o_taq1 = o; o += al((size_t)cap * 4);
-            size_t o_taj0 = o; o += al((size_t)cap * 32);
-            size_t o_taj1 = o; o += al((size_t)cap * 32);
-            size_t o_thb = o; o += al((size_t)cap * 2 * 32);
-            size_t o_thv = o; o += al((size_t)cap * 2 * 4);
-            size_t o_tjm = o; o += al((size_t)cap * 8);
+            for (uint32_t k = 0; k < r->n_sets; k++) {
+                Off &q = off[k];
+                q.qp = o; o += al(P * 16);
+                q.qd = o; o += al(P * 16);
+                q.pr = o; o += al(P * 16);
+                q.tg = o; o += al(P * 16);
+                q.il = o; o += al(P * 4);
+                q.tl = o; o += al((size_t)cap * 4);
+                q.qf = o; o += al(P);
+                q.taq0 = o; o += al((size_t)cap * 4);
+                q.taq1 = o; o += al((size_t)cap * 4);
+                q.taj0 = o; o += al((size_t)cap * 32);
+                q.taj1 = o; o += al((size_t)cap * 32);
+                q.thb = o; o += al((size_t)cap * 2 * 32);
+                q.thv = o; o += al((size_t)cap * 2 * 4);
+                q.tjm = o; o += al((size_t)cap * 8);
+            }
             DevBufPtr b;
             VRG_TRY(dev_alloc(s, o, b));
             VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, o, s));
             uint8_t *B = (uint8_t *)b->ptr;
-            r->q_pos = (float4 *)(B + o_qp);
-            r->q_dir = (float4 *)(B + o_qd);
-            r->pred = (float4 *)(B + o_pr);
-            r->target = (float4 *)(B + o_tg);
-            r->infer_list = (uint32_t *)(B + o_il);
-            r->train_list = (uint32_t *)(B + o_tl);
-            r->qflag = B + o_qf;
-            r->t_aqueue[0] = (uint32_t *)(B + o_taq0);
-            r->t_aqueue[1] = (uint32_t *)(B + o_taq1);
-            r->t_ajob[0] = (float4 *)(B + o_taj0);
-            r->t_ajob[1] = (float4 *)(B + o_taj1);
-            r->t_hitbuf = (uint4 *)(B + o_thb);
-            r->t_hitval = (float *)(B + o_thv);
-            r->t_jmeta = (uint2 *)(B + o_tjm);
+            for (uint32_t k = 0; k < r->n_sets; k++) {
+                const Off &q = off[k];
+                Renderer::CacheSet &Q = r->cs[k];
+                Q.q_pos = (float4 *)(B + q.qp);
+                Q.q_dir = (float4 *)(B + q.qd);
+                Q.pred = (float4 *)(B + q.pr);
+                Q.target = (float4 *)(B + q.tg);
+                Q.infer_list = (uint32_t *)(B + q.il);
+                Q.train_list = (uint32_t *)(B + q.tl);
+                Q.qflag = B + q.qf;
+                Q.t_aqueue[0] = (uint32_t *)(B + q.taq0);
+                Q.t_aqueue[1] = (uint32_t *)(B + q.taq1);
+                Q.t_ajob[0] = (float4 *)(B + q.taj0);
+                Q.t_ajob[1] = (float4 *)(B + q.taj1);
+                Q.t_hitbuf = (uint4 *)(B + q.thb);
+                Q.t_hitval = (float *)(B + q.thv);
+                Q.t_jmeta = (uint2 *)(B + q.tjm);
+            }
             r->cache_buf = b;
             r->cache_cap = cap;
         }
@@ -908,13 +921,16 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
     a.cache = cache ? 1u : 0u;
     a.train_cap = cache ? nrc_batch(r->cache) : 0u;
     a.restir = (pr->flags & VRG_RENDER_PLAIN_ONLY) ? 0u : 1u;
-    a.q_pos = r->q_pos;
-    a.q_dir = r->q_dir;
-    a.pred = r->pred;
-    a.target = r->target;
-    a.infer_list = r->infer_list;
-    a.train_list = r->train_list;
-    a.qflag = r->qflag;
+    {
+        const Renderer::CacheSet &Q = r->cs[frame_set(r)];
+        a.q_pos = Q.q_pos;
+        a.q_dir = Q.q_dir;
+        a.pred = Q.pred;
+        a.target = Q.target;
+        a.infer_list = Q.infer_list;
+        a.train_list = Q.train_list;
+        a.qflag = Q.qflag;
+    }
     a.nee_type = pr->nee_type;
     a.mode = pr->mode;
     a.spatial_iters = pr->spatial_iterations;
@@ -991,15 +1007,17 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // stream beside its own bounces, before its queries and its own training
 // (the frames see the same cache as with the step at the end of each frame).
 // With capture the frame stays on one stream.
-// Frames in flight (pipelined, plain frames: no stats, cache or capture).
+// Frames in flight (pipelined: frames without stats or capture).
 // A frame's bounces (closest hit, shading, light-pdf walks) read the committed
 // scene, the camera and the material table, and write only the arrays of the
-// frame's set (sets are taken in turn by frame index).  So they run on the
-// set's own bounce stream as soon as the set's previous frame, SETS frames
-// back, has finished (ev_done), beside the previous frames' bounces and their
-// resolve and spatial passes.  The library stream waits for the bounces (ev_bounced) and
-// then runs the frame's resolve and spatial passes, in frame order, so the
-// frame is complete when the library stream has passed it.  Scene commits and
+// frame's set, its cache arrays included (sets are taken in turn by frame
+// index).  So they run on the set's own bounce stream as soon as the set's
+// previous frame, n_sets frames back, has finished (ev_done), beside the
+// previous frames' bounces, resolve and spatial passes and cache work.  The
+// library stream waits for the bounces (ev_bounced) and then runs the frame's
+// cache queries, resolve and spatial passes in frame order (a cache frame's
+// training branch forks from there), so the frame is complete when the
+// library stream has passed it.  Scene commits and
 // material / atlas changes synchronize the library stream before they return,
 // so a scene's device data is final before any frame reads it; a resize
 // clears the arrays on the library stream and re-records ev_done.
@@ -1010,7 +1028,7 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     const uint32_t k = frame_set(r);
     const bool fork = a.cache && !a.capture;
     const uint32_t nb_main = fork ? a.nb_render : a.nb;
-    const bool own = pipelined && !a.cache && !a.capture && !timed && !in_graph;
+    const bool own = pipelined && !a.capture && !timed && !in_graph;
     cudaStream_t bs = own ? r->bs[k] : s;  // stream of the bounces
     cudaStream_t lp = r->lps[k];
     if (own) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_done[k], 0));
@@ -1065,13 +1083,14 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         // own, so they need not wait for the main walks still running (which
         // read the main job buffers and write their own bounces' records).
         FrameArgs at = a;
+        const Renderer::CacheSet &Q = r->cs[k];
         for (int q = 0; q < 2; q++) {
-            at.aqueue[q] = r->t_aqueue[q];
-            at.ajob[q] = r->t_ajob[q];
+            at.aqueue[q] = Q.t_aqueue[q];
+            at.ajob[q] = Q.t_ajob[q];
         }
-        at.hitbuf = r->t_hitbuf;
-        at.hitval = r->t_hitval;
-        at.jmeta = r->t_jmeta;
+        at.hitbuf = Q.t_hitbuf;
+        at.hitval = Q.t_hitval;
+        at.jmeta = Q.t_jmeta;
         at.hit_cap = 2 * a.train_cap;
         at.hit_count = a.counters + CNT_HITS_TRAIN;
         // As on the main path, training bounce b's light-pdf walk runs on a
@@ -1097,14 +1116,14 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         // main walk of that bounce completes
         VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_lpdone[k][last_lp], 0));
         VRG_TRY(launch_train_targets(st, at));
-        VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, false, a.counters + CNT_ERROR));
+        VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, a.train_list, a.q_pos, a.q_dir,
+                          nullptr, a.target, false, a.counters + CNT_ERROR));
     }
     if (a.cache) {  // radiance-cache queries of every path that ends into the cache
         if (updated) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_updated, 0));
         if (!fork) VRG_TRY(nrc_flush(r->cache, s));
-        VRG_TRY(nrc_infer(r->cache, s, a.P, a.counters + CNT_INFER, r->infer_list, r->q_pos, r->q_dir, nullptr,
-                          r->pred, a.counters + CNT_ERROR));
+        VRG_TRY(nrc_infer(r->cache, s, a.P, a.counters + CNT_INFER, a.infer_list, a.q_pos, a.q_dir, nullptr,
+                          a.pred, a.counters + CNT_ERROR));
     }
     if (fork) {
         // This frame's Adam step would rewrite the weights and table that its
@@ -1117,8 +1136,8 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     VRG_TRY(launch_resolve(s, a));
     if (a.cache && !fork) {  // one training step on this frame's long paths
         VRG_TRY(launch_train_targets(s, a));
-        VRG_TRY(nrc_train(r->cache, s, a.train_cap, a.counters + CNT_TRAIN, r->train_list, r->q_pos, r->q_dir,
-                          nullptr, r->target, true, a.counters + CNT_ERROR));
+        VRG_TRY(nrc_train(r->cache, s, a.train_cap, a.counters + CNT_TRAIN, a.train_list, a.q_pos, a.q_dir,
+                          nullptr, a.target, true, a.counters + CNT_ERROR));
     }
     if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev[a.nb + 1], s));
     VRG_TRY(launch_spatial(s, a));
@@ -1190,6 +1209,7 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
 // after the frame's launches and copies out: its fence, then the counters
 static vrg_status frame_done(vrg_renderer *r, const FrameArgs &a, const vrg_render_params *pr) {
     VRG_CUDA_TRY(cudaEventRecord(r->ev_fence[r->frame % Renderer::FENCES], r->ctx->stream));
+    if (a.cache) r->last_cache_set = (int)frame_set(r);
     r->last_nb = a.nb;
     r->captured = a.capture != 0;
     if (pr->accumulate) r->accum_n++;
@@ -1348,7 +1368,7 @@ VRG_API vrg_status vrg_render_batched(vrg_renderer *r, const vrg_view *views, ui
     // stream once the set's previous frame is done; any other frame on the
     // library stream.
     const uint32_t set = frame_set(r);
-    const bool in_flight = !graph && !stats && !a.cache;
+    const bool in_flight = !graph && !stats;
     cudaStream_t cs = in_flight ? r->bs[set] : s;
     if (in_flight) VRG_CUDA_TRY(cudaStreamWaitEvent(cs, r->ev_done[set], 0));
     VRG_CUDA_TRY(
@@ -1594,12 +1614,13 @@ VRG_API vrg_status vrg_debug_readback(vrg_renderer *r, uint32_t what, void *dst,
     if (!r || !dst || what >= VRG_DBG_COUNT) return VRG_ERR_INVALID_ARGUMENT;
     if (what == VRG_DBG_CACHE_TARGET) {
         const size_t n = (size_t)r->P * 16;
-        if (!r->target) {
+        if (r->last_cache_set < 0 || !r->cs[r->last_cache_set].target) {
             set_error("no cache frame rendered");
             return VRG_ERR_STATE;
         }
         if (bytes < n) return VRG_ERR_INVALID_ARGUMENT;
-        VRG_CUDA_TRY(cudaMemcpyAsync(dst, r->target, n, cudaMemcpyDeviceToHost, r->ctx->stream));
+        VRG_CUDA_TRY(cudaMemcpyAsync(dst, r->cs[r->last_cache_set].target, n, cudaMemcpyDeviceToHost,
+                                     r->ctx->stream));
         VRG_CUDA_TRY(cudaStreamSynchronize(r->ctx->stream));
         return VRG_OK;
     }

@@ -270,16 +270,22 @@ struct Renderer {
     Nrc *cache = nullptr;                 // attached radiance cache (not owned)
     DevBufPtr cache_buf;                  // per-pixel cache queries / predictions / targets
     uint32_t cache_cap = 0;               // training paths cache_buf was sized for
-    float4 *q_pos = nullptr, *q_dir = nullptr, *pred = nullptr, *target = nullptr;
-    uint32_t *infer_list = nullptr, *train_list = nullptr;
+    // a cache frame's arrays, one set per array set: cache queries,
+    // predictions and targets per pixel, the query and training lists, and
     // the training branch's light-pdf jobs and hits (its walks run beside the
     // main walk of the query bounce), sized for the training paths
-    uint32_t *t_aqueue[2] = {};
-    float4 *t_ajob[2] = {};
-    uint4 *t_hitbuf = nullptr;
-    float *t_hitval = nullptr;
-    uint2 *t_jmeta = nullptr;
-    uint8_t *qflag = nullptr;
+    struct CacheSet {
+        float4 *q_pos = nullptr, *q_dir = nullptr, *pred = nullptr, *target = nullptr;
+        uint32_t *infer_list = nullptr, *train_list = nullptr;
+        uint8_t *qflag = nullptr;
+        uint32_t *t_aqueue[2] = {};
+        float4 *t_ajob[2] = {};
+        uint4 *t_hitbuf = nullptr;
+        float *t_hitval = nullptr;
+        uint2 *t_jmeta = nullptr;
+    };
+    CacheSet cs[3];
+    int last_cache_set = -1;              // the set of the last cache frame (its targets)
     int grid_bounce = 0;
     vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
 };
