@@ -412,6 +412,24 @@ def run_large(args, d):
                 errs.append(np.mean([quality.relmse(rads[v], gt[v]) for v in range(4)]))
         out[name] = {"ms_per_frame": round(ms / args.steps, 3), "mrays_s": round(rays / (ms / 1000.0) / 1e6, 3),
                      "rays_per_frame": rays // args.steps, "relmse_1spp": round(float(np.mean(errs)), 5)}
+        # the same frames back to back (no stats: frames in flight), CUDA
+        # events on the library stream; rays per frame from the frames above
+        import torch
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", torch.cuda.current_device()))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s_ in range(args.steps):
+            views = (vrg.View * 4)()
+            for v in range(4):
+                views[v] = vrg.View(scenes[v].h, cams[v], seeds.next(), seeds.next())
+            p = params(nb, flags, view)
+            vrg.check(ctx.lib.vrg_render_batched(br.h, views, 4, C.byref(p), None, None), "vrg_render_batched")
+        e1.record(stream)
+        e1.synchronize()
+        ms_f = e0.elapsed_time(e1) / args.steps
+        out[name]["ms_per_frame_in_flight"] = round(ms_f, 3)
+        out[name]["mrays_s_in_flight"] = round((rays / args.steps) / (ms_f / 1000.0) / 1e6, 3)
     # plain accumulated over at least the cache frame's time
     k = max(1, int(np.ceil(out["restir_cache"]["ms_per_frame"] / out["plain"]["ms_per_frame"] - 1e-9)))
     br.set_cache(None)

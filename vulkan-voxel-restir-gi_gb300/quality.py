@@ -17,6 +17,7 @@ Equal time, two ways:
     the method's time from below, and the gain computed with it bounds the
     equal-time gain from below.
 """
+import ctypes as C
 import math
 
 import numpy as np
@@ -67,17 +68,7 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
     singles, ms = [], []
     stages = None
     for f in range(warmup + frames):
-        if method == "plain":
-            p = _params(3, vrg.RENDER_PLAIN_ONLY, seed0 + f, accumulate=0)
-        elif method == "restir":
-            p = _params(3, 0, seed0 + f, accumulate=0)
-            p.debug_view = 1
-            p.spatial_iterations = 3
-        else:
-            p = _params(2, vrg.RENDER_CACHE, seed0 + f, accumulate=0)
-            if method == "restir_cache":
-                p.debug_view = 1
-                p.spatial_iterations = 3
+        p = method_params(method, seed0 + f)
         _, rad = renderer.render_params(scene, cam, p, want_image=False, want_radiance=True)
         if f >= warmup:
             singles.append(rad.astype(np.float32))
@@ -92,6 +83,43 @@ def run_method(renderer, scene, cam, method, frames, seed0=0, warmup=0, cache=No
 
 
 METHODS = ("plain", "restir", "cache", "restir_cache")
+
+
+def method_params(method, seed):
+    """The render parameters run_method uses for `method`."""
+    if method == "plain":
+        return _params(3, vrg.RENDER_PLAIN_ONLY, seed, accumulate=0)
+    if method == "restir":
+        p = _params(3, 0, seed, accumulate=0)
+    else:
+        p = _params(2, vrg.RENDER_CACHE, seed, accumulate=0)
+        if method != "restir_cache":
+            return p
+    p.debug_view = 1
+    p.spatial_iterations = 3
+    return p
+
+
+def in_flight_ms(renderer, scene, cam, method, frames, seed0=0, cache=None):
+    """Device ms per frame of `frames` frames of `method` enqueued back to back
+    (no stats, no outputs: frames in flight), CUDA events on the library's
+    stream; None without torch."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    ctx = renderer.ctx
+    renderer.set_cache(cache if method in ("cache", "restir_cache") else None)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", torch.cuda.current_device()))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for f in range(frames):
+        p = method_params(method, seed0 + f)
+        vrg.check(ctx.lib.vrg_render(renderer.h, scene.h, C.byref(cam), C.byref(p), None, None), "vrg_render")
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / frames
 
 
 def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames=16, cache_warmup=64, seed=7):
@@ -110,6 +138,11 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
                        "nonfinite": round(float(np.mean([nonfinite_fraction(s) for s in singles])), 8),
                        "relmse_mean_of_frames": round(relmse(mean_img, gt), 6), "frames": frames,
                        "stages_ms_last_frame": run_method.last_stages}
+    # the same methods' frames back to back, as an interactive loop renders
+    # them (frames in flight); the relMSE figures above do not depend on it
+    for method in METHODS:
+        t = in_flight_ms(renderer, scene, cam, method, frames, seed0=9000, cache=cache)
+        out[method]["ms_per_frame_in_flight"] = None if t is None else round(t, 4)
     renderer.set_cache(None)
     # equal time: each method's 1-spp frame against the plain tracer
     # accumulated over at least the same device time
@@ -129,5 +162,21 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
                       "gain": round(plain_acc[k] / rel_m, 3),
                       "gain_lower_bound": round(out["plain"]["relmse_1spp"] / n_eq / rel_m, 3)}
     out["equal_time"] = eq
+    # the same comparison with every method timed in flight
+    t_plain_f = out["plain"].get("ms_per_frame_in_flight")
+    if t_plain_f:
+        eqf = {}
+        for method in METHODS[1:]:
+            t_m = out[method]["ms_per_frame_in_flight"]
+            k = max(1, int(math.ceil(t_m / t_plain_f - 1e-9)))
+            if k not in plain_acc:
+                acc_img, _, _ = run_method(renderer, scene, cam, "plain", k, seed0=5000)
+                plain_acc[k] = relmse(acc_img, gt)
+            n_eq = max(1.0, t_m / t_plain_f)
+            rel_m = max(out[method]["relmse_1spp"], 1e-12)
+            eqf[method] = {"plain_frames": k, "plain_time_ratio": round(k * t_plain_f / t_m, 3),
+                           "gain": round(plain_acc[k] / rel_m, 3),
+                           "gain_lower_bound": round(out["plain"]["relmse_1spp"] / n_eq / rel_m, 3)}
+        out["equal_time_in_flight"] = eqf
     cache.close()
     return out
