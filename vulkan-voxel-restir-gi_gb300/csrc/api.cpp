@@ -19,7 +19,6 @@ vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint
 vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a);
 vrg_status launch_train_targets(cudaStream_t s, const FrameArgs &a);
-int bounce_blocks_per_sm();
 void bounce_occupancy(bool batch, int occ[3], int *sms);
 
 static thread_local char g_err[512] = "";
@@ -559,7 +558,9 @@ static vrg_status renderer_events(vrg_renderer *r) {
     for (auto &row : r->ev_k)
         for (auto &e : row) VRG_CUDA_TRY(cudaEventCreate(&e));
     for (auto &e : r->ev_fence) VRG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    r->grid_bounce = r->ctx->num_sms * bounce_blocks_per_sm();
+    // the kernels' occupancy grids, queried once here (never inside a stream capture)
+    int occ[3], sms = 1;
+    bounce_occupancy(false, occ, &sms);
     return VRG_OK;
 }
 

@@ -1057,9 +1057,4 @@ vrg_status launch_light_pdf(cudaStream_t s, const FrameArgs &a, uint32_t b, uint
     return VRG_OK;
 }
 
-int bounce_blocks_per_sm() {
-    init_grids();
-    return 1;
-}
-
 }  // namespace vrg

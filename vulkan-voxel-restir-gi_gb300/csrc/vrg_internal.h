@@ -286,7 +286,6 @@ struct Renderer {
     };
     CacheSet cs[3];
     int last_cache_set = -1;              // the set of the last cache frame (its targets)
-    int grid_bounce = 0;
     vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
 };
 
