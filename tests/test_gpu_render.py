@@ -227,3 +227,33 @@ def test_texture_atlas_mirror_glass_bit_exact(gpu_ctx, orc):
     finally:
         gpu_ctx.set_atlas(None)
         OW.close()
+
+
+@pytest.mark.parametrize("nb", [2, 3])
+def test_plain_frames_equal_captured_frames(gpu_ctx, nb):
+    """Frames rendered without VRG_RENDER_CAPTURE (the fast path: no per-bounce
+    arrays kept, and the last vertex's continuation skipped because only its
+    emission reaches the image) equal, bit for bit, the captured frames that
+    the other tests compare with the oracle."""
+    mats, n, world = terrain_world(6, 2, 1, 0.01)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    W, H = 88, 52
+    outs = []
+    for flags in (vrg.RENDER_CAPTURE, 0):
+        r = vrg.Renderer(gpu_ctx, W, H, nb)
+        frames = []
+        for f in range(3):
+            cam = vrg.orbit_camera(2, 1, f, 16, W, H)
+            p = params(nee=1, view=1, spatial=3, nb=nb, seeds=(f, 40 + f, 80 + f), flags=flags)
+            img, rad = r.render_params(scene, cam, p, want_image=True, want_radiance=True)
+            assert r.last_stats.error_flags == 0
+            frames.append((img.copy(), rad.copy()))
+        outs.append(frames)
+        r.close()
+    for (ia, ra), (ib, rb) in zip(*outs):
+        assert np.array_equal(ia, ib)
+        assert np.array_equal(ra.view(np.uint32), rb.view(np.uint32))
+    scene.close()
+    for o in objs:
+        o.release()

@@ -456,8 +456,13 @@ struct ShadeOut {
     int4 rc;
 };
 
+// need_dir false: the path ends at this vertex (its last bounce, no capture)
+// and only its emission reaches the image: the outgoing radiance of the last
+// vertex is E + (R * 0) * w = E for any finite R >= 0 and w > 0, and the
+// vertex position keeps its offset; the Lambertian continuation (light-BVH
+// descent and direction sampling) is skipped, with mis 0 and pdf 1.
 __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_type, uint32_t b, uint32_t seed, f3 o,
-                                             f3 d, int4 hv, ShadeOut &out) {
+                                             f3 d, int4 hv, bool need_dir, ShadeOut &out) {
     f3 n, E, R, new_o, new_d;
     float mis = 0.0f, pdf = 1.0f;
     int face = 0, half = 0;
@@ -523,6 +528,10 @@ __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_typ
         } else {
             new_o = add3(new_o, lscl3(EPS_TRACE * 1.5f, n));
             R = f3{R.x / PI_F, R.y / PI_F, R.z / PI_F};
+            if (!need_dir) {
+                new_d = f3{0.0f, 0.0f, 0.0f};
+                goto done;
+            }
             Descent res;
             res.success = false;
             res.importance = 0.0f;
@@ -548,6 +557,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_typ
             pdf = dot3(new_d, n) / PI_F;
         }
     }
+done:
     out.n = n;
     out.E = E;
     out.R = R;
@@ -605,7 +615,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
             const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
             const int4 hv = a.hits[p];
             ShadeOut so;
-            shade_vertex(V.sc, a.nee_type, b, seed, o, d, hv, so);
+            shade_vertex(V.sc, a.nee_type, b, seed, o, d, hv, CAPTURE || b + 1 < nb, so);
             const f3 n = so.n, E = so.E;
             f3 R = so.R;
             const float mis = so.mis;
