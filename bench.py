@@ -604,6 +604,7 @@ def run_ours(args, d):
     ms, rays, ms_b, ms_res, ms_sp = [], 0, [0.0] * NB, 0.0, 0.0
     ms_tr, ms_sh, ms_ah = [0.0] * NB, [0.0] * NB, [0.0] * NB
     closest, nodes, leaves = 0, 0, 0
+    any_rays, l_nodes, l_leaves, l_hits = 0, 0, 0, 0
     for s in range(args.steps):
         render(args.warmup + s, out_dev, stats)
         if stats.error_flags:
@@ -613,6 +614,10 @@ def run_ours(args, d):
         closest += stats.rays_closest
         nodes += stats.nodes_visited
         leaves += stats.leaves_visited
+        any_rays += stats.rays_any
+        l_nodes += stats.light_nodes_visited
+        l_leaves += stats.light_leaves_visited
+        l_hits += stats.light_hits
         for b in range(NB):
             ms_b[b] += stats.ms_bounce[b]
             ms_tr[b] += stats.ms_trace[b]
@@ -737,6 +742,9 @@ def run_ours(args, d):
                       "leaves_per_ray": round(leaves / max(closest, 1), 2),
                       "l1_l2_bytes_per_s_gbs": round(trav_bytes / trace_s / 1e9, 1) if trace_s > 0 else None,
                       "grays_per_s": round(closest / trace_s / 1e9, 3) if trace_s > 0 else None},
+        "light_walk": {"kernel": "k_anyhit", "nodes_per_ray": round(l_nodes / max(any_rays, 1), 2),
+                       "leaves_per_ray": round(l_leaves / max(any_rays, 1), 2),
+                       "hits_per_ray": round(l_hits / max(any_rays, 1), 3)},
         "stream_roofline": {"kernels": "k_resolve+k_spatial", "achieved": round(stream_gbs, 2), "peak": hbm_peak,
                             "unit": "GB/s", "frac": round(stream_gbs / hbm_peak, 4), "bytes_per_px": 252},
         "e2e": {"value": None if e2e_value is None else round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(vrg.Camera) + C.sizeof(vrg.RenderParams),

@@ -172,6 +172,9 @@ typedef struct vrg_frame_stats {
                                   k_hit_sum) on its stream */
     uint64_t nodes_visited;    /* closest-hit traversal: 4-wide inner nodes fetched (128 B each) */
     uint64_t leaves_visited;   /* closest-hit traversal: surface-block records tested (16 B each) */
+    uint64_t light_nodes_visited;   /* light-hit collection: 4-wide lamp nodes fetched (112 B each) */
+    uint64_t light_leaves_visited;  /* light-hit collection: lamp-block records tested (16 B each) */
+    uint64_t light_hits;            /* light-hit collection: light triangles crossed */
 } vrg_frame_stats;
 
 typedef struct vrg_context vrg_context;

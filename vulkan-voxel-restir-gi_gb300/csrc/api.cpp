@@ -1208,6 +1208,9 @@ static vrg_status frame_stats(vrg_renderer *r, const FrameArgs &a, bool per_kern
     stats->rays_any = any;
     stats->nodes_visited = nn;
     stats->leaves_visited = nlv;
+    memcpy(&stats->light_nodes_visited, cnt + CNT_ANODES, 8);
+    memcpy(&stats->light_leaves_visited, cnt + CNT_ALEAVES, 8);
+    memcpy(&stats->light_hits, cnt + CNT_AHITS, 8);
     stats->error_flags = cnt[CNT_ERROR];
     if (cnt[CNT_ERROR]) {
         set_error("device error flags 0x%x", cnt[CNT_ERROR]);

@@ -769,6 +769,8 @@ __device__ __forceinline__ void finish_job(const FrameArgs &a, uint32_t b, uint3
 
 template <bool CAPTURE, bool BATCH>
 __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ FrameArgs a, uint32_t b) {
+    // walk statistics, per lane: lamp nodes fetched, lamp blocks tested, light hits
+    __shared__ uint32_t s_stat[3][128];
     const int lane = threadIdx.x & 31;
     const int REFILL = (int)a.refill_any;
     const uint32_t n_in = a.counters[CNT_AQUEUE + b];
@@ -789,6 +791,9 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
     float b1s[LIGHT_LIST], b2s[LIGHT_LIST];
     if (blockIdx.x == 0 && threadIdx.x == 0 && n_in)
         atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANY), (unsigned long long)n_in);
+    s_stat[0][threadIdx.x] = 0;
+    s_stat[1][threadIdx.x] = 0;
+    s_stat[2][threadIdx.x] = 0;
     while (true) {
         const uint32_t need = __ballot_sync(FULL, !has);
         if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
@@ -866,6 +871,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                 }
             }
             if (!done) {  // leaf: one lamp block; each emissive face hit names one light triangle
+                s_stat[1][threadIdx.x]++;
                 const int4 r = __ldg(recs + (~node));
                 const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
                 const uint32_t ii = rec_inst(r);
@@ -895,6 +901,8 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                 else node = stack[--sp];
             }
             if (done) {
+                s_stat[0][threadIdx.x] += steps;
+                s_stat[2][threadIdx.x] += (uint32_t)nh;
                 uint32_t hb = 0;
                 if (nh > 0) {
                     hb = atomicAdd(a.hit_count, (uint32_t)nh);
@@ -917,6 +925,14 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                 has = false;
             }
         }
+    }
+    const uint32_t n_nodes = __reduce_add_sync(FULL, s_stat[0][threadIdx.x]);
+    const uint32_t n_leaves = __reduce_add_sync(FULL, s_stat[1][threadIdx.x]);
+    const uint32_t n_hits = __reduce_add_sync(FULL, s_stat[2][threadIdx.x]);
+    if (lane == 0 && n_nodes) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ANODES), (unsigned long long)n_nodes);
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_ALEAVES), (unsigned long long)n_leaves);
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.counters + CNT_AHITS), (unsigned long long)n_hits);
     }
 }
 

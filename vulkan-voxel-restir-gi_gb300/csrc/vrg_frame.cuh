@@ -18,6 +18,9 @@ constexpr int CNT_NODES = 50;    // u64 at words 50-51: inner nodes fetched by k
 constexpr int CNT_LEAVES = 52;   // u64 at words 52-53: leaf records tested by k_trace
 constexpr int CNT_HITS = 54;     // light hits collected by k_anyhit for the current bounce
 constexpr int CNT_HITS_TRAIN = 55;  // the same for a cache frame's training branch (its own job and hit buffers)
+constexpr int CNT_ANODES = 56;   // u64 at words 56-57: 4-wide lamp nodes fetched by k_anyhit
+constexpr int CNT_ALEAVES = 58;  // u64 at words 58-59: lamp-block records tested by k_anyhit
+constexpr int CNT_AHITS = 60;    // u64 at words 60-61: light hits collected by k_anyhit
 constexpr int CNT_INFER = 48;    // radiance-cache queries of the frame
 constexpr int CNT_TRAIN = 49;    // radiance-cache training paths of the frame
 constexpr int CNT_WORDS = 64;

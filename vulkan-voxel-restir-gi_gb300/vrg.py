@@ -108,7 +108,8 @@ class FrameStats(C.Structure):
                 ("ms_spatial", C.c_float), ("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
                 ("error_flags", C.c_uint32), ("reserved", C.c_uint32), ("ms_trace", C.c_float * 8),
                 ("ms_shade", C.c_float * 8), ("ms_anyhit", C.c_float * 8), ("nodes_visited", C.c_uint64),
-                ("leaves_visited", C.c_uint64)]
+                ("leaves_visited", C.c_uint64), ("light_nodes_visited", C.c_uint64),
+                ("light_leaves_visited", C.c_uint64), ("light_hits", C.c_uint64)]
 
 
 _lib = None
