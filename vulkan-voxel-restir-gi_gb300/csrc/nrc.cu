@@ -5,16 +5,18 @@
 // the path tracer produces (Müller et al. 2021, "Real-time Neural Radiance
 // Caching") with a relative L2 loss and Adam.
 //
-// GB300 mapping: BF16 weights and activations on the tensor cores
-// (mma m16n8k16, FP32 accumulate) in fully fused per-warp tiles: a warp
-// encodes 32 queries into shared memory, then runs the whole MLP with the
-// activations in registers (the f32 C fragment of layer l is repacked as the
-// bf16 A fragment of layer l+1 without shuffles) and the weights resident in
-// shared memory (row stride padded to 72 bf16: conflict-free fragment loads).
+// GB300 mapping: BF16 weights and activations on the tensor cores, FP32
+// accumulate.  Inference encodes one query per thread (many hash-grid gathers
+// in flight), then runs the MLP on the 5th-generation tensor cores: tiles of
+// 128 queries, tcgen05.mma from shared-memory operands into tensor-memory
+// accumulators, one issuing thread per tile, ReLU epilogues from tcgen05.ld.
 // Training fuses encode, forward, loss, backward through the layers and the
-// hash-grid gradient scatter; weight gradients are a split-K tensor-core
-// reduction over the batch; Adam runs over FP32 master copies and refreshes
-// the BF16 / FP16 working copies.
+// hash-grid gradient scatter in per-warp tiles on mma m16n8k16 (the
+// activations stay in registers: the f32 C fragment of layer l is repacked as
+// the bf16 A fragment of layer l+1 without shuffles; the weights are resident
+// in shared memory, row stride padded to 72 bf16); weight gradients are a
+// split-K tensor-core reduction over the batch; Adam runs over FP32 master
+// copies and refreshes the BF16 / FP16 working copies.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -290,7 +292,6 @@ __device__ __forceinline__ void store_a(__nv_bfloat16 *dst, const uint32_t a[4][
 
 constexpr int NRC_WARPS = 4;   // training kernel (more warps per SM only add contention on the
                                // hash-grid gradient atomics of the coarse levels)
-constexpr int NRC_IWARPS = 12; // inference kernel: 12 warps share one copy of the weights (2 CTAs per SM)
 
 struct InferArgs {
     NrcParams P;
@@ -330,58 +331,209 @@ __global__ void __launch_bounds__(256) k_nrc_encode(InferArgs a) {
     }
 }
 
-// Inference, MLP pass: per warp 32 queries per iteration (2 tiles of 16),
-// their encoded rows read coalesced into the warp's tile
-__global__ void __launch_bounds__(NRC_IWARPS * 32, 2) k_nrc_infer(InferArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16 *W = reinterpret_cast<__nv_bfloat16 *>(smem);
-    __nv_bfloat16 *tiles = W + WFWD_ELEMS;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
-    __shared__ __align__(8) uint64_t bar;
-    if (!stage_bulk(W, a.wpack, (uint32_t)(WFWD_ELEMS * 2), &bar, a.err)) return;  // forward weights
-    __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
-    const uint32_t warps = gridDim.x * NRC_IWARPS;
+// ---------------------------------------------------------------------------
+// Inference, MLP pass on the 5th-generation tensor cores (tcgen05).  A CTA of
+// TC_GROUPS warpgroups; warpgroup g owns a tile of 128 queries:
+//   - its input rows, then its activations, in shared memory as bf16 in the
+//     canonical K-major layout without swizzle: 8-row x 16-byte core matrices
+//     of 128 contiguous bytes, the 8 of a row group's 64 columns side by side
+//     (1 KB per 8 rows);
+//   - its accumulator in tensor memory: lanes 0-127 (row = query), columns
+//     64 g .. 64 g + 63 (FP32).
+// Per layer one thread of the group issues four M128 x N64 x K16 MMAs (N16
+// for the output layer) and commits them to the group's mbarrier; each thread
+// then reads its row of the accumulator (tcgen05.ld), applies ReLU and writes
+// the row back as the next layer's bf16 operand.  The weights (42 KB, the same
+// layout, out x in) are shared by the groups.  Every wait is bounded: past the
+// limit the kernel flags ERR_MMA, waits once more (bounded) for the MMAs in
+// flight, and frees its tensor memory before it returns.
+// ---------------------------------------------------------------------------
+constexpr int TC_GROUPS = 4;
+constexpr int TC_THREADS = 128 * TC_GROUPS;
+constexpr uint32_t TC_COLS = 64 * TC_GROUPS;                 // tensor-memory columns (a power of 2, >= 32)
+constexpr uint32_t TC_LBYTES = (uint32_t)NRC_W * NRC_W * 2;  // one 64 x 64 layer (8 KB)
+constexpr uint32_t TC_WBYTES = 5 * TC_LBYTES + (uint32_t)NRC_OUT * NRC_W * 2;
+constexpr uint32_t TC_TILE = 128u * NRC_W * 2;               // one group's operand tile (16 KB)
+constexpr uint32_t TC_WAIT = 1u << 22;                       // iteration bound of an mbarrier wait
+
+// byte offset of (row r, 8-column group kg) in a K-major tile of 64 columns
+__device__ __forceinline__ uint32_t kmaj_off(uint32_t r, uint32_t kg) {
+    return (r >> 3) * 1024u + kg * 128u + (r & 7u) * 16u;
+}
+
+// shared-memory matrix descriptor: start address, leading byte offset (the
+// next core matrix along K: 128 B), stride byte offset (the next 8 rows:
+// 1 KB), the fixed 0b001 at bits 46-48, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M = 128
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void group_sync(int grp) {
+    asm volatile("bar.sync %0, 128;\n" ::"r"(grp + 1) : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t v[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, uint32_t v[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t relu_bf16x2(uint32_t a, uint32_t b) {
+    return pack_bf16(fmaxf(__uint_as_float(a), 0.0f), fmaxf(__uint_as_float(b), 0.0f));
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_infer_tc(InferArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[TC_GROUPS];
+    __shared__ uint32_t tmem_base_s, fail_s[TC_GROUPS];
+    const int tid = threadIdx.x, grp = tid >> 7, t = tid & 127, warp = tid >> 5;
+    unsigned char *Wc = smem;
+    unsigned char *tile = smem + TC_WBYTES + (size_t)grp * TC_TILE;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&bars[grp]);
+    // the forward weights (row-major, rows of NRC_STRIDE bf16) into the K-major layout
+    for (uint32_t c = tid; c < (5u * NRC_W + NRC_OUT) * 8u; c += TC_THREADS) {
+        const uint32_t row = c >> 3, kg = c & 7u;
+        const uint32_t l = row < 5u * NRC_W ? row / NRC_W : 5u, n = l < 5u ? row % NRC_W : row - 5u * NRC_W;
+        const __nv_bfloat16 *src = a.wpack + (l < 5u ? w_off((int)l) : W5_OFF) + (size_t)n * NRC_STRIDE + kg * 8u;
+        *reinterpret_cast<uint4 *>(Wc + l * TC_LBYTES + kmaj_off(n, kg)) = *reinterpret_cast<const uint4 *>(src);
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        fail_s[grp] = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&tmem_base_s)),
+                     "r"(TC_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_s + (uint32_t)grp * 64u;         // this group's columns
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
     const int words = a.P.levels + 2;
-    for (uint32_t base = (blockIdx.x * NRC_IWARPS + w) * 32; base < n; base += warps * 32) {
-        const uint32_t i = base + lane;
-        uint32_t id = 0;
-        uint32_t *row32 = reinterpret_cast<uint32_t *>(tile + lane * NRC_STRIDE);
-        if (i < n) {
-            id = a.list ? a.list[i] : i;
-            for (int k = 0; k < NRC_W / 2; k++) row32[k] = k < words ? a.enc[(size_t)k * a.enc_cap + i] : 0u;
-        } else {
-            for (int k = 0; k < NRC_W / 2; k++) row32[k] = 0u;
+    const uint32_t tiles = (n + 127u) / 128u;
+    const uint32_t a_s = (uint32_t)__cvta_generic_to_shared(tile), w_s = (uint32_t)__cvta_generic_to_shared(Wc);
+    uint32_t phase = 0;
+    bool failed = false;
+    for (uint32_t ti = blockIdx.x * TC_GROUPS + grp; ti < tiles && !failed; ti += gridDim.x * TC_GROUPS) {
+        const uint32_t i = ti * 128u + (uint32_t)t;
+        const uint32_t id = i < n ? (a.list ? a.list[i] : i) : 0u;
+#pragma unroll
+        for (int kg = 0; kg < 8; kg++) {
+            uint32_t w4[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int k = 4 * kg + j;
+                w4[j] = (i < n && k < words) ? a.enc[(size_t)k * a.enc_cap + i] : 0u;
+            }
+            *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, (uint32_t)kg)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
         }
-        __syncwarp();
-#pragma unroll 1
-        for (int t = 0; t < 2; t++) {
-            uint32_t act[4][4];
-            float c[8][4];
-            load_a(tile + t * 16 * NRC_STRIDE, g, q, act);
-#pragma unroll 1
-            for (int l = 0; l < 5; l++) {
-                layer64(W + w_off(l), act, g, q, c);
-                relu_pack(c, act);
+        fence_async_smem();
+        tc_fence_before();
+        group_sync(grp);
+        for (int l = 0; l < NRC_LAYERS && !failed; l++) {
+            if (t == 0) {
+                tc_fence_after();
+                const uint32_t wl = w_s + (uint32_t)l * TC_LBYTES;
+                const uint32_t idesc = tc_idesc(l < 5 ? (uint32_t)NRC_W : (uint32_t)NRC_OUT);
+#pragma unroll
+                for (int s = 0; s < 4; s++)
+                    tc_mma(tmem, tc_desc(a_s + 256u * s), tc_desc(wl + 256u * s), idesc, s > 0 ? 1u : 0u);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                             : "memory");
             }
-            float y[2][4];
-            layer_out(W + W5_OFF, act, g, q, y);
-            // outputs 0..2 live in n-tile 0, columns 2q, 2q+1 (q = 0, 1)
-            float *ys = reinterpret_cast<float *>(tile + t * 16 * NRC_STRIDE);  // reuse: 16 rows x 4 floats
-            __syncwarp();
-            if (q < 2) {
-                ys[g * 4 + 2 * q] = y[0][0];
-                ys[g * 4 + 2 * q + 1] = y[0][1];
-                ys[(g + 8) * 4 + 2 * q] = y[0][2];
-                ys[(g + 8) * 4 + 2 * q + 1] = y[0][3];
+            if (!mbar_wait(bar, phase, TC_WAIT)) {
+                fail_s[grp] = 1;
+                atomicOr(a.err, ERR_MMA);
             }
             __syncwarp();
-            if (lane >= 16 * t && lane < 16 * t + 16 && i < n) {
-                const float *r = ys + (lane - 16 * t) * 4;
-                a.out[id] = make_float4(r[0], r[1], r[2], 0.0f);
+            tc_fence_after();
+            if (l < NRC_LAYERS - 1) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    uint32_t v[32];
+                    tc_ld32(trow + 32u * h, v);
+                    tc_wait_ld();
+#pragma unroll
+                    for (int g4 = 0; g4 < 4; g4++) {
+                        const uint32_t *u = v + 8 * g4;
+                        *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, (uint32_t)(4 * h + g4))) =
+                            make_uint4(relu_bf16x2(u[0], u[1]), relu_bf16x2(u[2], u[3]), relu_bf16x2(u[4], u[5]),
+                                       relu_bf16x2(u[6], u[7]));
+                    }
+                }
+                fence_async_smem();
+            } else {
+                uint32_t v[4];
+                tc_ld4(trow, v);
+                tc_wait_ld();
+                if (i < n) a.out[id] = make_float4(__uint_as_float(v[0]), __uint_as_float(v[1]), __uint_as_float(v[2]), 0.0f);
             }
-            __syncwarp();
+            tc_fence_before();
+            group_sync(grp);
+            failed = fail_s[grp] != 0;  // the same for the whole group (read after the barrier)
+            if (!failed) phase ^= 1u;
         }
+    }
+    if (failed && t == 0) mbar_wait(bar, phase, TC_WAIT);  // the MMAs in flight, before their memory is freed
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_base_s), "r"(TC_COLS)
+                     : "memory");
     }
 }
 
@@ -737,7 +889,7 @@ struct Nrc {
     size_t act_rows = 0;
     __nv_bfloat16 *H = nullptr, *dZ = nullptr;
     uint32_t step = 0;
-    int grid_infer = 0, grid_train = 0;
+    int grid_train = 0, grid_tc = 0;
     DevBufPtr enc_buf;  // encoded query rows of inference
     size_t enc_cap = 0;
     // a cache frame's gradients wait for their Adam step, which the next user
@@ -745,7 +897,7 @@ struct Nrc {
     bool pending = false;
 };
 
-static size_t infer_smem() { return WFWD_ELEMS * 2 + (size_t)NRC_IWARPS * 32 * NRC_STRIDE * 2; }
+static size_t tc_smem() { return (size_t)TC_WBYTES + (size_t)TC_GROUPS * TC_TILE; }
 static size_t train_smem() {
     return WPACK_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2 + (size_t)NRC_WARPS * 32 * NRC_OUT * 4;
 }
@@ -774,6 +926,18 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
         set_error("nrc: levels 1..16, log2_table 4..24, features 2");
         return VRG_ERR_INVALID_ARGUMENT;
     }
+    // every CTA of the tensor-memory inference kernel that fits on an SM
+    // must get its columns (512 per SM), or its allocation would wait
+    int bc = 0;
+    if (cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem()) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bc, k_nrc_infer_tc, TC_THREADS, tc_smem()) != cudaSuccess ||
+        bc < 1 || (uint32_t)bc * TC_COLS > 512u) {
+        delete N;
+        set_error("radiance cache: %d tensor-core inference CTAs per SM, %u tensor-memory columns each", bc, TC_COLS);
+        return VRG_ERR_UNSUPPORTED;
+    }
+    N->grid_tc = ctx->num_sms * bc;
     N->T = (size_t)1 << P.log2_t;
     const double b = P.levels > 1 ? std::exp((std::log((double)d->max_resolution) - std::log((double)d->base_resolution)) /
                                              (double)(P.levels - 1))
@@ -839,12 +1003,9 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     VRG_CUDA_TRY(cudaMemcpyAsync(N->w_master, wm.data(), MASTER_ELEMS * 4, cudaMemcpyHostToDevice, s));
     k_pack_weights<<<(uint32_t)((WPACK_ELEMS + 255) / 256), 256, 0, s>>>(N->w_master, N->wpack);
     VRG_CUDA_TRY(cudaGetLastError());
-    VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
     VRG_CUDA_TRY(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
-    int bi = 0, bt = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bi, k_nrc_infer, NRC_IWARPS * 32, infer_smem());
+    int bt = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, k_nrc_train, NRC_WARPS * 32, train_smem());
-    N->grid_infer = std::max(1, ctx->num_sms * std::max(1, bi));
     N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
 
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -866,8 +1027,9 @@ vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     // one query per thread: short-lived CTAs, so that a higher-priority
     // stream's kernels (a cache frame's training branch) get SMs in between
     k_nrc_encode<<<(n + 255) / 256, 256, 0, s>>>(a);
-    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_infer, (n + NRC_IWARPS * 32 - 1) / (NRC_IWARPS * 32));
-    k_nrc_infer<<<blocks, NRC_IWARPS * 32, infer_smem(), s>>>(a);
+    const uint32_t tiles = (n + 127) / 128;
+    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_tc, (tiles + TC_GROUPS - 1) / TC_GROUPS);
+    k_nrc_infer_tc<<<blocks, TC_THREADS, tc_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

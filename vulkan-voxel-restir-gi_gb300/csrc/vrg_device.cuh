@@ -251,6 +251,7 @@ constexpr uint32_t ERR_STACK = 1u;
 constexpr uint32_t ERR_LIGHT_LIST = 2u;
 constexpr uint32_t ERR_GUARD = 4u;
 constexpr uint32_t ERR_COPY = 8u;           // a bulk copy into shared memory did not complete in time
+constexpr uint32_t ERR_MMA = 16u;           // a tensor-core MMA group did not complete in time
 constexpr uint32_t TRAV_GUARD = 1u << 22;  // iteration bound of every traversal loop
 
 }  // namespace vrg
