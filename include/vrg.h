@@ -184,6 +184,11 @@ typedef struct vrg_renderer vrg_renderer;
 
 /* ---- context ---------------------------------------------------------- */
 VRG_API vrg_status vrg_context_create(const vrg_context_desc *desc, vrg_context **out);
+/* Drops the handle.  Objects, scenes, renderers and caches made from the
+ * context each hold a reference to it (as the reference's Arc-shared queue and
+ * allocators, scene.rs:112): the context, its stream and its buffers are freed
+ * when the last of them is destroyed, so handles may be destroyed in any
+ * order, and a child keeps working after the context handle is gone. */
 VRG_API vrg_status vrg_context_destroy(vrg_context *ctx);
 /* The cudaStream_t the context submits on (the queue the reference's Scene
  * and Renderer submit to, scene.rs:112, interactive_rendering.rs:447).  A

@@ -58,6 +58,28 @@ static void release_object(Object *o) {
 using namespace vrg;
 
 struct vrg_context : Context {};
+
+namespace vrg {
+
+void ctx_retain(Context *c) { c->refs++; }
+
+void ctx_release(Context *c) {
+    if (--c->refs) return;
+    for (Object *o : c->pending) release_object(o);
+    c->pending.clear();
+    c->d_mats.reset();
+    c->d_atlas.reset();
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+    delete static_cast<vrg_context *>(c);
+}
+
+Object::~Object() {
+    batch.reset();  // stream-ordered free on the context's stream, before the context may go
+    if (ctx) ctx_release(ctx);
+}
+
+}  // namespace vrg
 struct vrg_object : Object {};
 struct vrg_scene : Scene {};
 struct vrg_renderer : Renderer {};
@@ -129,12 +151,12 @@ VRG_API vrg_status vrg_context_synchronize(vrg_context *ctx) {
 
 VRG_API vrg_status vrg_context_destroy(vrg_context *ctx) {
     if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
-    for (Object *o : ctx->pending) release_object(o);
-    ctx->pending.clear();
-    ctx->d_mats.reset();
-    cudaStreamSynchronize(ctx->stream);
-    cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        for (Object *o : ctx->pending) release_object(o);  // the pending list's references
+        ctx->pending.clear();
+    }
+    ctx_release(ctx);  // the handle's reference; children still alive keep the context
     return VRG_OK;
 }
 
@@ -228,6 +250,7 @@ VRG_API vrg_status vrg_upload_chunk(vrg_context *ctx, const uint8_t *blocks, con
         }
     vrg_object *o = new vrg_object();
     o->ctx = ctx;
+    ctx_retain(ctx);
     o->blocks.assign(blocks, blocks + VRG_CHUNK_BLOCKS);
     o->slabs.assign(6 * 1024, (uint8_t)air);
     for (int f = 0; f < 6; f++) {
@@ -329,6 +352,7 @@ VRG_API vrg_status vrg_scene_create(vrg_context *ctx, vrg_scene **out) {
     if (!ctx || !out) return VRG_ERR_INVALID_ARGUMENT;
     vrg_scene *s = new vrg_scene();
     s->ctx = ctx;
+    ctx_retain(ctx);
     *out = s;
     return VRG_OK;
 }
@@ -338,7 +362,9 @@ VRG_API vrg_status vrg_scene_destroy(vrg_scene *scene) {
     cudaStreamSynchronize(scene->ctx->stream);
     for (auto &kv : scene->objects) release_object(kv.second.obj);
     for (Object *o : scene->retired) release_object(o);
+    Context *c = scene->ctx;
     delete scene;
+    ctx_release(c);
     return VRG_OK;
 }
 
@@ -571,6 +597,7 @@ VRG_API vrg_status vrg_renderer_create(vrg_context *ctx, uint32_t width, uint32_
     if ((uint64_t)width * height >= (1ull << 31)) return VRG_ERR_UNSUPPORTED;
     vrg_renderer *r = new vrg_renderer();
     r->ctx = ctx;
+    ctx_retain(ctx);
     r->W = r->out_w = width;
     r->H = r->out_h = height;
     r->P = (uint64_t)width * height;
@@ -604,6 +631,7 @@ VRG_API vrg_status vrg_renderer_create_batched(vrg_context *ctx, uint32_t n_view
     }
     vrg_renderer *r = new vrg_renderer();
     r->ctx = ctx;
+    ctx_retain(ctx);
     r->W = r->out_w = widths[0];
     r->H = r->out_h = heights[0];
     r->P = P;
@@ -704,7 +732,9 @@ VRG_API vrg_status vrg_renderer_destroy(vrg_renderer *r) {
     if (r->h_pinned) cudaFreeHost(r->h_pinned);
     if (r->h_views) cudaFreeHost(r->h_views);
     r->res_buf.reset();
-    delete r;
+    Context *c = r->ctx;
+    delete r;  // its buffers are freed on the context's stream, before the context may go
+    ctx_release(c);
     return VRG_OK;
 }
 

@@ -1009,6 +1009,7 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     N->grid_train = std::max(1, ctx->num_sms * std::max(1, bt));
 
     VRG_CUDA_TRY(cudaStreamSynchronize(s));
+    ctx_retain(ctx);  // dropped by nrc_destroy
     *out = N;
     return VRG_OK;
 }
@@ -1102,7 +1103,9 @@ uint32_t nrc_batch(const Nrc *N) { return N->desc.batch ? N->desc.batch : 65536u
 void nrc_destroy(Nrc *N) {
     if (!N) return;
     cudaStreamSynchronize(N->ctx->stream);
-    delete N;
+    Context *c = N->ctx;
+    delete N;  // its buffers are freed on the context's stream, before the context may go
+    ctx_release(c);
 }
 
 // ---- host-array entry points (tests and tools) ------------------------------

@@ -103,7 +103,7 @@ struct Object {
     const uint32_t *light_leaf_tri = nullptr;  // per light node (leaf payload, same packing)
     uint32_t levels = 0;                  // SAH level passes of the batch (depth bound)
     std::atomic<int> refs{1};
-    virtual ~Object() = default;
+    virtual ~Object();  // frees its buffers, then drops its reference to the context
 };
 
 struct Context {
@@ -118,7 +118,14 @@ struct Context {
     std::mutex mu;                       // guards pending + stream use from upload threads
     std::vector<Object *> pending;
     int num_sms = 0;
+    // references: the handle, and every object, scene, renderer and cache made
+    // from it (as the reference's Arc-shared queues and allocators): the
+    // context, its stream and its buffers are freed when the last one is
+    // dropped, whatever the order in which the handles are destroyed
+    std::atomic<int> refs{1};
 };
+void ctx_retain(Context *c);
+void ctx_release(Context *c);
 
 vrg_status extract_and_build(Context *ctx, std::vector<Object *> &batch);
 
