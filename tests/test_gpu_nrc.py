@@ -74,6 +74,29 @@ def test_gradients_match_oracle(gpu_ctx):
     c.close()
 
 
+def test_gradients_after_a_larger_batch(gpu_ctx):
+    """The activation buffers grow to the largest batch seen; a smaller batch
+    afterwards must write and read them with the same row pitch."""
+    rng = np.random.default_rng(6)
+    c = _cache(gpu_ctx)
+    tab = (rng.normal(size=c.levels * (1 << c.log2_table) * 2) * 0.5).astype(np.float32)
+    c.write(vrg.NRC_TABLE, tab)
+    big = _samples(rng, 4000)
+    c.train(*big, update=False)  # grows the buffers to 4000 rows per layer
+    pos, nrm, d, target = _samples(rng, 700)
+    c.write(vrg.NRC_ZERO_GRADS)
+    c.train(pos, nrm, d, target, update=False)
+    gw = c.read(vrg.NRC_WEIGHT_GRADS)
+    sc, dn, r1 = c.layout()
+    m = Model(c.read(vrg.NRC_WEIGHTS), c.read(vrg.NRC_TABLE), c.levels, c.log2_table)
+    m.loss(m.forward(corners(pos, LO, HI, sc, dn, r1, c.log2_table), nrm, d), target).backward()
+    for l in range(5):
+        ref = m.Ws[l].grad.numpy().reshape(-1)
+        assert _rel(gw[l * 4096:(l + 1) * 4096], ref) < 5e-2, (l, _rel(gw[l * 4096:(l + 1) * 4096], ref))
+    assert _rel(gw[5 * 4096:5 * 4096 + 192], m.W5.grad.numpy().reshape(-1)) < 5e-2
+    c.close()
+
+
 def test_training_converges(gpu_ctx):
     rng = np.random.default_rng(4)
     c = _cache(gpu_ctx, levels=12, log2_t=14)

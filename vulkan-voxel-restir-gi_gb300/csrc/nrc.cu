@@ -548,6 +548,7 @@ struct TrainArgs {
     const float4 *target;
     __nv_bfloat16 *H;           // [6][n_pad][64] layer inputs (H0 = encoding)
     __nv_bfloat16 *dZ;          // [6][n_pad][64] pre-activation gradients (layer 5: 16 used)
+    size_t n_pad;               // rows per layer of H and dZ (the buffers' allocation, >= n)
     float2 *gtable;             // hash-grid gradients (fp32)
     float *loss;                // summed loss
     uint32_t *err;              // error word (ERR_COPY)
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
     if (!stage_bulk(W, a.wpack, (uint32_t)(WPACK_ELEMS * 2), &bar, a.err)) return;  // weights and transposes
     __nv_bfloat16 *tile = tiles + (size_t)w * 32 * NRC_STRIDE;
     float *ybuf = reinterpret_cast<float *>(tiles + (size_t)NRC_WARPS * 32 * NRC_STRIDE) + (size_t)w * 32 * NRC_OUT;
-    const size_t n_pad = ((size_t)a.n + 31) & ~(size_t)31;
+    const size_t n_pad = a.n_pad;
     const uint32_t warps = gridDim.x * NRC_WARPS;
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
     const float inv_n = n ? 1.0f / (float)n : 0.0f;
@@ -1057,8 +1058,10 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     VRG_TRY(nrc_flush(N, s));  // new gradients start from the updated cache
     VRG_TRY(ensure_act(N, n));
     const size_t n_pad = N->act_rows;
-    TrainArgs a{N->P,   N->table, N->wpack, n,        n_dev,    list,   pos, dir, nrm, target,
-                N->H,   N->dZ,    N->t_grad, N->loss, err ? err : N->err};
+    // H and dZ hold n_pad rows per layer (the allocation, possibly made for a
+    // larger batch): the training pass writes and k_nrc_dw reads with that pitch
+    TrainArgs a{N->P,  N->table, N->wpack, n,         n_dev,   list,  pos, dir, nrm, target,
+                N->H,  N->dZ,    n_pad,    N->t_grad, N->loss, err ? err : N->err};
     const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
     k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());
