@@ -192,10 +192,10 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
 
 
 # k_trace DRAM bytes (read + write) per pixel per frame, all bounces, from one
-# ncu --set full capture of the workload at 960x540 (5.65 + 25.34 + 20.96 MB over
+# ncu --set full capture of the workload at 960x540 (4.03 + 25.31 + 20.98 MB over
 # 518,400 pixels; profiles/k_trace_restir540p.md); the 1080p launches are too
 # large to capture with --set full, and the traffic scales with the pixel count
-TRACE_DRAM_BYTES_PER_PX = 51.95e6 / (960 * 540)
+TRACE_DRAM_BYTES_PER_PX = 50.31e6 / (960 * 540)
 
 C3_N = 8  # chunks per side of the learned-cache workload
 E2E_SLOTS = 3  # host image buffers of the end-to-end loop (frames in flight)
