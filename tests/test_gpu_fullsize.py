@@ -46,3 +46,58 @@ def test_headline_workload_frames_bit_exact(gpu_ctx, orc):
         scene.close()
         for o in objs:
             o.release()
+
+
+def test_batched_workload_views_match_single_view_renders(gpu_ctx):
+    """The 64-scene batched workload (chunk grids 1x1..8x8, extents from 256^2
+    to 1920x1080, 56 M pixels, 2 bounces + ReSTIR), two frames replayed from a
+    CUDA graph: every view bit for bit as a single-view renderer fed the same
+    scene, camera, seeds and frame index (which the test above ties to the
+    oracle at the full 1080p extent)."""
+    C2_SEED, C2_SCENES = 20240602, 64
+    C2_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
+    mats, n = vrg.terrain_materials(SEED)
+    gpu_ctx.set_materials(mats, n)
+    rng = np.random.default_rng(C2_SEED)
+    grids = rng.integers(1, 9, size=(C2_SCENES, 2))
+    res = [C2_RES[i] for i in rng.integers(0, len(C2_RES), size=C2_SCENES)]
+    scenes, keep = [], []
+    for i in range(C2_SCENES):
+        sc, objs = vrg.build_world(gpu_ctx, vrg.terrain_blocks(C2_SEED + 1 + i, int(grids[i, 0]), int(grids[i, 1]),
+                                                              EMISSIVE))
+        scenes.append(sc)
+        keep.append(objs)
+
+    def params(flags):
+        return vrg.RenderParams(1, 1, 3, 2, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, 0, flags, 4)
+
+    def cams(f):
+        return [vrg.orbit_camera(int(grids[v, 0]), int(grids[v, 1]), f, 64, w, h) for v, (w, h) in enumerate(res)]
+
+    def seeds(v, f):
+        return (3000 + 7 * v + 11 * f, 5000 + 13 * v + 17 * f)
+
+    br = vrg.BatchRenderer(gpu_ctx, res, 2)
+    try:
+        batched = []
+        for f in range(2):
+            imgs, rads = br.render(scenes, cams(f), params(vrg.RENDER_GRAPH), [seeds(v, f) for v in range(C2_SCENES)],
+                                   want_image=True, want_radiance=True)
+            assert br.last_stats.error_flags == 0
+            batched.append((imgs, rads))
+        for v, (w, h) in enumerate(res):
+            r = vrg.Renderer(gpu_ctx, w, h, 2)
+            for f in range(2):
+                p = params(0)
+                p.temporal_seed, p.spatial_seed = seeds(v, f)
+                img, rad = r.render_params(scenes[v], cams(f)[v], p, want_image=True, want_radiance=True)
+                assert np.array_equal(img.reshape(-1), batched[f][0][v].reshape(-1)), (v, f)
+                assert np.array_equal(rad.view(np.uint32).reshape(-1), batched[f][1][v].view(np.uint32).reshape(-1)), (v, f)
+            r.close()
+    finally:
+        br.close()
+        for sc in scenes:
+            sc.close()
+        for objs in keep:
+            for o in objs:
+                o.release()
