@@ -42,6 +42,7 @@ def test_headline_workload_frames_bit_exact(gpu_ctx, orc):
             assert gr.last_stats.rays_closest > W * H
     finally:
         gr.close()
+        orr.close()
         OW.close()
         scene.close()
         for o in objs:
@@ -101,3 +102,35 @@ def test_batched_workload_views_match_single_view_renders(gpu_ctx):
         for objs in keep:
             for o in objs:
                 o.release()
+
+
+def test_large_scene_frame_bit_exact(gpu_ctx, orc):
+    """The large workload's scene (32x32 chunks, about 2 M surface blocks, 0.2%
+    emissive) seen at its full 3840x2160 view extent: one ReSTIR frame, every
+    captured array bit for bit against the oracle (the deepest BVH of the
+    workloads: the traversal stack bound and the lamp walk at full scale)."""
+    n4, em4, w4, h4 = 32, 0.002, 3840, 2160
+    mats, n, world = terrain_world(SEED, n4, n4, em4)
+    gpu_ctx.set_materials(mats, n)
+    scene, objs = vrg.build_world(gpu_ctx, world)
+    OW = orc.build_world(mats, n, world)
+    gr = vrg.Renderer(gpu_ctx, w4, h4, NB)
+    orr = orc.Renderer(w4, h4, NB)
+    try:
+        cam = vrg.orbit_camera(n4, n4, 0, 64, w4, h4)
+        p = params(nee=1, view=1, spatial=3, nb=NB, mode=vrg.MODE_CONFIG, seeds=(5, 1005, 2005), radius=30.0,
+                   m_cap=20, slots=1)
+        img, _ = gr.render_params(scene, cam, p)
+        orr.render(OW, cam, p)
+        oimg, _ = orr.image()
+        diffs = compare_frame(gr, orr, NB)
+        assert all(v == 0 for v in diffs.values()), {k: v for k, v in diffs.items() if v}
+        assert np.array_equal(img.reshape(-1), oimg.reshape(-1))
+        assert gr.last_stats.error_flags == 0
+    finally:
+        gr.close()
+        orr.close()
+        OW.close()
+        scene.close()
+        for o in objs:
+            o.release()
