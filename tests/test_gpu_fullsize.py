@@ -105,7 +105,7 @@ def test_batched_workload_views_match_single_view_renders(gpu_ctx):
 
 
 def test_large_scene_frame_bit_exact(gpu_ctx, orc):
-    """The large workload's scene (32x32 chunks, about 2 M surface blocks, 0.2%
+    """The large workload's scene (32x32 chunks, 1.1 M surface blocks, 0.2%
     emissive) seen at its full 3840x2160 view extent: one ReSTIR frame, every
     captured array bit for bit against the oracle (the deepest BVH of the
     workloads: the traversal stack bound and the lamp walk at full scale)."""
