@@ -164,8 +164,9 @@ class OracleSampler:
 
     def frame(self, f):
         """Renders orbit frame f; returns (seconds, rays)."""
-        import vrg
-        cam = vrg.orbit_camera(NX, NZ, f % ORBIT, ORBIT, W, H)
+        import oracle
+        import vrg  # struct layouts only
+        cam = oracle.orbit_camera(NX, NZ, f % ORBIT, ORBIT, W, H)
         p = vrg.RenderParams(1, 1, 3, NB, vrg.MODE_CONFIG, f, 1000 + f, 2000 + f, 30.0, 20, 1, 0, 0)
         y0 = H // 2 - self.rows // 2
         t0 = time.perf_counter()
@@ -191,11 +192,27 @@ def oracle_sample(world, mats, n, rows, frames=1, start_frame=0):
     return rays / dt / 1e6, dt, rays, smp.build_s
 
 
-# k_trace DRAM bytes (read + write) per pixel per frame, all bounces, from one
-# ncu --set full capture of the workload at 960x540 (4.03 + 25.31 + 20.98 MB over
-# 518,400 pixels; profiles/k_trace_restir540p.md); the 1080p launches are too
-# large to capture with --set full, and the traffic scales with the pixel count
-TRACE_DRAM_BYTES_PER_PX = 50.31e6 / (960 * 540)
+# The k_trace DRAM traffic comes from a committed ncu capture of the current
+# build (dram__bytes_read.sum + dram__bytes_write.sum per launch at 960x540,
+# the command that made it stored beside the figures); it is scaled to the
+# bench's extent by the pixel count.  The 1080p launches are too large to
+# capture with many metrics.
+TRACE_PROFILE = os.path.join(ROOT, "profiles", "k_trace_dram_restir540p.json")
+
+
+def trace_traffic_per_launch(pixels, bounces):
+    """(DRAM bytes per k_trace launch scaled to `pixels`, source string), or (None, reason)."""
+    try:
+        with open(TRACE_PROFILE) as f:
+            prof = json.load(f)
+    except (OSError, ValueError) as e:
+        return None, f"no committed k_trace profile ({e.__class__.__name__})"
+    per_frame = sum(prof["dram_bytes_per_launch"])  # one launch per bounce
+    scale = pixels / float(prof["pixels"])
+    return round(per_frame * scale / bounces), (
+        f"ncu dram__bytes_read.sum+dram__bytes_write.sum of k_trace at {prof['resolution']} "
+        f"({prof['build']}), scaled by pixels, per launch")
+
 
 C3_N = 8  # chunks per side of the learned-cache workload
 E2E_SLOTS = 3  # host image buffers of the end-to-end loop (frames in flight)
@@ -345,18 +362,17 @@ def update_commit_ms(scene, nx, nz, reps=5):
     return round(float(np.median(ms)), 3)
 
 
-def run_large(args, d):
+def large_block(ctx, steps, warmup, gt_spp, extent=(C4_W, C4_H), cache_warmup=64):
     """Large workload: 32x32 chunks (1024x32x1024 blocks, 0.2% emissive), four
-    3840x2160 views of one orbit eye rendered as one batch, 1 spp ReSTIR over
-    paths that end into the radiance cache (trained online in the same
-    frames), judged against an FP64 plain 8-bounce ground truth of the same
-    views; the plain 3-bounce tracer is measured beside it at >= equal time."""
+    views of one orbit eye rendered as one batch, 1 spp ReSTIR over paths
+    that end into the radiance cache (trained online in the same frames),
+    judged against an FP64 plain 8-bounce ground truth of `gt_spp` frames of
+    the same views; the plain 3-bounce tracer is measured beside it at >=
+    equal time.  Each method is timed one frame at a time (with stats) and
+    with its frames in flight (back to back, no stats)."""
     import vrg
     import quality
-    if d.rank != 0:
-        d.close()
-        return
-    ctx = vrg.Context(0)
+    import torch
     mats, n = vrg.terrain_materials(SEED)
     ctx.set_materials(mats, n)
     t0 = time.perf_counter()
@@ -368,17 +384,15 @@ def run_large(args, d):
     lt, gtl = scene.get_tlas()
     t_commit = time.perf_counter() - t0
     prims = sum(o.info()["surface_blocks"] for o in objs)
-    W4, H4 = (C4_W, C4_H) if not args.resolution else (W, H)
-    ext = [(W4, H4)] * 4
-    br = vrg.BatchRenderer(ctx, ext, 8)
+    W4, H4 = extent
+    br = vrg.BatchRenderer(ctx, [(W4, H4)] * 4, 8)
     cams = view_cameras(C4_N, C4_N, 0, W4, H4)
     scenes = [scene] * 4
     seeds = vrg.Pcg32(SEED + 4)
 
     def params(nb, flags, view, accumulate=0):
-        p = vrg.RenderParams(1, view, 3, nb, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, accumulate,
-                             flags | vrg.RENDER_NO_PACK, 4)
-        return p
+        return vrg.RenderParams(1, view, 3, nb, vrg.MODE_CONFIG, 0, 0, 0, 30.0, 20, 1, accumulate,
+                                flags | vrg.RENDER_NO_PACK, 4)
 
     def frame(p, want_rad=False):
         _, rads = br.render(scenes, cams, p, [(seeds.next(), seeds.next()) for _ in range(4)],
@@ -391,35 +405,34 @@ def run_large(args, d):
     # ground truth: plain 8-bounce tracer accumulated in FP64
     br.reset_accumulation()
     t0 = time.perf_counter()
-    for f in range(args.gt_spp):
+    for f in range(gt_spp):
         frame(params(8, vrg.RENDER_PLAIN_ONLY, 0, accumulate=1))
     gt, n_gt = br.read_accumulation()
     gt_s = time.perf_counter() - t0
     cache = vrg.RadianceCache(ctx, gtl[0]["min"], gtl[0]["max"], seed=7)
     br.set_cache(cache)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", torch.cuda.current_device()))
     out = {}
     methods = (("plain", 3, vrg.RENDER_PLAIN_ONLY, 0), ("restir_cache", 2, vrg.RENDER_CACHE, 1))
     for name, nb, flags, view in methods:
-        warm = 64 if name == "restir_cache" else args.warmup
+        warm = cache_warmup if name == "restir_cache" else warmup
         for f in range(warm):
             frame(params(nb, flags, view))
         ms, rays, errs = 0.0, 0, []
-        for s_ in range(args.steps):
+        for s_ in range(steps):
             m, r_, rads = frame(params(nb, flags, view), want_rad=(s_ < 4))
             ms += m
             rays += r_
             if rads[0] is not None:
                 errs.append(np.mean([quality.relmse(rads[v], gt[v]) for v in range(4)]))
-        out[name] = {"ms_per_frame": round(ms / args.steps, 3), "mrays_s": round(rays / (ms / 1000.0) / 1e6, 3),
-                     "rays_per_frame": rays // args.steps, "relmse_1spp": round(float(np.mean(errs)), 5)}
+        out[name] = {"ms_per_frame": round(ms / steps, 3), "mrays_s": round(rays / (ms / 1000.0) / 1e6, 3),
+                     "rays_per_frame": rays // steps, "relmse_1spp": round(float(np.mean(errs)), 5)}
         # the same frames back to back (no stats: frames in flight), CUDA
         # events on the library stream; rays per frame from the frames above
-        import torch
-        stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", torch.cuda.current_device()))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        for s_ in range(args.steps):
+        for s_ in range(steps):
             views = (vrg.View * 4)()
             for v in range(4):
                 views[v] = vrg.View(scenes[v].h, cams[v], seeds.next(), seeds.next())
@@ -427,10 +440,10 @@ def run_large(args, d):
             vrg.check(ctx.lib.vrg_render_batched(br.h, views, 4, C.byref(p), None, None), "vrg_render_batched")
         e1.record(stream)
         e1.synchronize()
-        ms_f = e0.elapsed_time(e1) / args.steps
+        ms_f = e0.elapsed_time(e1) / steps
         out[name]["ms_per_frame_in_flight"] = round(ms_f, 3)
-        out[name]["mrays_s_in_flight"] = round((rays / args.steps) / (ms_f / 1000.0) / 1e6, 3)
-    # plain accumulated over at least the cache frame's time
+        out[name]["mrays_s_in_flight"] = round((rays / steps) / (ms_f / 1000.0) / 1e6, 3)
+    # plain accumulated over at least the cache frame's time (frames one at a time)
     k = max(1, int(np.ceil(out["restir_cache"]["ms_per_frame"] / out["plain"]["ms_per_frame"] - 1e-9)))
     br.set_cache(None)
     br.reset_accumulation()
@@ -438,47 +451,86 @@ def run_large(args, d):
         frame(params(3, vrg.RENDER_PLAIN_ONLY, 0, accumulate=1))
     acc, _ = br.read_accumulation()
     rel_plain_k = float(np.mean([quality.relmse(acc[v], gt[v]) for v in range(4)]))
+    rc = out["restir_cache"]
+    res = {
+        "workload": f"large-32x32chunks-4x{W4}x{H4}", "chunks": [C4_N, C4_N], "surface_blocks": prims,
+        "emissive_fraction": C4_EMISSIVE, "views": 4, "resolution": [W4, H4],
+        "method": "2 bounces ending into the radiance cache + ReSTIR (3 spatial, 30 px, M-cap 20), "
+                  "1/16 paths trace 4 more bounces and train the cache",
+        "scene_build": {"blas_ms": round(1000 * t_blas, 1), "commit_ms": round(1000 * t_commit, 1),
+                        "update_commit_ms": update_commit_ms(scene, C4_N, C4_N)},
+        "methods": out,
+        "ground_truth": {"spp": n_gt, "bounces": 8, "accumulation": "fp64 on the GPU", "seconds": round(gt_s, 1)},
+        "equal_time": {"plain_frames": k, "plain_time_ratio": round(k * out["plain"]["ms_per_frame"] /
+                                                                    rc["ms_per_frame"], 3),
+                       "relmse_plain": round(rel_plain_k, 5), "relmse_restir_cache_1spp": rc["relmse_1spp"],
+                       "gain": round(rel_plain_k / max(rc["relmse_1spp"], 1e-12), 3),
+                       "gain_lower_bound": round(out["plain"]["relmse_1spp"] / max(
+                           1.0, rc["ms_per_frame"] / out["plain"]["ms_per_frame"]) /
+                           max(rc["relmse_1spp"], 1e-12), 3),
+                       "in_flight_plain_slower": out["plain"]["ms_per_frame_in_flight"] >=
+                           rc["ms_per_frame_in_flight"]},
+    }
+    cache.close()
+    br.close()
+    scene.close()
+    for o in objs:
+        o.release()
+    return res
+
+
+def run_large(args, d):
+    """The large workload as its own line (--workload large), ground truth at
+    --gt-spp frames (4096 by default)."""
+    import vrg
+    if d.rank != 0:
+        d.close()
+        return
+    ctx = vrg.Context(0)
+    ext = (C4_W, C4_H) if not args.resolution else (W, H)
+    blk = large_block(ctx, args.steps, args.warmup, args.gt_spp, ext)
     hbm_peak = None
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
             hbm_peak = json.load(fh).get("hbm_gbs")
     except (OSError, ValueError):
         pass
+    rc = blk["methods"]["restir_cache"]
     line = {
-        "metric": METRIC, "value": out["restir_cache"]["mrays_s"], "unit": "Mrays/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["restir_cache"]["ms_per_frame"],
+        "metric": METRIC, "value": rc["mrays_s"], "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rc["ms_per_frame"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded value-noise voxel terrain, no dataset)",
-        "config": {"workload": "large-32x32chunks-4x3840x2160", "chunks": [C4_N, C4_N], "surface_blocks": prims,
-                   "emissive_fraction": C4_EMISSIVE, "views": 4, "resolution": [W4, H4],
-                   "method": "2 bounces ending into the radiance cache + ReSTIR (3 spatial, 30 px, M-cap 20), "
-                             "1/16 paths trace 4 more bounces and train the cache",
-                   "parallelism": "single GPU, one batched launch sequence"},
-        "scene_build": {"blas_ms": round(1000 * t_blas, 1), "commit_ms": round(1000 * t_commit, 1),
-                        "update_commit_ms": update_commit_ms(scene, C4_N, C4_N)},
-        "methods": out,
-        "ground_truth": {"spp": n_gt, "bounces": 8, "accumulation": "fp64 on the GPU", "seconds": round(gt_s, 1)},
-        "equal_time": {"plain_frames": k, "relmse_plain": round(rel_plain_k, 5),
-                       "relmse_restir_cache_1spp": out["restir_cache"]["relmse_1spp"],
-                       "gain": round(rel_plain_k / max(out["restir_cache"]["relmse_1spp"], 1e-12), 3),
-                       "gain_lower_bound": round(out["plain"]["relmse_1spp"] / max(
-                           1.0, out["restir_cache"]["ms_per_frame"] / out["plain"]["ms_per_frame"]) /
-                           max(out["restir_cache"]["relmse_1spp"], 1e-12), 3)},
-        "hbm_peak_gbs": hbm_peak,
+        "config": {"workload": blk["workload"], "chunks": blk["chunks"], "surface_blocks": blk["surface_blocks"],
+                   "emissive_fraction": C4_EMISSIVE, "views": 4, "resolution": blk["resolution"],
+                   "method": blk["method"], "parallelism": "single GPU, one batched launch sequence"},
+        "scene_build": blk["scene_build"], "methods": blk["methods"], "ground_truth": blk["ground_truth"],
+        "equal_time": blk["equal_time"], "hbm_peak_gbs": hbm_peak,
     }
-    cache.close()
-    br.close()
     print(json.dumps(line), flush=True)
     d.close()
 
 
+def headline_config(gpus):
+    """The workload of the headline line, the same dict in both arms."""
+    return {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
+            "bounces": NB, "temporal_history": 1, "spatial_neighbours": 3, "radius_px": 30,
+            "m_cap": 20, "emissive_fraction": EMISSIVE, "orbit_frames": ORBIT,
+            "l2": "per-frame state (~1.2 GB of rays, records, reservoirs) exceeds L2; BVH L2-resident",
+            "parallelism": f"replicas{gpus}"}
+
+
 def run_reference(args, d):
-    import vrg
+    """The reference's CPU path (the oracle restatement, OpenMP over pixels on
+    every host core).  Its inputs come from the generator compiled into the
+    oracle library, so this process never loads the CUDA library."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
     if d.rank != 0:
         d.close()
         return
-    mats, n = vrg.terrain_materials(SEED)
-    world = vrg.terrain_blocks(SEED, NX, NZ, EMISSIVE)
+    mats, n = oracle.terrain_materials(SEED)
+    world = oracle.terrain_blocks(SEED, NX, NZ, EMISSIVE)
     # Full frames (the CPU path's stream passes run over the whole image in any
     # case, so a band of rows would understate its throughput), bounded to the
     # first REF_MAX_FRAMES of the K timed frames: about 12 s on 16 cores.
@@ -500,10 +552,9 @@ def run_reference(args, d):
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
         "n_gpus": args.gpus, "steps": frames, "requested_steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total / frames, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value-noise voxel terrain)",
-        "config": {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
-                   "bounces": NB, "spatial_neighbours": 3, "radius_px": 30, "m_cap": 20,
-                   "sample_rows_per_frame": rows},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value-noise voxel terrain, no dataset)",
+        "config": headline_config(args.gpus),
+        "timing": "wall clock around each frame of the oracle on the host cores",
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{rows} of {H} rows per frame, orbit frames {args.warmup}-"
                                    f"{args.warmup + frames - 1} (the first {frames} of the {args.steps} timed)"},
@@ -671,7 +722,31 @@ def run_ours(args, d):
     achieved = trace_bytes / trace_s / 1e9 if trace_s > 0 else 0.0
     trav_bytes = 128 * nodes + 16 * leaves  # 4-wide nodes (128 B) and surface-block records (16 B)
     stream_bytes = W * H * 252  # ReSTIR compulsory stream bytes per frame (reservoirs + radiance)
-    stream_gbs = stream_bytes * args.steps / ((ms_res + ms_sp) / 1000.0) / 1e9 if ms_res + ms_sp > 0 else 0.0
+    stream_s = (ms_res + ms_sp) / 1000.0
+    stream_gbs = stream_bytes * args.steps / stream_s / 1e9 if stream_s > 0 else 0.0
+    # L2 read bandwidth of this device, measured now by the library's own
+    # sweep kernel: the peak of the BVH walks, whose node and record fetches
+    # are L1/L2 traffic (a 32 MiB buffer, 64 sweeps, best of 3)
+    l2_peak = max(ctx.l2_read_gbs(32, 64) for _ in range(3))
+    trace_l2_gbs = trav_bytes / trace_s / 1e9 if trace_s > 0 else 0.0
+    # light-hit collection: 4-wide lamp nodes (112 B: six plane rows and the
+    # refs) and lamp-block records (16 B), over the light-pdf walk's time
+    any_s = sum(ms_ah) / 1000.0
+    walk_bytes = 112 * l_nodes + 16 * l_leaves
+    walk_l2_gbs = walk_bytes / any_s / 1e9 if any_s > 0 else 0.0
+    # shading, HBM: ray + hit in (48 B) and the bounce record out (32 B) per
+    # ray, the next ray and its queue slot (36 B) per continuing ray, and the
+    # two vertices of the ReSTIR sample geometry (64 B) per pixel
+    shade_s = sum(ms_sh) / 1000.0
+    shade_bytes = 80 * closest + 36 * (closest - P * args.steps) + 64 * P * args.steps
+    shade_gbs = shade_bytes / shade_s / 1e9 if shade_s > 0 else 0.0
+    parts = [("k_trace", trace_s, trace_l2_gbs / l2_peak if l2_peak else 0.0, "l2"),
+             ("k_shade", shade_s, shade_gbs / hbm_peak, "hbm"),
+             ("light_pdf_walk", any_s, walk_l2_gbs / l2_peak if l2_peak else 0.0, "l2"),
+             ("k_resolve+k_spatial", stream_s, stream_gbs / hbm_peak, "hbm")]
+    t_all = sum(t for _, t, _, _ in parts)
+    weighted = sum(t * f for _, t, f, _ in parts) / t_all if t_all > 0 else 0.0
+    traffic, traffic_src = trace_traffic_per_launch(W * H, NB)
     quality_block = None
     if not args.no_quality:
         import quality
@@ -700,6 +775,12 @@ def run_ours(args, d):
     if not args.no_batched:
         r.close()  # the batch needs the memory of the 1080p renderer
         batched = batched_block(ctx, steps=16, warmup=3, tuning=best_tuning)
+    large = None
+    if not args.no_large:
+        # the large workload, compact: a 256-spp ground truth (the full
+        # 4096-spp run is --workload large) and 6 frames per method
+        large = large_block(ctx, steps=6, warmup=3, gt_spp=args.large_gt_spp)
+        ctx.set_materials(mats, n)
     upd_ms = update_commit_ms(scene, NX, NZ)
     cpu_frames = args.cpu_frames
     cpu_mr, cpu_dt, cpu_rays, cpu_build_s = (oracle_sample(world, mats, n, args.ref_rows, cpu_frames, 0)
@@ -709,14 +790,9 @@ def run_ours(args, d):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total_s_max / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded value-noise voxel terrain, no dataset)",
-        "config": {"workload": "restir-1080p-4x4chunks", "resolution": [W, H], "chunks": [NX, NZ],
-                   "bounces": NB, "temporal_history": 1, "spatial_neighbours": 3, "radius_px": 30,
-                   "m_cap": 20, "emissive_fraction": EMISSIVE, "orbit_frames": ORBIT,
-                   "l2": "per-frame state (~1.2 GB of rays, records, reservoirs) exceeds L2; BVH L2-resident",
-                   "timing": "K frames enqueued back to back on the library stream (frames in flight), "
-                             "CUDA events on that stream; ray counts and stage times from a replay of the "
-                             "same frames one at a time",
-                   "parallelism": f"replicas{args.gpus}"},
+        "config": headline_config(args.gpus),
+        "timing": "K frames enqueued back to back on the library stream (frames in flight), CUDA events on "
+                  "that stream; ray counts and stage times from a replay of the same frames one at a time",
         "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b],
                          "k_trace": [round(x / args.steps, 4) for x in ms_tr],
                          "k_shade": [round(x / args.steps, 4) for x in ms_sh],
@@ -732,12 +808,20 @@ def run_ours(args, d):
         "update_commit_ms": upd_ms,
         "roofline": {"bound": "hbm", "kernel": "k_trace", "achieved": round(achieved, 2), "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                     "traffic": round(TRACE_DRAM_BYTES_PER_PX * W * H / NB),
-                     "traffic_source": "ncu dram__bytes_read+write of k_trace at 960x540, scaled by pixels, per launch",
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "algorithmic_bytes_per_launch": round(trace_bytes / max(args.steps, 1) / NB),
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
                      "algorithmic_bytes": "16 B hit per ray + 36 B ray/queue per secondary ray",
-                     "note": "k_trace is issue/latency bound: its BVH walk is served from L1/L2 (see traversal)"},
+                     "note": "k_trace is issue/latency bound: its BVH walk is served from L1/L2, see l2",
+                     "l2": {"kernel": "k_trace", "achieved": round(trace_l2_gbs, 1), "peak": round(l2_peak, 1),
+                            "unit": "GB/s", "frac": round(trace_l2_gbs / l2_peak, 4) if l2_peak else None,
+                            "bytes_per_launch": round(trav_bytes / max(args.steps, 1) / NB),
+                            "bytes": "128 B per 4-wide node + 16 B per surface-block record visited",
+                            "peak_source": "measured in this run (vrg_measure_l2_bandwidth: 32 MiB, 64 sweeps, "
+                                           "best of 3)"},
+                     "time_weighted": {"frac": round(weighted, 4),
+                                       "kernels": {k: {"ms_per_frame": round(1000 * t / max(args.steps, 1), 4),
+                                                       "frac": round(f, 4), "peak": pk} for k, t, f, pk in parts}}},
         "traversal": {"kernel": "k_trace", "nodes_per_ray": round(nodes / max(closest, 1), 2),
                       "leaves_per_ray": round(leaves / max(closest, 1), 2),
                       "l1_l2_bytes_per_s_gbs": round(trav_bytes / trace_s / 1e9, 1) if trace_s > 0 else None,
@@ -755,6 +839,7 @@ def run_ours(args, d):
         "quality": quality_block,
         "autotune": tuning,
         "batched": batched,
+        "large": large,
         "clocks": clocks,
         "cpu_baseline": None if cpu_mr is None else {
             "value": round(cpu_mr, 4), "unit": "Mrays/s", "cores": cpu_threads(), "kind": "port",
@@ -778,9 +863,12 @@ def main():
     ap.add_argument("--resolution", default=None, help="WxH override (profiling cases only)")
     ap.add_argument("--no-quality", action="store_true", help="skip the FP64 ground truth / relMSE study")
     ap.add_argument("--gt-spp", type=int, default=None,
-                    help="ground-truth samples per pixel (4096; 512 for the large workload)")
+                    help="ground-truth samples per pixel (4096)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="time the default launch configuration")
+    ap.add_argument("--no-large", action="store_true", help="skip the compact large-workload block")
+    ap.add_argument("--large-gt-spp", type=int, default=256,
+                    help="ground-truth frames of the compact large-workload block")
     ap.add_argument("--workload", default="restir", choices=["restir", "large"],
                     help="restir: the 1080p ReSTIR headline line; large: the 32x32-chunk four-view 4K workload")
     args = ap.parse_args()
@@ -790,7 +878,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.gt_spp is None:
-        args.gt_spp = 512 if args.workload == "large" else 4096
+        args.gt_spp = 4096
     import vrg
     if not os.path.exists(vrg.LIB_PATH):
         sys.path.insert(0, ROOT)

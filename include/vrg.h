@@ -439,14 +439,24 @@ VRG_API vrg_status vrg_build_bl_bvh_batched(vrg_context *ctx, uint32_t count, co
  * prim_order n u32.  stream is a cudaStream_t (NULL = legacy default).
  * n must be 1..32768; larger n returns VRG_ERR_INVALID_ARGUMENT.
  * Scratch is one fixed device array of about 2.4 MiB inside the library,
- * held by every GPU that loads it until the process exits.  The first call
- * on a device looks up that array's device address (cudaGetSymbolAddress),
- * so make the first call on each device before any stream capture.  Every
- * call shares the array: calls that overlap on the GPU (other threads or
- * streams) race and must be serialized by the caller.  The call returns
- * after the build has finished on `stream`. */
+ * held by every GPU that loads it until the process exits.  Each call looks
+ * up that array's device address in the current context
+ * (cudaGetSymbolAddress, which allocates nothing).  Every call shares the
+ * array: calls that overlap on the GPU (other threads or streams) race and
+ * must be serialized by the caller.  The call copies small host values to
+ * the device, synchronizes `stream` once per BVH level (it reads each
+ * level's work count back to the host) and returns after the build has
+ * finished on `stream`; an error return also synchronizes `stream` first. */
 VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const float *power, const uint32_t *ids,
                                             uint32_t n, vrg_bvh_node *nodes, uint32_t *prim_order, void *stream);
+
+/* ---- roofline denominator (no reference counterpart) ------------------
+ * Measures the device's L2 read bandwidth: a library kernel sweeps a buffer
+ * of `bytes` (1..96 MiB, small enough to stay in L2) `reps` times with
+ * 16-byte loads that bypass L1, on the context's stream; *gbs = bytes * reps
+ * / the CUDA-event time of that launch.  The BVH walks are held against it
+ * (their node fetches are L1/L2 traffic).  Synchronizes the stream. */
+VRG_API vrg_status vrg_measure_l2_bandwidth(vrg_context *ctx, uint64_t bytes, uint32_t reps, float *gbs);
 
 /* ---- neural radiance cache (no reference counterpart) ----------------
  * Multiresolution hash-grid encoding of the position (levels x 2 features,

@@ -53,6 +53,11 @@ def lib():
             ("orc_world_set_atlas", C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32]),
             ("orc_read_accum", C.c_uint32, [_P, _P]),
             ("orc_ray_counts", None, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+            ("orc_terrain_materials", C.c_int32, [C.c_uint64, C.POINTER(vrg.Material), C.c_uint32,
+                                                  C.POINTER(C.c_uint32)]),
+            ("orc_terrain_generate", C.c_int32, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P]),
+            ("orc_orbit_camera", C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                             C.c_uint32, C.POINTER(vrg.Camera)]),
         ]
         for name, res, args in sig:
             f = getattr(L, name)
@@ -64,6 +69,27 @@ def lib():
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+# The synthetic inputs (the library's generator compiled into the oracle), so
+# that CPU-only callers build the same scenes without the CUDA library.
+def terrain_materials(seed):
+    mats = (vrg.Material * (6 * 22))()
+    n = C.c_uint32()
+    assert lib().orc_terrain_materials(seed, mats, len(mats), C.byref(n)) == 0
+    return mats, n.value
+
+
+def terrain_blocks(seed, nx, nz, emissive):
+    out = np.empty(nx * nz * vrg.CHUNK_BLOCKS, dtype=np.uint8)
+    assert lib().orc_terrain_generate(seed, nx, nz, emissive, _p(out)) == 0
+    return out.reshape(nx, nz, vrg.CHUNK_BLOCKS)
+
+
+def orbit_camera(nx, nz, frame, n_frames, width, height):
+    cam = vrg.Camera()
+    assert lib().orc_orbit_camera(nx, nz, frame, n_frames, width, height, C.byref(cam)) == 0
+    return cam
 
 
 def build_tl_bvh(aabbs, power, ids, translations=None):

@@ -4,10 +4,12 @@ Some callers cannot allocate device memory while they run (an engine that
 owns the device-memory budget, a streaming worker next to a frame in flight),
 so this entry point builds with scratch held in a fixed array inside the
 library.  Checked through the C ABI against the allocating entry point,
-vrg_build_tl_bvh_batched, on two calls in a row: node arrays and primitive
-order must match bit for bit (tolerance 0, the tolerance of every BVH parity
-test here).  This file is collected last so that a run stopping at the first
-failure has already run every other test.
+vrg_build_tl_bvh_batched, and against the oracle's build_tl_bvh, on calls in
+a row (each one runs on scratch left over by the one before): node arrays and
+primitive order must match bit for bit (tolerance 0, the tolerance of every
+BVH parity test here).  The sizes include roots of one, two and three prims
+and the capacity edge, 32768 prims.  This file is collected last so that a
+run stopping at the first failure has already run every other test.
 """
 import ctypes as C
 
@@ -43,7 +45,7 @@ def _reference_build(lib, vrg, ctx, aabbs, power, ids):
     return nodes, order
 
 
-def test_noalloc_matches_allocating_build_twice(vrglib):
+def test_noalloc_matches_allocating_build_twice(vrglib, orc):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -57,9 +59,11 @@ def test_noalloc_matches_allocating_build_twice(vrglib):
         rng = np.random.default_rng(2024)
         dev = torch.device("cuda:0")
         stream = torch.cuda.current_stream(dev)
-        # two calls in a row: a large grid-of-voxels set, then a smaller random set,
-        # so the second call runs on scratch left over by the first
-        for n, grid in ((20000, True), (3001, False)):
+        # calls in a row: a large grid-of-voxels set, then a smaller random set,
+        # so the second call runs on scratch left over by the first; then the
+        # small roots (1, 2 and 3 prims) and the capacity edge
+        for n, grid in ((20000, True), (3001, False), (1, False), (2, True), (3, False), (32768, True),
+                        (3, True)):
             aabbs, power, ids = _inputs(rng, n, grid)
             ref_nodes, ref_order = _reference_build(lib, vrg, ctx, aabbs, power, ids)
             d_aabbs = torch.from_numpy(aabbs).to(dev)
@@ -76,6 +80,9 @@ def test_noalloc_matches_allocating_build_twice(vrglib):
             order = d_order.cpu().numpy().view(np.uint32)
             assert nodes.tobytes() == ref_nodes.tobytes(), f"node array differs (n={n})"
             assert np.array_equal(order, ref_order), f"prim order differs (n={n})"
+            o_nodes, o_order = orc.build_tl_bvh(aabbs, power, ids)
+            assert nodes.tobytes() == o_nodes.tobytes(), f"node array differs from the oracle (n={n})"
+            assert np.array_equal(order, o_order), f"prim order differs from the oracle (n={n})"
     finally:
         ctx.close()
 

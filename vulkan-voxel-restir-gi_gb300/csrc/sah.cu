@@ -459,11 +459,6 @@ __global__ void k_noalloc_prep(const float *aabbs, const float *power, uint32_t 
 // that loads the library holds it until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[vrg::NOALLOC_BYTES];
 
-namespace {
-std::mutex g_noalloc_mu;
-void *g_noalloc_dev_ptr[256] = {};  // device address of the array, per device ordinal
-}  // namespace
-
 extern "C" VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const float *power, const uint32_t *ids,
                                                        uint32_t n, vrg_bvh_node *nodes, uint32_t *prim_order,
                                                        void *stream) {
@@ -478,71 +473,72 @@ extern "C" VRG_API vrg_status vrg_build_tl_bvh_noalloc(const float *aabbs, const
         return VRG_ERR_INVALID_ARGUMENT;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    int dev = 0;
-    VRG_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) return VRG_ERR_UNSUPPORTED;
-    // set-up, once per device with that device current: the device address of
-    // the array (its name in host code is only a host-side stand-in)
+    // The device address of the array in the context current now (its name in
+    // host code is only a host-side stand-in).  Looked up on every call, so a
+    // device reset or another current context never leaves a stale address;
+    // the lookup allocates nothing.
     void *base = nullptr;
     {
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_dev_ptr[dev]) {
-            void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
-                return VRG_ERR_CUDA;
-            }
-            g_noalloc_dev_ptr[dev] = p;
+        cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+        if (e != cudaSuccess || !base) {
+            set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
+            return VRG_ERR_CUDA;
         }
-        base = g_noalloc_dev_ptr[dev];
     }
-    uint8_t *B = (uint8_t *)base;
-    float4 *lo = (float4 *)(B + NOALLOC_OFF_LO), *hi = (float4 *)(B + NOALLOC_OFF_HI),
-           *cen = (float4 *)(B + NOALLOC_OFF_CEN);
-    Item *q0 = (Item *)(B + NOALLOC_OFF_Q0), *q1 = (Item *)(B + NOALLOC_OFF_Q1);
-    uint32_t *cnt = (uint32_t *)(B + NOALLOC_OFF_CNT);
-    SahTree *d_tree = (SahTree *)(B + NOALLOC_OFF_TREE);
-    uint32_t *arrive = (uint32_t *)(B + NOALLOC_OFF_ARRIVE);
-    uint32_t *leaf = (uint32_t *)(B + NOALLOC_OFF_LEAF);
-    const uint32_t n_nodes = 2 * n - 1;
-    // the array keeps the previous call's contents: reset what must start at zero
-    VRG_CUDA_TRY(cudaMemsetAsync(arrive, 0, (size_t)n_nodes * 4, s));
-    VRG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 256, s));
-    // tree descriptor and root work item: copies of host stack values
-    SahTree tree{n, 0, 0, 0};
-    Item root{0, 0, 1, 0, n, INVALID};
-    uint32_t one = 1;
-    VRG_CUDA_TRY(cudaMemcpyAsync(d_tree, &tree, sizeof(tree), cudaMemcpyHostToDevice, s));
-    VRG_CUDA_TRY(cudaMemcpyAsync(q0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
-    VRG_CUDA_TRY(cudaMemcpyAsync(cnt, &one, 4, cudaMemcpyHostToDevice, s));
-    k_noalloc_prep<<<(n + 255) / 256, 256, 0, s>>>(aabbs, power, n, lo, hi, cen);
-    VRG_CUDA_TRY(cudaGetLastError());
-    SahInputs in{lo, hi, cen, ids};
-    SahOutputs out{nodes, prim_order, leaf};
-    k_perm_init<<<dim3(std::max(1u, (n + 255) / 256), 1), 256, 0, s>>>(d_tree, prim_order);
-    VRG_CUDA_TRY(cudaGetLastError());
-    uint32_t n_cur = 1, cur_slot = 0, lv = 0;
-    Item *cur = q0, *nxt = q1;
-    while (n_cur > 0) {
-        uint32_t next_slot = cur_slot ^ 1u;
-        VRG_CUDA_TRY(cudaMemsetAsync(cnt + next_slot, 0, 4, s));
-        uint32_t blocks = std::min<uint32_t>((n_cur + SAH_WARPS - 1) / SAH_WARPS, 152u * 16u);
-        k_sah_level<<<blocks, SAH_WARPS * 32, 0, s>>>(d_tree, in, out, cur, cnt + cur_slot, nxt, cnt + next_slot);
+    // Everything from the first enqueue on: on an error return the stream is
+    // synchronized first, so no work that uses the shared array is still
+    // queued when the call returns.
+    auto build = [&]() -> vrg_status {
+        uint8_t *B = (uint8_t *)base;
+        float4 *lo = (float4 *)(B + NOALLOC_OFF_LO), *hi = (float4 *)(B + NOALLOC_OFF_HI),
+               *cen = (float4 *)(B + NOALLOC_OFF_CEN);
+        Item *q0 = (Item *)(B + NOALLOC_OFF_Q0), *q1 = (Item *)(B + NOALLOC_OFF_Q1);
+        uint32_t *cnt = (uint32_t *)(B + NOALLOC_OFF_CNT);
+        SahTree *d_tree = (SahTree *)(B + NOALLOC_OFF_TREE);
+        uint32_t *arrive = (uint32_t *)(B + NOALLOC_OFF_ARRIVE);
+        uint32_t *leaf = (uint32_t *)(B + NOALLOC_OFF_LEAF);
+        const uint32_t n_nodes = 2 * n - 1;
+        // the array keeps the previous call's contents: reset what must start at zero
+        VRG_CUDA_TRY(cudaMemsetAsync(arrive, 0, (size_t)n_nodes * 4, s));
+        VRG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 256, s));
+        // tree descriptor and root work item: copies of host stack values
+        SahTree tree{n, 0, 0, 0};
+        Item root{0, 0, 1, 0, n, INVALID};
+        uint32_t one = 1;
+        VRG_CUDA_TRY(cudaMemcpyAsync(d_tree, &tree, sizeof(tree), cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(q0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+        VRG_CUDA_TRY(cudaMemcpyAsync(cnt, &one, 4, cudaMemcpyHostToDevice, s));
+        k_noalloc_prep<<<(n + 255) / 256, 256, 0, s>>>(aabbs, power, n, lo, hi, cen);
         VRG_CUDA_TRY(cudaGetLastError());
-        uint32_t h_next = 0;
-        VRG_CUDA_TRY(cudaMemcpyAsync(&h_next, cnt + next_slot, 4, cudaMemcpyDeviceToHost, s));
-        VRG_CUDA_TRY(cudaStreamSynchronize(s));
-        n_cur = h_next;
-        std::swap(cur, nxt);
-        cur_slot = next_slot;
-        if (++lv > 4 * NOALLOC_MAX_PRIMS) {
-            set_error("vrg_build_tl_bvh_noalloc: level loop did not terminate");
-            return VRG_ERR_STATE;
+        SahInputs in{lo, hi, cen, ids};
+        SahOutputs out{nodes, prim_order, leaf};
+        k_perm_init<<<dim3(std::max(1u, (n + 255) / 256), 1), 256, 0, s>>>(d_tree, prim_order);
+        VRG_CUDA_TRY(cudaGetLastError());
+        uint32_t n_cur = 1, cur_slot = 0, lv = 0;
+        Item *cur = q0, *nxt = q1;
+        while (n_cur > 0) {
+            uint32_t next_slot = cur_slot ^ 1u;
+            VRG_CUDA_TRY(cudaMemsetAsync(cnt + next_slot, 0, 4, s));
+            uint32_t blocks = std::min<uint32_t>((n_cur + SAH_WARPS - 1) / SAH_WARPS, 152u * 16u);
+            k_sah_level<<<blocks, SAH_WARPS * 32, 0, s>>>(d_tree, in, out, cur, cnt + cur_slot, nxt, cnt + next_slot);
+            VRG_CUDA_TRY(cudaGetLastError());
+            uint32_t h_next = 0;
+            VRG_CUDA_TRY(cudaMemcpyAsync(&h_next, cnt + next_slot, 4, cudaMemcpyDeviceToHost, s));
+            VRG_CUDA_TRY(cudaStreamSynchronize(s));
+            n_cur = h_next;
+            std::swap(cur, nxt);
+            cur_slot = next_slot;
+            if (++lv > 4 * NOALLOC_MAX_PRIMS) {
+                set_error("vrg_build_tl_bvh_noalloc: level loop did not terminate");
+                return VRG_ERR_STATE;
+            }
         }
-    }
-    k_power_up<<<dim3(std::max(1u, (n_nodes + 255) / 256), 1), 256, 0, s>>>(d_tree, nodes, arrive);
-    VRG_CUDA_TRY(cudaGetLastError());
-    VRG_CUDA_TRY(cudaStreamSynchronize(s));
-    return VRG_OK;
+        k_power_up<<<dim3(std::max(1u, (n_nodes + 255) / 256), 1), 256, 0, s>>>(d_tree, nodes, arrive);
+        VRG_CUDA_TRY(cudaGetLastError());
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        return VRG_OK;
+    };
+    const vrg_status st = build();
+    if (st != VRG_OK) (void)cudaStreamSynchronize(s);
+    return st;
 }

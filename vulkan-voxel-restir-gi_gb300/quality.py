@@ -162,6 +162,27 @@ def equal_time_study(ctx, scene, renderer, cam, gt, scene_min, scene_max, frames
                       "gain": round(plain_acc[k] / rel_m, 3),
                       "gain_lower_bound": round(out["plain"]["relmse_1spp"] / n_eq / rel_m, 3)}
     out["equal_time"] = eq
+    # What the trained network adds under ReSTIR: ReSTIR over cache-terminated
+    # paths against ReSTIR over plain 3-bounce paths given at least the same
+    # device time (the mean of ceil(t_restir_cache / t_restir) consecutive
+    # ReSTIR frames; consecutive frames share reservoirs, so this is what
+    # ReSTIR reaches in that time, not an independent-sample bound).
+    vs = {}
+    for key, t_rc, t_r in (("frames_one_at_a_time", out["restir_cache"]["ms_per_frame"], out["restir"]["ms_per_frame"]),
+                           ("frames_in_flight", out["restir_cache"].get("ms_per_frame_in_flight"),
+                            out["restir"].get("ms_per_frame_in_flight"))):
+        if not t_rc or not t_r:
+            continue
+        k = max(1, int(math.ceil(t_rc / t_r - 1e-9)))
+        if ("restir", k) not in plain_acc:
+            acc_img, _, _ = run_method(renderer, scene, cam, "restir", k, seed0=6000, warmup=2)
+            plain_acc[("restir", k)] = relmse(acc_img, gt)
+        rel_m = max(out["restir_cache"]["relmse_1spp"], 1e-12)
+        vs[key] = {"restir_frames": k, "restir_time_ratio": round(k * t_r / t_rc, 3),
+                   "relmse_restir": round(plain_acc[("restir", k)], 6),
+                   "relmse_restir_cache_1spp": out["restir_cache"]["relmse_1spp"],
+                   "gain": round(plain_acc[("restir", k)] / rel_m, 3)}
+    out["restir_cache_vs_restir"] = vs
     # the same comparison with every method timed in flight
     t_plain_f = out["plain"].get("ms_per_frame_in_flight")
     if t_plain_f:

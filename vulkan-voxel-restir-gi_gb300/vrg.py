@@ -150,6 +150,7 @@ SIGNATURES = [
     ("vrg_renderer_read_accumulation", C.c_int32, [_P, _P, C.POINTER(C.c_uint32)]),
     ("vrg_debug_readback", C.c_int32, [_P, C.c_uint32, _P, C.c_uint64]),
     ("vrg_build_tl_bvh_batched", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("vrg_measure_l2_bandwidth", C.c_int32, [_P, C.c_uint64, C.c_uint32, C.POINTER(C.c_float)]),
     ("vrg_build_bl_bvh_batched", C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("vrg_terrain_materials", C.c_int32, [C.c_uint64, C.POINTER(Material), C.c_uint32, C.POINTER(C.c_uint32)]),
     ("vrg_terrain_generate", C.c_int32, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P]),
@@ -308,6 +309,12 @@ class Context:
         n, maps, h, w, c = rgba.shape
         assert maps == 3 and c == 4
         check(self.lib.vrg_texture_atlas_set(self.h, _ptr(rgba), n, w, h), "vrg_texture_atlas_set")
+
+    def l2_read_gbs(self, mib=32, reps=64):
+        """The device's L2 read bandwidth in GB/s (vrg_measure_l2_bandwidth)."""
+        g = C.c_float()
+        check(self.lib.vrg_measure_l2_bandwidth(self.h, mib << 20, reps, C.byref(g)), "vrg_measure_l2_bandwidth")
+        return float(g.value)
 
     def flush(self):
         check(self.lib.vrg_flush_uploads(self.h), "vrg_flush_uploads")
