@@ -87,6 +87,16 @@ typedef struct vrg_material {
     uint32_t reserved[2];
 } vrg_material;
 
+/* One vertex of an uploaded triangle mesh, the reference's Vertex3D
+ * (vertex.rs:4-14, 24 bytes): position, texture index t (a material-table
+ * slot; a triangle's slot is its first vertex's t, raytrace.rs:455 and
+ * scene.rs:559) and texture coordinate (interpolated for the atlas). */
+typedef struct vrg_vertex3d {
+    float position[3];
+    uint32_t t;
+    float uv[2];
+} vrg_vertex3d;
+
 typedef struct vrg_context_desc {
     int32_t device;          /* CUDA device ordinal */
     uint32_t flags;          /* reserved, 0 */
@@ -228,6 +238,15 @@ VRG_API vrg_status vrg_texture_atlas_set(vrg_context *ctx, const uint8_t *rgba8,
  * reference's SceneUploadedObjectHandle::Empty).  Thread-safe. */
 VRG_API vrg_status vrg_upload_chunk(vrg_context *ctx, const uint8_t *blocks,
                                     const uint8_t *const neighbours[6], vrg_object **out);
+/* SceneUploader::upload_object (scene.rs:547-725) for arbitrary triangles:
+ * nverts vertices, three per triangle (a multiple of 3, as the reference
+ * asserts).  A triangle is a light iff the luminance of its slot is > 0; its
+ * power is luminance * area (scene.rs:555-571).  Before the call returns,
+ * the GPU builds the light BLAS over the light triangles (build_bl_bvh, leaf
+ * prim ids = triangle indices) and a geometry BVH over all triangles (the
+ * same builder) that replaces the driver BLAS.  nverts == 0 yields an empty
+ * object.  Every t must be a slot of the material table.  Thread-safe. */
+VRG_API vrg_status vrg_upload_mesh(vrg_context *ctx, const vrg_vertex3d *v, uint64_t nverts, vrg_object **out);
 /* Runs every pending upload now (one batched launch sequence). */
 VRG_API vrg_status vrg_flush_uploads(vrg_context *ctx);
 VRG_API vrg_status vrg_object_release(vrg_object *obj);
@@ -245,8 +264,13 @@ VRG_API vrg_status vrg_object_read_bvh(vrg_object *obj, uint32_t which /*0 light
 /* ---- scene (Scene, scene.rs:86-497) ----------------------------------- */
 VRG_API vrg_status vrg_scene_create(vrg_context *ctx, vrg_scene **out);
 VRG_API vrg_status vrg_scene_destroy(vrg_scene *scene);
-/* xform3x4 is row-major [R|t]; only identity rotation is supported (chunks
- * are translated, chunk_manager.rs:234-248). */
+/* xform3x4 is the instance transform as a row-major 3x4 matrix [R|t] (the
+ * matrix of the reference's Isometry3, InstanceData.transform, scene.rs:407-416;
+ * NULL = identity).  Mesh objects take any finite matrix (the reference passes
+ * isometries, e.g. its ego cube, main.rs:86-101, scene_manager.rs:23-35).
+ * Chunk objects take identity R and an integral translation within +-16384
+ * (the reference only translates chunks, chunk_manager.rs:234-248);
+ * anything else returns VRG_ERR_UNSUPPORTED. */
 VRG_API vrg_status vrg_scene_add(vrg_scene *scene, uint64_t key, vrg_object *obj, const float xform3x4[12]);
 VRG_API vrg_status vrg_scene_update(vrg_scene *scene, uint64_t key, const float xform3x4[12]);
 VRG_API vrg_status vrg_scene_remove(vrg_scene *scene, uint64_t key);

@@ -30,6 +30,7 @@ def lib():
             ("orc_build_tl_bvh", C.c_int, [C.c_uint32, _P, _P, _P, _P, _P, _P]),
             ("orc_build_bl_bvh", C.c_int, [C.c_uint32, _P, _P, _P, _P, _P, _P, _P]),
             ("orc_sincos_turns", None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            ("orc_tri_test", C.c_int, [_P, _P, _P, C.c_float, C.c_float, _P]),
             ("orc_mm_combine", C.c_uint32, [C.c_uint32, C.c_uint32]),
             ("orc_mm_rand", C.c_float, [C.c_uint32]),
             ("orc_world_create", _P, [C.POINTER(vrg.Material), C.c_uint32]),
@@ -39,6 +40,8 @@ def lib():
             ("orc_chunk_info", None, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             ("orc_chunk_read_bvh", C.c_int, [_P, C.c_uint32, _P, _P]),
             ("orc_world_add", None, [_P, C.c_uint64, _P, C.c_float, C.c_float, C.c_float]),
+            ("orc_world_add_xform", None, [_P, C.c_uint64, _P, _P]),
+            ("orc_mesh_build", _P, [_P, _P, C.c_uint64]),
             ("orc_world_remove", None, [_P, C.c_uint64]),
             ("orc_world_commit", None, [_P]),
             ("orc_world_read_tl", C.c_uint32, [_P, C.c_uint32, _P, C.c_uint32]),
@@ -105,6 +108,17 @@ def build_tl_bvh(aabbs, power, ids, translations=None):
     return nodes, order
 
 
+def tri_test(tri9, o, d, tmin=1e-3, tmax=1000.0):
+    """The oracle's watertight ray/triangle test: (t, b1, b2) or None."""
+    t = np.ascontiguousarray(tri9, np.float32).reshape(9)
+    oo = np.ascontiguousarray(o, np.float32).reshape(3)
+    dd = np.ascontiguousarray(d, np.float32).reshape(3)
+    out = np.zeros(3, np.float32)
+    if lib().orc_tri_test(_p(t), _p(oo), _p(dd), tmin, tmax, _p(out)):
+        return tuple(out)
+    return None
+
+
 def build_bl_bvh(tris, lum, ids):
     """build_bl_bvh (build.rs:249-372). tris (n,9) float32."""
     tris = np.ascontiguousarray(tris, np.float32)
@@ -140,6 +154,16 @@ class World:
         arr = (C.c_void_p * 6)(*[None if x is None else x.ctypes.data for x in keep])
         c = lib().orc_chunk_build(self.h, _p(blocks), arr)
         lib().orc_world_add(self.h, key, c, *[float(t) for t in translation])
+        self.chunks[key] = c
+        return c
+
+    def add_mesh(self, key, vertexes, transform):
+        """upload_object of a triangle mesh, added with a 3x4 / 4x4 transform (or a translation)."""
+        v = vrg.as_vertices(vertexes)
+        c = lib().orc_mesh_build(self.h, _p(v) if len(v) else None, len(v))
+        assert c, "oracle mesh build failed"
+        m = np.ascontiguousarray(np.frombuffer(bytes(vrg._xform(transform)), np.float32))
+        lib().orc_world_add_xform(self.h, key, c, _p(m))
         self.chunks[key] = c
         return c
 

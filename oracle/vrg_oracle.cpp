@@ -18,8 +18,18 @@
 //     restated as an exact closed-rectangle test against each exposed voxel
 //     face (padded by 2^-12 so neighbouring faces overlap and no ray leaks
 //     through an edge), the triangle half chosen by the face diagonal, ties
-//     on t broken by the smaller (instance, triangle) key.  Light any-hit
-//     sums are added in ascending (instance, BVH leaf) order.
+//     on t broken by the smaller (instance, triangle) key.  Triangles of
+//     uploaded meshes are tested in world space (the instance transform
+//     applied to their vertices, raytrace.rs:155-159) by the watertight
+//     ray/triangle test of Woop, Benthin and Wald (JCGT 2(1), 2013), with
+//     the same tie rule.  Light any-hit sums are added in ascending
+//     (instance, BVH leaf) order.
+//   * nalgebra's isometry arithmetic (crate 0.34.1, not available): the
+//     instance transform is the row-major 3x4 matrix [R|t] of the C ABI,
+//     applied as ((r0*x + r1*y) + r2*z) + t (the mat4x3 * vec4(p, 1) of the
+//     shaders, raytrace.rs:155-159,184-185); an identity R takes the exact
+//     translation p + t.  Aabb::transform (aabb.rs:75-92) applies that to
+//     the 8 corners.
 //   * GLSL built-ins with implementation-defined precision: dot/cross/length
 //     evaluated left to right, normalize(v) = v / length(v) per component,
 //     sin/cos(2*pi*u) from the quarter-turn reduction + Taylor polynomials
@@ -184,6 +194,29 @@ static inline OAabb aabb_translate(const OAabb &a, const float t[3]) {
     for (int i = 0; i < 3; i++) { lo[i] = a.mn[i] + t[i]; hi[i] = a.mx[i] + t[i]; }
     for (int k = 0; k < 8; k++)
         c[k] = v3((k & 4) ? hi[0] : lo[0], (k & 2) ? hi[1] : lo[1], (k & 1) ? hi[2] : lo[2]);
+    return aabb_from_points(c, 8);
+}
+
+// Instance transform: row-major 3x4 [R|t].  tonly: R is exactly the
+// identity, and points move by the exact translation p + t.
+struct OXform {
+    float m[12];
+    bool tonly;
+};
+static const OXform XF_IDENTITY = {{1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, true};
+static inline V3 xf_point(const OXform &X, V3 p) {
+    if (X.tonly) return v3(p.x + X.m[3], p.y + X.m[7], p.z + X.m[11]);
+    return v3(((X.m[0] * p.x + X.m[1] * p.y) + X.m[2] * p.z) + X.m[3],
+              ((X.m[4] * p.x + X.m[5] * p.y) + X.m[6] * p.z) + X.m[7],
+              ((X.m[8] * p.x + X.m[9] * p.y) + X.m[10] * p.z) + X.m[11]);
+}
+// Aabb::transform (aabb.rs:75-92): the AABB of the 8 transformed corners, in
+// the reference's corner order
+static inline OAabb aabb_transform(const OAabb &a, const OXform &X) {
+    if (a.empty) return a;
+    V3 c[8];
+    for (int k = 0; k < 8; k++)
+        c[k] = xf_point(X, v3((k & 4) ? a.mx[0] : a.mn[0], (k & 2) ? a.mx[1] : a.mn[1], (k & 1) ? a.mx[2] : a.mn[2]));
     return aabb_from_points(c, 8);
 }
 
@@ -465,11 +498,17 @@ struct OChunk {
     std::vector<uint32_t> light_order;
     OAabb light_aabb;
     float light_power = 0.0f;
-    // geometry BLAS over per-block AABBs (build_tl_bvh semantics)
+    // geometry BLAS over per-block AABBs (build_tl_bvh semantics); for a
+    // mesh, over its triangles (build_bl_bvh inputs, leaf prim = triangle)
     uint32_t n_geo = 0;
     std::vector<vrg_bvh_node> geo_nodes;
     std::vector<uint32_t> geo_order;
     OAabb geo_aabb;
+    // an uploaded triangle mesh (upload_object, scene.rs:547-725) instead of a chunk
+    bool mesh = false;
+    std::vector<V3> mpos;          // 3 per triangle, object space
+    std::vector<uint32_t> mslot;   // per triangle: its first vertex's t
+    std::vector<float> muv;        // 6 per triangle
 };
 
 struct OMaterials {
@@ -575,18 +614,76 @@ static void build_chunk(OChunk &ch, const OMaterials &M, const uint8_t *const nb
     }
 }
 
+// upload_object (scene.rs:547-725) of arbitrary triangles: the light BLAS over
+// triangles whose slot luminance is > 0 (power = luminance * area, leaf prim
+// id = triangle index), and the geometry BVH over all triangles
+static bool build_mesh(OChunk &ch, const OMaterials &M, const vrg_vertex3d *v, uint64_t nverts) {
+    if (nverts % 3) return false;
+    const uint32_t n = (uint32_t)(nverts / 3);
+    ch.mesh = true;
+    ch.n_tris = n;
+    ch.mpos.resize(3 * (size_t)n);
+    ch.mslot.resize(n);
+    ch.muv.resize(6 * (size_t)n);
+    std::vector<float> lum;
+    std::vector<V3> ltri;
+    std::vector<uint32_t> lids;
+    for (uint32_t i = 0; i < n; i++) {
+        for (int j = 0; j < 3; j++) {
+            const vrg_vertex3d &x = v[3 * (size_t)i + j];
+            ch.mpos[3 * (size_t)i + j] = v3(x.position[0], x.position[1], x.position[2]);
+            ch.muv[6 * (size_t)i + 2 * j] = x.uv[0];
+            ch.muv[6 * (size_t)i + 2 * j + 1] = x.uv[1];
+        }
+        const uint32_t t = v[3 * (size_t)i].t;
+        if (t >= M.mats.size()) return false;
+        ch.mslot[i] = t;
+        const float L = M.mats[t].luminance;
+        if (L > 0.0f) {
+            const V3 a = ch.mpos[3 * (size_t)i], b = ch.mpos[3 * (size_t)i + 1], c = ch.mpos[3 * (size_t)i + 2];
+            const float area = length3(cross3(b - a, c - a)) / 2.0f;
+            ltri.push_back(a);
+            ltri.push_back(b);
+            ltri.push_back(c);
+            lum.push_back(L * area);
+            lids.push_back(i);
+        }
+    }
+    ch.n_light = (uint32_t)lum.size();
+    if (ch.n_light) {
+        build_bl(ch.n_light, lum.data(), ltri.data(), lids.data(), ch.light_nodes, ch.light_order, &ch.light_aabb,
+                 &ch.light_power);
+    } else {
+        ch.light_aabb = aabb_empty();
+        ch.light_power = 0.0f;
+    }
+    ch.n_geo = n;
+    if (n) {
+        std::vector<float> zero(n, 0.0f);
+        std::vector<uint32_t> ids(n);
+        for (uint32_t i = 0; i < n; i++) ids[i] = i;
+        float pw;
+        build_bl(n, zero.data(), ch.mpos.data(), ids.data(), ch.geo_nodes, ch.geo_order, &ch.geo_aabb, &pw);
+    } else {
+        ch.geo_aabb = aabb_empty();
+    }
+    return true;
+}
+
 // ------------------------------------------------------------------------
 // world (Scene, scene.rs:86-497)
 // ------------------------------------------------------------------------
 struct OInstance {
     const OChunk *ch;
-    float off[3];
+    float off[3];        // the translation (chunks: their whole transform)
+    OXform X;            // the instance transform
+    std::vector<V3> wpos;  // mesh: world-space vertices, 3 per triangle
     uint32_t light_bvh_tl_idx;
 };
 
 struct OWorld {
     OMaterials M;
-    std::map<uint64_t, std::pair<std::shared_ptr<OChunk>, std::array<float, 3>>> objects;
+    std::map<uint64_t, std::pair<std::shared_ptr<OChunk>, OXform>> objects;
     std::vector<OInstance> inst;
     std::vector<vrg_bvh_node> light_tl;   // light TL BVH (scene.rs:248-279)
     std::vector<vrg_bvh_node> geo_tl;     // geometry TL BVH over chunks
@@ -599,10 +696,29 @@ static void world_commit(OWorld &W) {
         if (kv.second.first->n_tris == 0) continue;  // SceneUploadedObjectHandle::Empty
         OInstance in;
         in.ch = kv.second.first.get();
-        for (int i = 0; i < 3; i++) in.off[i] = kv.second.second[i];
+        in.X = kv.second.second;
+        in.off[0] = in.X.m[3];
+        in.off[1] = in.X.m[7];
+        in.off[2] = in.X.m[11];
+        if (in.ch->mesh) {  // triangleTransform (raytrace.rs:155-159) of every triangle
+            in.wpos.resize(in.ch->mpos.size());
+            for (size_t k = 0; k < in.ch->mpos.size(); k++) in.wpos[k] = xf_point(in.X, in.ch->mpos[k]);
+        }
         in.light_bvh_tl_idx = 0;
-        W.inst.push_back(in);
+        W.inst.push_back(std::move(in));
     }
+    // An instance's top-level prim: its root AABB moved by its transform
+    // (Aabb::transform, build.rs:391-395); a translation goes to build_tl as
+    // such, any other transform is applied here and build_tl gets 0.
+    auto tl_prim = [](const OInstance &I, const OAabb &a, std::vector<float> &tr, std::vector<OAabb> &ab) {
+        if (I.X.tonly) {
+            for (int k = 0; k < 3; k++) tr.push_back(I.off[k]);
+            ab.push_back(a);
+        } else {
+            for (int k = 0; k < 3; k++) tr.push_back(0.0f);
+            ab.push_back(aabb_transform(a, I.X));
+        }
+    };
     // light TL (scene.rs:248-287)
     std::vector<float> tr, pw;
     std::vector<OAabb> ab;
@@ -610,8 +726,7 @@ static void world_commit(OWorld &W) {
     for (uint32_t i = 0; i < W.inst.size(); i++) {
         const OChunk *c = W.inst[i].ch;
         if (c->light_aabb.empty) continue;
-        for (int k = 0; k < 3; k++) tr.push_back(W.inst[i].off[k]);
-        ab.push_back(c->light_aabb);
+        tl_prim(W.inst[i], c->light_aabb, tr, ab);
         pw.push_back(c->light_power);
         ids.push_back(i);
     }
@@ -633,8 +748,7 @@ static void world_commit(OWorld &W) {
     for (uint32_t i = 0; i < W.inst.size(); i++) {
         const OChunk *c = W.inst[i].ch;
         if (c->n_geo == 0) continue;
-        for (int k = 0; k < 3; k++) tr.push_back(W.inst[i].off[k]);
-        ab.push_back(c->geo_aabb);
+        tl_prim(W.inst[i], c->geo_aabb, tr, ab);
         pw.push_back(0.0f);
         ids.push_back(i);
     }
@@ -687,6 +801,46 @@ static bool face_test(int bx, int by, int bz, int f, V3 o, V3 d, V3 inv, float t
     return true;
 }
 
+// Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2(1), 2013), both
+// faces: the ray's dominant axis kz (the largest |d| component, the first on
+// ties), the shear S, edge functions U, V, W of the sheared vertices (each
+// recomputed in double when it is exactly 0), a hit iff they do not differ in
+// sign and det = U + V + W != 0, t = T / det in [tmin, tmax]; barycentrics of
+// v1, v2 are V / det, W / det.
+struct TriHit {
+    float t, b1, b2;
+};
+static bool tri_test(V3 v0, V3 v1, V3 v2, V3 o, V3 d, float tmin, float tmax, TriHit *h) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > (kz == 0 ? ax : ay)) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1, ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (comp(d, kz) < 0.0f) std::swap(kx, ky);
+    const float Sx = comp(d, kx) / comp(d, kz), Sy = comp(d, ky) / comp(d, kz), Sz = 1.0f / comp(d, kz);
+    const V3 A = v0 - o, B = v1 - o, C = v2 - o;
+    const float Ax = comp(A, kx) - Sx * comp(A, kz), Ay = comp(A, ky) - Sy * comp(A, kz);
+    const float Bx = comp(B, kx) - Sx * comp(B, kz), By = comp(B, ky) - Sy * comp(B, kz);
+    const float Cx = comp(C, kx) - Sx * comp(C, kz), Cy = comp(C, ky) - Sy * comp(C, kz);
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    const float Az = Sz * comp(A, kz), Bz = Sz * comp(B, kz), Cz = Sz * comp(C, kz);
+    const float T = (U * Az + V * Bz) + W * Cz;
+    const float t = T / det;
+    if (!(t >= tmin && t <= tmax)) return false;
+    h->t = t;
+    h->b1 = V / det;
+    h->b2 = W / det;
+    return true;
+}
+
 static inline bool box_test(const float mn[3], const float mx[3], const float off[3], V3 o, V3 inv,
                             float tmin, float tmax) {
     float tn = tmin, tf = tmax;
@@ -732,6 +886,28 @@ static OHit closest_hit(const OWorld &W, V3 o, V3 d, float tmin, float tmax) {
         uint32_t ii = n.right_node_idx_or_prim_idx;
         const OInstance &I = W.inst[ii];
         const OChunk &C = *I.ch;
+        if (C.mesh) {  // every triangle, in world space
+            for (uint32_t tri = 0; tri < C.n_tris; tri++) {
+                TriHit th;
+                if (!tri_test(I.wpos[3 * tri], I.wpos[3 * tri + 1], I.wpos[3 * tri + 2], o, d, tmin, best.t, &th))
+                    continue;
+                uint64_t key = ((uint64_t)ii << 32) | tri;
+                if (th.t < best.t || (th.t == best.t && key < best_key)) {
+                    best.hit = true;
+                    best.t = th.t;
+                    best_key = key;
+                    best.inst = ii;
+                    best.tri = tri;
+                    best.block = 0xFFFFFFFFu;
+                    best.face = 0;
+                    best.half = 0;
+                    best.b1 = th.b1;
+                    best.b2 = th.b2;
+                    best.bx = best.by = best.bz = 0;
+                }
+            }
+            continue;
+        }
         std::vector<uint32_t> st{0};
         while (!st.empty()) {
             uint32_t bi = st.back();
@@ -780,6 +956,12 @@ static OHit closest_hit(const OWorld &W, V3 o, V3 d, float tmin, float tmax) {
 static void tri_vertices(const OWorld &W, uint32_t ii, uint32_t tri, V3 out[3], int *face, int *half) {
     const OInstance &I = W.inst[ii];
     const OChunk &C = *I.ch;
+    if (C.mesh) {
+        for (int j = 0; j < 3; j++) out[j] = I.wpos[3 * (size_t)tri + j];
+        if (face) *face = -1;
+        if (half) *half = 0;
+        return;
+    }
     uint32_t blk = C.tri_block[tri];
     int f = C.tri_fh[tri] & 15, h = C.tri_fh[tri] >> 4;
     int lx = (int)(blk >> 10), ly = (int)((blk >> 5) & 31), lz = (int)(blk & 31);
@@ -795,11 +977,11 @@ static void tri_vertices(const OWorld &W, uint32_t ii, uint32_t tri, V3 out[3], 
 // light BVH: importance, stochastic descent, reverse walk, nee pdf
 // ------------------------------------------------------------------------
 // raytrace.rs:174-208 (uint visibility, EPS 1e-3) and nee_pdf.rs:119-152
-// (float visibility, EPS 1e-4); the instance transform is a translation.
-static float node_importance(bool nee_variant, V3 point, V3 normal, const float off[3],
-                             const vrg_bvh_node &node) {
-    V3 v000 = v3(node.min[0] + off[0], node.min[1] + off[1], node.min[2] + off[2]);
-    V3 v111 = v3(node.max[0] + off[0], node.max[1] + off[1], node.max[2] + off[2]);
+// (float visibility, EPS 1e-4): the corners are the axis-aligned box spanned
+// by the transformed min and max (not the transformed box).
+static float node_importance(bool nee_variant, V3 point, V3 normal, const OXform &X, const vrg_bvh_node &node) {
+    V3 v000 = xf_point(X, v3(node.min[0], node.min[1], node.min[2]));
+    V3 v111 = xf_point(X, v3(node.max[0], node.max[1], node.max[2]));
     V3 c[8] = {v000, v3(v000.x, v000.y, v111.z), v3(v000.x, v111.y, v000.z), v3(v000.x, v111.y, v111.z),
                v3(v111.x, v000.y, v000.z), v3(v111.x, v000.y, v111.z), v3(v111.x, v111.y, v000.z), v111};
     float dist_sq = fmaxf(dot3(v111 - v000, v111 - v000),
@@ -830,7 +1012,7 @@ static TraverseResult traverse_bvh(const OWorld &W, V3 point, V3 normal, uint32_
         return R;
     }
     float probability = 1.0f, importance = 0.0f;
-    const float *off = ZERO3;
+    const OXform *X = &XF_IDENTITY;  // mat4x3(1.0) at the top level
     uint32_t inst = 0xFFFFFFFFu;
     uint32_t node_idx = 0;
     bool top = true;
@@ -838,12 +1020,12 @@ static TraverseResult traverse_bvh(const OWorld &W, V3 point, V3 normal, uint32_
         if (top && node->left_node_idx == 0xFFFFFFFFu) {
             inst = node->right_node_idx_or_prim_idx;
             const OInstance &I = W.inst[inst];
-            off = I.off;
+            X = &I.X;
             top = false;
             root = I.ch->light_nodes.data();
             node = &root[0];
             node_idx = 0;
-            if (importance == 0.0f) importance = node_importance(false, point, normal, off, *node);
+            if (importance == 0.0f) importance = node_importance(false, point, normal, *X, *node);
         }
         if (!top && node->left_node_idx == 0xFFFFFFFFu) {
             R.success = true; R.inst = inst; R.prim = node->right_node_idx_or_prim_idx; R.leaf = node_idx;
@@ -853,8 +1035,8 @@ static TraverseResult traverse_bvh(const OWorld &W, V3 point, V3 normal, uint32_
         uint32_t li = node->left_node_idx, ri = node->right_node_idx_or_prim_idx;
         const vrg_bvh_node &left = root[li];
         const vrg_bvh_node &right = root[ri];
-        float lI = node_importance(false, point, normal, off, left);
-        float rI = node_importance(false, point, normal, off, right);
+        float lI = node_importance(false, point, normal, *X, left);
+        float rI = node_importance(false, point, normal, *X, right);
         float tot = lI + rI;
         float ln = lI / tot, rn = rI / tot;
         if (mm_rand(seed) < ln) { node = &left; node_idx = li; probability *= ln; importance = lI; }
@@ -868,7 +1050,7 @@ static float reverse_traverse(const OWorld &W, V3 point, V3 normal, uint32_t ii,
     const OInstance &I = W.inst[ii];
     const vrg_bvh_node *root = I.ch->light_nodes.data();
     float probability = 1.0f;
-    const float *off = I.off;
+    const OXform *X = &I.X;
     bool top = false;
     const vrg_bvh_node *node = &root[leaf];
     uint32_t node_idx = leaf;
@@ -883,15 +1065,15 @@ static float reverse_traverse(const OWorld &W, V3 point, V3 normal, uint32_t ii,
             if (tl_leaf.parent_idx == 0xFFFFFFFFu) return probability;
             node_idx = tl_leaf.parent_idx;
             node = &root[node_idx];
-            off = ZERO3;
+            X = &XF_IDENTITY;
         } else {
             node_idx = node->parent_idx;
             node = &root[node_idx];
         }
         const vrg_bvh_node &left = root[node->left_node_idx];
         const vrg_bvh_node &right = root[node->right_node_idx_or_prim_idx];
-        float lI = node_importance(true, point, normal, off, left);
-        float rI = node_importance(true, point, normal, off, right);
+        float lI = node_importance(true, point, normal, *X, left);
+        float rI = node_importance(true, point, normal, *X, right);
         float tot = lI + rI;
         float ln = lI / tot, rn = rI / tot;
         if (old == node->left_node_idx) probability *= ln;
@@ -942,6 +1124,21 @@ static float nee_pdf_any_hit(const OWorld &W, V3 o, V3 d, V3 normal) {
         uint32_t ii = n.right_node_idx_or_prim_idx;
         const OInstance &I = W.inst[ii];
         const OChunk &C = *I.ch;
+        if (C.mesh) {  // every light triangle (light BLAS leaf), in world space
+            for (uint32_t bi = 0; bi < C.light_nodes.size(); bi++) {
+                const vrg_bvh_node &b = C.light_nodes[bi];
+                if (b.left_node_idx != 0xFFFFFFFFu) continue;
+                const uint32_t tri = b.right_node_idx_or_prim_idx;
+                TriHit th;
+                if (!tri_test(I.wpos[3 * tri], I.wpos[3 * tri + 1], I.wpos[3 * tri + 2], o, d, tmin, tmax, &th))
+                    continue;
+                LightHit lh;
+                lh.key = ((uint64_t)ii << 32) | bi;
+                lh.value = compute_nee_pdf(W, o, normal, d, ii, bi, th.b1, th.b2);
+                hits.push_back(lh);
+            }
+            continue;
+        }
         std::vector<uint32_t> st{0};
         while (!st.empty()) {
             uint32_t bi = st.back();
@@ -1116,8 +1313,10 @@ static void render_frame(ORenderer &R, const OWorld &W, const vrg_camera &cam, c
             V3 tan = v01;
             V3 bit = cross3(nrm, tan);
             V3 n = normalize3(nrm), tg = normalize3(tan), bt = normalize3(bit);
-            uint8_t blk = W.inst[info.inst].ch->blocks[info.block];
-            const uint32_t slot = 6u * blk + (uint32_t)info.face;
+            const OChunk &HC = *W.inst[info.inst].ch;
+            // texture index: a mesh triangle's first vertex's t (raytrace.rs:455); a
+            // chunk face's 6 * block + face (block.rs:116-119)
+            const uint32_t slot = HC.mesh ? HC.mslot[info.tri] : 6u * HC.blocks[info.block] + (uint32_t)info.face;
             const vrg_material &m = W.M.mats[slot];
             V3 new_origin = (tri[0] * b0 + tri[1] * info.b1) + tri[2] * info.b2;
             V3 new_dir;
@@ -1129,7 +1328,8 @@ static void render_frame(ORenderer &R, const OWorld &W, const vrg_camera &cam, c
             if (!W.M.atlas.empty()) {
                 // raytrace.rs:457-480: uv = v0.uv*b0 + v1.uv*b1 + v2.uv*b2; texture()
                 // with the default sampler taken as nearest, clamp to edge
-                const float(*uv)[2] = FACE_UV[info.face][info.half];
+                const float(*uv)[2] = HC.mesh ? reinterpret_cast<const float(*)[2]>(&HC.muv[6 * (size_t)info.tri])
+                                              : FACE_UV[info.face][info.half];
                 const float u = ((uv[0][0] * b0) + (uv[1][0] * info.b1)) + (uv[2][0] * info.b2);
                 const float vv = ((uv[0][1] * b0) + (uv[1][1] * info.b1)) + (uv[2][1] * info.b2);
                 const int aw = (int)W.M.atlas_w, ah = (int)W.M.atlas_h;
@@ -1389,6 +1589,17 @@ ORC_API int orc_build_bl_bvh(uint32_t n, const float *lum, const float *tris, co
 }
 
 ORC_API void orc_sincos_turns(float x, float *s, float *c) { sincos_turns(x, s, c); }
+// the watertight ray/triangle test: 1 and (t, b1, b2) on a hit, else 0
+ORC_API int orc_tri_test(const float *v9, const float *o3, const float *d3, float tmin, float tmax, float *out3) {
+    TriHit h;
+    if (!tri_test(v3(v9[0], v9[1], v9[2]), v3(v9[3], v9[4], v9[5]), v3(v9[6], v9[7], v9[8]), v3(o3[0], o3[1], o3[2]),
+                  v3(d3[0], d3[1], d3[2]), tmin, tmax, &h))
+        return 0;
+    out3[0] = h.t;
+    out3[1] = h.b1;
+    out3[2] = h.b2;
+    return 1;
+}
 ORC_API uint32_t orc_mm_combine(uint32_t h, uint32_t k) { return mm_combine(h, k); }
 ORC_API float orc_mm_rand(uint32_t h) { return mm_rand(h); }
 
@@ -1449,7 +1660,30 @@ ORC_API int orc_chunk_read_bvh(orc_chunk *c, uint32_t which, vrg_bvh_node *nodes
     return 0;
 }
 ORC_API void orc_world_add(orc_world *w, uint64_t key, orc_chunk *c, float tx, float ty, float tz) {
-    w->W.objects[key] = std::make_pair(c->c, std::array<float, 3>{tx, ty, tz});
+    OXform X = XF_IDENTITY;
+    X.m[3] = tx;
+    X.m[7] = ty;
+    X.m[11] = tz;
+    w->W.objects[key] = std::make_pair(c->c, X);
+}
+// any row-major 3x4 transform [R|t]; an exactly identity R is a translation
+ORC_API void orc_world_add_xform(orc_world *w, uint64_t key, orc_chunk *c, const float *m12) {
+    OXform X;
+    memcpy(X.m, m12, sizeof(X.m));
+    X.tonly = true;
+    for (int r = 0; r < 3; r++)
+        for (int k = 0; k < 3; k++) X.tonly = X.tonly && m12[4 * r + k] == (r == k ? 1.0f : 0.0f);
+    w->W.objects[key] = std::make_pair(c->c, X);
+}
+// upload_object of a triangle mesh (nverts a multiple of 3; slots in the table)
+ORC_API orc_chunk *orc_mesh_build(orc_world *w, const vrg_vertex3d *v, uint64_t nverts) {
+    orc_chunk *c = new orc_chunk();
+    c->c = std::make_shared<OChunk>();
+    if (!build_mesh(*c->c, w->W.M, v, nverts)) {
+        delete c;
+        return nullptr;
+    }
+    return c;
 }
 ORC_API void orc_world_remove(orc_world *w, uint64_t key) { w->W.objects.erase(key); }
 ORC_API void orc_world_commit(orc_world *w) { world_commit(w->W); }

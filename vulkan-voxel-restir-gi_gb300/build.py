@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvrg.so")
 
-SOURCES = ["api.cpp", "terrain.cpp", "image.cpp", "sah.cu", "extract.cu", "scene.cu", "trace.cu", "restir.cu", "nrc.cu", "peaks.cu"]
+SOURCES = ["api.cpp", "terrain.cpp", "image.cpp", "sah.cu", "extract.cu", "scene.cu", "trace.cu", "restir.cu", "nrc.cu", "peaks.cu", "mesh.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17",

@@ -287,6 +287,29 @@ VRG_API vrg_status vrg_upload_chunk(vrg_context *ctx, const uint8_t *blocks, con
     return VRG_OK;
 }
 
+VRG_API vrg_status vrg_upload_mesh(vrg_context *ctx, const vrg_vertex3d *v, uint64_t nverts, vrg_object **out) {
+    if (!ctx || !out || (nverts && !v)) return VRG_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (ctx->n_types == 0) {
+        set_error("material table not set");
+        return VRG_ERR_STATE;
+    }
+    vrg_object *o = new vrg_object();
+    o->ctx = ctx;
+    ctx_retain(ctx);
+    vrg_status st;
+    {  // one upload at a time on the context's stream (the builder synchronizes it)
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        st = mesh_upload(ctx, v, nverts, o);
+    }
+    if (st != VRG_OK) {
+        release_object(o);
+        return st;
+    }
+    *out = o;
+    return VRG_OK;
+}
+
 VRG_API vrg_status vrg_flush_uploads(vrg_context *ctx) {
     if (!ctx) return VRG_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -368,32 +391,56 @@ VRG_API vrg_status vrg_scene_destroy(vrg_scene *scene) {
     return VRG_OK;
 }
 
-static vrg_status parse_xform(const float *x, float off[3]) {
-    if (!x) {
-        off[0] = off[1] = off[2] = 0.0f;
-        return VRG_OK;
-    }
-    const float I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+// The instance transform of add_object / update_object (scene.rs:150,205),
+// as a row-major [R|t].  A chunk takes a translation by whole blocks (its
+// voxel records hold integer world coordinates); a mesh takes a rotation-like
+// R (entries within +-1, as an isometry's) and |t| <= 4096, which keeps the
+// rounding of its transformed vertices inside the traversal boxes' margin.
+static vrg_status parse_xform(const Object *obj, const float *x, SceneEntry &e) {
+    static const float I12[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    const float *m = x ? x : I12;
+    bool tonly = true, ok = true;
     for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++)
-            if (x[4 * r + c] != I[r][c]) {
-                set_error("only translations are supported (chunks are translated, not rotated)");
+        for (int c = 0; c < 4; c++) {
+            const float v = m[4 * r + c];
+            if (c < 3) {
+                tonly = tonly && v == (r == c ? 1.0f : 0.0f);
+                ok = ok && fabsf(v) <= 1.0f;
+            } else {
+                ok = ok && fabsf(v) <= (obj->mesh ? 4096.0f : 16384.0f);
+            }
+        }
+    if (!obj->mesh) {
+        if (!tonly) {
+            set_error("a chunk takes a translation only (chunks are translated, chunk_manager.rs:234-248)");
+            return VRG_ERR_UNSUPPORTED;
+        }
+        for (int r = 0; r < 3; r++)
+            if (m[4 * r + 3] != floorf(m[4 * r + 3]) || !ok) {
+                set_error("a chunk translation must be integral and within +-16384");
                 return VRG_ERR_UNSUPPORTED;
             }
-    off[0] = x[3];
-    off[1] = x[7];
-    off[2] = x[11];
+    } else if (!ok) {
+        set_error("a mesh transform needs finite R entries within +-1 and |t| <= 4096");
+        return VRG_ERR_UNSUPPORTED;
+    }
+    memcpy(e.m, m, sizeof(e.m));
+    e.off[0] = m[3];
+    e.off[1] = m[7];
+    e.off[2] = m[11];
+    e.tonly = tonly;
     return VRG_OK;
 }
 
 VRG_API vrg_status vrg_scene_add(vrg_scene *scene, uint64_t key, vrg_object *obj, const float xform3x4[12]) {
     if (!scene || !obj) return VRG_ERR_INVALID_ARGUMENT;
-    float off[3];
-    VRG_TRY(parse_xform(xform3x4, off));
+    SceneEntry e{};
+    e.obj = obj;
+    VRG_TRY(parse_xform(obj, xform3x4, e));
     obj->refs++;
     auto it = scene->objects.find(key);
     if (it != scene->objects.end()) scene->retired.push_back(it->second.obj);
-    scene->objects[key] = SceneEntry{obj, {off[0], off[1], off[2]}};
+    scene->objects[key] = e;
     scene->dirty = true;
     return VRG_OK;
 }
@@ -405,9 +452,9 @@ VRG_API vrg_status vrg_scene_update(vrg_scene *scene, uint64_t key, const float 
         set_error("object with key %llu does not exist", (unsigned long long)key);
         return VRG_ERR_NOT_FOUND;  // reference panics (scene.rs:214)
     }
-    float off[3];
-    VRG_TRY(parse_xform(xform3x4, off));
-    for (int a = 0; a < 3; a++) it->second.off[a] = off[a];
+    SceneEntry e = it->second;
+    VRG_TRY(parse_xform(e.obj, xform3x4, e));
+    it->second = e;
     scene->dirty = true;
     return VRG_OK;
 }

@@ -309,7 +309,10 @@ struct InferArgs {
     uint32_t enc_cap;
 };
 
+// the normal of a query: a voxel face index 0..5, or a mesh normal packed
+// with bit 31 set (pack_normal10)
 __device__ __forceinline__ f3 face_normal(int f) {
+    if (f < 0) return unpack_normal10((uint32_t)f);
     f3 n = f3{0.0f, 0.0f, 0.0f};
     const float s = (f & 1) ? 1.0f : -1.0f;
     if ((f >> 1) == 0) n.x = s;

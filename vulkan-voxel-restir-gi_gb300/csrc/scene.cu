@@ -17,6 +17,7 @@
 // Several scenes commit together with one SAH build for all their top-level
 // trees and one for all their lamp trees.
 #include <algorithm>
+#include <cstring>
 
 #include "vrg_internal.h"
 
@@ -25,18 +26,50 @@ namespace vrg {
 namespace {
 
 struct InstBuild {
-    const vrg_bvh_node *bl;    // BLAS nodes (chunk-local)
+    const vrg_bvh_node *bl;    // BLAS nodes (object space)
     const uint32_t *leaf;      // leaf -> local prim
-    const int2 *geo_local;     // geometry only
-    const uint32_t *light_tri; // light only
+    const int2 *geo_local;     // geometry of a chunk only
+    const uint32_t *light_tri; // light only (mesh: triangle index per light prim)
+    const float4 *mesh_tri;    // mesh only: object-space triangles
     uint32_t n_prims;
-    uint32_t wbase, rbase;
+    uint32_t wbase, rbase;     // first traversal node; first record (blocks / light prims) it owns
+    uint32_t tbase;            // first world-space triangle record it owns (meshes)
+    uint32_t refbase;          // record index of its local prim 0 in the leaf references
+    uint32_t flags;            // INST_*
     float off[3];
     int ioff[3];
+    float m[12];               // the transform, row-major [R|t]
 };
 
 __device__ __forceinline__ int bl_root_ref(const InstBuild &I) {
-    return I.bl[0].left_node_idx != INVALID ? (int)I.wbase : ~(int)(I.rbase + I.leaf[0]);
+    return I.bl[0].left_node_idx != INVALID ? (int)I.wbase : ~(int)(I.refbase + I.leaf[0]);
+}
+
+// world-space box of an object-space node box: translated, or for another
+// transform the AABB of its 8 transformed corners (Aabb::transform, aabb.rs:75-92)
+__device__ __forceinline__ void world_box(const vrg_bvh_node *c, const InstBuild *I, const float off[3], float lo[3],
+                                          float hi[3]) {
+    if (!I || !(I->flags & INST_XFORM)) {
+        for (int a = 0; a < 3; a++) {
+            lo[a] = c->min[a] + off[a];
+            hi[a] = c->max[a] + off[a];
+        }
+        return;
+    }
+    const float4 r0 = make_float4(I->m[0], I->m[1], I->m[2], I->m[3]);
+    const float4 r1 = make_float4(I->m[4], I->m[5], I->m[6], I->m[7]);
+    const float4 r2 = make_float4(I->m[8], I->m[9], I->m[10], I->m[11]);
+    for (int k = 0; k < 8; k++) {
+        const f3 p = xf_rows(r0, r1, r2, f3{(k & 4) ? c->max[0] : c->min[0], (k & 2) ? c->max[1] : c->min[1],
+                                            (k & 1) ? c->max[2] : c->min[2]});
+        if (k == 0) {
+            lo[0] = hi[0] = p.x; lo[1] = hi[1] = p.y; lo[2] = hi[2] = p.z;
+        } else {
+            lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
+            lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
+            lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
+        }
+    }
 }
 
 // 4-wide traversal node for every inner node g of the combined index space:
@@ -50,7 +83,7 @@ struct ChildRef {
     float off[3];
     int ref;        // node / ~record
     int inner;      // combined index of an inner child (to expand), -1 otherwise
-    int k;          // instance of a BLAS child, -1 for top level
+    int k;          // instance of a BLAS child (its box is in that instance's object space), -1 for top level
 };
 
 __device__ __forceinline__ void child_of(const vrg_bvh_node *tl, const InstBuild *inst, int k, uint32_t c,
@@ -75,7 +108,7 @@ __device__ __forceinline__ void child_of(const vrg_bvh_node *tl, const InstBuild
             out.ref = (int)I.wbase;
             out.inner = (int)I.wbase;
         } else {
-            out.ref = ~(int)(I.rbase + I.leaf[0]);
+            out.ref = ~(int)(I.refbase + I.leaf[0]);
             out.inner = -1;
         }
         return;
@@ -88,7 +121,7 @@ __device__ __forceinline__ void child_of(const vrg_bvh_node *tl, const InstBuild
         out.ref = (int)(I.wbase + c);
         out.inner = (int)(I.wbase + c);
     } else {
-        out.ref = ~(int)(I.rbase + I.leaf[c]);
+        out.ref = ~(int)(I.refbase + I.leaf[c]);
         out.inner = -1;
     }
 }
@@ -128,10 +161,11 @@ __global__ void k_wide4(const vrg_bvh_node *tl, uint32_t n_tl, const InstBuild *
     int refs[4];
     for (int i = 0; i < 4; i++) {
         if (i < n) {
-            const vrg_bvh_node *c = out[i].node;
+            float lo[3], hi[3];
+            world_box(out[i].node, out[i].k >= 0 ? &inst[out[i].k] : nullptr, out[i].off, lo, hi);
             for (int a = 0; a < 3; a++) {
-                b[2 * a][i] = (c->min[a] + out[i].off[a]) - BOX_MARGIN;
-                b[2 * a + 1][i] = (c->max[a] + out[i].off[a]) + BOX_MARGIN;
+                b[2 * a][i] = lo[a] - BOX_MARGIN;
+                b[2 * a + 1][i] = hi[a] + BOX_MARGIN;
             }
             refs[i] = out[i].ref;
         } else {
@@ -178,6 +212,44 @@ __global__ void k_geo_records(const InstBuild *inst, uint32_t n_inst, uint32_t n
     }
 }
 
+// world-space triangle records of every mesh instance, one thread per record
+// (records of instance k start at its tbase): (v0, instance) (v1, triangle)
+// (v2, material slot) — the triangleTransform of the vertex buffer
+// (raytrace.rs:155-159)
+__global__ void k_tri_records(const InstBuild *inst, uint32_t n_inst, uint32_t n_rec, float4 *rec) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_rec; g += gridDim.x * blockDim.x) {
+        const uint32_t k = inst_of(inst, n_inst, g, [](const InstBuild &I) { return I.tbase; });
+        const InstBuild &I = inst[k];
+        const uint32_t t = g - I.tbase;
+        const float4 *q = I.mesh_tri + 3 * (size_t)t;
+        const float4 r0 = make_float4(I.m[0], I.m[1], I.m[2], I.m[3]);
+        const float4 r1 = make_float4(I.m[4], I.m[5], I.m[6], I.m[7]);
+        const float4 r2 = make_float4(I.m[8], I.m[9], I.m[10], I.m[11]);
+        const uint32_t w[3] = {k, t, __float_as_uint(q[0].w)};
+        for (int j = 0; j < 3; j++) {
+            const f3 p = f3{q[j].x, q[j].y, q[j].z};
+            const f3 v = (I.flags & INST_XFORM) ? xf_rows(r0, r1, r2, p) : add3(p, f3{I.off[0], I.off[1], I.off[2]});
+            rec[3 * (size_t)g + j] = make_float4(v.x, v.y, v.z, __uint_as_float(w[j]));
+        }
+    }
+}
+
+// The light-BLAS nodes of an instance whose transform is not a translation,
+// with min and max replaced by the transform applied to them: the v000 and
+// v111 of nodeImportance (raytrace.rs:184-185, nee_pdf.rs:127-128), computed
+// once here so the light walks move these nodes by a zero translation
+__global__ void k_xform_light_nodes(const vrg_bvh_node *in, uint32_t n, float4 r0, float4 r1, float4 r2,
+                                    vrg_bvh_node *out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    vrg_bvh_node nd = in[j];
+    const f3 a = xf_rows(r0, r1, r2, f3{nd.min[0], nd.min[1], nd.min[2]});
+    const f3 b = xf_rows(r0, r1, r2, f3{nd.max[0], nd.max[1], nd.max[2]});
+    nd.min[0] = a.x; nd.min[1] = a.y; nd.min[2] = a.z;
+    nd.max[0] = b.x; nd.max[1] = b.y; nd.max[2] = b.z;
+    out[j] = nd;
+}
+
 // world-space light-triangle records of every instance, one thread per light
 // BLAS node (node j of instance k is index wbase - base + j); leaves write
 // their prim's record
@@ -193,6 +265,13 @@ __global__ void k_light_records(const InstBuild *inst, uint32_t n_inst, uint32_t
         const uint32_t p = I.leaf[j];
         if (p == INVALID) continue;
         const uint32_t t = I.light_tri[p];
+        if (I.flags & INST_MESH) {
+            // a light triangle of a mesh: its own lamp (x is the record index,
+            // unique), z = bit 31 | its world-space triangle record
+            rec[I.rbase + p] = make_int4((int)(I.rbase + p), (int)(0xFFFFu | (k << 16)),
+                                         (int)(0x80000000u | (I.tbase + t)), (int)j);
+            continue;
+        }
         const int wx = (int)(t & 31u) + I.ioff[0], wy = (int)((t >> 5) & 31u) + I.ioff[1],
                   wz = (int)((t >> 10) & 31u) + I.ioff[2];
         const uint32_t f = (t >> 15) & 7u, h = (t >> 18) & 1u;
@@ -285,12 +364,28 @@ __global__ void __launch_bounds__(1024) k_scan_inclusive(uint32_t *v, uint32_t n
     if (threadIdx.x == 0) *total = s_carry;
 }
 
-__global__ void k_lamp_fill(const int4 *rec, const uint32_t *grp, uint32_t n, int4 *lamp, uint32_t *table,
-                            float4 *lo, float4 *hi, float4 *cen, uint32_t *id) {
+__global__ void k_lamp_fill(const int4 *rec, const uint32_t *grp, uint32_t n, const float4 *tri_rec, int4 *lamp,
+                            uint32_t *table, float4 *lo, float4 *hi, float4 *cen, uint32_t *id) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int4 r = rec[i];
     const uint32_t g = grp[i] - 1u;
+    if (r.z < 0) {  // a mesh light triangle: table (leaf, triangle record), its world AABB
+        const uint32_t t = (uint32_t)r.z & 0x7FFFFFFFu;
+        table[12u * g] = (uint32_t)r.w;
+        table[12u * g + 1u] = t;
+        lamp[g] = make_int4(r.x, r.y, (int)0x80000000u, (int)(12u * g));
+        const float4 a = tri_rec[3 * (size_t)t], b = tri_rec[3 * (size_t)t + 1], c = tri_rec[3 * (size_t)t + 2];
+        const float4 l = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y),
+                                     fminf(fminf(a.z, b.z), c.z), 0.0f);
+        const float4 h = make_float4(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y),
+                                     fmaxf(fmaxf(a.z, b.z), c.z), 0.0f);
+        lo[g] = l;
+        hi[g] = h;
+        cen[g] = make_float4((l.x + h.x) * 0.5f, (l.y + h.y) * 0.5f, (l.z + h.z) * 0.5f, 0.0f);
+        id[g] = g;
+        return;
+    }
     const int f = r.z & 7, h = (r.z >> 3) & 1;
     table[12u * g + 2u * (uint32_t)f + (uint32_t)h] = (uint32_t)r.w;
     atomicOr(&lamp[g].z, 1 << f);
@@ -464,11 +559,13 @@ struct CommitPrep {
     std::vector<float> tl_in;        // [prims][10]: lo3 hi3 off3 power
     std::vector<uint32_t> tl_ids;
     std::vector<InstBuild> gb, lb;
-    uint64_t geo_recs = 0, light_recs = 0, n_geo_wide = 0, n_light_nodes_all = 0;
+    uint64_t geo_recs = 0, light_recs = 0, tri_recs = 0, n_geo_wide = 0, n_light_nodes_all = 0;
+    uint64_t blk_cursor = 0;
     uint32_t max_levels = 0;
     DevBufPtr buf;
     uint8_t *B = nullptr;
-    uint64_t o_gw = 0, o_gr = 0, o_lr = 0, o_tln = 0, o_inst = 0, o_gb = 0, o_lb = 0;
+    uint64_t o_gw = 0, o_gr = 0, o_tr = 0, o_lr = 0, o_tln = 0, o_inst = 0, o_gb = 0, o_lb = 0, o_xln = 0;
+    uint64_t xf_light_nodes = 0;     // light-BLAS nodes of the instances with a transform that is not a translation
     uint32_t tl_prim_off = 0, tl_node_off = 0;  // in the shared top-level build
     uint64_t lamp_off = 0;                      // in the shared lamp build
     uint32_t n_lamps = 0;
@@ -482,6 +579,8 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
     // instances: non-empty objects in key order (scene.rs:245-260)
     sc->inst_objs.clear();
     sc->inst_off.clear();
+    sc->inst_xf.clear();
+    sc->inst_tonly.clear();
     for (auto &kv : sc->objects) {
         Object *o = kv.second.obj;
         if (!o->flushed) {
@@ -491,6 +590,10 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
         if (o->sum.n_tris == 0) continue;
         sc->inst_objs.push_back(o);
         sc->inst_off.push_back({kv.second.off[0], kv.second.off[1], kv.second.off[2]});
+        std::array<float, 12> m;
+        memcpy(m.data(), kv.second.m, sizeof(kv.second.m));
+        sc->inst_xf.push_back(m);
+        sc->inst_tonly.push_back(kv.second.tonly ? 1 : 0);
     }
     const uint32_t ni = (uint32_t)sc->inst_objs.size();
     if (ni > 65535) {
@@ -498,55 +601,98 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
         return VRG_ERR_UNSUPPORTED;
     }
     cp.ni = ni;
-    // top-level inputs: light roots, then geometry roots
+    // Top-level inputs: light roots, then geometry roots.  An instance's prim
+    // is its root AABB moved by its transform (Aabb::transform, build.rs:391-395):
+    // a translation goes to the builder as such; any other transform is
+    // applied here, to the 8 corners in the reference's order, and the
+    // builder gets a zero translation.
+    auto tl_prim = [&](uint32_t i, const float lo[3], const float hi[3], float power) {
+        float r[10];
+        if (sc->inst_tonly[i]) {
+            const float *o = sc->inst_off[i].data();
+            for (int a = 0; a < 3; a++) {
+                r[a] = lo[a];
+                r[3 + a] = hi[a];
+                r[6 + a] = o[a];
+            }
+        } else {
+            const float *m = sc->inst_xf[i].data();
+            const float4 r0 = make_float4(m[0], m[1], m[2], m[3]), r1 = make_float4(m[4], m[5], m[6], m[7]),
+                         r2 = make_float4(m[8], m[9], m[10], m[11]);
+            f3 c[8];
+            for (int k = 0; k < 8; k++)
+                c[k] = xf_rows(r0, r1, r2, f3{(k & 4) ? hi[0] : lo[0], (k & 2) ? hi[1] : lo[1], (k & 1) ? hi[2] : lo[2]});
+            float mn[3] = {c[0].x, c[0].y, c[0].z}, mx[3] = {c[0].x, c[0].y, c[0].z};
+            for (int k = 0; k < 8; k++) {  // aabb.rs:10-22 (from_points)
+                mn[0] = fminf(mn[0], c[k].x); mx[0] = fmaxf(mx[0], c[k].x);
+                mn[1] = fminf(mn[1], c[k].y); mx[1] = fmaxf(mx[1], c[k].y);
+                mn[2] = fminf(mn[2], c[k].z); mx[2] = fmaxf(mx[2], c[k].z);
+            }
+            for (int a = 0; a < 3; a++) {
+                r[a] = mn[a];
+                r[3 + a] = mx[a];
+                r[6 + a] = 0.0f;
+            }
+        }
+        r[9] = power;
+        cp.tl_in.insert(cp.tl_in.end(), r, r + 10);
+        cp.tl_ids.push_back(i);
+    };
     for (uint32_t i = 0; i < ni; i++) {
         const ChunkSummary &cs = sc->inst_objs[i]->sum;
         if (cs.n_light == 0) continue;
-        const float *o = sc->inst_off[i].data();
-        float r[10] = {cs.light_lo[0], cs.light_lo[1], cs.light_lo[2], cs.light_hi[0], cs.light_hi[1],
-                       cs.light_hi[2], o[0], o[1], o[2], cs.light_power};
-        cp.tl_in.insert(cp.tl_in.end(), r, r + 10);
-        cp.tl_ids.push_back(i);
+        tl_prim(i, cs.light_lo, cs.light_hi, cs.light_power);
         cp.n_light_inst++;
     }
     for (uint32_t i = 0; i < ni; i++) {
         const ChunkSummary &cs = sc->inst_objs[i]->sum;
         if (cs.n_geo == 0) continue;
-        const float *o = sc->inst_off[i].data();
-        float r[10] = {cs.geo_lo[0], cs.geo_lo[1], cs.geo_lo[2], cs.geo_hi[0], cs.geo_hi[1], cs.geo_hi[2],
-                       o[0], o[1], o[2], 0.0f};
-        cp.tl_in.insert(cp.tl_in.end(), r, r + 10);
-        cp.tl_ids.push_back(i);
+        tl_prim(i, cs.geo_lo, cs.geo_hi, 0.0f);
         cp.n_geo_inst++;
     }
     cp.n_light_tl = cp.n_light_inst ? 2 * cp.n_light_inst - 1 : 1;
     cp.n_geo_tl = cp.n_geo_inst ? 2 * cp.n_geo_inst - 1 : 0;
-    // per-instance layout
+    // Per-instance layout.  Leaf references: the surface-block records of all
+    // chunks first (geo_rec), then the world-space triangles of all meshes
+    // (tri_rec), so a reference ~r with r >= geo_recs names triangle
+    // r - geo_recs.  Each instance owns a range of each record kind (empty
+    // for the kind it does not have), in instance order.
     uint64_t geo_nodes = 0, light_nodes = 0;
     cp.gb.resize(ni);
     cp.lb.resize(ni);
+    for (uint32_t i = 0; i < ni; i++) {
+        const Object *o = sc->inst_objs[i];
+        if (!o->mesh) cp.geo_recs += o->sum.n_geo;
+    }
     for (uint32_t i = 0; i < ni; i++) {
         Object *o = sc->inst_objs[i];
         const ChunkSummary &cs = o->sum;
         InstBuild &g = cp.gb[i], &l = cp.lb[i];
         for (int a = 0; a < 3; a++) {
-            float t = sc->inst_off[i][a];
-            if (t != floorf(t) || fabsf(t) > 16384.0f) {
-                set_error("instance translation must be integral and within +-16384");
-                return VRG_ERR_UNSUPPORTED;
-            }
+            const float t = sc->inst_off[i][a];
             g.off[a] = l.off[a] = t;
-            g.ioff[a] = l.ioff[a] = (int)t;
+            g.ioff[a] = l.ioff[a] = o->mesh ? 0 : (int)t;
         }
+        memcpy(g.m, sc->inst_xf[i].data(), sizeof(g.m));
+        memcpy(l.m, g.m, sizeof(g.m));
+        g.flags = l.flags = (o->mesh ? INST_MESH : 0u) | (sc->inst_tonly[i] ? 0u : INST_XFORM);
+        g.mesh_tri = l.mesh_tri = o->mesh_tri;
         g.bl = o->geo_nodes;
         g.leaf = o->geo_leaf;
         g.geo_local = o->geo_local;
         g.light_tri = nullptr;
         g.n_prims = cs.n_geo;
         g.wbase = cp.n_geo_tl + (uint32_t)geo_nodes;
-        g.rbase = (uint32_t)cp.geo_recs;
+        g.rbase = (uint32_t)cp.blk_cursor;
+        g.tbase = l.tbase = (uint32_t)cp.tri_recs;
+        if (o->mesh) {
+            g.refbase = (uint32_t)(cp.geo_recs + cp.tri_recs);
+            cp.tri_recs += cs.n_tris;
+        } else {
+            g.refbase = g.rbase;
+            cp.blk_cursor += cs.n_geo;
+        }
         geo_nodes += cs.n_geo ? 2 * (uint64_t)cs.n_geo - 1 : 0;
-        cp.geo_recs += cs.n_geo;
         l.bl = o->light_nodes;
         l.leaf = o->light_leaf;
         l.geo_local = nullptr;
@@ -554,12 +700,14 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
         l.n_prims = cs.n_light;
         l.wbase = cp.n_light_tl + (uint32_t)light_nodes;
         l.rbase = (uint32_t)cp.light_recs;
+        l.refbase = l.rbase;
         light_nodes += cs.n_light ? 2 * (uint64_t)cs.n_light - 1 : 0;
         cp.light_recs += cs.n_light;
+        if (!sc->inst_tonly[i] && cs.n_light) cp.xf_light_nodes += 2 * (uint64_t)cs.n_light - 1;
         cp.max_levels = std::max(cp.max_levels, o->levels);
     }
     cp.n_light_nodes_all = light_nodes;
-    if (cp.n_geo_tl + geo_nodes >= 0x7FFFFFFFull || cp.geo_recs >= 0x7FFFFFFFull) {
+    if (cp.n_geo_tl + geo_nodes >= 0x7FFFFFFFull || cp.geo_recs + cp.tri_recs >= 0x7FFFFFFFull) {
         set_error("scene too large for 31-bit node references");
         return VRG_ERR_UNSUPPORTED;
     }
@@ -568,6 +716,8 @@ vrg_status commit_prepare(Scene *sc, CommitPrep &cp) {
     cp.n_geo_wide = cp.n_geo_tl + geo_nodes;
     cp.o_gw = o; o += al(cp.n_geo_wide * 128);
     cp.o_gr = o; o += al(cp.geo_recs * 16);
+    cp.o_tr = o; o += al(cp.tri_recs * 48);
+    cp.o_xln = o; o += al(cp.xf_light_nodes * sizeof(vrg_bvh_node));
     cp.o_lr = o; o += al(cp.light_recs * 16);
     cp.o_tln = o; o += al((uint64_t)(cp.n_light_tl + cp.n_geo_tl) * sizeof(vrg_bvh_node));
     cp.o_inst = o; o += al((uint64_t)ni * sizeof(InstDev));
@@ -664,11 +814,29 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
     uint8_t *B = cp.B;
     // instance table (prim2node, scene.rs:282-287)
     std::vector<InstDev> idev(ni);
+    uint64_t xln = 0;
     for (uint32_t i = 0; i < ni; i++) {
+        const Object *ob = sc->inst_objs[i];
         for (int a = 0; a < 3; a++) idev[i].off[a] = sc->inst_off[i][a];
         idev[i].light_bvh_tl_idx = 0;
-        idev[i].light_bl = sc->inst_objs[i]->light_nodes;
-        idev[i].light_leaf_tri = sc->inst_objs[i]->light_leaf_tri;
+        idev[i].light_bl = ob->light_nodes;
+        idev[i].light_leaf_tri = ob->light_leaf_tri;
+        idev[i].flags = cp.gb[i].flags;
+        idev[i].tri_base = cp.gb[i].tbase;
+        idev[i].uv = ob->mesh_uv;
+        if (!sc->inst_tonly[i] && ob->sum.n_light) {
+            // the light walks read this instance's nodes already transformed
+            const uint32_t nn = 2 * ob->sum.n_light - 1;
+            const float *m = sc->inst_xf[i].data();
+            vrg_bvh_node *dst = (vrg_bvh_node *)(B + cp.o_xln) + xln;
+            k_xform_light_nodes<<<(nn + 127) / 128, 128, 0, s>>>(
+                ob->light_nodes, nn, make_float4(m[0], m[1], m[2], m[3]), make_float4(m[4], m[5], m[6], m[7]),
+                make_float4(m[8], m[9], m[10], m[11]), dst);
+            VRG_CUDA_TRY(cudaGetLastError());
+            idev[i].light_bl = dst;
+            idev[i].off[0] = idev[i].off[1] = idev[i].off[2] = 0.0f;
+            xln += nn;
+        }
     }
     if (cp.n_light_inst)
         for (uint32_t j = 0; j < cp.n_light_tl; j++)
@@ -690,6 +858,10 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
         const uint32_t n = (uint32_t)cp.geo_recs;
         k_geo_records<<<std::min(4096u, (n + 255) / 256), 256, 0, s>>>(d_gb, ni, n, (int4 *)(B + cp.o_gr));
     }
+    if (cp.tri_recs) {
+        const uint32_t n = (uint32_t)cp.tri_recs;
+        k_tri_records<<<std::min(4096u, (n + 255) / 256), 256, 0, s>>>(d_gb, ni, n, (float4 *)(B + cp.o_tr));
+    }
     if (cp.light_recs) {
         const uint32_t n = (uint32_t)(cp.n_light_nodes_all);
         k_light_records<<<std::min(4096u, (n + 255) / 256), 256, 0, s>>>(d_lb, ni, cp.n_light_tl, n,
@@ -699,6 +871,8 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
     DevScene &D = cp.dev;
     D.geo_wide = (const float4 *)(B + cp.o_gw);
     D.geo_rec = (const int4 *)(B + cp.o_gr);
+    D.tri_rec = (const float4 *)(B + cp.o_tr);
+    D.n_blk_rec = (uint32_t)cp.geo_recs;
     D.light_tl = d_tl;
     D.inst = (const InstDev *)(B + cp.o_inst);
     D.mats = (const vrg_material *)sc->ctx->d_mats->ptr;
@@ -717,7 +891,7 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
         } else {
             uint32_t p0;
             VRG_CUDA_TRY(cudaMemcpy(&p0, cp.gb[k].leaf, 4, cudaMemcpyDeviceToHost));
-            D.geo_root = ~(int)(cp.gb[k].rbase + p0);
+            D.geo_root = ~(int)(cp.gb[k].refbase + p0);
         }
     }
     return VRG_OK;
@@ -772,7 +946,7 @@ vrg_status commit_lamps(cudaStream_t s, std::vector<CommitPrep> &cps) {
         k_lamp_flags<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(light_rec, (uint32_t)n, flag);
         k_scan_inclusive<<<1, 1024, 0, s>>>(flag, (uint32_t)n, tot + c);
         k_lamp_fill<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(
-            light_rec, flag, (uint32_t)n, lamp, table, (float4 *)(S + o_lo) + cp.lamp_off,
+            light_rec, flag, (uint32_t)n, (const float4 *)(cp.B + cp.o_tr), lamp, table, (float4 *)(S + o_lo) + cp.lamp_off,
             (float4 *)(S + o_hi) + cp.lamp_off, (float4 *)(S + o_cen) + cp.lamp_off,
             (uint32_t *)(S + o_id) + cp.lamp_off);
         VRG_CUDA_TRY(cudaGetLastError());

@@ -49,7 +49,12 @@ __device__ __forceinline__ NodeV ldnode(const vrg_bvh_node *n) {
 }
 
 // nodeImportance (raytrace.rs:181-208: uint visibility, EPS 1e-3;
-// nee_pdf.rs:125-152: float visibility, EPS 1e-4); translation transforms
+// nee_pdf.rs:125-152: float visibility, EPS 1e-4).  v000 and v111 are the
+// instance transform applied to the node's min and max; the 8 corners are the
+// axis-aligned box they span (as in the reference, not the transformed box).
+// An instance moves its light-BLAS nodes by the translation off here; an
+// instance with any other transform has its nodes' min and max transformed
+// once at commit (its off is 0), which gives the same importance bits.
 template <bool NEE>
 __device__ __forceinline__ float node_importance(f3 point, f3 normal, const float off[3], const NodeV &n) {
     f3 v000 = f3{n.mn.x + off[0], n.mn.y + off[1], n.mn.z + off[2]};
@@ -174,9 +179,18 @@ __device__ float reverse_walk(const DevScene &sc, f3 point, f3 normal, uint32_t 
     return probability;
 }
 
+// world-space vertices of the light triangle of light-BLAS leaf `leaf` of
+// instance ii (the triangleTransform of raytrace.rs:155-159, nee_pdf.rs:95-101)
 __device__ __forceinline__ void light_tri_world(const DevScene &sc, uint32_t ii, uint32_t leaf, f3 tv[3]) {
     const InstDev &I = sc.inst[ii];
     uint32_t t = __ldg(I.light_leaf_tri + leaf);
+    if (I.flags & INST_MESH) {
+        const float4 *r = sc.tri_rec + 3 * (size_t)(I.tri_base + t);
+        tv[0] = ld3(__ldg(r));
+        tv[1] = ld3(__ldg(r + 1));
+        tv[2] = ld3(__ldg(r + 2));
+        return;
+    }
     int lx = (int)(t & 31u), ly = (int)((t >> 5) & 31u), lz = (int)((t >> 10) & 31u);
     int f = (int)((t >> 15) & 7u), h = (int)((t >> 18) & 1u);
 #pragma unroll
@@ -325,6 +339,8 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
     uint32_t *err = a.counters + CNT_ERROR;
     const float4 *wide = a.v0.sc.geo_wide;
     const int4 *recs = a.v0.sc.geo_rec;
+    const float4 *tris = a.v0.sc.tri_rec;
+    uint32_t nblk = a.v0.sc.n_blk_rec;
     int root = a.v0.sc.geo_root;
     bool has = false, exhausted = false;
     uint32_t p = 0, steps = 0, traced = 0, n_nodes = 0, n_leaves = 0;
@@ -354,6 +370,8 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                     if constexpr (BATCH) {
                         wide = V.sc.geo_wide;
                         recs = V.sc.geo_rec;
+                        tris = V.sc.tri_rec;
+                        nblk = V.sc.n_blk_rec;
                         root = V.sc.geo_root;
                     }
                     if (b == 0) raygen(V, p - V.pix_off, o, d);
@@ -403,7 +421,24 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                     done = true;
                 }
             }
-            if (!done) {  // leaf: the exposed faces of one surface block
+            if (!done && (uint32_t)(~node) >= nblk) {  // leaf: one world-space mesh triangle
+                const float4 *tr = tris + 3 * (size_t)((uint32_t)(~node) - nblk);
+                const float4 A = __ldg(tr), B = __ldg(tr + 1), C = __ldg(tr + 2);
+                n_leaves++;
+                TriHit th;
+                if (tri_test(ld3(A), ld3(B), ld3(C), o, d, EPS_TRACE, best_t, th)) {
+                    const uint64_t key = ((uint64_t)__float_as_uint(A.w) << 32) | __float_as_uint(B.w);
+                    if (th.t < best_t || key < best_key) {
+                        best_t = th.t;
+                        best_key = key;
+                        hrec = ~node;
+                        hfh = 0;
+                        hb1 = th.b1;
+                        hb2 = th.b2;
+                    }
+                }
+                done = !pop_near(stack, sp, best_t, node);
+            } else if (!done) {  // leaf: the exposed faces of one surface block
                 const int4 r = __ldg(recs + (~node));
                 n_leaves++;
                 const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
@@ -475,29 +510,56 @@ __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_typ
         E = f3{sky, sky, sky};
         R = f3{0.0f, 0.0f, 0.0f};
     } else {
-        rc = __ldg(S.geo_rec + hv.x);
-        face = hv.y & 7;
-        half = (hv.y >> 3) & 1;
         const float b1 = __int_as_float(hv.z), b2 = __int_as_float(hv.w);
-        const int wx = rec_wx(rc), wy = rec_wy(rc), wz = rec_wz(rc);
-        const f3 t0 = corner_pos(wx, wy, wz, face_corner(face, half, 0));
-        const f3 t1 = corner_pos(wx, wy, wz, face_corner(face, half, 1));
-        const f3 t2 = corner_pos(wx, wy, wz, face_corner(face, half, 2));
-        const Frame fr = c_frames[2 * face + half];
-        n = fr.n;
-        const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
-        const uint32_t slot = 6u * blk_id + (uint32_t)face;
         const float b0 = (1.0f - b1) - b2;
+        f3 t0, t1, t2;
+        Frame fr;
+        uint32_t slot;
+        float u = 0.0f, v = 0.0f;  // the texture coordinate (read with an atlas only)
+        if ((uint32_t)hv.x >= S.n_blk_rec) {
+            // a mesh triangle: its world-space vertices and material slot;
+            // localCoordinateSystem of the triangle (raytrace.rs:319-331);
+            // face carries bit 31 | its record (the normal of the light-pdf walk)
+            const uint32_t tr = (uint32_t)hv.x - S.n_blk_rec;
+            const float4 *q = S.tri_rec + 3 * (size_t)tr;
+            const float4 A = __ldg(q), B = __ldg(q + 1), C = __ldg(q + 2);
+            t0 = ld3(A);
+            t1 = ld3(B);
+            t2 = ld3(C);
+            fr = tri_frame(t0, t1, t2);
+            slot = __float_as_uint(C.w);
+            face = (int)(0x80000000u | tr);
+            rc = make_int4((int)__float_as_uint(A.w), (int)__float_as_uint(B.w), -1, 0);
+            if (S.atlas) {  // uv = v0.uv * b0 + v1.uv * b1 + v2.uv * b2 (raytrace.rs:457)
+                const float *uv = S.inst[rc.x].uv + 6 * (size_t)rc.y;
+                u = ((__ldg(uv) * b0) + (__ldg(uv + 2) * b1)) + (__ldg(uv + 4) * b2);
+                v = ((__ldg(uv + 1) * b0) + (__ldg(uv + 3) * b1)) + (__ldg(uv + 5) * b2);
+            }
+        } else {
+            rc = __ldg(S.geo_rec + hv.x);
+            face = hv.y & 7;
+            half = (hv.y >> 3) & 1;
+            const int wx = rec_wx(rc), wy = rec_wy(rc), wz = rec_wz(rc);
+            t0 = corner_pos(wx, wy, wz, face_corner(face, half, 0));
+            t1 = corner_pos(wx, wy, wz, face_corner(face, half, 1));
+            t2 = corner_pos(wx, wy, wz, face_corner(face, half, 2));
+            fr = c_frames[2 * face + half];
+            const uint32_t blk_id = ((uint32_t)rc.z >> 21) & 0xFFu;
+            slot = 6u * blk_id + (uint32_t)face;
+            if (S.atlas) {  // gen_mesh's corner uvs
+                const uint32_t q0 = face_uv(face, half, 0), q1 = face_uv(face, half, 1),
+                               q2 = face_uv(face, half, 2);
+                u = (((float)(q0 & 1u) * b0) + ((float)(q1 & 1u) * b1)) + ((float)(q2 & 1u) * b2);
+                v = (((float)(q0 >> 1) * b0) + ((float)(q1 >> 1) * b1)) + ((float)(q2 >> 1) * b2);
+            }
+        }
+        n = fr.n;
         new_o = add3(add3(scl3(t0, b0), scl3(t1, b1)), scl3(t2, b2));
         const float ndd = -dot3(d, n);
         float alpha, metal;
         if (S.atlas) {
             // texture atlas: the three maps at the interpolated uv
             // (raytrace.rs:457-480), nearest texel clamped to the edge
-            const uint32_t q0 = face_uv(face, half, 0), q1 = face_uv(face, half, 1),
-                           q2 = face_uv(face, half, 2);
-            const float u = (((float)(q0 & 1u) * b0) + ((float)(q1 & 1u) * b1)) + ((float)(q2 & 1u) * b2);
-            const float v = (((float)(q0 >> 1) * b0) + ((float)(q1 >> 1) * b1)) + ((float)(q2 >> 1) * b2);
             const int aw = (int)S.atlas_w, ah = (int)S.atlas_h;
             const int ix = min(max((int)floorf(u * (float)aw), 0), aw - 1);
             const int iy = min(max((int)floorf(v * (float)ah), 0), ah - 1);
@@ -635,7 +697,9 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                 qhit = hv.x >= 0;
                 a.qflag[p] = qhit ? 1 : 0;
                 if (qhit) {
-                    a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+                    // the cache's normal: a face index, or a mesh normal packed in 32 bits
+                    a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z,
+                                             face >= 0 ? __int_as_float(face) : __uint_as_float(pack_normal10(so.n)));
                     a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
                     want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
                 }
@@ -712,7 +776,9 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                 a.c_pdf[s0] = pdf;
                 a.c_nee[s0] = 0.0f;
                 uint4 hw;
-                if (hv.x >= 0) {
+                if (face < 0) {  // a mesh triangle: (instance, triangle)
+                    hw = make_uint4((uint32_t)rc.x, (uint32_t)rc.y, INVALID, 0u);
+                } else if (hv.x >= 0) {
                     const uint32_t mask = ((uint32_t)rc.z >> 15) & 63u;
                     hw.x = rec_inst(rc);
                     hw.y = (uint32_t)rc.w + 2u * __popc(mask & ((1u << face) - 1u)) + (uint32_t)half;
@@ -778,6 +844,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
     const float4 *wide = a.v0.sc.lamp_wide;
     const int4 *recs = a.v0.sc.lamp_rec;
     const uint32_t *table = a.v0.sc.lamp_table;
+    const float4 *tris = a.v0.sc.tri_rec;
     int root = a.v0.sc.lamp_root;
     const float tmin = EPS_NEE, tmax = 1000.0f;
     bool has = false, exhausted = false;
@@ -811,6 +878,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                         wide = V.sc.lamp_wide;
                         recs = V.sc.lamp_rec;
                         table = V.sc.lamp_table;
+                        tris = V.sc.tri_rec;
                         root = V.sc.lamp_root;
                     }
                     const float4 ro = a.ajob[b & 1][2 * (size_t)idx], rd = a.ajob[b & 1][2 * (size_t)idx + 1];
@@ -875,7 +943,29 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                 const int4 r = __ldg(recs + (~node));
                 const int wx = rec_wx(r), wy = rec_wy(r), wz = rec_wz(r);
                 const uint32_t ii = rec_inst(r);
-                for (uint32_t fm = (uint32_t)r.z; fm; fm &= fm - 1u) {
+                if (r.z < 0) {  // a mesh light triangle: (leaf, world-space triangle record) in the table
+                    const uint32_t leaf = __ldg(table + r.w), t = __ldg(table + r.w + 1);
+                    const float4 *q = tris + 3 * (size_t)t;
+                    TriHit th;
+                    if (tri_test(ld3(__ldg(q)), ld3(__ldg(q + 1)), ld3(__ldg(q + 2)), o, d, tmin, tmax, th)) {
+                        const uint64_t key = ((uint64_t)ii << 32) | leaf;
+                        if (nh < LIGHT_LIST) {
+                            int j = nh++;
+                            while (j > 0 && keys[j - 1] > key) {
+                                keys[j] = keys[j - 1];
+                                b1s[j] = b1s[j - 1];
+                                b2s[j] = b2s[j - 1];
+                                j--;
+                            }
+                            keys[j] = key;
+                            b1s[j] = th.b1;
+                            b2s[j] = th.b2;
+                        } else {
+                            atomicOr(err, ERR_LIGHT_LIST);
+                        }
+                    }
+                }
+                for (uint32_t fm = r.z < 0 ? 0u : (uint32_t)r.z; fm; fm &= fm - 1u) {
                     const int f = __ffs(fm) - 1;
                     FaceHit fh;
                     if (!face_test(wx, wy, wz, f, o, d, inv, tmin, tmax, fh)) continue;
@@ -943,8 +1033,18 @@ __global__ void __launch_bounds__(128) k_hit_eval(const __grid_constant__ FrameA
         const uint4 A = a.hitbuf[2 * (size_t)h], B = a.hitbuf[2 * (size_t)h + 1];
         const uint32_t p = A.x;
         const float4 ro = a.ajob[b & 1][2 * (size_t)B.y], rd = a.ajob[b & 1][2 * (size_t)B.y + 1];
-        const f3 n3 = c_frames[2 * __float_as_int(ro.w)].n;
-        a.hitval[h] = nee_pdf_of(view_of<BATCH>(a, p).sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
+        const DevScene &sc = view_of<BATCH>(a, p).sc;
+        // the shading normal of the job's vertex: a voxel face's, or a mesh
+        // triangle's, recomputed as its shading computed it
+        const int fw = __float_as_int(ro.w);
+        f3 n3;
+        if (fw >= 0) {
+            n3 = c_frames[2 * fw].n;
+        } else {
+            const float4 *q = sc.tri_rec + 3 * (size_t)((uint32_t)fw & 0x7FFFFFFFu);
+            n3 = tri_frame(ld3(__ldg(q)), ld3(__ldg(q + 1)), ld3(__ldg(q + 2))).n;
+        }
+        a.hitval[h] = nee_pdf_of(sc, ld3(ro), n3, ld3(rd), A.y, A.z, __uint_as_float(A.w), __uint_as_float(B.x));
     }
 }
 

@@ -219,16 +219,104 @@ __host__ __device__ __forceinline__ int rec_wz(int4 r) { return r.x >> 16; }
 __host__ __device__ __forceinline__ int rec_wy(int4 r) { return (int)(short)(r.y & 0xFFFF); }
 __host__ __device__ __forceinline__ uint32_t rec_inst(int4 r) { return ((uint32_t)r.y) >> 16; }
 
+// InstDev::flags
+constexpr uint32_t INST_MESH = 1u;    // an uploaded triangle mesh (else a voxel chunk)
+constexpr uint32_t INST_XFORM = 2u;   // a transform other than a translation
+
 struct InstDev {
-    float off[3];
+    float off[3];                     // the translation (0 with INST_XFORM)
     uint32_t light_bvh_tl_idx;        // prim2node (scene.rs:282-287)
-    const vrg_bvh_node *light_bl;     // light BLAS nodes (chunk-local)
-    const uint32_t *light_leaf_tri;   // per light BLAS node: lx | ly<<5 | lz<<10 | face<<15 | half<<18
+    const vrg_bvh_node *light_bl;     // light BLAS nodes (object space; with INST_XFORM their min and
+                                      // max already transformed, the v000 / v111 of nodeImportance)
+    const uint32_t *light_leaf_tri;   // per light BLAS node: chunk lx | ly<<5 | lz<<10 | face<<15 | half<<18,
+                                      // mesh: its triangle index
+    uint32_t flags;                   // INST_*
+    uint32_t tri_base;                // mesh: its first world-space triangle record (DevScene::tri_rec)
+    const float *uv;                  // mesh: vertex uvs, 6 floats per triangle
 };
+
+// The instance transform applied to a point: a translation exactly (p + t),
+// any other row-major 3x4 [R|t] as ((r0*x + r1*y) + r2*z) + t per row — the
+// mat4x3 * vec4(p, 1) of the reference shaders (raytrace.rs:155-159,184-185).
+__host__ __device__ __forceinline__ f3 xf_rows(const float4 &r0, const float4 &r1, const float4 &r2, f3 p) {
+    return f3{((r0.x * p.x + r0.y * p.y) + r0.z * p.z) + r0.w, ((r1.x * p.x + r1.y * p.y) + r1.z * p.z) + r1.w,
+              ((r2.x * p.x + r2.y * p.y) + r2.z * p.z) + r2.w};
+}
+
+// Watertight ray/triangle test (Woop, Benthin, Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013), both faces: the ray's
+// dominant axis kz (largest |d| component, the first on ties), the shear,
+// the edge functions U, V, W of the sheared vertices (recomputed in double
+// when one is exactly 0), a hit iff they do not differ in sign and
+// det = U + V + W != 0, t = T / det in [tmin, tmax]; the barycentrics of v1
+// and v2 are V / det and W / det.  Vertices sharing an edge give the same
+// edge function, so no ray passes between two triangles of a mesh.
+struct TriHit {
+    float t, b1, b2;
+};
+__host__ __device__ __forceinline__ bool tri_test(f3 v0, f3 v1, f3 v2, f3 o, f3 d, float tmin, float tmax,
+                                                  TriHit &h) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > (kz == 0 ? ax : ay)) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1, ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (cmp3(d, kz) < 0.0f) {
+        const int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    const float dz = cmp3(d, kz);
+    const float Sx = cmp3(d, kx) / dz, Sy = cmp3(d, ky) / dz, Sz = 1.0f / dz;
+    const f3 A = sub3(v0, o), B = sub3(v1, o), C = sub3(v2, o);
+    const float Ax = cmp3(A, kx) - Sx * cmp3(A, kz), Ay = cmp3(A, ky) - Sy * cmp3(A, kz);
+    const float Bx = cmp3(B, kx) - Sx * cmp3(B, kz), By = cmp3(B, ky) - Sy * cmp3(B, kz);
+    const float Cx = cmp3(C, kx) - Sx * cmp3(C, kz), Cy = cmp3(C, ky) - Sy * cmp3(C, kz);
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    const float Az = Sz * cmp3(A, kz), Bz = Sz * cmp3(B, kz), Cz = Sz * cmp3(C, kz);
+    const float T = (U * Az + V * Bz) + W * Cz;
+    const float t = T / det;
+    if (!(t >= tmin && t <= tmax)) return false;
+    h.t = t;
+    h.b1 = V / det;
+    h.b2 = W / det;
+    return true;
+}
+
+// localCoordinateSystem (raytrace.rs:319-331) of a world-space triangle
+__host__ __device__ __forceinline__ Frame tri_frame(f3 v0, f3 v1, f3 v2) {
+    const f3 e1 = sub3(v1, v0), e2 = sub3(v2, v0);
+    const f3 n = cross3(e1, e2);
+    const f3 bt = cross3(n, e1);
+    return Frame{norm3(n), norm3(e1), norm3(bt)};
+}
+
+// A shading normal carried in one 32-bit word (ray and query .w lanes): a
+// voxel face index 0..5, or a mesh normal as bit 31 | three 10-bit snorm
+// components (read only as an input feature of the radiance cache)
+__host__ __device__ __forceinline__ uint32_t pack_normal10(f3 n) {
+    auto q = [](float c) -> uint32_t { return (uint32_t)((int)rintf(fminf(fmaxf(c, -1.0f), 1.0f) * 511.0f) & 1023); };
+    return 0x80000000u | q(n.x) | (q(n.y) << 10) | (q(n.z) << 20);
+}
+__host__ __device__ __forceinline__ f3 unpack_normal10(uint32_t w) {
+    auto u = [](uint32_t v) -> float { return (float)((int)(v << 22) >> 22) / 511.0f; };
+    return f3{u(w & 1023u), u((w >> 10) & 1023u), u((w >> 20) & 1023u)};
+}
 
 struct DevScene {
     const float4 *geo_wide;   // 8 float4 per node: 4-wide child boxes (world, +margin, SoA) and refs
-    const int4 *geo_rec;
+    const int4 *geo_rec;      // records [0, n_blk_rec): surface blocks; [n_blk_rec, ...): mesh triangles
+    const float4 *tri_rec;    // world-space mesh triangles, 3 float4 each: (v0, instance) (v1, triangle)
+                              // (v2, material slot), .w as u32 bits
+    uint32_t n_blk_rec;
     int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
     const float4 *lamp_wide;  // any-hit layout over lamp blocks: 8 float4 per node, 4-wide as geo_wide
     const int4 *lamp_rec;     // per lamp block: x/y packed coords + instance, z emissive face mask, w table base

@@ -102,6 +102,13 @@ struct Object {
     const uint32_t *light_tri = nullptr;  // per light prim: lx|ly<<5|lz<<10|face<<15|half<<18
     const uint32_t *light_leaf_tri = nullptr;  // per light node (leaf payload, same packing)
     uint32_t levels = 0;                  // SAH level passes of the batch (depth bound)
+    // an uploaded triangle mesh (vrg_upload_mesh) instead of a chunk: its
+    // object-space triangles (3 float4: v0 | material slot bits, v1, v2) and
+    // vertex uvs (6 floats per triangle); geo_* is the BVH over the triangles
+    // (leaf prim = triangle), light_tri / light_leaf_tri hold triangle indices
+    bool mesh = false;
+    const float4 *mesh_tri = nullptr;
+    const float *mesh_uv = nullptr;
     std::atomic<int> refs{1};
     virtual ~Object();  // frees its buffers, then drops its reference to the context
 };
@@ -128,11 +135,16 @@ void ctx_retain(Context *c);
 void ctx_release(Context *c);
 
 vrg_status extract_and_build(Context *ctx, std::vector<Object *> &batch);
+// upload_object of a triangle mesh: validates, builds the light BLAS and the
+// geometry BVH on the GPU and fills the object (mesh.cu)
+vrg_status mesh_upload(Context *ctx, const vrg_vertex3d *v, uint64_t nverts, Object *o);
 
 // ---- scene -------------------------------------------------------------
 struct SceneEntry {
     Object *obj;
-    float off[3];
+    float off[3];       // the translation
+    float m[12];        // the transform, row-major [R|t]
+    bool tonly;         // R is exactly the identity: points move by p + off
 };
 
 struct Scene {
@@ -142,6 +154,8 @@ struct Scene {
     // committed state
     std::vector<Object *> inst_objs;      // instance order (key order, non-empty)
     std::vector<std::array<float, 3>> inst_off;
+    std::vector<std::array<float, 12>> inst_xf;
+    std::vector<uint8_t> inst_tonly;
     DevBufPtr d_buf;                      // wide layouts, records, TLs, instance table
     DevBufPtr lamp_buf;                   // lamp-block any-hit layout
     DevScene dev{};

@@ -56,6 +56,14 @@ class Material(C.Structure):
                 ("reserved", C.c_uint32 * 2)]
 
 
+class Vertex3D(C.Structure):
+    """Vertex3D (vertex.rs:4-14): position, texture index t, uv (24 bytes)."""
+    _fields_ = [("position", C.c_float * 3), ("t", C.c_uint32), ("uv", C.c_float * 2)]
+
+
+VERTEX_DTYPE = np.dtype([("position", np.float32, 3), ("t", np.uint32), ("uv", np.float32, 2)])
+
+
 class ContextDesc(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
 
@@ -127,6 +135,7 @@ SIGNATURES = [
     ("vrg_material_table_set", C.c_int32, [_P, C.POINTER(Material), C.c_uint32]),
     ("vrg_texture_atlas_set", C.c_int32, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("vrg_upload_chunk", C.c_int32, [_P, _P, C.POINTER(_P), C.POINTER(_P)]),
+    ("vrg_upload_mesh", C.c_int32, [_P, _P, C.c_uint64, C.POINTER(_P)]),
     ("vrg_flush_uploads", C.c_int32, [_P]),
     ("vrg_object_release", C.c_int32, [_P]),
     ("vrg_object_info", C.c_int32, [_P] + [C.POINTER(C.c_uint32)] * 4),
@@ -386,10 +395,37 @@ class SceneUploader:
         check(self.ctx.lib.vrg_upload_chunk(self.ctx.h, _ptr(blocks), arr, C.byref(h)), "vrg_upload_chunk")
         return UploadedObject(self.ctx, h)
 
+    def upload_object(self, vertexes) -> UploadedObject:
+        """upload_object (scene.rs:547-725) of a triangle mesh: a VERTEX_DTYPE
+        array (or (n, 6) floats: position, t, u, v), three vertices per triangle."""
+        v = as_vertices(vertexes)
+        h = C.c_void_p()
+        check(self.ctx.lib.vrg_upload_mesh(self.ctx.h, _ptr(v) if len(v) else None, len(v), C.byref(h)),
+              "vrg_upload_mesh")
+        return UploadedObject(self.ctx, h)
+
+
+def as_vertices(vertexes) -> np.ndarray:
+    """A contiguous VERTEX_DTYPE array from structured or (n, 6) [x, y, z, t, u, v] input."""
+    a = np.asarray(vertexes)
+    if a.dtype == VERTEX_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.asarray(a, np.float64).reshape(-1, 6)
+    v = np.zeros(len(a), VERTEX_DTYPE)
+    v["position"] = a[:, :3]
+    v["t"] = a[:, 3].astype(np.uint32)
+    v["uv"] = a[:, 4:6]
+    return v
+
 
 def _xform(t):
-    x = (C.c_float * 12)(1, 0, 0, float(t[0]), 0, 1, 0, float(t[1]), 0, 0, 1, float(t[2]))
-    return x
+    """A transform for vrg_scene_add / update: a translation (3 values) or a
+    3x4 / 4x4 matrix [R|t] (the matrix of an Isometry3)."""
+    m = np.asarray(t, np.float32)
+    if m.size == 3:
+        m = np.array([[1, 0, 0, m[0]], [0, 1, 0, m[1]], [0, 0, 1, m[2]]], np.float32)
+    m = m.reshape(-1, 4)[:3]
+    return (C.c_float * 12)(*[float(x) for x in m.reshape(-1)])
 
 
 class Scene:
@@ -402,12 +438,14 @@ class Scene:
         self._objs = {}
         ctx.adopt(self)
 
-    def add_object(self, key: int, obj: UploadedObject, translation=(0, 0, 0)):
-        check(self.ctx.lib.vrg_scene_add(self.h, key, obj.h, _xform(translation)), "vrg_scene_add")
+    def add_object(self, key: int, obj: UploadedObject, isometry=(0, 0, 0)):
+        """add_object (scene.rs:150): isometry is a translation or a 3x4 / 4x4 matrix."""
+        check(self.ctx.lib.vrg_scene_add(self.h, key, obj.h, _xform(isometry)), "vrg_scene_add")
         self._objs[key] = obj
 
-    def update_object(self, key: int, translation):
-        check(self.ctx.lib.vrg_scene_update(self.h, key, _xform(translation)), "vrg_scene_update")
+    def update_object(self, key: int, isometry):
+        """update_object (scene.rs:205): VrgError(ERR_NOT_FOUND) where the reference panics."""
+        check(self.ctx.lib.vrg_scene_update(self.h, key, _xform(isometry)), "vrg_scene_update")
 
     def remove_object(self, key: int):
         check(self.ctx.lib.vrg_scene_remove(self.h, key), "vrg_scene_remove")
