@@ -375,7 +375,11 @@ typedef struct vrg_tuning {
     uint32_t anyhit_blocks_per_sm;  /* light-hit collection grid */
     uint32_t anyhit_refill;         /* as trace_refill, for the light-hit collection (8) */
     uint32_t stream_block;          /* threads per CTA of the per-pixel kernels: 64, 128 or 256 (256) */
-    uint32_t reserved[2];
+    uint32_t spatial_staging;       /* how the spatial pass reads reservoirs: 1 each CTA's 32x8-pixel tile
+                                       staged in shared memory by one tensor copy (TMA; single-view
+                                       renderers of at least 32x8 pixels), 2 per-thread loads; 0 = 1 where
+                                       it applies, else 2 */
+    uint32_t reserved[1];
 } vrg_tuning;
 
 VRG_API vrg_status vrg_renderer_set_tuning(vrg_renderer *r, const vrg_tuning *t);
@@ -500,8 +504,19 @@ typedef struct vrg_nrc_desc {
     uint32_t seed;
     float scene_min[3];        /* box mapped to the unit cube */
     float scene_max[3];
+    uint32_t flags;            /* VRG_NRC_* below */
+    uint32_t reserved;
 } vrg_nrc_desc;
-enum { VRG_NRC_WEIGHTS = 0, VRG_NRC_WEIGHT_GRADS, VRG_NRC_TABLE, VRG_NRC_TABLE_GRADS, VRG_NRC_ZERO_GRADS };
+/* Training runs on the 5th-generation tensor cores (tcgen05: 128-sample tiles,
+ * tensor-memory accumulators) unless VRG_NRC_TRAIN_WARP_MMA selects the
+ * warp-level mma.sync training kernel (32-sample tiles). */
+#define VRG_NRC_TRAIN_WARP_MMA 1u
+/* vrg_nrc_read / vrg_nrc_write selectors.  VRG_NRC_TRAIN_PREDICTIONS (read
+ * only): the network's outputs for the last vrg_nrc_train batch, n x 3 floats,
+ * from the training pass's own forward pass (the tensor-core path of the
+ * training kernel, next to vrg_nrc_query's). */
+enum { VRG_NRC_WEIGHTS = 0, VRG_NRC_WEIGHT_GRADS, VRG_NRC_TABLE, VRG_NRC_TABLE_GRADS, VRG_NRC_ZERO_GRADS,
+       VRG_NRC_TRAIN_PREDICTIONS };
 VRG_API vrg_status vrg_nrc_create(vrg_context *ctx, const vrg_nrc_desc *desc, vrg_nrc **out);
 VRG_API vrg_status vrg_nrc_destroy(vrg_nrc *nrc);
 /* Host arrays: pos/normal/dir n x 3 floats (dir = the incoming ray direction;

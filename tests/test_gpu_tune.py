@@ -47,7 +47,8 @@ def test_tuning_does_not_change_frames(gpu_ctx, world):
     ref = vrg.Renderer(gpu_ctx, W, H, 3)
     base = _frames(ref, world)
     ref.close()
-    for t in (vrg.Tuning(1, 1, 1, 1, 1, 64), vrg.Tuning(0, 32, 0, 0, 32, 128), vrg.Tuning(2, 4, 3, 2, 16, 0)):
+    for t in (vrg.Tuning(1, 1, 1, 1, 1, 64), vrg.Tuning(0, 32, 0, 0, 32, 128), vrg.Tuning(2, 4, 3, 2, 16, 0),
+              vrg.Tuning(0, 0, 0, 0, 0, 0, 1), vrg.Tuning(3, 16, 0, 4, 8, 128, 2), vrg.Tuning(0, 0, 0, 0, 0, 0, 2)):
         r = vrg.Renderer(gpu_ctx, W, H, 3)
         r.set_tuning(t)
         assert _same(base, _frames(r, world)), t.as_dict()
@@ -75,6 +76,39 @@ def test_autotune_restores_state_and_installs_best(gpu_ctx, world):
 def test_tuning_rejects_out_of_range(gpu_ctx):
     r = vrg.Renderer(gpu_ctx, 8, 8, 2)
     lib = gpu_ctx.lib
-    for bad in (vrg.Tuning(0, 33, 0, 0, 0, 0), vrg.Tuning(0, 0, 0, 0, 0, 100), vrg.Tuning(65, 0, 0, 0, 0, 0)):
+    for bad in (vrg.Tuning(0, 33, 0, 0, 0, 0), vrg.Tuning(0, 0, 0, 0, 0, 100), vrg.Tuning(65, 0, 0, 0, 0, 0),
+                vrg.Tuning(0, 0, 0, 0, 0, 0, 3)):
         assert lib.vrg_renderer_set_tuning(r.h, C.byref(bad)) == vrg.ERR_INVALID_ARGUMENT
     r.close()
+
+
+@pytest.mark.parametrize("w,h", [(83, 45), (96, 64), (40, 8)], ids=["83x45", "96x64", "40x8"])
+def test_tma_staged_spatial_pass_bit_exact(gpu_ctx, world, orc, w, h):
+    """The spatial pass with each CTA's 32x8-pixel reservoir tile staged in
+    shared memory by a tensor copy (spatial_staging 1, the default) bit for bit
+    as with per-thread loads (2) and as the oracle, with edge tiles partly
+    outside the view."""
+    from helpers import compare_frame, params
+    mats, n, blocks = terrain_world(31, 2, 2, 0.01)
+    OW = orc.build_world(mats, n, blocks)
+    try:
+        a, b = vrg.Renderer(gpu_ctx, w, h, 3), vrg.Renderer(gpu_ctx, w, h, 3)
+        a.set_tuning(vrg.Tuning(0, 0, 0, 0, 0, 0, 2))
+        b.set_tuning(vrg.Tuning(0, 0, 0, 0, 0, 0, 1))
+        orr = orc.Renderer(w, h, 3)
+        for f in range(3):
+            cam = vrg.orbit_camera(2, 2, f, 64, w, h)
+            p = params(nee=1, view=1, spatial=3, nb=3, seeds=(f, 40 + f, 80 + f))
+            ia, ra = a.render_params(world, cam, p, want_image=True, want_radiance=True)
+            ib, rb = b.render_params(world, cam, p, want_image=True, want_radiance=True)
+            assert b.last_stats.error_flags == 0
+            assert np.array_equal(ra.view(np.uint32), rb.view(np.uint32)) and np.array_equal(ia, ib), f
+            orr.render(OW, cam, p)
+            diffs = compare_frame(b, orr, 3)
+            assert all(v == 0 for v in diffs.values()), (f, diffs)
+        assert b.get_tuning().spatial_staging == 1 and a.get_tuning().spatial_staging == 2
+        a.close()
+        b.close()
+        orr.close()
+    finally:
+        OW.close()

@@ -10,13 +10,16 @@
 // in flight), then runs the MLP on the 5th-generation tensor cores: tiles of
 // 128 queries, tcgen05.mma from shared-memory operands into tensor-memory
 // accumulators, one issuing thread per tile, ReLU epilogues from tcgen05.ld.
-// Training fuses encode, forward, loss, backward through the layers and the
-// hash-grid gradient scatter in per-warp tiles on mma m16n8k16 (the
-// activations stay in registers: the f32 C fragment of layer l is repacked as
-// the bf16 A fragment of layer l+1 without shuffles; the weights are resident
-// in shared memory, row stride padded to 72 bf16); weight gradients are a
-// split-K tensor-core reduction over the batch; Adam runs over FP32 master
-// copies and refreshes the BF16 / FP16 working copies.
+// Training encodes the samples with the same encoding pass, then runs the
+// forward, the loss, the backward through the layers and the hash-grid
+// gradient scatter on tcgen05 in the same 128-sample tiles (the backward's B
+// operands are the transposed weights).  A warp-level training kernel on mma
+// m16n8k16 remains selectable (the activations stay in registers: the f32 C
+// fragment of layer l is repacked as the bf16 A fragment of layer l+1 without
+// shuffles; the weights are resident in shared memory, row stride padded to
+// 72 bf16).  Weight gradients are a split-K tensor-core reduction over the
+// batch; Adam runs over FP32 master copies and refreshes the BF16 / FP16
+// working copies.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -555,6 +558,9 @@ struct TrainArgs {
     float2 *gtable;             // hash-grid gradients (fp32)
     float *loss;                // summed loss
     uint32_t *err;              // error word (ERR_COPY)
+    float4 *pred;               // optional: the forward pass's prediction per sample
+    const uint32_t *enc;        // tensor-core pass: the encoded input rows (k_nrc_encode layout)
+    uint32_t enc_cap;
 };
 
 __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
@@ -618,6 +624,7 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
                 float *yr = yt + (lane - 16 * t) * NRC_OUT;
                 // a non-finite target (the path estimator's 0*inf cases) carries no gradient
                 const bool finite_target = isfinite(tg.x) && isfinite(tg.y) && isfinite(tg.z);
+                if (a.pred && i < n) a.pred[i] = make_float4(yr[0], yr[1], yr[2], 0.0f);
                 if (i < n && finite_target) {
                     const float m = (yr[0] + yr[1] + yr[2]) * (1.0f / 3.0f);
                     const float den = m * m + 0.01f;
@@ -710,6 +717,251 @@ __global__ void __launch_bounds__(NRC_WARPS * 32) k_nrc_train(TrainArgs a) {
     }
     for (int o = 16; o; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
     if (lane == 0 && loss_acc != 0.0f) atomicAdd(a.loss, loss_acc);
+}
+
+// ---------------------------------------------------------------------------
+// Training on the 5th-generation tensor cores (tcgen05), the layout of the
+// inference pass: a CTA of TC_GROUPS warpgroups, each owning a tile of 128
+// samples (thread t of the group = sample row t), the tile's operand in shared
+// memory (K-major, no swizzle), its accumulator in tensor memory (64 FP32
+// columns per group).  Per tile:
+//   - forward: the encoded rows (k_nrc_encode) through the five hidden layers
+//     and the output layer, one M128 x N64 (N16) MMA group per layer; each
+//     thread keeps its row's ReLU mask per layer (64 bits) and stores the
+//     layer inputs H_l to global memory for the weight gradients;
+//   - loss: the relative L2 loss of its sample and dY (the output layer's dZ);
+//   - backward: dH_l = dZ_l * W_l, one MMA group per layer with the
+//     transposed weights (in x out, K-major) as the B operand; dZ_l = dH_{l+1}
+//     masked by the layer's ReLU; the dZ_l are stored for the weight
+//     gradients (k_nrc_dw);
+//   - the input gradient's hash-feature columns scattered into the table
+//     gradient (atomics), as the warp-level kernel does.
+// Every wait is bounded (ERR_MMA), and tensor memory is freed before return.
+// ---------------------------------------------------------------------------
+constexpr uint32_t TCT_WTBYTES = 6 * TC_LBYTES;  // WT_l (in x out) for l < 5, WT5 (in x 16) in a 64-column slot
+
+__device__ __forceinline__ void st_row_bf16(__nv_bfloat16 *dst, const uint32_t w[32]) {
+    uint4 *d = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+    for (int j = 0; j < 8; j++) d[j] = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_train_tc(TrainArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[TC_GROUPS];
+    __shared__ uint32_t tmem_base_s, fail_s[TC_GROUPS];
+    const int tid = threadIdx.x, grp = tid >> 7, t = tid & 127, warp = tid >> 5, lane = tid & 31;
+    unsigned char *Wc = smem, *WTc = smem + TC_WBYTES;
+    unsigned char *tile = smem + TC_WBYTES + TCT_WTBYTES + (size_t)grp * TC_TILE;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&bars[grp]);
+    // forward weights W_l (out x in) and backward weights WT_l (in x out) into the K-major layout
+    for (uint32_t c = tid; c < (5u * NRC_W + NRC_OUT) * 8u; c += TC_THREADS) {
+        const uint32_t row = c >> 3, kg = c & 7u;
+        const uint32_t l = row < 5u * NRC_W ? row / NRC_W : 5u, n = l < 5u ? row % NRC_W : row - 5u * NRC_W;
+        const __nv_bfloat16 *src = a.wpack + (l < 5u ? w_off((int)l) : W5_OFF) + (size_t)n * NRC_STRIDE + kg * 8u;
+        *reinterpret_cast<uint4 *>(Wc + l * TC_LBYTES + kmaj_off(n, kg)) = *reinterpret_cast<const uint4 *>(src);
+    }
+    for (uint32_t c = tid; c < 6u * NRC_W * 8u; c += TC_THREADS) {
+        const uint32_t l = c / (NRC_W * 8u), n = (c / 8u) % NRC_W, kg = c & 7u;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (l < 5u)
+            v = *reinterpret_cast<const uint4 *>(a.wpack + wt_off((int)l) + (size_t)n * NRC_STRIDE + kg * 8u);
+        else if (kg < 2u)  // WT5: in x 16 (rows of NRC_TSTRIDE5)
+            v = *reinterpret_cast<const uint4 *>(a.wpack + WT5_OFF + (size_t)n * NRC_TSTRIDE5 + kg * 8u);
+        *reinterpret_cast<uint4 *>(WTc + l * TC_LBYTES + kmaj_off(n, kg)) = v;
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        fail_s[grp] = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&tmem_base_s)),
+                     "r"(TC_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_s + (uint32_t)grp * 64u;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const float inv_n = n ? 1.0f / (float)n : 0.0f;
+    const int words = a.P.levels + 2;
+    const uint32_t tiles = (n + 127u) / 128u;
+    const size_t n_pad = a.n_pad;
+    const uint32_t a_s = (uint32_t)__cvta_generic_to_shared(tile), w_s = (uint32_t)__cvta_generic_to_shared(Wc),
+                   wt_s = (uint32_t)__cvta_generic_to_shared(WTc);
+    uint32_t phase = 0;
+    bool failed = false;
+    float loss_acc = 0.0f;
+    // one MMA group (n_k K16 steps into this group's columns), then the wait
+    auto mma_round = [&](uint32_t b_base, uint32_t nn, int n_k) {
+        if (t == 0) {
+            tc_fence_after();
+            const uint32_t idesc = tc_idesc(nn);
+            for (int s = 0; s < n_k; s++)
+                tc_mma(tmem, tc_desc(a_s + 256u * s), tc_desc(b_base + 256u * s), idesc, s > 0 ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                         : "memory");
+        }
+        if (mbar_wait(bar, phase, TC_WAIT)) {
+            phase ^= 1u;  // each commit completes one phase
+        } else {
+            fail_s[grp] = 1;
+            atomicOr(a.err, ERR_MMA);
+        }
+        __syncwarp();
+        tc_fence_after();
+    };
+    // the tile rewritten (and the accumulator read) before the next MMA group
+    auto round_end = [&]() {
+        fence_async_smem();
+        tc_fence_before();
+        group_sync(grp);
+        failed = fail_s[grp] != 0;
+    };
+    for (uint32_t ti = blockIdx.x * TC_GROUPS + grp; ti < tiles && !failed; ti += gridDim.x * TC_GROUPS) {
+        const uint32_t i = ti * 128u + (uint32_t)t;
+        const bool live = i < n;
+        const uint32_t id = live ? (a.list ? a.list[i] : i) : 0u;
+        {  // H_0: the encoded row
+            uint32_t w[32];
+#pragma unroll
+            for (int k = 0; k < 32; k++) w[k] = (live && k < words) ? a.enc[(size_t)k * a.enc_cap + i] : 0u;
+#pragma unroll
+            for (int kg = 0; kg < 8; kg++)
+                *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, (uint32_t)kg)) =
+                    make_uint4(w[4 * kg], w[4 * kg + 1], w[4 * kg + 2], w[4 * kg + 3]);
+            if (live) st_row_bf16(a.H + (size_t)i * NRC_W, w);
+        }
+        round_end();
+        if (failed) break;
+        uint32_t mask[5][2];
+        // forward through the hidden layers
+        for (int l = 0; l < 5 && !failed; l++) {
+            mma_round(w_s + (uint32_t)l * TC_LBYTES, NRC_W, 4);
+            uint32_t w[32];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint32_t v[32];
+                tc_ld32(trow + 32u * h, v);
+                tc_wait_ld();
+                uint32_t m = 0;
+#pragma unroll
+                for (int k = 0; k < 32; k++) {
+                    float z = __uint_as_float(v[k]);
+                    if (z > 0.0f) m |= 1u << k;
+                    else z = 0.0f;
+                    v[k] = __float_as_uint(z);
+                }
+                mask[l][h] = m;
+#pragma unroll
+                for (int k = 0; k < 16; k++) w[16 * h + k] = pack_bf16(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]));
+            }
+#pragma unroll
+            for (int kg = 0; kg < 8; kg++)
+                *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, (uint32_t)kg)) =
+                    make_uint4(w[4 * kg], w[4 * kg + 1], w[4 * kg + 2], w[4 * kg + 3]);
+            if (live) st_row_bf16(a.H + ((size_t)(l + 1) * n_pad + i) * NRC_W, w);
+            round_end();
+        }
+        if (failed) break;
+        // output layer, loss and dY
+        mma_round(w_s + 5u * TC_LBYTES, NRC_OUT, 4);
+        {
+            uint32_t v[4];
+            tc_ld4(trow, v);
+            tc_wait_ld();
+            const float y0 = __uint_as_float(v[0]), y1 = __uint_as_float(v[1]), y2 = __uint_as_float(v[2]);
+            float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
+            if (live) {
+                if (a.pred) a.pred[i] = make_float4(y0, y1, y2, 0.0f);
+                const float4 tg = a.target[id];
+                // a non-finite target (the path estimator's 0*inf cases) carries no gradient
+                if (isfinite(tg.x) && isfinite(tg.y) && isfinite(tg.z)) {
+                    const float m = (y0 + y1 + y2) * (1.0f / 3.0f);
+                    const float den = m * m + 0.01f;
+                    const float e0 = y0 - tg.x, e1 = y1 - tg.y, e2 = y2 - tg.z;
+                    loss_acc += (e0 * e0 + e1 * e1 + e2 * e2) / den * inv_n;
+                    d0 = 2.0f * e0 / den * inv_n;
+                    d1 = 2.0f * e1 / den * inv_n;
+                    d2 = 2.0f * e2 / den * inv_n;
+                }
+            }
+            // dZ6 (16 columns, 3 used) as the A operand of dH5 = dZ6 * W5 (K = 16)
+            const uint4 q0 = make_uint4(pack_bf16(d0, d1), pack_bf16(d2, 0.0f), 0u, 0u), q1 = make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, 0u)) = q0;
+            *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, 1u)) = q1;
+            if (live) {
+                uint4 *d5 = reinterpret_cast<uint4 *>(a.dZ + ((size_t)5 * n_pad + i) * NRC_W);
+                d5[0] = q0;
+                d5[1] = q1;
+            }
+        }
+        round_end();
+        if (failed) break;
+        // backward: dH5 = dZ6 * W5, then dZ_l = dH_{l+1} * relu'(Z_l), dH_l = dZ_l * W_l
+        mma_round(wt_s + 5u * TC_LBYTES, NRC_W, 1);
+        for (int l = 4; l >= 0 && !failed; l--) {
+            uint32_t w[32];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint32_t v[32];
+                tc_ld32(trow + 32u * h, v);
+                tc_wait_ld();
+                const uint32_t m = mask[l][h];
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const float g0 = ((m >> (2 * k)) & 1u) ? __uint_as_float(v[2 * k]) : 0.0f;
+                    const float g1 = ((m >> (2 * k + 1)) & 1u) ? __uint_as_float(v[2 * k + 1]) : 0.0f;
+                    w[16 * h + k] = pack_bf16(g0, g1);
+                }
+            }
+#pragma unroll
+            for (int kg = 0; kg < 8; kg++)
+                *reinterpret_cast<uint4 *>(tile + kmaj_off((uint32_t)t, (uint32_t)kg)) =
+                    make_uint4(w[4 * kg], w[4 * kg + 1], w[4 * kg + 2], w[4 * kg + 3]);
+            if (live) st_row_bf16(a.dZ + ((size_t)l * n_pad + i) * NRC_W, w);
+            round_end();
+            if (failed) break;
+            mma_round(wt_s + (uint32_t)l * TC_LBYTES, NRC_W, 4);
+        }
+        if (failed) break;
+        // dX: the hash features' gradients into the table gradient
+        {
+            uint32_t v[32];
+            tc_ld32(trow, v);
+            tc_wait_ld();
+            if (live) {
+                const f3 p = normalize_pos(a.P, ld3(a.pos[id]));
+                const size_t T = (size_t)1 << a.P.log2_t;
+                for (int l = 0; l < a.P.levels; l++) {
+                    Corner cr;
+                    level_corners(a.P, l, p, cr);
+                    const float g0 = __uint_as_float(v[2 * l]), g1 = __uint_as_float(v[2 * l + 1]);
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        atomicAdd(&a.gtable[(size_t)l * T + cr.idx[k]], make_float2(cr.w[k] * g0, cr.w[k] * g1));
+                }
+            }
+        }
+        tc_fence_before();
+        group_sync(grp);
+    }
+    for (int o = 16; o; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+    if (lane == 0 && loss_acc != 0.0f) atomicAdd(a.loss, loss_acc);
+    if (failed && t == 0) mbar_wait(bar, phase, TC_WAIT);  // the MMAs in flight, before their memory is freed
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_base_s), "r"(TC_COLS)
+                     : "memory");
+    }
 }
 
 // 8x8 b16 matrices from shared memory, transposed (ldmatrix .trans): thread t
@@ -893,15 +1145,21 @@ struct Nrc {
     size_t act_rows = 0;
     __nv_bfloat16 *H = nullptr, *dZ = nullptr;
     uint32_t step = 0;
-    int grid_train = 0, grid_tc = 0;
+    int grid_train = 0, grid_tc = 0, grid_train_tc = 0;
+    bool train_tc = true;             // training on tcgen05 (false: the warp-level mma.sync kernel)
+    DevBufPtr train_enc_buf;          // the training samples' encoded rows (own buffer: training
+    size_t train_enc_cap = 0;         // runs beside inference in a cache frame)
     DevBufPtr enc_buf;  // encoded query rows of inference
     size_t enc_cap = 0;
+    DevBufPtr pred_buf;  // the last host-array training batch's predictions
+    uint32_t pred_n = 0;
     // a cache frame's gradients wait for their Adam step, which the next user
     // of the cache runs first (a cache frame: beside its own bounces)
     bool pending = false;
 };
 
 static size_t tc_smem() { return (size_t)TC_WBYTES + (size_t)TC_GROUPS * TC_TILE; }
+static size_t train_tc_smem() { return (size_t)TC_WBYTES + TCT_WTBYTES + (size_t)TC_GROUPS * TC_TILE; }
 static size_t train_smem() {
     return WPACK_ELEMS * 2 + (size_t)NRC_WARPS * 32 * NRC_STRIDE * 2 + (size_t)NRC_WARPS * 32 * NRC_OUT * 4;
 }
@@ -942,6 +1200,22 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
         return VRG_ERR_UNSUPPORTED;
     }
     N->grid_tc = ctx->num_sms * bc;
+    // the tensor-memory training kernel likewise, also beside inference CTAs
+    // when both fit on an SM
+    int bt_tc = 0, smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
+    if (cudaFuncSetAttribute(k_nrc_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_tc_smem()) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt_tc, k_nrc_train_tc, TC_THREADS, train_tc_smem()) !=
+            cudaSuccess ||
+        bt_tc < 1 || (uint32_t)bt_tc * TC_COLS > 512u ||
+        (tc_smem() + train_tc_smem() <= (size_t)smem_sm && (uint32_t)(bc + bt_tc) * TC_COLS > 512u)) {
+        delete N;
+        set_error("radiance cache: %d tensor-core training CTAs per SM, %u tensor-memory columns each", bt_tc, TC_COLS);
+        return VRG_ERR_UNSUPPORTED;
+    }
+    N->grid_train_tc = ctx->num_sms * bt_tc;
+    N->train_tc = (d->flags & VRG_NRC_TRAIN_WARP_MMA) == 0;
     N->T = (size_t)1 << P.log2_t;
     const double b = P.levels > 1 ? std::exp((std::log((double)d->max_resolution) - std::log((double)d->base_resolution)) /
                                              (double)(P.levels - 1))
@@ -1056,7 +1330,7 @@ static vrg_status ensure_act(Nrc *N, size_t rows) {
 // also runs the Adam step
 vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
-                     uint32_t *err) {
+                     uint32_t *err, float4 *pred) {
     if (n == 0) return VRG_OK;
     VRG_TRY(nrc_flush(N, s));  // new gradients start from the updated cache
     VRG_TRY(ensure_act(N, n));
@@ -1064,9 +1338,29 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     // H and dZ hold n_pad rows per layer (the allocation, possibly made for a
     // larger batch): the training pass writes and k_nrc_dw reads with that pitch
     TrainArgs a{N->P,  N->table, N->wpack, n,         n_dev,   list,  pos, dir, nrm, target,
-                N->H,  N->dZ,    n_pad,    N->t_grad, N->loss, err ? err : N->err};
-    const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
-    k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
+                N->H,  N->dZ,    n_pad,    N->t_grad, N->loss, err ? err : N->err, pred, nullptr, 0};
+    if (N->train_tc) {
+        // the samples' encoded rows (the inference encoding pass), then the
+        // tensor-memory training pass over 128-sample tiles
+        if (N->train_enc_cap < n) {
+            DevBufPtr b;
+            VRG_TRY(dev_alloc(s, (size_t)(N->P.levels + 2) * n * 4, b));
+            N->train_enc_buf = b;
+            N->train_enc_cap = n;
+        }
+        a.enc = (const uint32_t *)N->train_enc_buf->ptr;
+        a.enc_cap = (uint32_t)N->train_enc_cap;
+        InferArgs e{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, nullptr, a.err,
+                    (uint32_t *)N->train_enc_buf->ptr, (uint32_t)N->train_enc_cap};
+        k_nrc_encode<<<(n + 255) / 256, 256, 0, s>>>(e);
+        const uint32_t tiles = (n + 127) / 128;
+        const uint32_t blocks = std::min<uint32_t>((uint32_t)N->grid_train_tc, (tiles + TC_GROUPS - 1) / TC_GROUPS);
+        k_nrc_train_tc<<<blocks, TC_THREADS, train_tc_smem(), s>>>(a);
+    } else {
+        const uint32_t blocks =
+            std::min<uint32_t>((uint32_t)N->grid_train, (n + NRC_WARPS * 32 - 1) / (NRC_WARPS * 32));
+        k_nrc_train<<<blocks, NRC_WARPS * 32, train_smem(), s>>>(a);
+    }
     VRG_CUDA_TRY(cudaGetLastError());
     const uint32_t rows_per_cta = 512;
     dim3 g((n + rows_per_cta - 1) / rows_per_cta, NRC_LAYERS);
@@ -1160,7 +1454,12 @@ vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, nrm, n, 3, dn));
     VRG_TRY(stage4(s, target, n, 3, dt));
     VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 8, s));  // loss and error word
-    VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0, nullptr));
+    if (N->pred_n < n || !N->pred_buf) {
+        VRG_TRY(dev_alloc(s, (size_t)n * 16, N->pred_buf));
+        N->pred_n = n;
+    }
+    N->pred_n = n;
+    VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0, nullptr, (float4 *)N->pred_buf->ptr));
     float l = 0.0f;
     uint32_t err = 0;
     VRG_CUDA_TRY(cudaMemcpyAsync(&l, N->loss, 4, cudaMemcpyDeviceToHost, s));
@@ -1184,6 +1483,16 @@ vrg_status nrc_read(Nrc *N, uint32_t what, void *dst, uint64_t bytes) {
     case VRG_NRC_WEIGHT_GRADS: src = N->w_grad; nb = MASTER_ELEMS * 4; break;
     case VRG_NRC_TABLE: src = N->t_master; nb = N->table_entries * 8; break;
     case VRG_NRC_TABLE_GRADS: src = N->t_grad; nb = N->table_entries * 8; break;
+    case VRG_NRC_TRAIN_PREDICTIONS: {
+        if (!N->pred_buf) return VRG_ERR_STATE;
+        if (bytes < (uint64_t)N->pred_n * 12) return VRG_ERR_INVALID_ARGUMENT;
+        std::vector<float4> h(N->pred_n);
+        VRG_CUDA_TRY(cudaMemcpyAsync(h.data(), N->pred_buf->ptr, (size_t)N->pred_n * 16, cudaMemcpyDeviceToHost, s));
+        VRG_CUDA_TRY(cudaStreamSynchronize(s));
+        float *d = (float *)dst;
+        for (uint32_t i = 0; i < N->pred_n; i++) { d[3 * i] = h[i].x; d[3 * i + 1] = h[i].y; d[3 * i + 2] = h[i].z; }
+        return VRG_OK;
+    }
     default: return VRG_ERR_INVALID_ARGUMENT;
     }
     if (bytes < nb) return VRG_ERR_INVALID_ARGUMENT;

@@ -10,6 +10,8 @@
 //     registers and written only for parity capture.
 // Reservoirs are five float4 planes per pixel (SoA, coalesced 16-byte loads):
 //   0 (x_v, ucw)  1 (n_v, w_sum)  2 (x_s, m)  3 (n_s, p_omega)  4 (l_o_hat, seed)
+#include <cuda.h>
+
 #include "vrg_frame.cuh"
 #include "vrg_internal.h"
 
@@ -158,11 +160,44 @@ __device__ __forceinline__ uint8_t to_u8(float x) {
     return (uint8_t)(int)v;
 }
 
-template <bool CAPTURE, bool BATCH>
-__global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameArgs a) {
+// Where the spatial pass reads reservoirs: straight from the ring slot, or
+// (ResTile) from the CTA's tile of it staged in shared memory when the pixel
+// lies in that tile.  The arithmetic is the same either way.
+struct ResGlobal {
+    const float4 *res;
+    uint32_t P;
+    __device__ __forceinline__ float4 plane(int k, uint32_t p, uint32_t, uint32_t) const {
+        return res[(size_t)k * P + p];
+    }
+};
+constexpr uint32_t ST_W = 32, ST_H = 8;  // staged tile: 32 x 8 pixels, 5 planes (20 KB)
+struct ResTile {
+    const float4 *res;
+    uint32_t P, x0, y0;
+    const float4 *tile;  // [5][ST_H][ST_W]
+    __device__ __forceinline__ float4 plane(int k, uint32_t p, uint32_t x, uint32_t y) const {
+        if (x - x0 < ST_W && y - y0 < ST_H) return tile[((uint32_t)k * ST_H + (y - y0)) * ST_W + (x - x0)];
+        return res[(size_t)k * P + p];
+    }
+};
+
+template <typename Src>
+__device__ __forceinline__ Res load_res_src(const Src &src, uint32_t p, uint32_t x, uint32_t y) {
+    const float4 a = src.plane(0, p, x, y), b = src.plane(1, p, x, y), c = src.plane(2, p, x, y),
+                 d = src.plane(3, p, x, y), e = src.plane(4, p, x, y);
+    Res r;
+    r.x_v = ld3(a); r.ucw = a.w;
+    r.n_v = ld3(b); r.w_sum = b.w;
+    r.x_s = ld3(c); r.m = __float_as_uint(c.w);
+    r.n_s = ld3(d); r.p_omega = d.w;
+    r.l = ld3(e); r.seed = __float_as_uint(e.w);
+    return r;
+}
+
+// spatial resampling, finalize, pack and accumulation of pixel p
+template <bool CAPTURE, bool BATCH, typename Src>
+__device__ __forceinline__ void spatial_pixel(const FrameArgs &a, uint32_t p, const Src &src) {
     const uint32_t P = a.P;
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
     f3 fin = f3{0.0f, 0.0f, 0.0f};
     float ucw_view = 0.0f;
     if (a.nb >= 2 && a.restir) {
@@ -171,7 +206,7 @@ __global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameAr
         const uint32_t lp = p - V.pix_off;
         const uint32_t qx = lp % V.W, qy = lp / V.W;
         const uint32_t ps = mm_combine(V.spatial_seed, lp);
-        Res Rs = load_res(a.res, P, p);
+        Res Rs = load_res_src(src, p, qx, qy);
         const f3 Sx_v = Rs.x_v, Sn_v = Rs.n_v;
         uint32_t Z = (luminance3(Rs.l) > 0.0f) ? Rs.m : 0u;
         for (uint32_t s = 0; s < a.spatial_iters; s++) {
@@ -184,11 +219,11 @@ __global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameAr
             ny = min(max(ny, 0), (int)V.H - 1);
             const uint32_t np = V.pix_off + (uint32_t)nx + (uint32_t)ny * V.W;
             // geometricallySimilar (restir_spatial_resampling.rs:277-288)
-            const float4 nvn = a.res[P + np];
+            const float4 nvn = src.plane(1, np, (uint32_t)nx, (uint32_t)ny);
             const f3 nn = ld3(nvn);
             if (zero3(Sn_v) || zero3(nn)) continue;
             if (dot3(Sn_v, nn) < COS25) continue;
-            const Res Rn = load_res(a.res, P, np);
+            const Res Rn = load_res_src(src, np, (uint32_t)nx, (uint32_t)ny);
             // computeJacobianQToR (restir_spatial_resampling.rs:299-311)
             float J;
             if (zero3(Rn.n_s)) {
@@ -243,6 +278,65 @@ __global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameAr
         a.accum[3 * (size_t)p + 1] += (double)c.y;
         a.accum[3 * (size_t)p + 2] += (double)c.z;
     }
+}
+
+template <bool CAPTURE, bool BATCH>
+__global__ void __launch_bounds__(256) k_spatial(const __grid_constant__ FrameArgs a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    spatial_pixel<CAPTURE, BATCH>(a, p, ResGlobal{a.res, a.P});
+}
+
+// The spatial pass over 32 x 8 pixel tiles of a single view, the CTA's own
+// reservoirs staged in shared memory by one tensor copy (cp.async.bulk.tensor,
+// a 3-D box of the ring slot: 32 pixels x 8 rows x 5 planes, completing on an
+// mbarrier; parts outside the view are zero-filled and never read).  A pixel
+// reads its own reservoir, and its neighbours' when they fall in the tile,
+// from shared memory, the rest from L2 / HBM as k_spatial does.  The wait is
+// bounded: past the limit the kernel flags ERR_COPY, waits once more
+// (bounded) for the copy in flight, and returns.
+template <bool CAPTURE>
+__global__ void __launch_bounds__(256) k_spatial_tma(const __grid_constant__ FrameArgs a,
+                                                     const __grid_constant__ CUtensorMap map) {
+    __shared__ __align__(128) float4 tile[5 * ST_H * ST_W];
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t W = a.v0.W, H = a.v0.H;
+    const uint32_t x0 = blockIdx.x * ST_W, y0 = blockIdx.y * ST_H;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar), d = (uint32_t)__cvta_generic_to_shared(tile);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b),
+                     "r"((uint32_t)sizeof(tile))
+                     : "memory");
+        // x in floats: 4 per pixel, so 16-byte aligned
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];\n" ::"r"(d),
+            "l"(&map), "r"((int)(4 * x0)), "r"((int)y0), "r"(0), "r"(b)
+            : "memory");
+    }
+    __syncthreads();
+    auto wait = [&](uint32_t limit) {
+        for (uint32_t it = 0; it < limit; it++) {
+            uint32_t done;
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(b)
+                : "memory");
+            if (done) return true;
+        }
+        return false;
+    };
+    if (!wait(1u << 22)) {
+        if (threadIdx.x == 0) atomicOr(a.counters + CNT_ERROR, ERR_COPY);
+        wait(1u << 22);
+        return;
+    }
+    const uint32_t x = x0 + (threadIdx.x % ST_W), y = y0 + (threadIdx.x / ST_W);
+    if (x >= W || y >= H) return;
+    spatial_pixel<CAPTURE, false>(a, y * W + x, ResTile{a.res, a.P, x0, y0, tile});
 }
 
 // postprocess with scale > 1 (postprocess.rs:39-88, srcscale = scale,
@@ -305,10 +399,14 @@ vrg_status launch_resolve(cudaStream_t s, const FrameArgs &a) {
     return VRG_OK;
 }
 
-vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a) {
+vrg_status launch_spatial(cudaStream_t s, const FrameArgs &a, const CUtensorMap *res_map) {
     const uint32_t t = stream_block(a);
     dim3 g((a.P + t - 1) / t);
-    if (a.views) k_spatial<false, true><<<g, t, 0, s>>>(a);
+    if (res_map && !a.views) {  // single view with its ring slot's tensor map: tiles staged by TMA
+        const dim3 gt((a.v0.W + ST_W - 1) / ST_W, (a.v0.H + ST_H - 1) / ST_H);
+        if (a.capture) k_spatial_tma<true><<<gt, ST_W * ST_H, 0, s>>>(a, *res_map);
+        else k_spatial_tma<false><<<gt, ST_W * ST_H, 0, s>>>(a, *res_map);
+    } else if (a.views) k_spatial<false, true><<<g, t, 0, s>>>(a);
     else if (a.capture) k_spatial<true, false><<<g, t, 0, s>>>(a);
     else k_spatial<false, false><<<g, t, 0, s>>>(a);
     VRG_CUDA_TRY(cudaGetLastError());

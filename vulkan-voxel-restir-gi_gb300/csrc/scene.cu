@@ -873,6 +873,7 @@ vrg_status commit_layouts(cudaStream_t s, CommitPrep &cp, const vrg_bvh_node *d_
     D.geo_rec = (const int4 *)(B + cp.o_gr);
     D.tri_rec = (const float4 *)(B + cp.o_tr);
     D.n_blk_rec = (uint32_t)cp.geo_recs;
+    D.n_tri_rec = (uint32_t)cp.tri_recs;
     D.light_tl = d_tl;
     D.inst = (const InstDev *)(B + cp.o_inst);
     D.mats = (const vrg_material *)sc->ctx->d_mats->ptr;

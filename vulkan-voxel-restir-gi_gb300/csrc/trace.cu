@@ -330,7 +330,7 @@ __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY
 // strictly beyond the current best t.  In a batched frame each lane reads the
 // scene of its ray's view when it takes the ray.
 // ---------------------------------------------------------------------------
-template <bool BATCH>
+template <bool BATCH, bool MESH>
 __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const int REFILL = (int)a.refill_trace;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                     done = true;
                 }
             }
-            if (!done && (uint32_t)(~node) >= nblk) {  // leaf: one world-space mesh triangle
+            if (MESH && !done && (uint32_t)(~node) >= nblk) {  // leaf: one world-space mesh triangle
                 const float4 *tr = tris + 3 * (size_t)((uint32_t)(~node) - nblk);
                 const float4 A = __ldg(tr), B = __ldg(tr + 1), C = __ldg(tr + 2);
                 n_leaves++;
@@ -496,6 +496,7 @@ struct ShadeOut {
 // vertex is E + (R * 0) * w = E for any finite R >= 0 and w > 0, and the
 // vertex position keeps its offset; the Lambertian continuation (light-BVH
 // descent and direction sampling) is skipped, with mis 0 and pdf 1.
+template <bool MESH>
 __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_type, uint32_t b, uint32_t seed, f3 o,
                                              f3 d, int4 hv, bool need_dir, ShadeOut &out) {
     f3 n, E, R, new_o, new_d;
@@ -516,7 +517,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene &S, uint32_t nee_typ
         Frame fr;
         uint32_t slot;
         float u = 0.0f, v = 0.0f;  // the texture coordinate (read with an atlas only)
-        if ((uint32_t)hv.x >= S.n_blk_rec) {
+        if (MESH && (uint32_t)hv.x >= S.n_blk_rec) {
             // a mesh triangle: its world-space vertices and material slot;
             // localCoordinateSystem of the triangle (raytrace.rs:319-331);
             // face carries bit 31 | its record (the normal of the light-pdf walk)
@@ -637,7 +638,7 @@ done:
 // (raytrace.rs:405-577).  Rays whose light pdf is needed are queued for
 // k_anyhit; the others get their (E, w) (R, q) record here.
 // ---------------------------------------------------------------------------
-template <bool CAPTURE, bool BATCH>
+template <bool CAPTURE, bool BATCH, bool MESH>
 __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
@@ -677,7 +678,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
             const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
             const int4 hv = a.hits[p];
             ShadeOut so;
-            shade_vertex(V.sc, a.nee_type, b, seed, o, d, hv, CAPTURE || b + 1 < nb, so);
+            shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv, CAPTURE || b + 1 < nb, so);
             const f3 n = so.n, E = so.E;
             f3 R = so.R;
             const float mis = so.mis;
@@ -1091,12 +1092,12 @@ static void init_grids_once() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     g_sms = std::max(1, g_sms);
-    g_shade[0] = occupancy_grid((const void *)k_shade<false, false>, 128);
-    g_shade[1] = occupancy_grid((const void *)k_shade<false, true>, 128);
+    g_shade[0] = occupancy_grid((const void *)k_shade<false, false, false>, 128);
+    g_shade[1] = occupancy_grid((const void *)k_shade<false, true, false>, 128);
     g_any[0] = occupancy_grid((const void *)k_anyhit<false, false>, 128);
     g_any[1] = occupancy_grid((const void *)k_anyhit<false, true>, 128);
-    g_trace[1] = occupancy_grid((const void *)k_trace<true>, 128);
-    g_trace[0] = occupancy_grid((const void *)k_trace<false>, 128);
+    g_trace[1] = occupancy_grid((const void *)k_trace<true, false>, 128);
+    g_trace[0] = occupancy_grid((const void *)k_trace<false, false>, 128);
 }
 
 // (thread-safe: renderers may be created from several threads)
@@ -1135,8 +1136,15 @@ static void bounce_grids(const FrameArgs &a, uint32_t max_rays, int &gt, int &gs
 vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
     int gt, gs, ga;
     bounce_grids(a, max_rays, gt, gs, ga);
-    if (a.views) k_trace<true><<<gt, 128, 0, s>>>(a, b);
-    else k_trace<false><<<gt, 128, 0, s>>>(a, b);
+    // the mesh-capable builds only for frames whose scenes hold meshes
+    if (a.views) {
+        if (a.mesh) k_trace<true, true><<<gt, 128, 0, s>>>(a, b);
+        else k_trace<true, false><<<gt, 128, 0, s>>>(a, b);
+    } else if (a.mesh) {
+        k_trace<false, true><<<gt, 128, 0, s>>>(a, b);
+    } else {
+        k_trace<false, false><<<gt, 128, 0, s>>>(a, b);
+    }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }
@@ -1145,9 +1153,15 @@ vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t
 vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
     int gt, gs, ga;
     bounce_grids(a, max_rays, gt, gs, ga);
-    if (a.views) k_shade<false, true><<<gs, 128, 0, s>>>(a, b);
-    else if (a.capture) k_shade<true, false><<<gs, 128, 0, s>>>(a, b);
-    else k_shade<false, false><<<gs, 128, 0, s>>>(a, b);
+    if (a.mesh) {
+        if (a.views) k_shade<false, true, true><<<gs, 128, 0, s>>>(a, b);
+        else if (a.capture) k_shade<true, false, true><<<gs, 128, 0, s>>>(a, b);
+        else k_shade<false, false, true><<<gs, 128, 0, s>>>(a, b);
+    } else {
+        if (a.views) k_shade<false, true, false><<<gs, 128, 0, s>>>(a, b);
+        else if (a.capture) k_shade<true, false, false><<<gs, 128, 0, s>>>(a, b);
+        else k_shade<false, false, false><<<gs, 128, 0, s>>>(a, b);
+    }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
 }

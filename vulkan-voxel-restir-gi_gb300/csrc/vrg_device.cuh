@@ -316,7 +316,7 @@ struct DevScene {
     const int4 *geo_rec;      // records [0, n_blk_rec): surface blocks; [n_blk_rec, ...): mesh triangles
     const float4 *tri_rec;    // world-space mesh triangles, 3 float4 each: (v0, instance) (v1, triangle)
                               // (v2, material slot), .w as u32 bits
-    uint32_t n_blk_rec;
+    uint32_t n_blk_rec, n_tri_rec;
     int geo_root;             // >=0 wide node, <0 ~record, INT32_MIN empty
     const float4 *lamp_wide;  // any-hit layout over lamp blocks: 8 float4 per node, 4-wide as geo_wide
     const int4 *lamp_rec;     // per lamp block: x/y packed coords + instance, z emissive face mask, w table base

@@ -46,6 +46,8 @@ struct FrameArgs {
     const ViewDev *views;         // batched frame: the views (device), else null
     const uint16_t *vtab;         // batched frame: view of pixel group p >> VIEW_SHIFT
     uint32_t n_views;
+    uint32_t mesh;                // a scene of the frame holds mesh triangles (the bounce kernels
+                                  // built with mesh support run; voxel-only frames run without it)
     uint32_t P;                   // pixels of the frame (all views)
     uint32_t n0, tiles_x;         // bounce-0 slots and 8x4 tiles per row (bounce0_pixel)
     uint32_t nb, nee_type;

@@ -1,6 +1,7 @@
 // Host-side internals shared by the library's translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <array>
@@ -185,9 +186,10 @@ vrg_status nrc_set_bounds(Nrc *N, const float lo[3], const float hi[3]);
 // checked by the host-array entry points)
 vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out, uint32_t *err);
+// pred (optional): the forward pass's prediction of each sample
 vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, const float4 *target, bool update,
-                     uint32_t *err);
+                     uint32_t *err, float4 *pred = nullptr);
 vrg_status nrc_update(Nrc *N, cudaStream_t s);
 vrg_status nrc_flush(Nrc *N, cudaStream_t s);
 bool nrc_pending(const Nrc *N);
@@ -308,6 +310,10 @@ struct Renderer {
     CacheSet cs[3];
     int last_cache_set = -1;              // the set of the last cache frame (its targets)
     vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
+    // per reservoir-ring slot: a 3-D tensor map (4*W floats x H rows x 5
+    // planes) for the TMA-staged spatial pass of a single view
+    CUtensorMap res_map[8];
+    bool res_map_ok = false;
 };
 
 }  // namespace vrg

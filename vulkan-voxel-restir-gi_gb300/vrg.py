@@ -21,7 +21,8 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libvrg.so")
+# VRG_LIBRARY names another build of the library (for A/B runs of builds)
+LIB_PATH = os.environ.get("VRG_LIBRARY") or os.path.join(HERE, "libvrg.so")
 
 CHUNK = 32
 CHUNK_BLOCKS = 32 * 32 * 32
@@ -33,7 +34,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_NOT_FOUND, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_UNSUPP
 MODE_PARITY, MODE_CONFIG = 0, 1
 MAT_TRANSLUCENT = 1
 RENDER_CAPTURE, RENDER_NO_PACK, RENDER_CACHE, RENDER_PLAIN_ONLY, RENDER_GRAPH = 1, 2, 4, 8, 16
-NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS = range(5)
+NRC_WEIGHTS, NRC_WEIGHT_GRADS, NRC_TABLE, NRC_TABLE_GRADS, NRC_ZERO_GRADS, NRC_TRAIN_PREDICTIONS = range(6)
 (DBG_ORIGIN, DBG_DIRECTION, DBG_NORMAL, DBG_EMISSIVITY, DBG_REFLECTIVITY, DBG_MIS, DBG_BSDF_PDF,
  DBG_NEE_PDF, DBG_RADIANCE, DBG_Q, DBG_HIT, DBG_TEMPORAL, DBG_SPATIAL, DBG_FINAL, DBG_CACHE_TARGET) = range(15)
 
@@ -85,14 +86,18 @@ class NrcDesc(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("log2_table", C.c_uint32), ("features", C.c_uint32),
                 ("base_resolution", C.c_uint32), ("max_resolution", C.c_uint32), ("batch", C.c_uint32),
                 ("learning_rate", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
-                ("scene_max", C.c_float * 3)]
+                ("scene_max", C.c_float * 3), ("flags", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+NRC_TRAIN_WARP_MMA = 1
 
 
 class Tuning(C.Structure):
     """Launch configuration (scheduling only); 0 fields mean the default."""
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill", C.c_uint32),
                 ("shade_blocks_per_sm", C.c_uint32), ("anyhit_blocks_per_sm", C.c_uint32),
-                ("anyhit_refill", C.c_uint32), ("stream_block", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("anyhit_refill", C.c_uint32), ("stream_block", C.c_uint32), ("spatial_staging", C.c_uint32),
+                ("reserved", C.c_uint32 * 1)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -721,11 +726,11 @@ class RadianceCache:
     """Neural radiance cache (no reference counterpart): hash grid + 5x64 MLP."""
 
     def __init__(self, ctx: Context, scene_min, scene_max, levels=16, log2_table=19, base_resolution=16,
-                 max_resolution=2048, batch=65536, learning_rate=1e-2, seed=1):
+                 max_resolution=2048, batch=65536, learning_rate=1e-2, seed=1, flags=0):
         self.ctx = ctx
         self.levels, self.log2_table = levels, log2_table
         d = NrcDesc(levels, log2_table, 2, base_resolution, max_resolution, batch, learning_rate, seed,
-                    (C.c_float * 3)(*scene_min), (C.c_float * 3)(*scene_max))
+                    (C.c_float * 3)(*scene_min), (C.c_float * 3)(*scene_max), flags, 0)
         self.h = C.c_void_p()
         check(ctx.lib.vrg_nrc_create(ctx.h, C.byref(d), C.byref(self.h)), "vrg_nrc_create")
         ctx.adopt(self)
@@ -743,7 +748,14 @@ class RadianceCache:
         loss = C.c_float()
         check(self.ctx.lib.vrg_nrc_train(self.h, len(pos), _ptr(pos), _ptr(normal), _ptr(direction), _ptr(target),
                                          1 if update else 0, C.byref(loss)), "vrg_nrc_train")
+        self._last_train_n = len(pos)
         return loss.value
+
+    def train_predictions(self):
+        """The last train() batch's outputs from the training pass's own forward pass (n x 3)."""
+        out = np.zeros((self._last_train_n, 3), np.float32)
+        check(self.ctx.lib.vrg_nrc_read(self.h, NRC_TRAIN_PREDICTIONS, _ptr(out), out.nbytes), "vrg_nrc_read")
+        return out
 
     def read(self, what):
         n = NRC_MASTER if what in (NRC_WEIGHTS, NRC_WEIGHT_GRADS) else self.levels * (1 << self.log2_table) * 2
