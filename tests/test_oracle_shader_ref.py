@@ -1,0 +1,94 @@
+"""Pins the oracle's frame against a second restatement of the reference's
+shaders (tests/py_shader_ref.py, written from the GLSL, not from the oracle):
+on a two-chunk terrain world, four frames through the reservoir ring (the
+fourth reuses the first frame's slot), every
+captured slice (per-bounce origin, direction, normal, emissivity,
+reflectivity, MIS weight, BSDF pdf, NEE pdf, outgoing radiance, sampling pdf;
+the temporal and spatial reservoirs; the ReSTIR target; the packed image)
+bit for bit.  The chunk meshes, light BLASes and light TL of the restatement
+are checked against the oracle's first."""
+import numpy as np
+import pytest
+
+import py_shader_ref as ref
+import vrg
+from helpers import params
+from test_gpu_mesh import look_at
+
+pytestmark = pytest.mark.filterwarnings("ignore::RuntimeWarning")  # the reference's 0/0 NaNs
+
+W, H, NB = 28, 18, 3
+
+
+def _bits_equal(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    same = a.view(np.uint32) == b.view(np.uint32)
+    same |= np.isnan(a) & np.isnan(b)
+    return int((~same).sum())
+
+
+@pytest.fixture(scope="module")
+def worlds(orc):
+    mats, n = orc.terrain_materials(17)
+    blocks = orc.terrain_blocks(17, 2, 1, 0.15)
+    OW = orc.build_world(mats, n, blocks)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, np.uint8)
+    chunks = []
+    for cx in range(2):
+        c = ref.Chunk(blocks[cx, 0], vrg.chunk_neighbours(blocks, cx, 0, floor), mats, n)
+        chunks.append((c, (32 * cx, 0, 0)))
+    PW = ref.World(chunks, mats)
+    yield OW, PW
+    OW.close()
+
+
+def test_meshes_and_light_trees_match(worlds):
+    OW, PW = worlds
+    n_light = 0
+    for key, (c, _) in enumerate(PW.inst):
+        info = OW.chunk_info(key)
+        assert info["triangles"] == len(c.tris) and info["light_triangles"] == c.n_light
+        nodes, _ = OW.chunk_bvh(key, 0)
+        if c.n_light:
+            assert nodes.tobytes() == c.light_nodes.tobytes(), key
+        n_light += c.n_light
+    assert n_light >= 200  # lamps enough for deep descents and many NEE hits
+    assert OW.read_tl(0).tobytes() == PW.light_tl.tobytes()
+
+
+def test_frames_match_the_shader_restatement(orc, worlds):
+    OW, PW = worlds
+    orr = orc.Renderer(W, H, NB)
+    history = ref.empty_history(W * H)
+    n_nee = n_lamp_dirs = n_merged = 0
+    try:
+        for f, (nee, view) in enumerate([(1, 1), (2, 0), (1, 2), (1, 1)]):
+            cam = look_at((10.0 + 14 * f, 34.0, -14.0), (30.0 + 2 * f, 16.0, 18.0), W, H)
+            p = params(nee=nee, view=view, spatial=5, nb=NB, seeds=(f, 40 + 7 * f, 90 + 3 * f))
+            orr.render(OW, cam, p)
+            hit = orr.readback(vrg.DBG_HIT, NB)
+            hits = [[None if hit[b, q, 0] >= 0xFFFFFFFE else (int(hit[b, q, 0]), int(hit[b, q, 1]))
+                     for q in range(W * H)] for b in range(NB)]
+            out = ref.render(PW, cam, p, hits, f, history)
+            diffs = {}
+            for what, key in [(vrg.DBG_ORIGIN, "origin"), (vrg.DBG_DIRECTION, "direction"),
+                              (vrg.DBG_NORMAL, "normal"), (vrg.DBG_EMISSIVITY, "emissivity"),
+                              (vrg.DBG_REFLECTIVITY, "reflectivity"), (vrg.DBG_MIS, "mis"),
+                              (vrg.DBG_BSDF_PDF, "bsdf_pdf"), (vrg.DBG_NEE_PDF, "nee_pdf"),
+                              (vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_Q, "q")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.array(out[key], np.float32))
+            for what, key in [(vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_SPATIAL, "spatial")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.stack([ref.reservoir_row(r) for r in out[key]]))
+            diffs["final"] = _bits_equal(orr.readback(vrg.DBG_FINAL, NB), np.array(out["final"], np.float32))
+            img, _ = orr.image()
+            diffs["image"] = int((img != out["image"]).sum())
+            assert all(v == 0 for v in diffs.values()), f"frame {f}: {diffs}"
+            mis = np.array(out["mis"], np.float32)
+            n_lamp_dirs += int((mis > 0).sum())
+            n_nee += int((np.array(out["nee_pdf"], np.float32) > 0).sum())
+            n_merged += sum(s["m"] > t["m"] for s, t in zip(out["spatial"], out["temporal"]))
+        # the frames exercise the light descent, the reverse walk and the spatial merges
+        assert n_lamp_dirs > 1000 and n_nee > 300 and n_merged > 50, (n_lamp_dirs, n_nee, n_merged)
+    finally:
+        orr.close()

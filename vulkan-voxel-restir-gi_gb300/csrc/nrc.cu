@@ -1152,7 +1152,8 @@ struct Nrc {
     DevBufPtr enc_buf;  // encoded query rows of inference
     size_t enc_cap = 0;
     DevBufPtr pred_buf;  // the last host-array training batch's predictions
-    uint32_t pred_n = 0;
+    uint32_t pred_n = 0, pred_cap = 0;
+    cudaEvent_t ev_alloc = nullptr;  // orders a grown buffer between the context stream and its user
     // a cache frame's gradients wait for their Adam step, which the next user
     // of the cache runs first (a cache frame: beside its own bounces)
     bool pending = false;
@@ -1249,6 +1250,13 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
         delete N;
         return st;
     }
+    if (cudaEventCreateWithFlags(&N->ev_alloc, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        N->ev_alloc = nullptr;
+        delete N;
+        set_error("cudaEventCreateWithFlags failed");
+        return VRG_ERR_CUDA;
+    }
     uint8_t *B = (uint8_t *)N->buf->ptr;
     N->t_master = (float2 *)(B + o_tm);
     N->t_m = (float2 *)(B + o_t1);
@@ -1292,13 +1300,34 @@ vrg_status nrc_create(Context *ctx, const vrg_nrc_desc *d, Nrc **out) {
     return VRG_OK;
 }
 
+// Grows one of the cache's scratch buffers for use on stream s.  The buffer
+// lives on the context's stream, not on s: a cache frame trains on a
+// renderer's stream, and the renderer (with its streams) may be destroyed
+// before the cache frees the buffer.  The context stream frees the buffer
+// being replaced after s's earlier work (its last reader) and s waits for the
+// new allocation (and its zero fill, when asked).
+static vrg_status cache_alloc(Nrc *N, cudaStream_t s, size_t bytes, bool zero, DevBufPtr &buf) {
+    cudaStream_t cs = N->ctx->stream;
+    if (s != cs) {
+        VRG_CUDA_TRY(cudaEventRecord(N->ev_alloc, s));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(cs, N->ev_alloc, 0));
+    }
+    DevBufPtr b;
+    VRG_TRY(dev_alloc(cs, bytes, b));
+    if (zero) VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, bytes, cs));
+    buf = b;
+    if (s != cs) {
+        VRG_CUDA_TRY(cudaEventRecord(N->ev_alloc, cs));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(s, N->ev_alloc, 0));
+    }
+    return VRG_OK;
+}
+
 vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, const uint32_t *list,
                      const float4 *pos, const float4 *dir, const float4 *nrm, float4 *out, uint32_t *err) {
     if (n == 0) return VRG_OK;
-    if (N->enc_cap < n) {  // grows on the stream it is used on (stream-ordered allocation)
-        DevBufPtr b;
-        VRG_TRY(dev_alloc(s, (size_t)(N->P.levels + 2) * n * 4, b));
-        N->enc_buf = b;
+    if (N->enc_cap < n) {
+        VRG_TRY(cache_alloc(N, s, (size_t)(N->P.levels + 2) * n * 4, false, N->enc_buf));
         N->enc_cap = n;
     }
     InferArgs a{N->P, N->table, N->wpack, n, n_dev, list, pos, dir, nrm, out, err ? err : N->err,
@@ -1313,12 +1342,11 @@ vrg_status nrc_infer(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
     return VRG_OK;
 }
 
-static vrg_status ensure_act(Nrc *N, size_t rows) {
+static vrg_status ensure_act(Nrc *N, cudaStream_t s, size_t rows) {
     const size_t n_pad = (rows + 31) & ~(size_t)31;
     if (N->act && N->act_rows >= n_pad) return VRG_OK;
     DevBufPtr b;
-    VRG_TRY(dev_alloc(N->ctx->stream, 2 * 6 * n_pad * NRC_W * 2, b));
-    VRG_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, 2 * 6 * n_pad * NRC_W * 2, N->ctx->stream));
+    VRG_TRY(cache_alloc(N, s, 2 * 6 * n_pad * NRC_W * 2, true, b));
     N->act = b;
     N->act_rows = n_pad;
     N->H = (__nv_bfloat16 *)b->ptr;
@@ -1333,7 +1361,7 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
                      uint32_t *err, float4 *pred) {
     if (n == 0) return VRG_OK;
     VRG_TRY(nrc_flush(N, s));  // new gradients start from the updated cache
-    VRG_TRY(ensure_act(N, n));
+    VRG_TRY(ensure_act(N, s, n));
     const size_t n_pad = N->act_rows;
     // H and dZ hold n_pad rows per layer (the allocation, possibly made for a
     // larger batch): the training pass writes and k_nrc_dw reads with that pitch
@@ -1343,9 +1371,7 @@ vrg_status nrc_train(Nrc *N, cudaStream_t s, uint32_t n, const uint32_t *n_dev, 
         // the samples' encoded rows (the inference encoding pass), then the
         // tensor-memory training pass over 128-sample tiles
         if (N->train_enc_cap < n) {
-            DevBufPtr b;
-            VRG_TRY(dev_alloc(s, (size_t)(N->P.levels + 2) * n * 4, b));
-            N->train_enc_buf = b;
+            VRG_TRY(cache_alloc(N, s, (size_t)(N->P.levels + 2) * n * 4, false, N->train_enc_buf));
             N->train_enc_cap = n;
         }
         a.enc = (const uint32_t *)N->train_enc_buf->ptr;
@@ -1403,6 +1429,7 @@ uint32_t nrc_batch(const Nrc *N) { return N->desc.batch ? N->desc.batch : 65536u
 void nrc_destroy(Nrc *N) {
     if (!N) return;
     cudaStreamSynchronize(N->ctx->stream);
+    if (N->ev_alloc) cudaEventDestroy(N->ev_alloc);
     Context *c = N->ctx;
     delete N;  // its buffers are freed on the context's stream, before the context may go
     ctx_release(c);
@@ -1454,9 +1481,9 @@ vrg_status nrc_train_host(Nrc *N, uint32_t n, const float *pos, const float *nrm
     VRG_TRY(stage4(s, nrm, n, 3, dn));
     VRG_TRY(stage4(s, target, n, 3, dt));
     VRG_CUDA_TRY(cudaMemsetAsync(N->loss, 0, 8, s));  // loss and error word
-    if (N->pred_n < n || !N->pred_buf) {
-        VRG_TRY(dev_alloc(s, (size_t)n * 16, N->pred_buf));
-        N->pred_n = n;
+    if (N->pred_cap < n) {
+        VRG_TRY(cache_alloc(N, s, (size_t)n * 16, false, N->pred_buf));
+        N->pred_cap = n;
     }
     N->pred_n = n;
     VRG_TRY(nrc_train(N, s, n, nullptr, nullptr, dp, dd, dn, dt, update != 0, nullptr, (float4 *)N->pred_buf->ptr));
