@@ -269,3 +269,44 @@ def test_plain_frames_equal_captured_frames(gpu_ctx, nb):
     scene.close()
     for o in objs:
         o.release()
+
+
+def test_axis_parallel_rays_bit_exact(gpu_ctx, orc):
+    """Cameras looking exactly along -z and +x: the middle row and column of
+    pixels get directions with a component of exactly 0 (parallel to the
+    block planes of that axis).  Bit for bit as
+    the oracle; and their primary rays walk about as many nodes as those of a
+    camera tilted off the axes (a zero component culls on its axis like any
+    other, instead of keeping every box that the other two axes cross)."""
+    from test_gpu_mesh import look_at
+    W, H = 64, 48  # even: row 24 has v = 0 and column 32 has u = 0 exactly
+    scene, objs, OW, gr, orr = _setup(gpu_ctx, orc, 31, 2, 2, 0.02, W, H, 3)
+    try:
+        # eye heights above the highest block (its top is at y = 23): the
+        # middle row's rays run level over the whole terrain without a hit
+        for f, (eye, target) in enumerate([((21.0, 26.0, 70.0), (21.0, 26.0, 0.0)),
+                                           ((-6.0, 26.5, 37.0), (60.0, 26.5, 37.0))]):
+            cam = look_at(eye, target, W, H)
+            p = params(nee=1, view=1, spatial=3, nb=3, seeds=(f, 50 + f, 90 + f))
+            img, rad, oimg, orad = _frame(scene, OW, gr, orr, cam, p)
+            diffs = compare_frame(gr, orr, 3)
+            assert all(v == 0 for v in diffs.values()), (f, diffs)
+            assert np.array_equal(img.reshape(-1), oimg.reshape(-1))
+            dirs = gr.readback(vrg.DBG_DIRECTION, 3)[0].reshape(H, W, 3)
+            assert (dirs[H // 2, :, 1] == 0).all() and (dirs[:, W // 2, 0 if f == 0 else 2] == 0).all()
+            assert gr.last_stats.error_flags == 0
+            # nodes per closest-hit ray against the same view tilted off the
+            # axes (a renderer of its own: the frame counter of gr stays in
+            # step with the oracle's)
+            per_ray = []
+            rs = vrg.Renderer(gpu_ctx, W, H, 2)
+            for tgt in (target, (target[0] + 0.37, target[1] + 0.41, target[2] + 0.29)):
+                rs.render_params(scene, look_at(eye, tgt, W, H), params(nee=1, nb=2, flags=vrg.RENDER_PLAIN_ONLY),
+                                 want_image=False, want_radiance=True)
+                st = rs.last_stats
+                assert st.error_flags == 0 and st.rays_closest >= W * H
+                per_ray.append(st.nodes_visited / st.rays_closest)
+            rs.close()
+            assert per_ray[0] < 1.25 * per_ray[1], per_ray
+    finally:
+        OW.close()

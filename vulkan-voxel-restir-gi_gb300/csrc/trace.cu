@@ -289,14 +289,14 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
 // far planes per axis, picked per ray by the sign of its direction (so the
 // per-axis min/max of the classic slab test is not needed).  For such a pick
 // the near distance of a non-empty box is <= its far distance, exactly, since
-// rounding is monotonic; a NaN distance (a ray parallel to an axis starting
-// on a box plane) is ignored by min/max, which only keeps more boxes: the test
-// stays conservative and the closest hit does not depend on it.  An unused
+// rounding is monotonic; a NaN distance (only possible for a direction
+// component below 1e-30 in magnitude, whose inverse overflows) is ignored by
+// min/max, which only keeps more boxes: the test stays conservative and the
+// closest hit does not depend on it.  A component of exactly 0 has the finite
+// inverse +-1e30 (slab_inv), so that axis culls like any other.  An unused
 // slot holds the inverted box lo = +inf, hi = -inf: on an axis with a finite
-// inverse direction its near distance is +inf; on an axis the ray is parallel
-// to, the near distance is +inf, or the far distance -inf, or both are NaN
-// (origin on 0) and the axis is ignored; and a unit direction has at least one
-// finite axis.  So the slot is never entered and needs no test of its ref.
+// inverse its near distance is +inf, so the slot is never entered and needs
+// no test of its ref.
 __device__ __forceinline__ void slab4(float4 NX, float4 FX, float4 NY, float4 FY, float4 NZ, float4 FZ, float4 RF,
                                       f3 inv, f3 oi, float tmin, float tmax, float tk[4], int rk[4]) {
     const float nx[4] = {NX.x, NX.y, NX.z, NX.w}, fx[4] = {FX.x, FX.y, FX.z, FX.w};
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
                     }
                     if (b == 0) raygen(V, p - V.pix_off, o, d);
                     else { o = ld3(a.ray_o[p]); d = ld3(a.ray_d[p]); }
-                    inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                    inv = f3{slab_inv(d.x), slab_inv(d.y), slab_inv(d.z)};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
                     px = signbit(inv.x) ? 1 : 0;
                     py = signbit(inv.y) ? 3 : 2;
@@ -886,7 +886,7 @@ __global__ void __launch_bounds__(128, 8) k_anyhit(const __grid_constant__ Frame
                     o = ld3(ro);
                     d = ld3(rd);
                     pdf = rd.w;
-                    inv = f3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                    inv = f3{slab_inv(d.x), slab_inv(d.y), slab_inv(d.z)};
                     oi = f3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
                     px = signbit(inv.x) ? 1 : 0;
                     py = signbit(inv.y) ? 3 : 2;

@@ -166,11 +166,29 @@ struct FaceHit {
     int half;
     float b1, b2;
 };
+// The inverse direction of the traversal's slab tests and of face_test.  A
+// component of exactly 0 gets +-1e30 instead of +-inf.  With +-inf the FMA
+// form of the slab test, fma(plane, inv, -o * inv), is inf - inf = NaN on that
+// axis for every box, min/max ignore the NaN, and a ray parallel to an axis
+// plane entered every box that its other two axes cross: a Lambertian sample
+// whose normal component is exactly 0 (about one in 2^23) walked up to 44,000
+// nodes in the 32x32-chunk scene and held a whole bounce for ms.  With 1e30
+// that axis culls as (plane - o) * inf would.  The ray's coordinate on it is
+// constant, so a box that can hold a hit face has the origin at least
+// BOX_MARGIN - FACE_PAD inside its widened slab there: the distances on that
+// axis are beyond +-1e27 and the box is kept (the FMA rounding, about
+// |o| * 2^-24, is far below that depth).  A box whose slab lies wholly on one
+// side of the origin gets two distances of one sign, beyond +-1e27, and is
+// culled.  face_test rejects the faces of such an axis itself, as the true
+// inverse (t = +-inf or NaN) would.
+__host__ __device__ __forceinline__ float slab_inv(float d) { return d == 0.0f ? copysignf(1e30f, d) : 1.0f / d; }
+
 __host__ __device__ __forceinline__ bool face_test(int bx, int by, int bz, int f, f3 o, f3 d, f3 inv, float tmin,
                                                    float tmax, FaceHit &h) {
     int a, u, v;
     face_axes(f, a, u, v);
     int bc[3] = {bx, by, bz};
+    if (cmp3(d, a) == 0.0f) return false;  // parallel to the face: t = +-inf or NaN, no hit
     float c = (float)(bc[a] + (f & 1));
     float t = (c - cmp3(o, a)) * cmp3(inv, a);
     if (!(t >= tmin && t <= tmax)) return false;
