@@ -491,8 +491,9 @@ struct ShadeOut {
     int4 rc;
 };
 
-// need_dir false: the path ends at this vertex (its last bounce, no capture)
-// and only its emission reaches the image: the outgoing radiance of the last
+// need_dir false: the path ends at this vertex (its last bounce, or a cache
+// frame's query vertex of a path that does not train; no capture) and only
+// its emission (or the cache's prediction) reaches the image: the outgoing radiance of the last
 // vertex is E + (R * 0) * w = E for any finite R >= 0 and w > 0, and the
 // vertex position keeps its offset; the Lambertian continuation (light-BVH
 // descent and direction sampling) is skipped, with mis 0 and pdf 1.
@@ -677,8 +678,15 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
             }
             const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
             const int4 hv = a.hits[p];
+            // A cache frame's query vertex continues only on its training paths
+            // (one in 16): on the others the cache's prediction replaces the
+            // vertex's outgoing radiance, and its record, direction and light
+            // pdf are never read, so they skip the continuation as a last
+            // vertex does.
+            if (at_query) want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
             ShadeOut so;
-            shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv, CAPTURE || b + 1 < nb, so);
+            shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv,
+                               CAPTURE || (b + 1 < nb && (!at_query || want_train)), so);
             const f3 n = so.n, E = so.E;
             f3 R = so.R;
             const float mis = so.mis;
@@ -702,7 +710,6 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                     a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z,
                                              face >= 0 ? __int_as_float(face) : __uint_as_float(pack_normal10(so.n)));
                     a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
-                    want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
                 }
             }
             // stash for the second half (after the warp-level training-slot grant)
