@@ -642,18 +642,17 @@ def run_ours(args, d):
     # frames are in flight together as in an interactive loop), bracketed by
     # CUDA events on the library's own stream with a synchronize on both sides.
     blob = r.save_state()  # the breakdown pass below replays the same frames from here
-    torch.cuda.synchronize()
-    d.barrier()
     clk = ClockSampler(d.local)
     clk.start()
     time.sleep(0.25)  # the sampler's first reading lands before the region
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the W warm-up frames again right before the region, so that the GPU does
+    # not enter it from the idle wait above; then a synchronize and a barrier
     w0 = time.perf_counter()
-    # the W warm-up frames again, back to back right before the region (no
-    # synchronize after them): the region starts with frames in flight and the
-    # clocks up, as in a running interactive loop, not from an idle GPU
     for s in range(args.warmup):
         render(s, out_dev, None)
+    torch.cuda.synchronize()
+    d.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(lib_stream)
     for s in range(args.steps):
         render(args.warmup + s, out_dev, None)
@@ -810,9 +809,9 @@ def run_ours(args, d):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded value-noise voxel terrain, no dataset)",
         "config": headline_config(args.gpus),
-        "timing": "W warm-up frames then K frames enqueued back to back on the library stream (frames in "
-                  "flight), CUDA events on that stream around the K; ray counts and stage times from a replay "
-                  "of the same frames one at a time",
+        "timing": "K frames enqueued back to back on the library stream (frames in flight), bracketed by a "
+                  "synchronize and CUDA events on that stream (W warm-up frames just before); ray counts and stage "
+                  "times from a replay of the same frames one at a time",
         "ms_breakdown": {"bounce": [round(x / args.steps, 4) for x in ms_b],
                          "k_trace": [round(x / args.steps, 4) for x in ms_tr],
                          "k_shade": [round(x / args.steps, 4) for x in ms_sh],
