@@ -986,7 +986,7 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
             auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
             struct Off {
                 size_t qp, qd, pr, tg, il, tl, qf, taq0, taq1, taj0, taj1, thb, thv, tjm;
-            } off[3];
+            } off[Renderer::SETS];
             size_t o = 0;
             for (uint32_t k = 0; k < r->n_sets; k++) {
                 Off &q = off[k];

@@ -307,7 +307,7 @@ struct Renderer {
         float *t_hitval = nullptr;
         uint2 *t_jmeta = nullptr;
     };
-    CacheSet cs[3];
+    CacheSet cs[SETS];
     int last_cache_set = -1;              // the set of the last cache frame (its targets)
     vrg_tuning tune{};                    // launch configuration (0 fields = defaults)
     // per reservoir-ring slot: a 3-D tensor map (4*W floats x H rows x 5
