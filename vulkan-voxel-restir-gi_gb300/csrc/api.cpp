@@ -1159,9 +1159,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     // of small latency-bound launches which persistent bounce kernels beside
     // it would hold off the SMs (1080p, 8x8 chunks: 2.07 ms per frame in
     // flight with the wait, 2.20 without, 2.11 one at a time).  A batched
-    // frame's bounces are long enough to hide the branch (four 3840x2160
-    // views: 19.2 ms per frame without the wait, 23.8 with it, 20.3 one at a
-    // time).
+    // frame's bounces are long enough to hide the branch: four 3840x2160
+    // views of the 32x32-chunk scene take 15.6-15.7 ms per frame in flight
+    // with the wait and without it, so batched frames do not wait.
     if (own && fork && !a.views) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_join, 0));
     // a cache frame runs the previous cache frame's Adam step on the training
     // stream beside its own bounces (after all earlier work on the library
