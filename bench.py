@@ -799,7 +799,7 @@ def run_ours(args, d):
     if not args.no_large:
         # the large workload, compact: a 256-spp ground truth (the full
         # 4096-spp run is --workload large) and 6 frames per method
-        large = large_block(ctx, steps=6, warmup=3, gt_spp=args.large_gt_spp)
+        large = large_block(ctx, steps=16, warmup=3, gt_spp=args.large_gt_spp)
         ctx.set_materials(mats, n)
     upd_ms = update_commit_ms(scene, NX, NZ)
     cpu_frames = args.cpu_frames
