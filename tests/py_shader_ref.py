@@ -19,19 +19,27 @@ Covered, per pixel (file:line in src/render_system/):
   finalize                       shader/restir_finalize.rs:121-141
   postprocess (scale 1)          shader/postprocess.rs:39-88
 and the chunk mesh order of game_system/chunk.rs:158-292, the light BLAS of
-scene.rs:547-571 and the light TL of scene.rs:248-287 (built with the
-independent builder restatement of tests/py_build_ref.py).
+scene.rs:547-571 (upload_object, for chunk meshes and for uploaded triangle
+meshes alike), the light TL of scene.rs:248-287 over instances placed by
+translations or full isometries (Aabb::transform, bvh/aabb.rs:75-92; built
+with the independent builder restatement of tests/py_build_ref.py), and the
+per-instance transform of triangles and light-BVH nodes (triangleTransform,
+raytrace.rs:155-159; nodeImportance, raytrace.rs:181-208).
 
-Two things have no reference definition and follow this project's documented
-choices: which voxel face a ray hits (the ray query is the driver's; the hit
-triangle of each bounce is taken from the frame under test, its barycentrics
-recomputed from the face geometry), and sin/cos(2*pi*u) (the quarter-turn
-reduction with Taylor polynomials).  GLSL built-ins evaluate left to right:
+Four things have no reference definition and follow this project's
+documented choices: which triangle a ray hits (the ray query is the
+driver's; the hit of each bounce is taken from the frame under test, its
+barycentrics recomputed: from the face geometry for a voxel face, by the
+watertight test of tests/py_tri_ref.py for a mesh triangle), the arithmetic
+of an isometry (the 3x4 matrix form ((r0 x + r1 y) + r2 z) + t, or p + t for
+a translation), and sin/cos(2*pi*u) (the quarter-turn reduction with Taylor
+polynomials).  GLSL built-ins evaluate left to right:
 dot = (x*x' + y*y') + z*z', normalize(v) = v / length(v).
 """
 import numpy as np
 
 import py_build_ref
+import py_tri_ref
 
 F = np.float32
 M32 = 0xFFFFFFFF
@@ -90,6 +98,37 @@ def is_zero(a):
 
 def luminance(c):  # restir_*.rs luminance()
     return (F(0.2126) * c[0] + F(0.7152) * c[1]) + F(0.0722) * c[2]
+
+
+# ---- instance transforms ---------------------------------------------------
+def xform(m=None, translation=None):
+    """(3x4 row-major matrix as float32 scalars, translation only)."""
+    if m is None:
+        t = [F(x) for x in (translation or (0, 0, 0))]
+        return ((F(1), F(0), F(0), t[0], F(0), F(1), F(0), t[1], F(0), F(0), F(1), t[2]), True)
+    m = tuple(F(x) for x in m)
+    tonly = m[0] == 1 and m[5] == 1 and m[10] == 1 and all(m[k] == 0 for k in (1, 2, 4, 6, 8, 9))
+    return (m, bool(tonly))
+
+
+IDENT = xform()
+
+
+def xf_point(X, p):
+    m, tonly = X
+    if tonly:
+        return (p[0] + m[3], p[1] + m[7], p[2] + m[11])
+    return (((m[0] * p[0] + m[1] * p[1]) + m[2] * p[2]) + m[3],
+            ((m[4] * p[0] + m[5] * p[1]) + m[6] * p[2]) + m[7],
+            ((m[8] * p[0] + m[9] * p[1]) + m[10] * p[2]) + m[11])
+
+
+def aabb_transform(mn, mx, X):
+    """Aabb::transform (bvh/aabb.rs:75-92): the AABB of the 8 transformed corners."""
+    c = [xf_point(X, (mx[0] if k & 4 else mn[0], mx[1] if k & 2 else mn[1], mx[2] if k & 1 else mn[2]))
+         for k in range(8)]
+    a = py_build_ref.Aabb.from_points(c)
+    return [*a.mn, *a.mx]
 
 
 # ---- murmur3 chaining (raygen.rs:37-78) ------------------------------------
@@ -169,6 +208,7 @@ class Chunk:
                 return int(blk[x, y, z])
             return air if nbs[f] is None else int(nbs[f][x % 32, y % 32, z % 32])
 
+        self.mesh = False
         self.tris = []
         for x in range(32):
             for y in range(32):
@@ -209,24 +249,72 @@ class Chunk:
         _, _, _, f, h, _ = self.tris[k]
         return [FACES[f][3 * h + j][1] for j in range(3)]
 
+    def slot(self, k):
+        return self.tris[k][5]
+
+
+class Mesh:
+    """upload_object of a Vec<Vertex3D> (scene.rs:547-571): triangle k is
+    vertices 3k..3k+2, its texture slot that of its first vertex; luminous
+    triangles (luminance of that slot > 0) make the light BLAS, power =
+    luminance * area, ids = triangle index."""
+
+    def __init__(self, vertices, mats):
+        pos = np.asarray(vertices["position"], np.float32).reshape(-1, 3, 3)
+        slots = np.asarray(vertices["t"], np.uint32)[0::3]
+        self.mesh = True
+        self.pos = [[tuple(F(x) for x in pos[k, j]) for j in range(3)] for k in range(len(pos))]
+        self.slots = [int(t) for t in slots]
+        lum, ltri, lid = [], [], []
+        for k, tri in enumerate(self.pos):
+            L = F(mats[self.slots[k]].luminance)
+            if L > 0:
+                a, b, c = tri
+                lum.append(L * (length(cross(sub(b, a), sub(c, a))) / F(2.0)))
+                ltri.append([*a, *b, *c])
+                lid.append(k)
+        self.n_light = len(lum)
+        self.light_nodes = None
+        if self.n_light:
+            self.light_nodes, _ = py_build_ref.build_bl_bvh(np.array(ltri, np.float32), np.array(lum, np.float32),
+                                                           np.array(lid, np.uint32))
+
+    def local_vertices(self, k):
+        return self.pos[k]
+
+    def slot(self, k):
+        return self.slots[k]
+
 
 class World:
-    """Instances in key order (scene.rs:245-260), translations only; the light
-    TL over the instances with lights (scene.rs:248-287)."""
+    """Instances in key order (scene.rs:245-260), each an object (Chunk or
+    Mesh) and its transform (xform()); the light TL over the instances with
+    lights (scene.rs:248-287): a translated instance's light AABB goes to the
+    builder with its translation, any other's is transformed first
+    (Aabb::transform) and goes with translation 0."""
 
-    def __init__(self, chunks_and_offsets, mats):
+    def __init__(self, instances, mats):
         self.mats = mats
-        self.inst = [(c, tuple(F(t) for t in off)) for c, off in chunks_and_offsets]
+        self.inst = []
+        for c, x in instances:
+            if isinstance(x, tuple) and len(x) == 2 and isinstance(x[1], bool):
+                self.inst.append((c, x))
+            else:
+                self.inst.append((c, xform(translation=x)))
         aabbs, pw, ids, tr = [], [], [], []
-        for i, (c, off) in enumerate(self.inst):
+        for i, (c, X) in enumerate(self.inst):
             if not c.n_light:
                 continue
             # build_bl_bvh's light_aabb and power are its root's (build.rs:362-371)
             root = c.light_nodes[0]
-            aabbs.append([*root["min"], *root["max"]])
+            if X[1]:
+                aabbs.append([*root["min"], *root["max"]])
+                tr.append((X[0][3], X[0][7], X[0][11]))
+            else:
+                aabbs.append(aabb_transform(root["min"], root["max"], X))
+                tr.append((F(0), F(0), F(0)))
             pw.append(root["power"])
             ids.append(i)
-            tr.append(off)
         self.tl_idx = {}
         if aabbs:
             self.light_tl, _ = py_build_ref.build_tl_bvh(np.array(aabbs, np.float32), np.array(pw, np.float32),
@@ -238,17 +326,18 @@ class World:
             self.light_tl = None
 
     def world_vertices(self, inst, tri):
-        c, off = self.inst[inst]
-        return [add(p, off) for p in c.local_vertices(tri)]
+        c, X = self.inst[inst]
+        return [xf_point(X, p) for p in c.local_vertices(tri)]
 
 
 # ---- light BVH (raytrace.rs:181-281, nee_pdf.rs:119-228) --------------------
-def node_importance(nee, point, normal, off, node):
-    """nodeImportance: the transform of a translated instance adds off to the
-    node's min and max; raytrace.rs counts visible corners as uint (EPS 1e-3),
-    nee_pdf.rs sums 0.125 per visible corner as float (EPS 1e-4)."""
-    v000 = add(v3(*node["min"]), off)
-    v111 = add(v3(*node["max"]), off)
+def node_importance(nee, point, normal, X, node):
+    """nodeImportance: v000 and v111 are the instance transform X applied to
+    the node's min and max (the corners are the box they span); raytrace.rs
+    counts visible corners as uint (EPS 1e-3), nee_pdf.rs sums 0.125 per
+    visible corner as float (EPS 1e-4)."""
+    v000 = xf_point(X, v3(*node["min"]))
+    v111 = xf_point(X, v3(*node["max"]))
     corners = [v000, (v000[0], v000[1], v111[2]), (v000[0], v111[1], v000[2]), (v000[0], v111[1], v111[2]),
                (v111[0], v000[1], v000[2]), (v111[0], v000[1], v111[2]), (v111[0], v111[1], v000[2]), v111]
     eps = EPS_NEE if nee else EPS_TRACE
@@ -273,23 +362,23 @@ def traverse_bvh(W, point, normal, seed):
     root = W.light_tl
     node = root[0]
     importance = F(0)
-    off = ZERO3
+    X = IDENT
     inst, idx, top = 0xFFFFFFFF, 0, True
     while True:
         if top and node["left"] == 0xFFFFFFFF:
             inst = int(node["right"])
-            c, off = W.inst[inst]
+            c, X = W.inst[inst]
             top = False
             root = c.light_nodes
             node = root[0]
             idx = 0
             if importance == 0:
-                importance = node_importance(False, point, normal, off, node)
+                importance = node_importance(False, point, normal, X, node)
         if not top and node["left"] == 0xFFFFFFFF:
             return True, inst, idx, importance
         li, ri = int(node["left"]), int(node["right"])
-        lI = node_importance(False, point, normal, off, root[li])
-        rI = node_importance(False, point, normal, off, root[ri])
+        lI = node_importance(False, point, normal, X, root[li])
+        rI = node_importance(False, point, normal, X, root[ri])
         total = lI + rI
         ln = lI / total
         if finalizef(seed) < ln:
@@ -300,7 +389,7 @@ def traverse_bvh(W, point, normal, seed):
 
 
 def reverse_traverse(W, point, normal, inst, leaf):
-    c, off = W.inst[inst]
+    c, X = W.inst[inst]
     root = c.light_nodes
     prob = F(1.0)
     top = False
@@ -318,12 +407,12 @@ def reverse_traverse(W, point, normal, inst, leaf):
                 return prob
             idx = int(tl_leaf["parent"])
             node = root[idx]
-            off = ZERO3
+            X = IDENT
         else:
             idx = int(node["parent"])
             node = root[idx]
-        lI = node_importance(True, point, normal, off, root[int(node["left"])])
-        rI = node_importance(True, point, normal, off, root[int(node["right"])])
+        lI = node_importance(True, point, normal, X, root[int(node["left"])])
+        rI = node_importance(True, point, normal, X, root[int(node["right"])])
         total = lI + rI
         prob = prob * (lI / total if old == int(node["left"]) else rI / total)
 
@@ -346,7 +435,8 @@ def face_hit(W, inst, tri, o, d, tmin, tmax):
     """(t, b1, b2) of the ray on triangle `tri` of instance `inst` — the plane
     hit of its face, the point inside the closed face square padded by 2^-12,
     on this triangle's side of the face diagonal — or None."""
-    c, off = W.inst[inst]
+    c, X = W.inst[inst]
+    off = (X[0][3], X[0][7], X[0][11])  # chunks are placed by translations
     x, y, z, f, h, _ = c.tris[tri]
     axis = f >> 1
     u_ax = 0 if axis != 0 else 1
@@ -379,6 +469,17 @@ def face_hit(W, inst, tri, o, d, tmin, tmax):
         bits = (a, b, cc)
         bary.append(weight(bits[u_ax], bits[v_ax]))
     return t, bary[0], bary[1]
+
+
+def hit_of(W, inst, tri, o, d, tmin, tmax):
+    """(t, b1, b2) of the ray on triangle `tri` of instance `inst`, or None: a
+    voxel face by face_hit, a mesh triangle by the watertight test on its
+    world-space vertices."""
+    c, _ = W.inst[inst]
+    if c.mesh:
+        t = W.world_vertices(inst, tri)
+        return py_tri_ref.tri_test([*t[0], *t[1], *t[2]], o, d, tmin, tmax)
+    return face_hit(W, inst, tri, o, d, tmin, tmax)
 
 
 # ---- the frame ---------------------------------------------------------------
@@ -429,7 +530,7 @@ def render(W, cam, params, hits, frame_index, history):
                 refl[b][p] = ZERO3
                 continue
             inst, tri = hit
-            th = face_hit(W, inst, tri, origin, direction, EPS_TRACE, F(1000.0))
+            th = hit_of(W, inst, tri, origin, direction, EPS_TRACE, F(1000.0))
             assert th is not None, (b, p, hit)
             _, b1, b2 = th
             b0 = (F(1.0) - b1) - b2
@@ -438,7 +539,7 @@ def render(W, cam, params, hits, frame_index, history):
             e1, e2 = sub(t3[1], t3[0]), sub(t3[2], t3[0])
             n_raw = cross(e1, e2)
             n, tangent, bitangent = normalize(n_raw), normalize(e1), normalize(cross(n_raw, e1))
-            slot = W.inst[inst][0].tris[tri][5]
+            slot = W.inst[inst][0].slot(tri)
             m = W.mats[slot]
             new_o = add(add(vs(t3[0], b0), vs(t3[1], b1)), vs(t3[2], b2))
             R = v3(*m.reflectivity)
@@ -496,7 +597,7 @@ def render(W, cam, params, hits, frame_index, history):
                 for leaf, node in enumerate(c.light_nodes):
                     if node["left"] != 0xFFFFFFFF:
                         continue
-                    th = face_hit(W, i, int(node["right"]), org, d, EPS_NEE, F(1000.0))
+                    th = hit_of(W, i, int(node["right"]), org, d, EPS_NEE, F(1000.0))
                     if th is not None:
                         hits_l.append(((i << 32) | leaf, compute_nee_pdf(W, org, n, d, i, leaf, th[1], th[2])))
             total = F(0.0)

@@ -92,3 +92,71 @@ def test_frames_match_the_shader_restatement(orc, worlds):
         assert n_lamp_dirs > 1000 and n_nee > 300 and n_merged > 50, (n_lamp_dirs, n_nee, n_merged)
     finally:
         orr.close()
+
+
+def test_meshes_and_isometries_match_the_shader_restatement(orc):
+    """Two terrain chunks, the reference's unit cube with an emissive block's
+    slots turned and lifted above them, and two triangle soups of mixed slots
+    (one translated, one rotated): the light BLASes and the light TL over
+    transformed light AABBs, then three frames through the ring, every slice
+    bit for bit against the restatement (the mesh hits' barycentrics from the
+    watertight test, the isometries in their matrix form)."""
+    from test_gpu_mesh import iso, soup, unitcube
+    mats, n = orc.terrain_materials(17)
+    blocks = orc.terrain_blocks(17, 2, 1, 0.05)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, np.uint8)
+    rng = np.random.default_rng(23)
+    meshes = [(1000, unitcube(6), iso(0.5, 0.3, (20.25, 27.5, 14.75))),
+              (1001, soup(rng, 60, 0, 22, (40.0, 24.0, 10.0), 6.0), (1.5, 0.0, -2.0)),
+              (1002, soup(rng, 40, 0, 22, (0.0, 0.0, 0.0), 4.0), iso(1.1, -0.4, (30.0, 26.0, 5.0)))]
+    OW = orc.World(mats, n)
+    try:
+        insts = []
+        for cx in range(2):
+            nb_ = vrg.chunk_neighbours(blocks, cx, 0, floor)
+            OW.add_chunk(cx, blocks[cx, 0], nb_, (32 * cx, 0, 0))
+            insts.append((ref.Chunk(blocks[cx, 0], nb_, mats, n), (32 * cx, 0, 0)))
+        for key, verts, m in meshes:
+            OW.add_mesh(key, verts, m)
+            mm = np.asarray(m, np.float32)
+            X = ref.xform(translation=tuple(mm)) if mm.size == 3 else ref.xform(m=mm.reshape(-1))
+            insts.append((ref.Mesh(verts, mats), X))
+        OW.commit()
+        PW = ref.World(insts, mats)
+        for key, (c, _) in enumerate(PW.inst):
+            if c.n_light:
+                okey = key if key < 2 else meshes[key - 2][0]
+                nodes, _ = OW.chunk_bvh(okey, 0)
+                assert nodes.tobytes() == c.light_nodes.tobytes(), key
+        assert sum(c.n_light for c, _ in PW.inst if c.mesh) >= 12  # the cube and the soups' lamps
+        assert OW.read_tl(0).tobytes() == PW.light_tl.tobytes()
+        W_, H_ = 24, 16
+        orr = orc.Renderer(W_, H_, NB)
+        history = ref.empty_history(W_ * H_)
+        mesh_hits = 0
+        for f in range(3):
+            cam = look_at((8.0 + 6 * f, 33.0, -6.0), (24.0 + 4 * f, 22.0, 14.0), W_, H_)
+            p = params(nee=1, view=1, spatial=4, nb=NB, seeds=(f, 60 + f, 70 + f))
+            orr.render(OW, cam, p)
+            hit = orr.readback(vrg.DBG_HIT, NB)
+            hits = [[None if hit[b, q, 0] >= 0xFFFFFFFE else (int(hit[b, q, 0]), int(hit[b, q, 1]))
+                     for q in range(W_ * H_)] for b in range(NB)]
+            mesh_hits += int(((hit[:, :, 0] >= 2) & (hit[:, :, 0] < 0xFFFFFFFE)).sum())
+            out = ref.render(PW, cam, p, hits, f, history)
+            diffs = {}
+            for what, key in [(vrg.DBG_ORIGIN, "origin"), (vrg.DBG_DIRECTION, "direction"),
+                              (vrg.DBG_NORMAL, "normal"), (vrg.DBG_EMISSIVITY, "emissivity"),
+                              (vrg.DBG_REFLECTIVITY, "reflectivity"), (vrg.DBG_MIS, "mis"),
+                              (vrg.DBG_BSDF_PDF, "bsdf_pdf"), (vrg.DBG_NEE_PDF, "nee_pdf"),
+                              (vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_Q, "q")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.array(out[key], np.float32))
+            for what, key in [(vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_SPATIAL, "spatial")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.stack([ref.reservoir_row(r) for r in out[key]]))
+            diffs["final"] = _bits_equal(orr.readback(vrg.DBG_FINAL, NB), np.array(out["final"], np.float32))
+            img, _ = orr.image()
+            diffs["image"] = int((img != out["image"]).sum())
+            assert all(v == 0 for v in diffs.values()), f"frame {f}: {diffs}"
+        assert mesh_hits >= 20, mesh_hits
+        orr.close()
+    finally:
+        OW.close()
