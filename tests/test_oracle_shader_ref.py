@@ -160,3 +160,50 @@ def test_meshes_and_isometries_match_the_shader_restatement(orc):
         orr.close()
     finally:
         OW.close()
+
+
+def test_mirror_and_glass_blocks_match_the_shader_restatement(orc):
+    """The same two chunks with three block types made metallic (0.7, 0.4) and
+    translucent (alpha 0.45, flagged see-through, so the faces behind them are
+    meshed): the mirror and transmission branches of raytrace.rs:482-499, two
+    frames bit for bit against the restatement."""
+    mats, n = orc.terrain_materials(17)
+    for b, metal, alpha, see in ((1, 0.7, 1.0, 0), (2, 0.4, 1.0, 0), (3, 0.0, 0.45, 1)):
+        for f in range(6):
+            mats[6 * b + f].metallic = metal
+            mats[6 * b + f].alpha = alpha
+            mats[6 * b + f].flags = (mats[6 * b + f].flags & ~1) | see
+    blocks = orc.terrain_blocks(17, 2, 1, 0.15)
+    OW = orc.build_world(mats, n, blocks)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, np.uint8)
+    try:
+        PW = ref.World([(ref.Chunk(blocks[cx, 0], vrg.chunk_neighbours(blocks, cx, 0, floor), mats, n),
+                         (32 * cx, 0, 0)) for cx in range(2)], mats)
+        orr = orc.Renderer(W, H, NB)
+        history = ref.empty_history(W * H)
+        specular = 0
+        for f in range(2):
+            cam = look_at((10.0 + 9 * f, 34.0, -14.0), (30.0 + 2 * f, 16.0, 18.0), W, H)
+            p = params(nee=1, view=1, spatial=4, nb=NB, seeds=(f, 20 + f, 30 + f))
+            orr.render(OW, cam, p)
+            hit = orr.readback(vrg.DBG_HIT, NB)
+            hits = [[None if hit[b, q, 0] >= 0xFFFFFFFE else (int(hit[b, q, 0]), int(hit[b, q, 1]))
+                     for q in range(W * H)] for b in range(NB)]
+            out = ref.render(PW, cam, p, hits, f, history)
+            diffs = {}
+            for what, key in [(vrg.DBG_ORIGIN, "origin"), (vrg.DBG_DIRECTION, "direction"),
+                              (vrg.DBG_EMISSIVITY, "emissivity"), (vrg.DBG_REFLECTIVITY, "reflectivity"),
+                              (vrg.DBG_MIS, "mis"), (vrg.DBG_BSDF_PDF, "bsdf_pdf"), (vrg.DBG_NEE_PDF, "nee_pdf"),
+                              (vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_Q, "q")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.array(out[key], np.float32))
+            for what, key in [(vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_SPATIAL, "spatial")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.stack([ref.reservoir_row(r) for r in out[key]]))
+            diffs["final"] = _bits_equal(orr.readback(vrg.DBG_FINAL, NB), np.array(out["final"], np.float32))
+            assert all(v == 0 for v in diffs.values()), f"frame {f}: {diffs}"
+            # hits taken by the mirror or the transmission branch: bsdf pdf 1 at a hit
+            pdf = orr.readback(vrg.DBG_BSDF_PDF, NB)
+            specular += int(((hit[:, :, 0] < 0xFFFFFFFE) & (pdf == 1.0)).sum())
+        assert specular >= 20, specular
+        orr.close()
+    finally:
+        OW.close()
