@@ -265,6 +265,7 @@ class Mesh:
         self.mesh = True
         self.pos = [[tuple(F(x) for x in pos[k, j]) for j in range(3)] for k in range(len(pos))]
         self.slots = [int(t) for t in slots]
+        self.uv = np.asarray(vertices["uv"], np.float32).reshape(-1, 3, 2)
         lum, ltri, lid = [], [], []
         for k, tri in enumerate(self.pos):
             L = F(mats[self.slots[k]].luminance)
@@ -282,6 +283,9 @@ class Mesh:
     def local_vertices(self, k):
         return self.pos[k]
 
+    def uvs(self, k):
+        return [tuple(self.uv[k, j]) for j in range(3)]
+
     def slot(self, k):
         return self.slots[k]
 
@@ -293,8 +297,13 @@ class World:
     builder with its translation, any other's is transformed first
     (Aabb::transform) and goes with translation 0."""
 
-    def __init__(self, instances, mats):
+    def __init__(self, instances, mats, atlas=None):
         self.mats = mats
+        # texture atlas: (slots, 3 maps, h, w, RGBA8 sRGB) and the sRGB EOTF
+        # of a texel byte (the maps are sampled as sRGB textures)
+        self.atlas = None if atlas is None else np.asarray(atlas, np.uint8)
+        self.srgb = [F(c / 12.92 if c <= 0.04045 else ((c + 0.055) / 1.055) ** 2.4)
+                     for c in (i / 255.0 for i in range(256))]
         self.inst = []
         for c, x in instances:
             if isinstance(x, tuple) and len(x) == 2 and isinstance(x[1], bool):
@@ -547,6 +556,21 @@ def render(W, cam, params, hits, frame_index, history):
             ndd = -dot(direction, n)
             E = vs(v3(*m.emission), ndd)
             metal = F(m.metallic)
+            if W.atlas is not None:
+                # raytrace.rs:457-480: uv = v0.uv*b0 + v1.uv*b1 + v2.uv*b2, the three
+                # maps of slot t sampled there (nearest texel, clamped to the edge)
+                uvs = [tuple(F(x) for x in q) for q in W.inst[inst][0].uvs(tri)]
+                u = ((uvs[0][0] * b0) + (uvs[1][0] * b1)) + (uvs[2][0] * b2)
+                v = ((uvs[0][1] * b0) + (uvs[1][1] * b1)) + (uvs[2][1] * b2)
+                ah, aw = W.atlas.shape[2], W.atlas.shape[3]
+                ix = min(max(int(np.floor(u * F(aw))), 0), aw - 1)
+                iy = min(max(int(np.floor(v * F(ah))), 0), ah - 1)
+                t0, t1, t2 = (W.atlas[slot, k, iy, ix] for k in range(3))
+                lin = W.srgb
+                R = (lin[t0[0]], lin[t0[1]], lin[t0[2]])
+                alpha = F(int(t0[3])) / F(255.0)
+                E = ((F(1000.0) * lin[t1[0]]) * ndd, (F(1000.0) * lin[t1[1]]) * ndd, (F(1000.0) * lin[t1[2]]) * ndd)
+                metal = lin[t2[0]]
             r0 = finalizef(combine(seed, 0))
             w_mis = F(0.0)
             if r0 < metal:
@@ -726,3 +750,19 @@ def reservoir_row(R):
     a[18] = np.array([R["m"]], np.uint32).view(np.float32)[0]
     a[19] = R["w_sum"]
     return a
+
+
+def atlas_luminances(atlas):
+    """get_texture_luminances (utils.rs:223-235): per slot, the float sum over
+    the emissivity map's texels of (r + g) + b, in texel order, divided by the
+    texel count."""
+    atlas = np.asarray(atlas, np.uint8)
+    n, _, h, w, _ = atlas.shape
+    out = []
+    for t in range(n):
+        e = atlas[t, 1].reshape(-1, 4)
+        L = F(0.0)
+        for r, g, b, _a in e:
+            L = L + ((F(int(r)) + F(int(g))) + F(int(b)))
+        out.append(L / F(w * h))
+    return out

@@ -207,3 +207,58 @@ def test_mirror_and_glass_blocks_match_the_shader_restatement(orc):
         orr.close()
     finally:
         OW.close()
+
+
+def test_texture_atlas_matches_the_shader_restatement(orc):
+    """Texture-atlas materials: three sRGB maps per slot sampled at the hit's
+    uv (raytrace.rs:457-480), emission 1000 x the emissivity map, the light
+    powers from the maps' luminances (get_texture_luminances, utils.rs:223-235),
+    a mirror block type and a glass one.  Two frames bit for bit against the
+    restatement."""
+    import copy
+    from test_gpu_render import _atlas
+    rng = np.random.default_rng(77)
+    mats, n = orc.terrain_materials(6)
+    blocks = orc.terrain_blocks(6, 2, 1, 0.05)
+    blocks[blocks == 2] = 0  # more mirror blocks
+    blocks[blocks == 3] = 1  # and glass
+    mats[6].flags = vrg.MAT_TRANSLUCENT  # block type 1 (slots 6..11) is glass
+    atlas = _atlas(rng, mats, n // 6)
+    floor = np.zeros(vrg.CHUNK_BLOCKS, np.uint8)
+    OW = orc.World(mats, n)
+    OW.set_atlas(atlas)
+    for cx in range(2):
+        OW.add_chunk(cx, blocks[cx, 0], vrg.chunk_neighbours(blocks, cx, 0, floor), (32 * cx, 0, 0))
+    OW.commit()
+    try:
+        pm = copy.deepcopy(mats)  # the restatement's materials with the atlas luminances
+        for t, L in enumerate(ref.atlas_luminances(atlas)):
+            pm[t].luminance = float(L)
+        PW = ref.World([(ref.Chunk(blocks[cx, 0], vrg.chunk_neighbours(blocks, cx, 0, floor), pm, n),
+                         (32 * cx, 0, 0)) for cx in range(2)], pm, atlas=atlas)
+        assert OW.read_tl(0).tobytes() == PW.light_tl.tobytes()
+        orr = orc.Renderer(W, H, NB)
+        history = ref.empty_history(W * H)
+        for f in range(2):
+            cam = look_at((10.0 + 9 * f, 34.0, -14.0), (30.0 + 2 * f, 16.0, 18.0), W, H)
+            p = params(nee=1, view=1, spatial=4, nb=NB, seeds=(f, 20 + f, 30 + f))
+            orr.render(OW, cam, p)
+            hit = orr.readback(vrg.DBG_HIT, NB)
+            hits = [[None if hit[b, q, 0] >= 0xFFFFFFFE else (int(hit[b, q, 0]), int(hit[b, q, 1]))
+                     for q in range(W * H)] for b in range(NB)]
+            out = ref.render(PW, cam, p, hits, f, history)
+            diffs = {}
+            for what, key in [(vrg.DBG_ORIGIN, "origin"), (vrg.DBG_DIRECTION, "direction"),
+                              (vrg.DBG_EMISSIVITY, "emissivity"), (vrg.DBG_REFLECTIVITY, "reflectivity"),
+                              (vrg.DBG_MIS, "mis"), (vrg.DBG_BSDF_PDF, "bsdf_pdf"), (vrg.DBG_NEE_PDF, "nee_pdf"),
+                              (vrg.DBG_RADIANCE, "radiance"), (vrg.DBG_Q, "q")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.array(out[key], np.float32))
+            for what, key in [(vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_SPATIAL, "spatial")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.stack([ref.reservoir_row(r) for r in out[key]]))
+            diffs["final"] = _bits_equal(orr.readback(vrg.DBG_FINAL, NB), np.array(out["final"], np.float32))
+            img, _ = orr.image()
+            diffs["image"] = int((img != out["image"]).sum())
+            assert all(v == 0 for v in diffs.values()), f"frame {f}: {diffs}"
+        orr.close()
+    finally:
+        OW.close()
