@@ -17,7 +17,8 @@ Covered, per pixel (file:line in src/render_system/):
   temporal resampling            shader/restir_temporal_resampling.rs:256-301
   spatial resampling             shader/restir_spatial_resampling.rs:316-406
   finalize                       shader/restir_finalize.rs:121-141
-  postprocess (scale 1)          shader/postprocess.rs:39-88
+  postprocess (scale 1, and srcscale > 1 in postprocess_scaled)
+                                 shader/postprocess.rs:39-88
 and the chunk mesh order of game_system/chunk.rs:158-292, the light BLAS of
 scene.rs:547-571 (upload_object, for chunk meshes and for uploaded triangle
 meshes alike), the light TL of scene.rs:248-287 over instances placed by
@@ -766,3 +767,25 @@ def atlas_luminances(atlas):
             L = L + ((F(int(r)) + F(int(g))) + F(int(b)))
         out.append(L / F(w * h))
     return out
+
+
+def postprocess_scaled(view, scale):
+    """postprocess.rs:39-88 with srcscale = scale, dstscale = 1: each output
+    pixel the sum of its scale x scale source samples (rows outer, columns
+    inner, from vec3(0.0)) divided by float(scale*scale), then u8(bgr*255)."""
+    view = np.asarray(view, np.float32)
+    H, W = view.shape[:2]
+    oh, ow = H // scale, W // scale
+    img = np.zeros((oh, ow, 4), np.uint8)
+    out = np.zeros((oh, ow, 3), np.float32)
+    n = F(scale * scale)
+    for oy in range(oh):
+        for ox in range(ow):
+            c = ZERO3
+            for sy in range(scale):
+                for sx in range(scale):
+                    c = add(c, tuple(view[oy * scale + sy, ox * scale + sx]))
+            c = (c[0] / n, c[1] / n, c[2] / n)
+            out[oy, ox] = c
+            img[oy, ox] = (to_u8(c[2]), to_u8(c[1]), to_u8(c[0]), 255)
+    return img, out

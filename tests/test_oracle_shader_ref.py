@@ -262,3 +262,17 @@ def test_texture_atlas_matches_the_shader_restatement(orc):
         orr.close()
     finally:
         OW.close()
+
+
+@pytest.mark.parametrize("scale", [2, 3])
+def test_supersampled_postprocess_matches_the_restatement(orc, scale):
+    """postprocess.rs:39-88 at srcscale 2 and 3 on random view colours (values
+    outside 0..1, zeros and a NaN among them), bit for bit."""
+    rng = np.random.default_rng(scale)
+    view = (rng.random((6 * scale, 8 * scale, 3)) * 1.6 - 0.3).astype(np.float32)
+    view[0, 0] = 0.0
+    view[1, 2, 1] = np.nan
+    img, out = orc.postprocess_scaled(view, scale)
+    rimg, rout = ref.postprocess_scaled(view, scale)
+    assert np.array_equal(img, rimg)
+    assert _bits_equal(out, rout) == 0
