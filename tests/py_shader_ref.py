@@ -645,8 +645,12 @@ def render(W, cam, params, hits, frame_index, history):
                nee_pdf=nee, radiance=Lo, q=q)
     if nb < 2:
         return out
-    # initial sample (interactive_rendering.rs:1359-1414); the seed is never written
-    ring = history[frame_index % 3]
+    # initial sample (interactive_rendering.rs:1359-1414); the seed is never written.
+    # The ring of temporal reservoirs has params.history_slots slots (3 in the
+    # reference, frame % 3); CONFIG mode may cap the history's m (m_cap), scaling
+    # w_sum by m_cap / m after the reset test (this project's extension)
+    slots = params.history_slots if params.history_slots else 3
+    ring = history[frame_index % slots]
     radius = F(params.spatial_radius)  # spatialSearchRadius, 15 in the reference
     temporal = []
     for p in range(P):
@@ -655,6 +659,9 @@ def render(W, cam, params, hits, frame_index, history):
         ps = combine(params.temporal_seed, p)
         if finalizef(combine(ps, 0)) < F(0.4):
             R["w_sum"], R["m"] = F(0.0), 0
+        if params.mode == 1 and params.m_cap and R["m"] > params.m_cap:
+            R["w_sum"] = R["w_sum"] * (F(params.m_cap) / F(R["m"]))
+            R["m"] = params.m_cap
         w = luminance(S["l"]) / S["p_omega"]
         R["w_sum"] = R["w_sum"] + w
         R["m"] += 1
@@ -734,9 +741,9 @@ def to_u8(x):
     return 255 if v >= 255 else int(v)
 
 
-def empty_history(P):
+def empty_history(P, slots=3):
     z = dict(x_v=ZERO3, n_v=ZERO3, x_s=ZERO3, n_s=ZERO3, l=ZERO3, p_omega=F(0), seed=0)
-    return [[dict(z=dict(z), ucw=F(0), m=0, w_sum=F(0)) for _ in range(P)] for _ in range(3)]
+    return [[dict(z=dict(z), ucw=F(0), m=0, w_sum=F(0)) for _ in range(P)] for _ in range(slots)]
 
 
 def reservoir_row(R):

@@ -276,3 +276,33 @@ def test_supersampled_postprocess_matches_the_restatement(orc, scale):
     rimg, rout = ref.postprocess_scaled(view, scale)
     assert np.array_equal(img, rimg)
     assert _bits_equal(out, rout) == 0
+
+
+def test_config_mode_matches_the_shader_restatement(orc, worlds):
+    """The benchmark's CONFIG-mode parameters (a one-slot reservoir ring,
+    spatial radius 30) with the history capped at m = 2 so that the cap
+    applies within the frames: five frames at one camera, bit for bit."""
+    OW, PW = worlds
+    orr = orc.Renderer(W, H, NB)
+    history = ref.empty_history(W * H, 1)
+    capped = 0
+    try:
+        cam = look_at((10.0, 34.0, -14.0), (30.0, 16.0, 18.0), W, H)
+        for f in range(5):
+            p = params(nee=1, view=1, spatial=3, nb=NB, mode=vrg.MODE_CONFIG, seeds=(f, 50 + f, 60 + f),
+                       radius=30.0, m_cap=2, slots=1)
+            orr.render(OW, cam, p)
+            hit = orr.readback(vrg.DBG_HIT, NB)
+            hits = [[None if hit[b, q, 0] >= 0xFFFFFFFE else (int(hit[b, q, 0]), int(hit[b, q, 1]))
+                     for q in range(W * H)] for b in range(NB)]
+            out = ref.render(PW, cam, p, hits, f, history)
+            diffs = {}
+            for what, key in [(vrg.DBG_TEMPORAL, "temporal"), (vrg.DBG_SPATIAL, "spatial")]:
+                diffs[key] = _bits_equal(orr.readback(what, NB), np.stack([ref.reservoir_row(r) for r in out[key]]))
+            diffs["final"] = _bits_equal(orr.readback(vrg.DBG_FINAL, NB), np.array(out["final"], np.float32))
+            diffs["radiance"] = _bits_equal(orr.readback(vrg.DBG_RADIANCE, NB), np.array(out["radiance"], np.float32))
+            assert all(v == 0 for v in diffs.values()), f"frame {f}: {diffs}"
+            capped += sum(1 for t in out["temporal"] if t["m"] == 3)  # capped at 2, then this frame's sample
+        assert capped > 50, capped
+    finally:
+        orr.close()
