@@ -215,7 +215,7 @@ def trace_traffic_per_launch(pixels, bounces):
 
 
 C3_N = 8  # chunks per side of the learned-cache workload
-E2E_SLOTS = 3  # host image buffers of the end-to-end loop (frames in flight)
+E2E_SLOTS = 4  # host image buffers of the end-to-end loop (frames in flight)
 REF_MAX_FRAMES = 48  # full 1080p frames the reference arm times on the host cores
 
 C2_SEED = 20240602
