@@ -390,8 +390,9 @@ VRG_API vrg_status vrg_renderer_get_tuning(vrg_renderer *r, vrg_tuning *t);
  * descent, two passes).  Each candidate is timed as frames are rendered in
  * use: `frames` frames enqueued back to back (frames in flight), bracketed by
  * CUDA events on the library stream, after one untimed frame; the median of
- * three such runs, per frame.  Installs the fastest and returns it with its
- * time per frame.  The tuning frames do not count: the frame counter,
+ * three such runs, per frame.  A candidate that times faster than the current
+ * choice is timed again, beside the current choice, and taken only if it is
+ * still faster.  Installs the result and returns it with its time per frame.  The tuning frames do not count: the frame counter,
  * reservoir history and accumulation are restored afterwards.  Single-view
  * renderers; params must not carry VRG_RENDER_CACHE / CAPTURE / GRAPH (the
  * result applies to those frames as well). */

@@ -1731,8 +1731,21 @@ VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, cons
                 st = measure(t, &ms);
                 if (st != VRG_OK) break;
                 if (ms < cur_ms) {
-                    cur = t;
-                    cur_ms = ms;
+                    // A candidate that timed faster is timed again beside the
+                    // current choice before it is taken: out of dozens of
+                    // noisy timings some come out low by chance, and such a
+                    // configuration (often fewer closest-hit CTAs per SM)
+                    // then runs slower in use.
+                    float ms2 = 0.0f, cur2 = 0.0f;
+                    st = measure(t, &ms2);
+                    if (st == VRG_OK) st = measure(cur, &cur2);
+                    if (st != VRG_OK) break;
+                    if (ms2 < cur2) {
+                        cur = t;
+                        cur_ms = ms2;
+                    } else {
+                        cur_ms = cur2;
+                    }
                 }
             }
             if (st != VRG_OK) break;

@@ -665,8 +665,17 @@ done:
 // (raytrace.rs:405-577).  Rays whose light pdf is needed are queued for
 // k_anyhit; the others get their (E, w) (R, q) record here.
 // ---------------------------------------------------------------------------
-template <bool CAPTURE, bool BATCH, bool MESH>
+constexpr uint32_t SHADE_BATCH = 4;  // queue entries per lane of a surface-first shading batch
+
+// the bounces whose shading takes its queue in surface-first batches (k_shade)
+__host__ __device__ __forceinline__ bool shade_split(const FrameArgs &a, uint32_t b) {
+    return b > 0 && b + 1 < a.nb && !(a.cache && b + 1 == a.nb_render);
+}
+
+template <bool CAPTURE, bool BATCH, bool MESH, bool SPLIT>
 __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameArgs a, uint32_t b) {
+    // per warp: the batch's pixels, surface hits first
+    __shared__ uint32_t s_route[SPLIT ? 4 : 1][SPLIT ? 32 * SHADE_BATCH : 1];
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
     const uint32_t n_in = (b == 0) ? a.n0 : a.counters[CNT_QUEUE + b];
@@ -675,173 +684,219 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
     const float inv2pi = 1.0f / (2.0f * PI_F);
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    for (uint32_t base = wid * 32; base < n_in; base += warps * 32) {
-        const uint32_t i = base + lane;
-        uint32_t p = 0;
-        const bool active = i < n_in && (b == 0 ? bounce0_pixel<BATCH>(a, i, p) : (p = qin[i], true));
-        bool cont = false, anyj = false, qhit = false, want_train = false;
-        const bool at_query = a.cache && b + 1 == a.nb_render;
-        f3 stash_E = f3{0, 0, 0}, stash_R = f3{0, 0, 0}, stash_n = f3{0, 0, 0};
-        float stash_mis = 0.0f;
-        int4 stash_hit = make_int4(-1, 0, 0, 0), stash_rc = make_int4(0, 0, 0, 0);
-        int stash_half = 0;
-        f3 new_o = f3{0, 0, 0}, new_d = f3{0, 0, 0};
-        float pdf = 1.0f;
-        int face = 0;
-        if (active) {
-            const ViewDev &V = view_of<BATCH>(a, p);
-            const uint32_t lp = p - V.pix_off;
-            f3 o, d;
-            if (b == 0) {
-                raygen(V, lp, o, d);
-                if (CAPTURE) {
-                    st3(a.c_origin, p, o);
-                    st3(a.c_dir, p, d);
-                }
-            } else {
-                o = ld3(a.ray_o[p]);
-                d = ld3(a.ray_d[p]);
+    // SPLIT (secondary bounces that continue, but not the query vertex of a
+    // cache frame, whose training-slot grants follow queue order): each warp
+    // takes SHADE_BATCH x 32 queue entries and shades the surface hits first,
+    // 32 at a time, then the sky misses, so that a lane that only looks up
+    // the sky does not sit out the light-BVH descents of its neighbours.
+    // Every pixel's results are independent of the order of shading.
+    const bool split = SPLIT && shade_split(a, b);
+    const uint32_t span = split ? 32u * SHADE_BATCH : 32u;
+    uint32_t *route = s_route[threadIdx.x >> 5];
+    for (uint32_t base = wid * span; base < n_in; base += warps * span) {
+        uint32_t n_route = 0;
+        if (split) {
+            uint32_t pk[SHADE_BATCH], surf[SHADE_BATCH], valid[SHADE_BATCH];
+            uint32_t n_surf = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < SHADE_BATCH; k++) {
+                const uint32_t i = base + 32 * k + lane;
+                const bool v = i < n_in;
+                pk[k] = v ? qin[i] : 0u;
+                const bool sf = v && a.hits[pk[k]].x >= 0;
+                surf[k] = __ballot_sync(FULL, sf);
+                valid[k] = __ballot_sync(FULL, v);
+                n_surf += __popc(surf[k]);
             }
-            const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
-            const int4 hv = a.hits[p];
-            // A cache frame's query vertex continues only on its training paths
-            // (one in 16): on the others the cache's prediction replaces the
-            // vertex's outgoing radiance, and its record, direction and light
-            // pdf are never read, so they skip the continuation as a last
-            // vertex does.
-            if (at_query) want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
-            ShadeOut so;
-            shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv,
-                               CAPTURE || (b + 1 < nb && (!at_query || want_train)), so);
-            const f3 n = so.n, E = so.E;
-            f3 R = so.R;
-            const float mis = so.mis;
-            const int half = so.half;
-            const int4 rc = so.rc;
-            new_o = so.new_o;
-            new_d = so.new_d;
-            pdf = so.pdf;
-            face = so.face;
-            // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
-            if (hv.x >= 0) anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
-            // radiance cache: the vertex where rendered paths end into the cache
-            // (every pixel's flag is cleared at bounce 0, so a path that ends
-            // before the query vertex never reads a stale one)
-            if (a.cache && b == 0 && !at_query) a.qflag[p] = 0;
-            if (at_query) {
-                qhit = hv.x >= 0;
-                a.qflag[p] = qhit ? 1 : 0;
-                if (qhit) {
-                    // the cache's normal: a face index, or a mesh normal packed in 32 bits
-                    a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z,
-                                             face >= 0 ? __int_as_float(face) : __uint_as_float(pack_normal10(so.n)));
-                    a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
-                }
+            uint32_t before_s = 0, before_m = n_surf;
+#pragma unroll
+            for (uint32_t k = 0; k < SHADE_BATCH; k++) {
+                const uint32_t miss = valid[k] & ~surf[k];
+                if ((surf[k] >> lane) & 1u) route[before_s + __popc(surf[k] & lanemask_lt())] = pk[k];
+                else if ((miss >> lane) & 1u) route[before_m + __popc(miss & lanemask_lt())] = pk[k];
+                before_s += __popc(surf[k]);
+                before_m += __popc(miss);
             }
-            // stash for the second half (after the warp-level training-slot grant)
-            stash_E = E;
-            stash_R = R;
-            stash_n = n;
-            stash_mis = mis;
-            stash_hit = hv;
-            stash_rc = rc;
-            stash_half = half;
+            n_route = before_m;
+            __syncwarp();
         }
-        // training paths: up to train_cap per frame, granted per warp
-        bool is_train = false;
-        if (at_query) {
-            const uint32_t tm = __ballot_sync(FULL, active && qhit && want_train);
-            const uint32_t im = __ballot_sync(FULL, active && qhit);
-            uint32_t tb = 0, ib = 0;
-            if (lane == 0) {
-                if (tm) tb = atomicAdd(&a.counters[CNT_TRAIN], (uint32_t)__popc(tm));
-                if (im) ib = atomicAdd(&a.counters[CNT_INFER], (uint32_t)__popc(im));
-            }
-            tb = __shfl_sync(FULL, tb, 0);
-            ib = __shfl_sync(FULL, ib, 0);
-            if (active && qhit) a.infer_list[ib + __popc(im & lanemask_lt())] = p;
-            if (active && qhit && want_train) {
-                const uint32_t slot = tb + __popc(tm & lanemask_lt());
-                if (slot < a.train_cap) {
-                    a.train_list[slot] = p;
-                    is_train = true;
-                }
-            }
-            if (!is_train) anyj = false;  // the record of this bounce is replaced by the cache
-        }
-        if (active) {
-            const f3 E = stash_E, R = stash_R, n = stash_n;
-            const float mis = stash_mis;
-            const int4 hv = stash_hit, rc = stash_rc;
-            const int half = stash_half;
-            const size_t rb = (size_t)b * 2 * P;
-            if (anyj) {
-                a.rec[rb + p] = make_float4(E.x, E.y, E.z, 0.0f);
-                a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, 0.0f);
+        const uint32_t passes = split ? (n_route + 31u) / 32u : 1u;
+        for (uint32_t pass = 0; pass < passes; pass++) {
+            uint32_t p = 0;
+            bool active;
+            if (split) {
+                const uint32_t r = 32 * pass + lane;
+                active = r < n_route;
+                if (active) p = route[r];
             } else {
-                const float q = 0.0f * mis + (1.0f - mis) * inv2pi;
-                const float w = pdf / q;
-                a.rec[rb + p] = make_float4(E.x, E.y, E.z, w);
-                a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, q);
+                const uint32_t i = base + lane;
+                active = i < n_in && (b == 0 ? bounce0_pixel<BATCH>(a, i, p) : (p = qin[i], true));
             }
-            if (b == 0) {
-                a.xv[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
-                a.nv[p] = make_float4(n.x, n.y, n.z, 0.0f);
-            } else if (b == 1) {
-                a.xs[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
-                a.ns[p] = make_float4(n.x, n.y, n.z, 0.0f);
-            }
-            cont = !zero3(new_d) && (b + 1 < nb) && (!at_query || is_train);
-            if (cont) {
-                // .w of the ray carries the face and the bsdf pdf to k_anyhit
-                a.ray_o[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
-                a.ray_d[p] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
-            } else {
-                a.nlive[p] = (uint8_t)(b + 1);
-            }
-            if (CAPTURE) {
-                const size_t s1 = (size_t)(b + 1) * P + p, s0 = (size_t)b * P + p;
-                st3(a.c_origin, s1, new_o);
-                st3(a.c_dir, s1, new_d);
-                st3(a.c_normal, s0, n);
-                st3(a.c_emis, s0, E);
-                st3(a.c_refl, s0, R);
-                a.c_mis[s0] = mis;
-                a.c_pdf[s0] = pdf;
-                a.c_nee[s0] = 0.0f;
-                uint4 hw;
-                if (face < 0) {  // a mesh triangle: (instance, triangle)
-                    hw = make_uint4((uint32_t)rc.x, (uint32_t)rc.y, INVALID, 0u);
-                } else if (hv.x >= 0) {
-                    const uint32_t mask = ((uint32_t)rc.z >> 15) & 63u;
-                    hw.x = rec_inst(rc);
-                    hw.y = (uint32_t)rc.w + 2u * __popc(mask & ((1u << face) - 1u)) + (uint32_t)half;
-                    hw.z = (uint32_t)rc.z & 0x7FFFu;
-                    hw.w = (uint32_t)face | ((uint32_t)half << 8);
+            bool cont = false, anyj = false, qhit = false, want_train = false;
+            const bool at_query = a.cache && b + 1 == a.nb_render;
+            f3 stash_E = f3{0, 0, 0}, stash_R = f3{0, 0, 0}, stash_n = f3{0, 0, 0};
+            float stash_mis = 0.0f;
+            int4 stash_hit = make_int4(-1, 0, 0, 0), stash_rc = make_int4(0, 0, 0, 0);
+            int stash_half = 0;
+            f3 new_o = f3{0, 0, 0}, new_d = f3{0, 0, 0};
+            float pdf = 1.0f;
+            int face = 0;
+            if (active) {
+                const ViewDev &V = view_of<BATCH>(a, p);
+                const uint32_t lp = p - V.pix_off;
+                f3 o, d;
+                if (b == 0) {
+                    raygen(V, lp, o, d);
+                    if (CAPTURE) {
+                        st3(a.c_origin, p, o);
+                        st3(a.c_dir, p, d);
+                    }
                 } else {
-                    hw = make_uint4(INVALID, INVALID, INVALID, INVALID);
+                    o = ld3(a.ray_o[p]);
+                    d = ld3(a.ray_d[p]);
                 }
-                reinterpret_cast<uint4 *>(a.c_hit)[s0] = hw;
+                const uint32_t seed = mm_combine(V.frame * nb + b, lp);  // interactive_rendering.rs:1189
+                const int4 hv = a.hits[p];
+                // A cache frame's query vertex continues only on its training paths
+                // (one in 16): on the others the cache's prediction replaces the
+                // vertex's outgoing radiance, and its record, direction and light
+                // pdf are never read, so they skip the continuation as a last
+                // vertex does.
+                if (at_query) want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
+                ShadeOut so;
+                shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv,
+                                   CAPTURE || (b + 1 < nb && (!at_query || want_train)), so);
+                const f3 n = so.n, E = so.E;
+                f3 R = so.R;
+                const float mis = so.mis;
+                const int half = so.half;
+                const int4 rc = so.rc;
+                new_o = so.new_o;
+                new_d = so.new_d;
+                pdf = so.pdf;
+                face = so.face;
+                // the light pdf of the chosen direction (nee_pdf pass, bounce nb-1 never computed)
+                if (hv.x >= 0) anyj = (b + 1 < nb) && mis != 0.0f && len3(new_d) != 0.0f;
+                // radiance cache: the vertex where rendered paths end into the cache
+                // (every pixel's flag is cleared at bounce 0, so a path that ends
+                // before the query vertex never reads a stale one)
+                if (a.cache && b == 0 && !at_query) a.qflag[p] = 0;
+                if (at_query) {
+                    qhit = hv.x >= 0;
+                    a.qflag[p] = qhit ? 1 : 0;
+                    if (qhit) {
+                        // the cache's normal: a face index, or a mesh normal packed in 32 bits
+                        a.q_pos[p] = make_float4(new_o.x, new_o.y, new_o.z,
+                                                 face >= 0 ? __int_as_float(face) : __uint_as_float(pack_normal10(so.n)));
+                        a.q_dir[p] = make_float4(d.x, d.y, d.z, 0.0f);
+                    }
+                }
+                // stash for the second half (after the warp-level training-slot grant)
+                stash_E = E;
+                stash_R = R;
+                stash_n = n;
+                stash_mis = mis;
+                stash_hit = hv;
+                stash_rc = rc;
+                stash_half = half;
+            }
+            // training paths: up to train_cap per frame, granted per warp
+            bool is_train = false;
+            if (at_query) {
+                const uint32_t tm = __ballot_sync(FULL, active && qhit && want_train);
+                const uint32_t im = __ballot_sync(FULL, active && qhit);
+                uint32_t tb = 0, ib = 0;
+                if (lane == 0) {
+                    if (tm) tb = atomicAdd(&a.counters[CNT_TRAIN], (uint32_t)__popc(tm));
+                    if (im) ib = atomicAdd(&a.counters[CNT_INFER], (uint32_t)__popc(im));
+                }
+                tb = __shfl_sync(FULL, tb, 0);
+                ib = __shfl_sync(FULL, ib, 0);
+                if (active && qhit) a.infer_list[ib + __popc(im & lanemask_lt())] = p;
+                if (active && qhit && want_train) {
+                    const uint32_t slot = tb + __popc(tm & lanemask_lt());
+                    if (slot < a.train_cap) {
+                        a.train_list[slot] = p;
+                        is_train = true;
+                    }
+                }
+                if (!is_train) anyj = false;  // the record of this bounce is replaced by the cache
+            }
+            if (active) {
+                const f3 E = stash_E, R = stash_R, n = stash_n;
+                const float mis = stash_mis;
+                const int4 hv = stash_hit, rc = stash_rc;
+                const int half = stash_half;
+                const size_t rb = (size_t)b * 2 * P;
+                if (anyj) {
+                    a.rec[rb + p] = make_float4(E.x, E.y, E.z, 0.0f);
+                    a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, 0.0f);
+                } else {
+                    const float q = 0.0f * mis + (1.0f - mis) * inv2pi;
+                    const float w = pdf / q;
+                    a.rec[rb + p] = make_float4(E.x, E.y, E.z, w);
+                    a.rec[rb + P + p] = make_float4(R.x, R.y, R.z, q);
+                }
+                if (b == 0) {
+                    a.xv[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
+                    a.nv[p] = make_float4(n.x, n.y, n.z, 0.0f);
+                } else if (b == 1) {
+                    a.xs[p] = make_float4(new_o.x, new_o.y, new_o.z, 0.0f);
+                    a.ns[p] = make_float4(n.x, n.y, n.z, 0.0f);
+                }
+                cont = !zero3(new_d) && (b + 1 < nb) && (!at_query || is_train);
+                if (cont) {
+                    // .w of the ray carries the face and the bsdf pdf to k_anyhit
+                    a.ray_o[p] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+                    a.ray_d[p] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
+                } else {
+                    a.nlive[p] = (uint8_t)(b + 1);
+                }
+                if (CAPTURE) {
+                    const size_t s1 = (size_t)(b + 1) * P + p, s0 = (size_t)b * P + p;
+                    st3(a.c_origin, s1, new_o);
+                    st3(a.c_dir, s1, new_d);
+                    st3(a.c_normal, s0, n);
+                    st3(a.c_emis, s0, E);
+                    st3(a.c_refl, s0, R);
+                    a.c_mis[s0] = mis;
+                    a.c_pdf[s0] = pdf;
+                    a.c_nee[s0] = 0.0f;
+                    uint4 hw;
+                    if (face < 0) {  // a mesh triangle: (instance, triangle)
+                        hw = make_uint4((uint32_t)rc.x, (uint32_t)rc.y, INVALID, 0u);
+                    } else if (hv.x >= 0) {
+                        const uint32_t mask = ((uint32_t)rc.z >> 15) & 63u;
+                        hw.x = rec_inst(rc);
+                        hw.y = (uint32_t)rc.w + 2u * __popc(mask & ((1u << face) - 1u)) + (uint32_t)half;
+                        hw.z = (uint32_t)rc.z & 0x7FFFu;
+                        hw.w = (uint32_t)face | ((uint32_t)half << 8);
+                    } else {
+                        hw = make_uint4(INVALID, INVALID, INVALID, INVALID);
+                    }
+                    reinterpret_cast<uint4 *>(a.c_hit)[s0] = hw;
+                }
+            }
+            // compaction: continuing rays into the next bounce queue, light-pdf jobs
+            // into the any-hit queue (one ballot + one atomic per warp each)
+            const uint32_t cm = __ballot_sync(FULL, cont);
+            const uint32_t am = __ballot_sync(FULL, anyj);
+            uint32_t qb = 0, ab = 0;
+            if (lane == 0) {
+                if (cm) qb = atomicAdd(&a.counters[CNT_QUEUE + b + 1], (uint32_t)__popc(cm));
+                if (am) ab = atomicAdd(&a.counters[CNT_AQUEUE + b], (uint32_t)__popc(am));
+            }
+            qb = __shfl_sync(FULL, qb, 0);
+            ab = __shfl_sync(FULL, ab, 0);
+            if (cont) qout[qb + __popc(cm & lanemask_lt())] = p;
+            if (anyj) {
+                const uint32_t j = ab + __popc(am & lanemask_lt());
+                a.aqueue[b & 1][j] = p;
+                a.ajob[b & 1][2 * (size_t)j] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
+                a.ajob[b & 1][2 * (size_t)j + 1] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
             }
         }
-        // compaction: continuing rays into the next bounce queue, light-pdf jobs
-        // into the any-hit queue (one ballot + one atomic per warp each)
-        const uint32_t cm = __ballot_sync(FULL, cont);
-        const uint32_t am = __ballot_sync(FULL, anyj);
-        uint32_t qb = 0, ab = 0;
-        if (lane == 0) {
-            if (cm) qb = atomicAdd(&a.counters[CNT_QUEUE + b + 1], (uint32_t)__popc(cm));
-            if (am) ab = atomicAdd(&a.counters[CNT_AQUEUE + b], (uint32_t)__popc(am));
-        }
-        qb = __shfl_sync(FULL, qb, 0);
-        ab = __shfl_sync(FULL, ab, 0);
-        if (cont) qout[qb + __popc(cm & lanemask_lt())] = p;
-        if (anyj) {
-            const uint32_t j = ab + __popc(am & lanemask_lt());
-            a.aqueue[b & 1][j] = p;
-            a.ajob[b & 1][2 * (size_t)j] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(face));
-            a.ajob[b & 1][2 * (size_t)j + 1] = make_float4(new_d.x, new_d.y, new_d.z, pdf);
-        }
+        __syncwarp();
     }
 }
 
@@ -1125,8 +1180,8 @@ static void init_grids_once() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     g_sms = std::max(1, g_sms);
-    g_shade[0] = occupancy_grid((const void *)k_shade<false, false, false>, 128);
-    g_shade[1] = occupancy_grid((const void *)k_shade<false, true, false>, 128);
+    g_shade[0] = occupancy_grid((const void *)k_shade<false, false, false, false>, 128);
+    g_shade[1] = occupancy_grid((const void *)k_shade<false, true, false, false>, 128);
     g_any[0] = occupancy_grid((const void *)k_anyhit<false, false>, 128);
     g_any[1] = occupancy_grid((const void *)k_anyhit<false, true>, 128);
     g_trace[1] = occupancy_grid((const void *)k_trace<true, false>, 128);
@@ -1182,18 +1237,25 @@ vrg_status launch_trace(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t
     return VRG_OK;
 }
 
+template <bool CAPTURE, bool BATCH, bool MESH>
+static void shade_launch(int gs, cudaStream_t s, const FrameArgs &a, uint32_t b, bool split) {
+    if (split) k_shade<CAPTURE, BATCH, MESH, true><<<gs, 128, 0, s>>>(a, b);
+    else k_shade<CAPTURE, BATCH, MESH, false><<<gs, 128, 0, s>>>(a, b);
+}
+
 // shading of bounce b
 vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
     int gt, gs, ga;
     bounce_grids(a, max_rays, gt, gs, ga);
+    const bool split = shade_split(a, b);
     if (a.mesh) {
-        if (a.views) k_shade<false, true, true><<<gs, 128, 0, s>>>(a, b);
-        else if (a.capture) k_shade<true, false, true><<<gs, 128, 0, s>>>(a, b);
-        else k_shade<false, false, true><<<gs, 128, 0, s>>>(a, b);
+        if (a.views) shade_launch<false, true, true>(gs, s, a, b, split);
+        else if (a.capture) shade_launch<true, false, true>(gs, s, a, b, split);
+        else shade_launch<false, false, true>(gs, s, a, b, split);
     } else {
-        if (a.views) k_shade<false, true, false><<<gs, 128, 0, s>>>(a, b);
-        else if (a.capture) k_shade<true, false, false><<<gs, 128, 0, s>>>(a, b);
-        else k_shade<false, false, false><<<gs, 128, 0, s>>>(a, b);
+        if (a.views) shade_launch<false, true, false>(gs, s, a, b, split);
+        else if (a.capture) shade_launch<true, false, false>(gs, s, a, b, split);
+        else shade_launch<false, false, false>(gs, s, a, b, split);
     }
     VRG_CUDA_TRY(cudaGetLastError());
     return VRG_OK;
