@@ -628,14 +628,14 @@ def run_ours(args, d):
         # the renderer's frame counter and history are restored); both times
         # are per frame of frames run back to back (the default over the
         # orbit's first eight views, the tuner's candidates at its first
-        # view; eight frames, so that the first one of a run, which has no
-        # frame in flight beside it, weighs less in the choice)
+        # view; 24 frames per run, so that the first frames of a run, which
+        # have fewer frames in flight beside them, weigh little in the choice)
         blob0 = r.save_state()
         default_ms = [back_to_back_ms(8, 0) for _ in range(3)]
         r.load_state(blob0)
         cam0 = vrg.orbit_camera(NX, NZ, 0, ORBIT, W, H)
         t0 = time.perf_counter()
-        best, best_ms = r.autotune(scene, cam0, frame_params(0), frames=8)
+        best, best_ms = r.autotune(scene, cam0, frame_params(0), frames=24)
         best_tuning = best
         tuning = {"config": best.as_dict(), "tuned_ms": round(best_ms, 4),
                   "default_ms": round(float(np.median(default_ms)), 4),

@@ -377,8 +377,10 @@ typedef struct vrg_tuning {
     uint32_t stream_block;          /* threads per CTA of the per-pixel kernels: 64, 128 or 256 (256) */
     uint32_t spatial_staging;       /* how the spatial pass reads reservoirs: 1 each CTA's 32x8-pixel tile
                                        staged in shared memory by one tensor copy (TMA; single-view
-                                       renderers of at least 32x8 pixels), 2 per-thread loads; 0 = 1 where
-                                       it applies, else 2 */
+                                       renderers of at least 32x8 pixels, else 2), 2 per-thread loads;
+                                       0 = 2.  The autotuner keeps the value it is given: staged tiles
+                                       speed up the spatial pass alone but slow frames in flight, whose
+                                       walks beside it lose L1 to the tile's shared memory */
     uint32_t reserved[1];
 } vrg_tuning;
 

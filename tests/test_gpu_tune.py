@@ -85,8 +85,8 @@ def test_tuning_rejects_out_of_range(gpu_ctx):
 @pytest.mark.parametrize("w,h", [(83, 45), (96, 64), (40, 8)], ids=["83x45", "96x64", "40x8"])
 def test_tma_staged_spatial_pass_bit_exact(gpu_ctx, world, orc, w, h):
     """The spatial pass with each CTA's 32x8-pixel reservoir tile staged in
-    shared memory by a tensor copy (spatial_staging 1, the default) bit for bit
-    as with per-thread loads (2) and as the oracle, with edge tiles partly
+    shared memory by a tensor copy (spatial_staging 1) bit for bit as with
+    per-thread loads (2, the default) and as the oracle, with edge tiles partly
     outside the view."""
     from helpers import compare_frame, params
     mats, n, blocks = terrain_world(31, 2, 2, 0.01)

@@ -933,9 +933,12 @@ static vrg_tuning effective_tuning(const vrg_renderer *r) {
     e.trace_refill = t.trace_refill ? t.trace_refill : 8;
     e.anyhit_refill = t.anyhit_refill ? t.anyhit_refill : 8;
     e.stream_block = t.stream_block ? t.stream_block : 256;
-    // TMA-staged spatial tiles wherever they apply (the spatial pass: 0.113 against 0.117-0.119 ms
-    // per 1080p frame), unless per-thread loads are asked for
-    e.spatial_staging = (t.spatial_staging != 2 && r->n_views == 0 && r->W >= 32 && r->H >= 8) ? 1u : 2u;
+    // Per-thread loads unless TMA-staged tiles are asked for.  Staged tiles
+    // make the spatial pass itself faster (0.113 against 0.117-0.119 ms per
+    // 1080p frame), but the frame in flight slower (1.110-1.126 against
+    // 1.078-1.091 ms): their 20.5 KB of shared memory per CTA takes L1 from
+    // the closest-hit and light-hit walks of the next frames beside them.
+    e.spatial_staging = (t.spatial_staging == 1 && r->n_views == 0 && r->W >= 32 && r->H >= 8) ? 1u : 2u;
     return e;
 }
 
@@ -1716,7 +1719,6 @@ VRG_API vrg_status vrg_renderer_autotune(vrg_renderer *r, vrg_scene *scene, cons
         {&vrg_tuning::anyhit_refill, refills},
         {&vrg_tuning::anyhit_blocks_per_sm, bpsm_candidates(occ[2])},
         {&vrg_tuning::stream_block, {64, 128, 256}},
-        {&vrg_tuning::spatial_staging, r->res_map_ok ? std::vector<uint32_t>{1, 2} : std::vector<uint32_t>{2}},
     };
     vrg_tuning cur = effective_tuning(r);
     float cur_ms = 0.0f;
