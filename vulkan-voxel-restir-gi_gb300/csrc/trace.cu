@@ -667,9 +667,15 @@ done:
 // ---------------------------------------------------------------------------
 constexpr uint32_t SHADE_BATCH = 4;  // queue entries per lane of a surface-first shading batch
 
-// the bounces whose shading takes its queue in surface-first batches (k_shade)
+// the bounces whose shading takes its queue in routed batches (k_shade)
 __host__ __device__ __forceinline__ bool shade_split(const FrameArgs &a, uint32_t b) {
-    return b > 0 && b + 1 < a.nb && !(a.cache && b + 1 == a.nb_render);
+    return b > 0 && b + 1 < a.nb;
+}
+
+// A cache frame's query vertex continues on one path in 16: the training
+// paths, picked by a hash of the frame and the view's pixel.
+__device__ __forceinline__ bool want_train_of(const ViewDev &V, uint32_t lp) {
+    return (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
 }
 
 template <bool CAPTURE, bool BATCH, bool MESH, bool SPLIT>
@@ -684,13 +690,16 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
     const float inv2pi = 1.0f / (2.0f * PI_F);
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    // SPLIT (secondary bounces that continue, but not the query vertex of a
-    // cache frame, whose training-slot grants follow queue order): each warp
-    // takes SHADE_BATCH x 32 queue entries and shades the surface hits first,
-    // 32 at a time, then the sky misses, so that a lane that only looks up
-    // the sky does not sit out the light-BVH descents of its neighbours.
-    // Every pixel's results are independent of the order of shading.
+    // SPLIT (secondary bounces that continue): each warp takes SHADE_BATCH x
+    // 32 queue entries and shades first those that sample a continuation (the
+    // light-BVH descent and the direction), 32 at a time, then the others, so
+    // that a lane with little to do does not sit out its neighbours'
+    // descents.  Those are the surface hits, and at a cache frame's query
+    // vertex (without capture) the surface hits of the training paths; the
+    // others are the sky misses, and the query vertices that end into the
+    // cache.  Every pixel's results are independent of the order of shading.
     const bool split = SPLIT && shade_split(a, b);
+    const bool route_train = !CAPTURE && a.cache && b + 1 == a.nb_render;
     const uint32_t span = split ? 32u * SHADE_BATCH : 32u;
     uint32_t *route = s_route[threadIdx.x >> 5];
     for (uint32_t base = wid * span; base < n_in; base += warps * span) {
@@ -703,7 +712,11 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                 const uint32_t i = base + 32 * k + lane;
                 const bool v = i < n_in;
                 pk[k] = v ? qin[i] : 0u;
-                const bool sf = v && a.hits[pk[k]].x >= 0;
+                bool sf = v && a.hits[pk[k]].x >= 0;
+                if (sf && route_train) {
+                    const ViewDev &V = view_of<BATCH>(a, pk[k]);
+                    sf = want_train_of(V, pk[k] - V.pix_off);
+                }
                 surf[k] = __ballot_sync(FULL, sf);
                 valid[k] = __ballot_sync(FULL, v);
                 n_surf += __popc(surf[k]);
@@ -762,7 +775,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                 // vertex's outgoing radiance, and its record, direction and light
                 // pdf are never read, so they skip the continuation as a last
                 // vertex does.
-                if (at_query) want_train = (mm_finalize(mm_combine(V.frame * 0x9E3779B9u + 0x7a11u, lp)) & 15u) == 0u;
+                if (at_query) want_train = want_train_of(V, lp);
                 ShadeOut so;
                 shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv,
                                    CAPTURE || (b + 1 < nb && (!at_query || want_train)), so);
@@ -1247,7 +1260,9 @@ static void shade_launch(int gs, cudaStream_t s, const FrameArgs &a, uint32_t b,
 vrg_status launch_shade(cudaStream_t s, const FrameArgs &a, uint32_t b, uint32_t max_rays) {
     int gt, gs, ga;
     bounce_grids(a, max_rays, gt, gs, ga);
-    const bool split = shade_split(a, b);
+    // (not for the few rays of a cache frame's training bounces, bounded by
+    // max_rays: batches of 128 per warp would leave most of the grid idle)
+    const bool split = shade_split(a, b) && max_rays == 0;
     if (a.mesh) {
         if (a.views) shade_launch<false, true, true>(gs, s, a, b, split);
         else if (a.capture) shade_launch<true, false, true>(gs, s, a, b, split);
