@@ -988,7 +988,7 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
         if (!r->cache_buf || r->cache_cap < cap) {  // (a later cache may train larger batches)
             auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
             struct Off {
-                size_t qp, qd, pr, tg, il, tl, qf, taq0, taq1, taj0, taj1, thb, thv, tjm;
+                size_t qp, qd, pr, tg, il, tl, qf, taq0, taq1, taj0, taj1, thb, thv, tjm, tq, tq0, tq1;
             } off[Renderer::SETS];
             size_t o = 0;
             for (uint32_t k = 0; k < r->n_sets; k++) {
@@ -1007,6 +1007,9 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
                 q.thb = o; o += al((size_t)cap * 2 * 32);
                 q.thv = o; o += al((size_t)cap * 2 * 4);
                 q.tjm = o; o += al((size_t)cap * 8);
+                q.tq = o; o += al(P * 4);
+                q.tq0 = o; o += al((size_t)cap * 4);
+                q.tq1 = o; o += al((size_t)cap * 4);
             }
             DevBufPtr b;
             VRG_TRY(dev_alloc(s, o, b));
@@ -1029,6 +1032,9 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
                 Q.t_hitbuf = (uint4 *)(B + q.thb);
                 Q.t_hitval = (float *)(B + q.thv);
                 Q.t_jmeta = (uint2 *)(B + q.tjm);
+                Q.tq = (uint32_t *)(B + q.tq);
+                Q.t_queue[0] = (uint32_t *)(B + q.tq0);
+                Q.t_queue[1] = (uint32_t *)(B + q.tq1);
             }
             r->cache_buf = b;
             r->cache_cap = cap;
@@ -1055,7 +1061,11 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
         a.infer_list = Q.infer_list;
         a.train_list = Q.train_list;
         a.qflag = Q.qflag;
+        a.tq = Q.tq;
     }
+    // single-view cache frames that fork their training branch: the query
+    // bounce in two launches, the training candidates first
+    a.tq_split = (cache && !capture && !r->n_views) ? 1u : 0u;
     a.nee_type = pr->nee_type;
     a.mode = pr->mode;
     a.spatial_iters = pr->spatial_iterations;
@@ -1120,11 +1130,16 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
 // after spatial; r->ev_k: after k_trace / k_shade of each bounce); a graph
 // recording passes false.
 //
-// A cache frame forks after the shading of the query vertex, while that
-// bounce's light-pdf walk still runs: the training paths' extra bounces (with
-// light-pdf job and hit buffers of their own) and the cache's training step
-// run on the renderer's second stream while the main stream infers the cache
-// for the rendered paths and runs resolve (after the walk) and spatial.
+// A cache frame forks once the training paths' query vertices are shaded,
+// while that bounce's light-pdf walk still runs: the training paths' extra
+// bounces (with light-pdf job and hit buffers of their own) and the cache's
+// training step run on the renderer's second stream while the main stream
+// infers the cache for the rendered paths and runs resolve (after the walk)
+// and spatial.  A single-view frame traces its query bounce in two launches,
+// the training candidates (whose pixels the shading before queued apart)
+// first, and forks between them, before the other paths' query bounce; the
+// training bounces then take ray queues of their own.  A batched frame forks
+// after its whole query bounce.
 // Neither branch reads what the other writes, except the cache itself: the
 // training branch computes its gradients beside the queries, and their Adam
 // step, which rewrites the weights and the table the queries read, is left to
@@ -1184,44 +1199,40 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     // shading of b; the shading of b + 2 (which refills the job buffers of
     // parity b & 1) waits for the walk of b; resolve waits for every walk.
     int last_lp = -1;
-    for (uint32_t b = 0; b < nb_main; b++) {
-        if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][b - 2], 0));
-        VRG_TRY(launch_trace_shade(bs, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
-        if (timed) {  // (timed frames run their bounces on the library stream)
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
-            VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
-        }
-        if (b + 1 < a.nb) {
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[k][b], bs));
-            VRG_CUDA_TRY(cudaStreamWaitEvent(lp, r->ev_shaded[k][b], 0));
-            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], lp));
-            VRG_TRY(launch_light_pdf(lp, a, b, 0));
-            if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[1][b], lp));
-            VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[k][b], lp));
-            last_lp = (int)b;
-        }
-    }
-    // a cache frame's training branch and cache queries start before the last
-    // main walk ends: only resolve reads what that walk writes
-    if (last_lp >= 0 && !fork) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][last_lp], 0));
-    if (own) {
-        VRG_CUDA_TRY(cudaEventRecord(r->ev_bounced[k], bs));
-        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_bounced[k], 0));
-    }
+    auto walk = [&](uint32_t b) -> vrg_status {
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_shaded[k][b], bs));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(lp, r->ev_shaded[k][b], 0));
+        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[0][b], lp));
+        VRG_TRY(launch_light_pdf(lp, a, b, 0));
+        if (timed) VRG_CUDA_TRY(cudaEventRecord(r->ev_lp[1][b], lp));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_lpdone[k][b], lp));
+        last_lp = (int)b;
+        return VRG_OK;
+    };
+    // The training branch: the training paths' extra bounces (with light-pdf
+    // job and hit buffers of their own) and the cache's training step, on
+    // the renderer's second stream, forked from `from` once the training
+    // paths' query vertices are shaded.
     cudaStream_t st = s;  // stream of the training branch
-    if (fork) {
+    const Renderer::CacheSet &Q = r->cs[k];
+    auto branch = [&](cudaStream_t from, bool own_queues) -> vrg_status {
         st = r->aux;
-        VRG_CUDA_TRY(cudaEventRecord(r->ev_fork, s));
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_fork, from));
         VRG_CUDA_TRY(cudaStreamWaitEvent(st, r->ev_fork, 0));
         // The training bounces' light-pdf jobs and hits go to buffers of their
         // own, so they need not wait for the main walks still running (which
-        // read the main job buffers and write their own bounces' records).
+        // read the main job buffers and write their own bounces' records);
+        // forked before the main paths' query bounce, their ray queues too.
         FrameArgs at = a;
-        const Renderer::CacheSet &Q = r->cs[k];
         for (int q = 0; q < 2; q++) {
             at.aqueue[q] = Q.t_aqueue[q];
             at.ajob[q] = Q.t_ajob[q];
         }
+        if (own_queues) {  // training bounce nb_main reads queue[(nb_main + 1) & 1]
+            at.queue[(nb_main + 1) & 1] = Q.t_queue[0];
+            at.queue[nb_main & 1] = Q.t_queue[1];
+        }
+        at.qsel = 0;
         at.hitbuf = Q.t_hitbuf;
         at.hitval = Q.t_hitval;
         at.jmeta = Q.t_jmeta;
@@ -1252,7 +1263,42 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
         VRG_TRY(launch_train_targets(st, at));
         VRG_TRY(nrc_train(r->cache, st, a.train_cap, a.counters + CNT_TRAIN, a.train_list, a.q_pos, a.q_dir,
                           nullptr, a.target, false, a.counters + CNT_ERROR));
+        return VRG_OK;
+    };
+    const bool early = fork && a.tq_split;
+    for (uint32_t b = 0; b < nb_main; b++) {
+        if (b >= 2 && (int)b - 2 <= last_lp) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][b - 2], 0));
+        if (early && b + 1 == nb_main) {
+            // The query bounce of a single-view cache frame, first for the
+            // training candidates that the previous shading queued apart: it
+            // grants the training slots and queues the training paths' next
+            // rays and light-pdf jobs, so the training branch and the query
+            // bounce's walk start here, beside the other paths' query bounce.
+            // (max_rays = P: the plain mapping in the shading, no routed
+            // batches for this short queue.)
+            FrameArgs aT = a;
+            aT.qsel = 1;
+            aT.queue[b & 1] = Q.t_queue[0];  // its continuing rays: the first training bounce's queue
+            aT.queue[(b + 1) & 1] = Q.t_queue[1];
+            VRG_TRY(launch_trace_shade(bs, aT, b, nullptr, a.P));
+            if (b + 1 < a.nb) VRG_TRY(walk(b));
+            VRG_TRY(branch(bs, true));
+        }
+        VRG_TRY(launch_trace_shade(bs, a, b, timed ? r->ev_k[0][b] : nullptr, 0));
+        if (timed) {  // (timed frames run their bounces on the library stream)
+            VRG_CUDA_TRY(cudaEventRecord(r->ev_k[1][b], s));
+            VRG_CUDA_TRY(cudaEventRecord(r->ev[b + 1], s));
+        }
+        if (b + 1 < a.nb && !(early && b + 1 == nb_main)) VRG_TRY(walk(b));
     }
+    // a cache frame's training branch and cache queries start before the last
+    // main walk ends: only resolve reads what that walk writes
+    if (last_lp >= 0 && !fork) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_lpdone[k][last_lp], 0));
+    if (own) {
+        VRG_CUDA_TRY(cudaEventRecord(r->ev_bounced[k], bs));
+        VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_bounced[k], 0));
+    }
+    if (fork && !early) VRG_TRY(branch(s, false));
     if (a.cache) {  // radiance-cache queries of every path that ends into the cache
         if (updated) VRG_CUDA_TRY(cudaStreamWaitEvent(s, r->ev_updated, 0));
         if (!fork) VRG_TRY(nrc_flush(r->cache, s));

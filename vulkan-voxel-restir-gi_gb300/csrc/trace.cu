@@ -360,8 +360,9 @@ template <bool BATCH, bool MESH>
 __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs a, uint32_t b) {
     const int lane = threadIdx.x & 31;
     const int REFILL = (int)a.refill_trace;
-    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[CNT_QUEUE + b];
-    const uint32_t *qin = a.queue[(b + 1) & 1];
+    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[a.qsel ? CNT_TQUEUE : CNT_QUEUE + b];
+    const uint32_t *qin = a.qsel ? a.tq : a.queue[(b + 1) & 1];
+    uint32_t *fetch = a.counters + (a.qsel ? CNT_TFETCH : CNT_FETCH + b);
     uint32_t *err = a.counters + CNT_ERROR;
     const float4 *wide = a.v0.sc.geo_wide;
     const int4 *recs = a.v0.sc.geo_rec;
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ FrameArgs
         const uint32_t need = __ballot_sync(FULL, !has);
         if (!exhausted && need && (__popc(need) >= REFILL || need == FULL)) {
             uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&a.counters[CNT_FETCH + b], (uint32_t)__popc(need));
+            if (lane == 0) base = atomicAdd(fetch, (uint32_t)__popc(need));
             base = __shfl_sync(FULL, base, 0);
             if (base + (uint32_t)__popc(need) >= n_in) exhausted = true;
             if (!has) {
@@ -684,9 +685,11 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
     __shared__ uint32_t s_route[SPLIT ? 4 : 1][SPLIT ? 32 * SHADE_BATCH : 1];
     const int lane = threadIdx.x & 31;
     const uint32_t P = a.P, nb = a.nb;
-    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[CNT_QUEUE + b];
-    const uint32_t *qin = a.queue[(b + 1) & 1];
+    const uint32_t n_in = (b == 0) ? a.n0 : a.counters[a.qsel ? CNT_TQUEUE : CNT_QUEUE + b];
+    const uint32_t *qin = a.qsel ? a.tq : a.queue[(b + 1) & 1];
     uint32_t *qout = a.queue[b & 1];
+    // the bounce before a split query bounce: training candidates go to tq
+    const bool to_tq = a.tq_split && b + 2 == a.nb_render;
     const float inv2pi = 1.0f / (2.0f * PI_F);
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -775,7 +778,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
                 // vertex's outgoing radiance, and its record, direction and light
                 // pdf are never read, so they skip the continuation as a last
                 // vertex does.
-                if (at_query) want_train = want_train_of(V, lp);
+                if (at_query || to_tq) want_train = want_train_of(V, lp);
                 ShadeOut so;
                 shade_vertex<MESH>(V.sc, a.nee_type, b, seed, o, d, hv,
                                    CAPTURE || (b + 1 < nb && (!at_query || want_train)), so);
@@ -892,7 +895,8 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
             }
             // compaction: continuing rays into the next bounce queue, light-pdf jobs
             // into the any-hit queue (one ballot + one atomic per warp each)
-            const uint32_t cm = __ballot_sync(FULL, cont);
+            const bool cont_t = cont && to_tq && want_train;  // a training candidate's ray
+            const uint32_t cm = __ballot_sync(FULL, cont && !cont_t);
             const uint32_t am = __ballot_sync(FULL, anyj);
             uint32_t qb = 0, ab = 0;
             if (lane == 0) {
@@ -901,7 +905,14 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ FrameA
             }
             qb = __shfl_sync(FULL, qb, 0);
             ab = __shfl_sync(FULL, ab, 0);
-            if (cont) qout[qb + __popc(cm & lanemask_lt())] = p;
+            if (cont && !cont_t) qout[qb + __popc(cm & lanemask_lt())] = p;
+            if (to_tq) {
+                const uint32_t tm = __ballot_sync(FULL, cont_t);
+                uint32_t tb = 0;
+                if (lane == 0 && tm) tb = atomicAdd(&a.counters[CNT_TQUEUE], (uint32_t)__popc(tm));
+                tb = __shfl_sync(FULL, tb, 0);
+                if (cont_t) a.tq[tb + __popc(tm & lanemask_lt())] = p;
+            }
             if (anyj) {
                 const uint32_t j = ab + __popc(am & lanemask_lt());
                 a.aqueue[b & 1][j] = p;

@@ -10,6 +10,8 @@ constexpr int CNT_QUEUE = 0;     // [0..7]  rays queued for bounce b
 constexpr int CNT_FETCH = 8;     // [8..15] closest-hit work-fetch cursor of bounce b
 constexpr int CNT_ERROR = 16;    // error word
 constexpr int CNT_RAYS = 18;     // u64 at words 18-19: closest-hit queries
+constexpr int CNT_TQUEUE = 22;   // a cache frame's training candidates queued for its query bounce (FrameArgs::tq)
+constexpr int CNT_TFETCH = 23;   // their closest-hit work-fetch cursor
 constexpr int CNT_ANY = 20;      // u64 at words 20-21: light any-hit queries
 constexpr int CNT_AQUEUE = 24;   // [24..31] any-hit jobs queued by bounce b
 constexpr int CNT_AFETCH = 32;   // [32..39] any-hit work-fetch cursor of bounce b
@@ -66,6 +68,14 @@ struct FrameArgs {
     // wavefront state
     float4 *ray_o, *ray_d;
     uint32_t *queue[2];
+    // A single-view cache frame traces its query bounce in two launches: the
+    // training candidates (one pixel in 16) first, so that the training
+    // branch forks early, then the other paths.  tq_split: the shading of the
+    // bounce before the query bounce queues the candidates' rays in tq
+    // (CNT_TQUEUE) instead of queue[]; qsel: this launch of the query bounce
+    // takes its rays from tq.
+    uint32_t *tq;
+    uint32_t tq_split, qsel;
     // light-pdf jobs of bounce b in [b & 1] (double-buffered by bounce parity:
     // the jobs of bounce b are walked while bounce b + 1 traces and shades):
     // the pixel, and a copy of its ray (origin | face, direction | bsdf pdf)

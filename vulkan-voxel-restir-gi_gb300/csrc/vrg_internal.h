@@ -303,6 +303,11 @@ struct Renderer {
         uint8_t *qflag = nullptr;
         uint32_t *t_aqueue[2] = {};
         float4 *t_ajob[2] = {};
+        // a single-view frame's training candidates for the query bounce, and
+        // the training bounces' ray queues (the branch forks before the main
+        // paths' query bounce has read its own queue)
+        uint32_t *tq = nullptr;
+        uint32_t *t_queue[2] = {};
         uint4 *t_hitbuf = nullptr;
         float *t_hitval = nullptr;
         uint2 *t_jmeta = nullptr;
