@@ -1175,8 +1175,9 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     // A single-view cache frame in flight starts its bounces once the
     // previous cache frame's training branch is done: that branch is a chain
     // of small latency-bound launches which persistent bounce kernels beside
-    // it would hold off the SMs (1080p, 8x8 chunks: 2.07 ms per frame in
-    // flight with the wait, 2.20 without, 2.11 one at a time).  A batched
+    // it would hold off the SMs (1080p, 8x8 chunks, ReSTIR over the cache:
+    // 1.76 ms per frame in flight with the wait, 1.80-1.85 without, 1.80-1.83
+    // one at a time).  A batched
     // frame's bounces are long enough to hide the branch: four 3840x2160
     // views of the 32x32-chunk scene take 15.6-15.7 ms per frame in flight
     // with the wait and without it, so batched frames do not wait.
