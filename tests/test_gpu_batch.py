@@ -224,3 +224,52 @@ def test_batched_frames_in_flight_match(gpu_ctx, world):
             got = dev[f][v].cpu().numpy().reshape(h, w, 3)
             assert _same_bits(got, want[f][v]), (f, v)
     br.close()
+
+
+def test_batched_cache_frame_matches_single_views(gpu_ctx):
+    """A batched cache frame (2 bounces into the radiance cache, 4 training
+    bounces for the training paths, ReSTIR view) forks its training branch
+    after its whole query bounce; a single-view cache frame traces the
+    training candidates' query bounce first and forks there, beside the
+    other paths' query bounce.  The batch's first frame, before any training
+    step has changed the cache, equals view by view the first cache frame of
+    single-view renderers, each with a fresh cache of the same seed over the
+    same scene, bit for bit; a second batched frame, on the trained cache,
+    runs without device error flags."""
+    mats, n = vrg.terrain_materials(MAT_SEED)
+    gpu_ctx.set_materials(mats, n)
+    sc, objs = vrg.build_world(gpu_ctx, vrg.terrain_blocks(15, 2, 2, 0.02))
+    try:
+        _, gtl = sc.get_tlas()
+        lo, hi = gtl[0]["min"], gtl[0]["max"]
+        ext = [(64, 48), (97, 61), (40, 40)]
+        cams = [vrg.orbit_camera(2, 2, 5 + 9 * v, 64, w, h) for v, (w, h) in enumerate(ext)]
+        br = vrg.BatchRenderer(gpu_ctx, ext, 8)
+        cache = vrg.RadianceCache(gpu_ctx, lo, hi, seed=3)
+        br.set_cache(cache)
+        _, rads = br.render([sc] * len(ext), cams, _params(vrg.RENDER_CACHE),
+                            [_seeds(v, 0) for v in range(len(ext))], want_radiance=True)
+        assert br.last_stats.error_flags == 0
+        batched = [r.copy() for r in rads]
+        br.render([sc] * len(ext), cams, _params(vrg.RENDER_CACHE), [_seeds(v, 1) for v in range(len(ext))])
+        assert br.last_stats.error_flags == 0
+        br.set_cache(None)
+        cache.close()
+        br.close()
+        for v, (w, h) in enumerate(ext):
+            r = vrg.Renderer(gpu_ctx, w, h, 8)
+            c = vrg.RadianceCache(gpu_ctx, lo, hi, seed=3)
+            r.set_cache(c)
+            p = _params(vrg.RENDER_CACHE)
+            p.temporal_seed, p.spatial_seed = _seeds(v, 0)
+            _, rad = r.render_params(sc, cams[v], p, want_image=False, want_radiance=True)
+            assert r.last_stats.error_flags == 0
+            assert np.abs(np.nan_to_num(rad, nan=0.0, posinf=0.0, neginf=0.0)).sum() > 0, v
+            assert _same_bits(rad, batched[v]), v
+            r.set_cache(None)
+            c.close()
+            r.close()
+    finally:
+        sc.close()
+        for o in objs:
+            o.release()

@@ -1064,7 +1064,9 @@ static vrg_status frame_setup(vrg_renderer *r, const vrg_render_params *pr, bool
         a.tq = Q.tq;
     }
     // single-view cache frames that fork their training branch: the query
-    // bounce in two launches, the training candidates first
+    // bounce in two launches, the training candidates first (a batched
+    // frame's query bounce is long enough to hide its branch: four 3840x2160
+    // views took 15.14-15.23 ms per frame one at a time split, 14.85 whole)
     a.tq_split = (cache && !capture && !r->n_views) ? 1u : 0u;
     a.nee_type = pr->nee_type;
     a.mode = pr->mode;
@@ -1172,16 +1174,14 @@ static vrg_status frame_launch(vrg_renderer *r, const FrameArgs &a, bool timed, 
     cudaStream_t bs = own ? r->bs[k] : s;  // stream of the bounces
     cudaStream_t lp = r->lps[k];
     if (own) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_done[k], 0));
-    // A single-view cache frame in flight starts its bounces once the
-    // previous cache frame's training branch is done: that branch is a chain
-    // of small latency-bound launches which persistent bounce kernels beside
-    // it would hold off the SMs (1080p, 8x8 chunks, ReSTIR over the cache:
-    // 1.76 ms per frame in flight with the wait, 1.80-1.85 without, 1.80-1.83
-    // one at a time).  A batched
-    // frame's bounces are long enough to hide the branch: four 3840x2160
-    // views of the 32x32-chunk scene take 15.6-15.7 ms per frame in flight
-    // with the wait and without it, so batched frames do not wait.
-    if (own && fork && !a.views) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_join, 0));
+    // A cache frame in flight starts its bounces once the previous cache
+    // frame's training branch is done: that branch is a chain of small
+    // latency-bound launches which persistent bounce kernels beside it would
+    // hold off the SMs (ReSTIR over the cache, frames in flight: 1080p on 8x8
+    // chunks 1.76 ms per frame with the wait, 1.80-1.85 without; four
+    // 3840x2160 views of the 32x32-chunk scene 15.06-15.09 ms with the wait,
+    // 17.0-17.6 without).
+    if (own && fork) VRG_CUDA_TRY(cudaStreamWaitEvent(bs, r->ev_join, 0));
     // a cache frame runs the previous cache frame's Adam step on the training
     // stream beside its own bounces (after all earlier work on the library
     // stream); its cache queries wait for it
